@@ -1,0 +1,359 @@
+"""Benchmark: Fock builds/s (one J and one K build) on the Kr benchmark basis.
+
+Workload (the reference's Kr Fock-build kernel configuration): Z = 36,
+40 radial elements with boundaries r_i = 61^(i/40) - 1 bohr (exponential
+grid, zexp = 1, Rmax = 60), 15-node LIP elements, l = 0..2 with m = -2..2
+(Nang = 9, Nrad = 559, Nbf = 5031), multipoles L = 0..4. The density is
+P = C C^T from 18 columns with entries drawn from N(0,1) (seed 12345),
+Loewdin-orthonormalised against the FEM overlap. One step = J(P) + K(P),
+plain FP64. P is 202 MB, larger than L2 (129 MB), so no L2 flush is needed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0). Under torchrun (N > 1) every rank runs an
+independent replica (atoms do not shard: replicas only) and the value is the
+whole-job throughput over the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Fock builds/s (J+K, plain FP64)"
+UNIT = "builds/s"
+WORKLOAD = ("Kr (Z=36) J+K Fock build: 40 elements r_i=61^(i/40)-1, 15-node LIP, l<=2, m<=2, "
+            "Nbf=5031, L<=4, P=CC^T (18 cols, N(0,1), seed 12345, Loewdin in S)")
+KERNELS_PER_STEP = 6  # j_contract, j_scatter, k_block_norms, k_offdiag, k_diag, k_fixup
+
+
+def kr_basis():
+    from oracle import tabulate as tab
+    bval = tab.get_grid(60.0, 40, 4, 1.0)
+    lval, mval = tab.angular_basis(2, 2)
+    return 36, bval, lval, mval
+
+
+def kr_density(S: np.ndarray, nocc: int = 18, seed: int = 12345) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    C = rng.standard_normal((S.shape[0], nocc))
+    M = C.T @ S @ C
+    w, v = np.linalg.eigh(M)
+    C = C @ (v @ np.diag(w ** -0.5) @ v.T)
+    return C @ C.T
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count() or 1
+
+
+# --------------------------------------------------------------------------
+# CPU side: the oracle (C++/OpenMP restatement of the reference's path)
+# --------------------------------------------------------------------------
+
+_CPU = {}
+
+
+def cpu_reference_builds(min_seconds: float, max_builds: int, min_builds: int = 1):
+    """Time full-size oracle J+K builds on the host cores; returns
+    (builds/s, builds, seconds, threads)."""
+    import oracle
+    from oracle import tabulate as tab
+    if not _CPU:
+        Z, bval, lval, mval = kr_basis()
+        A = tab.build_atom(Z, 15, bval, 2, 2)
+        _CPU["P"] = kr_density(A.S)
+        _CPU["F"] = oracle.FockOracle(A)
+        _CPU["F"].coulomb(_CPU["P"])  # warm-up (page-in, thread pool)
+    F, P = _CPU["F"], _CPU["P"]
+    n, t0 = 0, time.perf_counter()
+    while n < max_builds and (n < min_builds or time.perf_counter() - t0 < min_seconds):
+        F.coulomb(P)
+        F.exchange(P)
+        n += 1
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt, oracle.lib().ora_num_threads()
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        except OSError:
+            rows = []
+        finally:
+            try:
+                os.unlink(self.f.name)
+            except OSError:
+                pass
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def fp64_peak_tflops(torch) -> float:
+    """cuBLAS DGEMM throughput, the FP64 denominator (not among the
+    measured peaks)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of k_offdiag from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_offdiag_kr.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+# --------------------------------------------------------------------------
+
+def dist_setup(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+    rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, ws, local, dist
+
+
+def run_reference(args):
+    rank, ws, local, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    per_step = []
+    threads = None
+    for i in range(args.warmup + args.steps):
+        rate, n, dt, threads = cpu_reference_builds(0.0, 1, 1)
+        if i >= args.warmup:
+            per_step.append(dt / n)
+    mean = sum(per_step) / len(per_step)
+    val = 1.0 / mean
+    out = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "inputs_vs_l2": "host run (no GPU)"},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full-size Kr J+K builds, one per step"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    rank, ws, local, dist = dist_setup(args.gpus)
+    if dist is not None:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import helfem_gb300 as hg
+
+    Z, bval, lval, mval = kr_basis()
+    atom = hg.Atom(Z, bval, lval, mval, nnodes=15)
+    S = atom.overlap()
+    P = kr_density(S)
+    nbf = atom.nbf
+    Pd = torch.from_numpy(np.ascontiguousarray(P.T)).cuda()
+    Jd, Kd = torch.empty_like(Pd), torch.empty_like(Pd)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        atom.coulomb(Pd, Jd, stream)
+        atom.exchange(Pd, Kd, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    atom.profile_enable(KERNELS_PER_STEP * args.steps + 16)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+    ms = e0.elapsed_time(e1)
+    prof = atom.profile_read(reset=True)
+    atom.profile_enable(0)
+    clocks = clk.summary()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * args.steps / (ms * 1e-3)
+
+    # end to end through the host-pointer drop-ins (pinned host buffers)
+    def pinned():
+        return torch.empty((nbf, nbf), dtype=torch.float64, pin_memory=True).numpy().T
+    Ph, Jh, Kh = pinned(), pinned(), pinned()
+    Ph[...] = P
+    atom.coulomb_host(Ph, out=Jh)
+    atom.exchange_host(Ph, out=Kh)
+    ne = max(3, min(args.steps, 10))
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ne):
+        atom.coulomb_host(Ph, out=Jh)
+        atom.exchange_host(Ph, out=Kh)
+    te = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([te], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    e2e = {"value": ws * ne / te, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nbf * nbf,
+           "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
+           "path": "hfg_coulomb_host + hfg_exchange_host (pinned host P, J, K)"}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    work = atom.work()
+    n_off, ms_off = prof["k_offdiag"]
+    off_ms = ms_off / max(n_off, 1)
+    achieved = work["k_offdiag_flops"] / (off_ms * 1e-3) / 1e12
+    peak = fp64_peak_tflops(torch)
+    traffic = profiled_traffic()
+    hbm_peak = measured_peaks().get("hbm_gbs")
+    kernel_ms = {k: (v[1] / max(v[0], 1)) for k, v in prof.items()}
+    roofline = {
+        "bound": "fp64", "kernel": "k_offdiag", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        "frac": achieved / peak if peak else None,
+        "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (no FP64 figure in MEASURED_PEAKS.json)",
+        "flops_per_launch": work["k_offdiag_flops"], "ms_per_launch": off_ms,
+        "traffic": traffic,
+        "hbm": {"achieved_gbs": (work["k_bytes"] / 2) / (off_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
+                "note": "k_offdiag reads P once; HBM is not its bound"},
+        "kernel_ms_per_launch": kernel_ms,
+    }
+    cpu_rate, cpu_n, cpu_dt, cpu_threads = cpu_reference_builds(args.cpu_seconds, 1000)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nbf": nbf, "parallelism": f"replicas x{ws}",
+                   "inputs_vs_l2": "P is 202 MB > 129 MB L2: no flush needed"},
+        "roofline": roofline,
+        "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
+                         "sample": f"{cpu_n} full-size Kr J+K builds in {cpu_dt:.1f} s (oracle, OpenMP)"},
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": KERNELS_PER_STEP * args.steps,
+    }
+    print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,252 @@
+"""helfem_gb300: GB300 Fock-build engine for HelFEM's atomic finite-element basis.
+
+Python mirror of the C ABI in ``include/helfem_gb300.h`` (ctypes). The
+compute path is the in-tree CUDA library ``libhelfem_gb300.so``; there is no
+CPU fallback: importing this package without the built library raises.
+
+Reference interfaces mirrored (HelFEM project paths):
+  ``TwoDBasisT::coulomb / exchange / compute_tei``  src/atomic/TwoDBasis.h:180-227
+  ``TwoDBasisT::overlap / kinetic / nuclear``       src/atomic/TwoDBasis.h:201-207
+  ``atomic::basis::angular_basis``                  src/atomic/basis.cpp:179-203
+  ``grid::get_grid``                                libhelfem/include/grid.h:37-101
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libhelfem_gb300.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        f"{LIB_PATH} is missing: build the CUDA extension first "
+        "(python helfem_gb300/build.py or __graft_entry__.build())")
+
+_lib = ctypes.CDLL(LIB_PATH)
+
+HFG_OK, HFG_ERR_ARG, HFG_ERR_CUDA, HFG_ERR_STATE, HFG_ERR_NOMEM, HFG_ERR_INTERNAL = range(6)
+
+
+class HfgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"helfem_gb300 error {status}: {msg}")
+        self.status = status
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [("Z", ctypes.c_int), ("nnodes", ctypes.c_int), ("nquad", ctypes.c_int),
+                ("nelem", ctypes.c_int), ("bval", ctypes.POINTER(ctypes.c_double)),
+                ("nang", ctypes.c_int), ("lval", ctypes.POINTER(ctypes.c_int)),
+                ("mval", ctypes.POINTER(ctypes.c_int)), ("chol_tol", ctypes.c_double),
+                ("host_only", ctypes.c_int)]
+
+
+class _Dims(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("nrad", "nang", "nbf", "nelem", "nnodes", "NL", "rmax")]
+
+
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_SIGS = {
+    "hfg_last_error": ([], ctypes.c_char_p),
+    "hfg_grid": ([ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double, _D], ctypes.c_int),
+    "hfg_angular_basis": ([ctypes.c_int, ctypes.c_int, _I, _I, _I], ctypes.c_int),
+    "hfg_atom_create": ([ctypes.POINTER(_Desc), ctypes.POINTER(_P)], ctypes.c_int),
+    "hfg_atom_destroy": ([_P], ctypes.c_int),
+    "hfg_atom_get_dims": ([_P, ctypes.POINTER(_Dims)], ctypes.c_int),
+    "hfg_overlap": ([_P, _D], ctypes.c_int),
+    "hfg_kinetic": ([_P, _D], ctypes.c_int),
+    "hfg_nuclear": ([_P, _D], ctypes.c_int),
+    "hfg_atom_radial_tables": ([_P, ctypes.c_int, ctypes.c_int, _I, _D, _D, _I, _D], ctypes.c_int),
+    "hfg_gaunt": ([ctypes.c_int] * 5 + [_D], ctypes.c_int),
+    "hfg_coulomb": ([_P, _P, _P, _P], ctypes.c_int),
+    "hfg_coulomb_acc": ([_P, _P, _P, _P], ctypes.c_int),
+    "hfg_exchange": ([_P, _P, _P, _P], ctypes.c_int),
+    "hfg_coulomb_host": ([_P, _D, _D], ctypes.c_int),
+    "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
+    "hfg_atom_work": ([_P, _P], ctypes.c_int),
+    "hfg_profile_enable": ([_P, ctypes.c_int], ctypes.c_int),
+    "hfg_profile_read": ([_P, _P, ctypes.c_int], ctypes.c_int),
+}
+KERNEL_CLASSES = ("j_contract", "j_scatter", "k_block_norms", "k_offdiag", "k_diag", "k_fixup")
+
+
+
+
+class _Work(ctypes.Structure):
+    _fields_ = [("k_offdiag_flops", ctypes.c_double), ("k_diag_flops", ctypes.c_double),
+                ("k_bytes", ctypes.c_double), ("j_flops", ctypes.c_double), ("j_bytes", ctypes.c_double),
+                ("n_k_entries", ctypes.c_int), ("n_k_terms", ctypes.c_int)]
+
+
+class _Prof(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_int * 6), ("ms", ctypes.c_double * 6)]
+
+
+for _name, (_args, _res) in _SIGS.items():
+    _f = getattr(_lib, _name)
+    _f.argtypes = _args
+    _f.restype = _res
+
+
+def lib():
+    return _lib
+
+
+def _check(status: int):
+    if status != HFG_OK:
+        raise HfgError(status, _lib.hfg_last_error().decode())
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def get_grid(rmax: float, nelem: int, igrid: int = 4, zexp: float = 2.0) -> np.ndarray:
+    b = np.zeros(nelem + 1)
+    _check(_lib.hfg_grid(rmax, nelem, igrid, zexp, _dptr(b)))
+    return b
+
+
+def angular_basis(lmax: int, mmax: int):
+    n = ctypes.c_int()
+    _check(_lib.hfg_angular_basis(lmax, mmax, ctypes.byref(n), None, None))
+    lv = np.zeros(n.value, dtype=np.int32)
+    mv = np.zeros(n.value, dtype=np.int32)
+    _check(_lib.hfg_angular_basis(lmax, mmax, ctypes.byref(n), lv.ctypes.data_as(_I), mv.ctypes.data_as(_I)))
+    return lv, mv
+
+
+def gaunt(L: int, M: int, l: int, m: int, lp: int) -> float:
+    v = ctypes.c_double()
+    _check(_lib.hfg_gaunt(L, M, l, m, lp, ctypes.byref(v)))
+    return v.value
+
+
+def _ptr(x):
+    """Device pointer of a torch tensor (or an int address)."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous (column-major matrices: pass M.T.contiguous().T)")
+        return x.data_ptr()
+    raise TypeError("expected a torch CUDA tensor or a device address")
+
+
+def _stream(stream):
+    if stream is None:
+        try:
+            import torch
+            return torch.cuda.current_stream().cuda_stream
+        except Exception:  # pragma: no cover
+            return 0
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
+    return int(stream)
+
+
+class Atom:
+    """One atomic basis with its cached two-electron tables (host FP64) and
+    their device copies. Mirrors TwoDBasisT construction + compute_tei."""
+
+    def __init__(self, Z: int, bval, lval, mval, nnodes: int = 15, nquad: int = 0,
+                 chol_tol: float = 0.0, host_only: bool = False):
+        self.Z = int(Z)
+        self.bval = np.ascontiguousarray(bval, dtype=np.float64)
+        self.lval = np.ascontiguousarray(lval, dtype=np.int32)
+        self.mval = np.ascontiguousarray(mval, dtype=np.int32)
+        d = _Desc(self.Z, nnodes, nquad, len(self.bval) - 1, _dptr(self.bval), len(self.lval),
+                  self.lval.ctypes.data_as(_I), self.mval.ctypes.data_as(_I), chol_tol, int(host_only))
+        h = _P()
+        _check(_lib.hfg_atom_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        dims = _Dims()
+        _check(_lib.hfg_atom_get_dims(h, ctypes.byref(dims)))
+        for n, _ in _Dims._fields_:
+            setattr(self, n, getattr(dims, n))
+        self.nel = self.nelem
+
+    @classmethod
+    def from_grid(cls, Z, nelem, rmax, lmax, mmax, igrid=4, zexp=2.0, nnodes=15, **kw):
+        lv, mv = angular_basis(lmax, mmax)
+        return cls(Z, get_grid(rmax, nelem, igrid, zexp), lv, mv, nnodes=nnodes, **kw)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.hfg_atom_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- one-electron (host) ----
+    def _full(self, fn):
+        M = np.zeros((self.nbf, self.nbf), order="F")
+        _check(fn(self._h, _dptr(M)))
+        return M
+
+    def overlap(self):
+        return self._full(_lib.hfg_overlap)
+
+    def kinetic(self):
+        return self._full(_lib.hfg_kinetic)
+
+    def nuclear(self):
+        return self._full(_lib.hfg_nuclear)
+
+    def radial_tables(self, L: int, iel: int):
+        ni, rank = ctypes.c_int(), ctypes.c_int()
+        _check(_lib.hfg_atom_radial_tables(self._h, L, iel, ctypes.byref(ni), None, None, ctypes.byref(rank), None))
+        n = ni.value
+        rs = np.zeros((n, n), order="F")
+        rb = np.zeros((n, n), order="F")
+        ch = np.zeros((n * n, rank.value), order="F")
+        _check(_lib.hfg_atom_radial_tables(self._h, L, iel, None, _dptr(rs), _dptr(rb), None, _dptr(ch)))
+        return rs, rb, ch
+
+    # ---- hot path: device pointers ----
+    def coulomb(self, P, J, stream=None):
+        _check(_lib.hfg_coulomb(self._h, _ptr(P), _ptr(J), _stream(stream)))
+
+    def coulomb_acc(self, P, F, stream=None):
+        _check(_lib.hfg_coulomb_acc(self._h, _ptr(P), _ptr(F), _stream(stream)))
+
+    def exchange(self, P, K, stream=None):
+        _check(_lib.hfg_exchange(self._h, _ptr(P), _ptr(K), _stream(stream)))
+
+    def work(self) -> dict:
+        w = _Work()
+        _check(_lib.hfg_atom_work(self._h, ctypes.byref(w)))
+        return {n: getattr(w, n) for n, _ in _Work._fields_}
+
+    # ---- per-kernel timing ----
+    def profile_enable(self, capacity: int = 4096):
+        _check(_lib.hfg_profile_enable(self._h, capacity))
+
+    def profile_read(self, reset: bool = True) -> dict:
+        pr = _Prof()
+        _check(_lib.hfg_profile_read(self._h, ctypes.byref(pr), int(reset)))
+        return {n: (pr.launches[i], pr.ms[i]) for i, n in enumerate(KERNEL_CLASSES)}
+
+    # ---- hot path: host arrays (drop-in value semantics) ----
+    def coulomb_host(self, P: np.ndarray, out: np.ndarray = None) -> np.ndarray:
+        P = np.asfortranarray(P, dtype=np.float64)
+        J = np.zeros_like(P, order="F") if out is None else out
+        assert J.flags.f_contiguous and J.shape == P.shape
+        _check(_lib.hfg_coulomb_host(self._h, _dptr(P), _dptr(J)))
+        return J
+
+    def exchange_host(self, P: np.ndarray, out: np.ndarray = None) -> np.ndarray:
+        P = np.asfortranarray(P, dtype=np.float64)
+        K = np.zeros_like(P, order="F") if out is None else out
+        assert K.flags.f_contiguous and K.shape == P.shape
+        _check(_lib.hfg_exchange_host(self._h, _dptr(P), _dptr(K)))
+        return K

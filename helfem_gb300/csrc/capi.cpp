@@ -1,0 +1,459 @@
+// C ABI of the engine (declarations and contract in include/helfem_gb300.h).
+// Every entry point converts exceptions and CUDA errors into status codes and
+// a thread-local message; nothing throws across the boundary.
+#include "helfem_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cuda/devatom.cuh"
+#include "host/atom.hpp"
+
+namespace {
+
+thread_local std::string g_err;
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw CudaError(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+template <class F>
+hfg_status guard(F&& f) {
+  try {
+    f();
+    g_err.clear();
+    return HFG_OK;
+  } catch (const std::invalid_argument& e) {
+    g_err = e.what();
+    return HFG_ERR_ARG;
+  } catch (const CudaError& e) {
+    g_err = e.what();
+    return HFG_ERR_CUDA;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return HFG_ERR_NOMEM;
+  } catch (const std::logic_error& e) {
+    g_err = e.what();
+    return HFG_ERR_STATE;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return HFG_ERR_INTERNAL;
+  } catch (...) {
+    g_err = "unknown error";
+    return HFG_ERR_INTERNAL;
+  }
+}
+
+// RAII device allocation
+struct DBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { if (p) cudaFree(p); }
+  void alloc(size_t bytes) {
+    if (p) { cudaFree(p); p = nullptr; }
+    n = bytes;
+    if (bytes == 0) return;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
+    ck(e, "cudaMalloc");
+  }
+  template <class T>
+  T* upload(const std::vector<T>& v) {
+    alloc(std::max<size_t>(1, v.size()) * sizeof(T));
+    if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+    return static_cast<T*>(p);
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct hfg_atom {
+  hfg::AtomHost host;
+  int device = 0;
+  bool on_device = false;
+  cudaStream_t own_stream = nullptr;
+  hfg::DevAtom dev{};
+  hfg::DevScratch scr{};
+  // device copies of the tables
+  DBuf d_rs, d_rb, d_cholp, d_rank, d_tk, d_chanL, d_jket_ptr, d_jket_blk, d_jket_coef, d_jbra_ptr,
+      d_jbra_chan, d_jbra_coef, d_kjk_ptr, d_kent_L, d_kent_ptr, d_kterm_blk, d_kterm_coef;
+  DBuf s_jin, s_jscal, s_khalo, s_active;
+  // staging for the host-pointer entry points (allocated on first use)
+  DBuf h_in, h_out;
+  hfg::Profiler prof;
+  std::vector<cudaEvent_t> prof_ev;
+  std::vector<int> prof_cls;
+
+  ~hfg_atom() {
+    free_profiler();
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+
+  void free_profiler() {
+    for (cudaEvent_t e : prof_ev) cudaEventDestroy(e);
+    prof_ev.clear();
+    prof_cls.clear();
+    prof = hfg::Profiler();
+  }
+
+  void enable_profiler(int cap) {
+    free_profiler();
+    if (cap <= 0) return;
+    prof_ev.resize(2 * (size_t)cap);
+    for (auto& e : prof_ev) ck(cudaEventCreate(&e), "cudaEventCreate");
+    prof_cls.assign(cap, 0);
+    prof.ev = prof_ev.data();
+    prof.cls = prof_cls.data();
+    prof.cap = cap;
+    prof.n = 0;
+    prof.on = true;
+  }
+
+  void check_device() const {
+    if (!on_device) throw std::logic_error("handle was created host-only; device entry points are unavailable");
+    int d = -1;
+    ck(cudaGetDevice(&d), "cudaGetDevice");
+    if (d != device) throw std::invalid_argument("handle used on a different CUDA device than it was created on");
+  }
+
+  void upload() {
+    using namespace hfg;
+    const AtomHost& H = host;
+    ck(cudaGetDevice(&device), "cudaGetDevice");
+    ck(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    DevAtom& A = dev;
+    A.nn = H.rad.nn;
+    A.nel = H.rad.nel;
+    A.nrad = H.rad.nrad;
+    A.nang = H.nang;
+    A.nbf = H.nbf;
+    A.NL = H.NL;
+    A.rmax = H.rmax;
+    A.rs = d_rs.upload(H.rs);
+    A.rb = d_rb.upload(H.rb);
+    A.cholp = d_cholp.upload(H.cholp);
+    A.rank = d_rank.upload(H.chol_rank);
+    A.tk = d_tk.upload(H.tk);
+    std::vector<int> chanL;
+    for (auto& c : H.chans) chanL.push_back(c.L);
+    A.nchan = (int)H.chans.size();
+    A.chanL = d_chanL.upload(chanL);
+    A.jket_ptr = d_jket_ptr.upload(H.jket_ptr);
+    A.jket_blk = d_jket_blk.upload(H.jket_blk);
+    A.jket_coef = d_jket_coef.upload(H.jket_coef);
+    A.jbra_ptr = d_jbra_ptr.upload(H.jbra_ptr);
+    A.jbra_chan = d_jbra_chan.upload(H.jbra_chan);
+    A.jbra_coef = d_jbra_coef.upload(H.jbra_coef);
+    A.kjk_ptr = d_kjk_ptr.upload(H.kjk_ptr);
+    A.kent_L = d_kent_L.upload(H.kent_L);
+    A.kent_ptr = d_kent_ptr.upload(H.kent_ptr);
+    A.kterm_blk = d_kterm_blk.upload(H.kterm_blk);
+    A.kterm_coef = d_kterm_coef.upload(H.kterm_coef);
+    int mx = 0;
+    for (int jk = 0; jk < H.nang * H.nang; ++jk) {
+      int n = 0;
+      for (int e = H.kjk_ptr[jk]; e < H.kjk_ptr[jk + 1]; ++e) n += H.kent_ptr[e + 1] - H.kent_ptr[e];
+      mx = std::max(mx, n);
+    }
+    A.max_terms_per_jk = mx;
+    for (int ij = 0; ij < H.nang * H.nang; ++ij)
+      if (H.jbra_ptr[ij + 1] - H.jbra_ptr[ij] > 64) throw std::invalid_argument("too many Coulomb bra terms");
+    const size_t n2 = (size_t)A.nn * A.nn;
+    s_jin.alloc(sizeof(double) * A.nchan * A.nel * n2);
+    s_jscal.alloc(sizeof(double) * A.nchan * A.nel * 2);
+    s_khalo.alloc(sizeof(double) * (size_t)A.nel * A.nel * A.nang * A.nang * (2 * A.nn - 1));
+    s_active.alloc((size_t)A.nang * A.nang);
+    scr.jin = s_jin.as<double>();
+    scr.jscal = s_jscal.as<double>();
+    scr.khalo = s_khalo.as<double>();
+    scr.active = s_active.as<unsigned char>();
+    on_device = true;
+  }
+
+  void staging() {
+    const size_t bytes = sizeof(double) * (size_t)host.nbf * host.nbf;
+    if (h_in.n != bytes) h_in.alloc(bytes);
+    if (h_out.n != bytes) h_out.alloc(bytes);
+  }
+};
+
+namespace {
+
+void need(bool c, const char* msg) {
+  if (!c) throw std::invalid_argument(msg);
+}
+
+void write_full(const hfg_atom* a, const std::vector<double>& rad, double scale, const std::vector<double>* lrad,
+                double* out) {
+  const int nr = a->host.rad.nrad, nb = a->host.nbf;
+  std::memset(out, 0, sizeof(double) * (size_t)nb * nb);
+  for (int ia = 0; ia < a->host.nang; ++ia) {
+    const double lf = lrad ? (double)a->host.lval[ia] * (a->host.lval[ia] + 1) : 0.0;
+    for (int c = 0; c < nr; ++c)
+      for (int r = 0; r < nr; ++r) {
+        double v = scale * rad[r + (size_t)c * nr];
+        if (lrad) v += lf * (*lrad)[r + (size_t)c * nr];
+        out[(size_t)(ia * nr + c) * nb + ia * nr + r] = v;
+      }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hfg_last_error(void) { return g_err.c_str(); }
+
+hfg_status hfg_grid(double rmax, int nelem, int igrid, double zexp, double* bval) {
+  return guard([&] {
+    need(bval != nullptr && nelem >= 1 && rmax > 0, "hfg_grid: bad arguments");
+    std::vector<double> b(nelem + 1);
+    switch (igrid) {
+      case 1:
+        for (int i = 0; i <= nelem; ++i) b[i] = (i == nelem) ? rmax : i * (rmax / nelem);
+        break;
+      case 2:
+        for (int i = 0; i <= nelem; ++i) b[i] = (double)i * i * rmax / ((double)nelem * nelem);
+        break;
+      case 3:
+        for (int i = 0; i <= nelem; ++i) b[i] = rmax * std::pow((double)i / nelem, zexp);
+        break;
+      case 4: {
+        const double up = std::pow(std::log(rmax + 1.0), 1.0 / zexp);
+        const double step = up / nelem;
+        for (int i = 0; i <= nelem; ++i) {
+          const double t = (i == nelem) ? up : i * step;
+          b[i] = std::exp(std::pow(t, zexp)) - 1.0;
+        }
+        break;
+      }
+      case 5: {
+        need(zexp > 0 && zexp < 1, "hfg_grid: geometric grid needs 0 < zexp < 1");
+        std::vector<double> hk(nelem);
+        hk[nelem - 1] = (1 - zexp) / (1 - std::pow(zexp, nelem)) * rmax;
+        for (int i = nelem - 2; i >= 0; --i) hk[i] = zexp * hk[i + 1];
+        b[0] = 0;
+        for (int i = 0; i < nelem; ++i) b[i + 1] = b[i] + hk[i];
+        break;
+      }
+      default:
+        throw std::invalid_argument("hfg_grid: unknown grid type");
+    }
+    b[0] = 0.0;
+    b[nelem] = rmax;
+    std::memcpy(bval, b.data(), sizeof(double) * (nelem + 1));
+  });
+}
+
+hfg_status hfg_angular_basis(int lmax, int mmax, int* nang, int* lval, int* mval) {
+  return guard([&] {
+    need(nang != nullptr && lmax >= 0 && mmax >= 0, "hfg_angular_basis: bad arguments");
+    int n = 0;
+    for (int mabs = 0; mabs <= mmax; ++mabs)
+      for (int l = mabs; l <= lmax; ++l) {
+        if (lval) { lval[n] = l; mval[n] = mabs; }
+        ++n;
+        if (mabs > 0) {
+          if (lval) { lval[n] = l; mval[n] = -mabs; }
+          ++n;
+        }
+      }
+    *nang = n;
+  });
+}
+
+hfg_status hfg_atom_create(const hfg_atom_desc* d, hfg_atom** out) {
+  return guard([&] {
+    need(d != nullptr && out != nullptr, "hfg_atom_create: null argument");
+    need(d->nnodes >= 3 && d->nnodes <= 17, "hfg_atom_create: nnodes must be in 3..17");
+    need(d->nelem >= 2, "hfg_atom_create: need at least two elements");
+    need(d->bval && d->lval && d->mval && d->nang >= 1, "hfg_atom_create: missing arrays");
+    std::vector<double> bval(d->bval, d->bval + d->nelem + 1);
+    std::vector<int> lv(d->lval, d->lval + d->nang), mv(d->mval, d->mval + d->nang);
+    for (int l : lv) need(l <= 3, "hfg_atom_create: l <= 3 supported");
+    std::unique_ptr<hfg_atom> a(new hfg_atom());
+    a->host.build(d->Z, d->nnodes, bval, lv, mv, d->nquad, d->chol_tol);
+    if (!d->host_only) a->upload();
+    *out = a.release();
+  });
+}
+
+hfg_status hfg_atom_destroy(hfg_atom* atom) {
+  return guard([&] { delete atom; });
+}
+
+hfg_status hfg_atom_get_dims(const hfg_atom* a, hfg_atom_dims_t* d) {
+  return guard([&] {
+    need(a && d, "hfg_atom_get_dims: null argument");
+    d->nrad = a->host.rad.nrad;
+    d->nang = a->host.nang;
+    d->nbf = a->host.nbf;
+    d->nelem = a->host.rad.nel;
+    d->nnodes = a->host.rad.nn;
+    d->NL = a->host.NL;
+    d->rmax = a->host.rmax;
+  });
+}
+
+hfg_status hfg_overlap(const hfg_atom* a, double* S) {
+  return guard([&] { need(a && S, "null argument"); write_full(a, a->host.Srad, 1.0, nullptr, S); });
+}
+
+hfg_status hfg_kinetic(const hfg_atom* a, double* T) {
+  return guard([&] { need(a && T, "null argument"); write_full(a, a->host.Trad, 1.0, &a->host.Tlrad, T); });
+}
+
+hfg_status hfg_nuclear(const hfg_atom* a, double* V) {
+  return guard([&] { need(a && V, "null argument"); write_full(a, a->host.Vrad, -(double)a->host.Z, nullptr, V); });
+}
+
+hfg_status hfg_atom_radial_tables(const hfg_atom* a, int L, int iel, int* ni, double* rsmall, double* rbig,
+                                  int* rank, double* chol) {
+  return guard([&] {
+    need(a != nullptr, "null handle");
+    const hfg::AtomHost& H = a->host;
+    need(L >= 0 && L < H.NL && iel >= 0 && iel < H.rad.nel, "L or iel out of range");
+    const int nn = H.rad.nn, p0 = H.rad.pfirst(iel), n = H.rad.nfun(iel);
+    const size_t le = (size_t)L * H.rad.nel + iel;
+    if (ni) *ni = n;
+    for (int b = 0; b < n; ++b)
+      for (int c = 0; c < n; ++c) {
+        if (rsmall) rsmall[c + (size_t)b * n] = H.rs[le * nn * nn + (c + p0) + (size_t)(b + p0) * nn];
+        if (rbig) rbig[c + (size_t)b * n] = H.rb[le * nn * nn + (c + p0) + (size_t)(b + p0) * nn];
+      }
+    if (rank) *rank = H.chol_rank[le];
+    if (chol) std::memcpy(chol, H.chol[le].data(), sizeof(double) * H.chol[le].size());
+  });
+}
+
+hfg_status hfg_gaunt(int L, int M, int l, int m, int lp, double* value) {
+  return guard([&] { need(value != nullptr, "null argument"); *value = hfg::gaunt_coeff(L, M, l, m, lp); });
+}
+
+hfg_status hfg_coulomb(hfg_atom* a, const double* P, double* J, void* stream) {
+  return guard([&] {
+    need(a && P && J, "hfg_coulomb: null argument");
+    a->check_device();
+    ck(hfg::launch_coulomb_fp64(a->dev, a->scr, P, J, true, (cudaStream_t)stream, &a->prof), "coulomb kernels");
+  });
+}
+
+hfg_status hfg_coulomb_acc(hfg_atom* a, const double* P, double* F, void* stream) {
+  return guard([&] {
+    need(a && P && F, "hfg_coulomb_acc: null argument");
+    a->check_device();
+    ck(hfg::launch_coulomb_fp64(a->dev, a->scr, P, F, false, (cudaStream_t)stream, &a->prof), "coulomb kernels");
+  });
+}
+
+hfg_status hfg_exchange(hfg_atom* a, const double* P, double* K, void* stream) {
+  return guard([&] {
+    need(a && P && K, "hfg_exchange: null argument");
+    a->check_device();
+    ck(hfg::launch_exchange_fp64(a->dev, a->scr, P, K, (cudaStream_t)stream, &a->prof), "exchange kernels");
+  });
+}
+
+static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb) {
+  need(a && P && out, "null argument");
+  a->check_device();
+  a->staging();
+  const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
+  cudaStream_t st = a->own_stream;
+  ck(cudaMemcpyAsync(a->h_in.p, P, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+  if (coulomb)
+    ck(hfg::launch_coulomb_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof), "coulomb");
+  else
+    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), st, &a->prof), "exchange");
+  ck(cudaMemcpyAsync(out, a->h_out.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
+  ck(cudaStreamSynchronize(st), "stream sync");
+}
+
+hfg_status hfg_coulomb_host(hfg_atom* a, const double* P, double* J) {
+  return guard([&] { host_call(a, P, J, true); });
+}
+
+hfg_status hfg_exchange_host(hfg_atom* a, const double* P, double* K) {
+  return guard([&] { host_call(a, P, K, false); });
+}
+
+hfg_status hfg_atom_work(const hfg_atom* a, hfg_work_t* w) {
+  return guard([&] {
+    need(a != nullptr && w != nullptr, "hfg_atom_work: null argument");
+    const hfg::AtomHost& H = a->host;
+    const int nel = H.rad.nel;
+    std::vector<double> N(nel);
+    double S2 = 0.0;
+    for (int e = 0; e < nel; ++e) { N[e] = H.rad.nfun(e); S2 += N[e] * N[e]; }
+    double off_pair = 0.0, off_prod = 0.0, diag_pair = 0.0, diag_prod = 0.0;
+    for (int x = 0; x < nel; ++x)
+      for (int y = 0; y < nel; ++y) {
+        if (x == y) {
+          diag_pair += N[x] * N[x];
+          diag_prod += 2.0 * N[x] * N[x] * N[x] * N[x];
+        } else {
+          off_pair += N[x] * N[y];
+          off_prod += 2.0 * N[x] * N[x] * N[y] + 2.0 * N[x] * N[y] * N[y];
+        }
+      }
+    const double nent = (double)H.kent_L.size(), nterm = (double)H.kterm_blk.size();
+    w->n_k_entries = (int)H.kent_L.size();
+    w->n_k_terms = (int)H.kterm_blk.size();
+    w->k_offdiag_flops = nent * off_prod + 2.0 * nterm * off_pair;
+    w->k_diag_flops = nent * diag_prod + 2.0 * nterm * diag_pair;
+    w->k_bytes = 16.0 * (double)H.nbf * H.nbf;
+    double jf = 0.0;
+    for (size_t ch = 0; ch < H.chans.size(); ++ch) {
+      const double nket = H.jket_ptr[ch + 1] - H.jket_ptr[ch];
+      const int L = H.chans[ch].L;
+      for (int e = 0; e < nel; ++e)
+        jf += 2.0 * nket * N[e] * N[e] + 4.0 * N[e] * N[e] + 4.0 * N[e] * N[e] * H.chol_rank[(size_t)L * nel + e];
+    }
+    jf += 6.0 * (double)H.jbra_chan.size() * S2;
+    w->j_flops = jf;
+    w->j_bytes = 16.0 * (double)H.nang * H.nang * S2;
+  });
+}
+
+hfg_status hfg_profile_enable(hfg_atom* a, int capacity) {
+  return guard([&] {
+    need(a != nullptr && capacity >= 0, "hfg_profile_enable: bad arguments");
+    a->check_device();
+    a->enable_profiler(capacity);
+  });
+}
+
+hfg_status hfg_profile_read(hfg_atom* a, hfg_profile_t* out, int reset) {
+  return guard([&] {
+    need(a != nullptr && out != nullptr, "hfg_profile_read: null argument");
+    std::memset(out, 0, sizeof(*out));
+    for (int i = 0; i < a->prof.n; ++i) {
+      ck(cudaEventSynchronize(a->prof.ev[2 * i + 1]), "cudaEventSynchronize");
+      float ms = 0.f;
+      ck(cudaEventElapsedTime(&ms, a->prof.ev[2 * i], a->prof.ev[2 * i + 1]), "cudaEventElapsedTime");
+      const int k = a->prof.cls[i];
+      out->launches[k] += 1;
+      out->ms[k] += ms;
+    }
+    if (reset) a->prof.n = 0;
+  });
+}
+
+}  // extern "C"

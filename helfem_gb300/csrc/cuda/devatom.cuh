@@ -1,0 +1,66 @@
+// Device-resident atom context shared by the Fock-build kernels.
+//
+// Radial layout: element e owns an nn x nn primitive tile; primitive p is the
+// global radial function g(e,p) = e*(nn-1) + p - 1, valid for 0 <= g < nrad.
+// AO index = iang*nrad + irad; matrices are column-major FP64 (nbf x nbf).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace hfg {
+
+struct DevAtom {
+  int nn, nel, nrad, nang, nbf, NL, rmax;
+  // per (L,e) padded tiles
+  const double* rs;     // [(L*nel+e)*nn*nn]
+  const double* rb;     // [(L*nel+e)*nn*nn] (zero for e = 0)
+  const double* cholp;  // [(L*nel+e)*nn*nn*rmax]
+  const int* rank;      // [L*nel+e]
+  const double* tk;     // [(L*nel+e)*(nn*nn)^2] exchange-ordered in-element tensor
+  // Coulomb coupling lists
+  int nchan;
+  const int* chanL;     // [nchan]
+  const int* jket_ptr;  // [nchan+1]
+  const int* jket_blk;
+  const double* jket_coef;
+  const int* jbra_ptr;  // [nang*nang+1]
+  const int* jbra_chan;
+  const double* jbra_coef;
+  // exchange recoupling lists
+  const int* kjk_ptr;   // [nang*nang+1] -> entries
+  const int* kent_L;
+  const int* kent_ptr;  // [nent+1] -> terms
+  const int* kterm_blk;
+  const double* kterm_coef;
+  int max_terms_per_jk; // bound on terms of one output block
+};
+
+// Scratch owned by the atom handle (sizes fixed at creation)
+struct DevScratch {
+  double* jin;          // [nchan*nel*nn*nn]
+  double* jscal;        // [nchan*nel*2]
+  double* khalo;        // [nel*nel*nang*nang*(2nn-1)]
+  unsigned char* active;// [nang*nang]
+};
+
+__host__ __device__ inline int gfun(const DevAtom& A, int e, int p) { return e * (A.nn - 1) + p - 1; }
+
+// Optional per-kernel timing (the engine's counterpart of the reference's
+// FockTimer): when enabled, every kernel launch is bracketed by a pair of
+// pre-created events on its stream; records are read back after the work.
+enum KernelClass { KC_J_CONTRACT = 0, KC_J_SCATTER, KC_K_NORMS, KC_K_OFFDIAG, KC_K_DIAG, KC_K_FIXUP, KC_COUNT };
+struct Profiler {
+  bool on = false;
+  int cap = 0, n = 0;
+  cudaEvent_t* ev = nullptr;  // [2*cap]
+  int* cls = nullptr;         // [cap]
+};
+
+// launchers (jk_fp64.cu)
+cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* J,
+                                bool zero_output, cudaStream_t st, Profiler* prof = nullptr);
+cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* K,
+                                 cudaStream_t st, Profiler* prof = nullptr);
+
+}  // namespace hfg

@@ -1,0 +1,384 @@
+// Plain-FP64 Coulomb (J) and exchange (K) builds for the atomic FE basis.
+//
+// J restates TwoDBasisT::coulomb (src/atomic/TwoDBasis.cpp:773-877) with the
+// per-multipole FE assembly of assemble_J_FE_one_multipole_cached_chol
+// (libhelfemqc/include/CoulombExchangeFE.h:432-482):
+//   j_contract : per (L,M) channel and element, the Gaunt-weighted ket
+//                contraction restricted to the element-diagonal tile (the only
+//                part of Paux the assembly reads), the two disjoint traces
+//                and the in-element Cholesky contraction L (L^T vec P).
+//   j_scatter  : per output angular block and element, the O(Nel) prefix
+//                sums of the disjoint traces (the reference's O(Nel^2) double
+//                loop) and the Gaunt-weighted bra scatter.
+// K restates TwoDBasisT::exchange (TwoDBasis.cpp:879-999) with
+// assemble_K_FE_one_multipole_cached_chol (CoulombExchangeFE.h:484-530):
+//   k_block_norms : density-block screening, ||P_il||_F < 10 eps skipped.
+//   k_offdiag     : one CTA per element pair (a != b) for every output angular
+//                   block: recouple the (a,b) tiles of P, then A_L X B_L^T
+//                   with A/B = r_small/r_big by element order.
+//   k_diag        : diagonal element tiles through the exchange-ordered
+//                   in-element tensor (equal to sum_p M_p X M_p^T).
+//   k_fixup       : adds the contributions of neighbouring tiles on the
+//                   shared boundary functions, in a fixed order (no atomics,
+//                   bitwise reproducible).
+#include <cfloat>
+
+#include "devatom.cuh"
+
+namespace hfg {
+namespace {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-wide sum, result valid in every thread; red needs >= 32 doubles
+__device__ double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < nw; ++i) s += red[i];
+  return s;
+}
+
+__device__ __forceinline__ bool gvalid(const DevAtom& A, int g) { return g >= 0 && g < A.nrad; }
+
+// ------------------------------------------------------------------ Coulomb
+__global__ void j_contract(DevAtom A, DevScratch S, const double* __restrict__ P) {
+  const int ch = blockIdx.x, e = blockIdx.y;
+  const int nn = A.nn, n2 = nn * nn, L = A.chanL[ch];
+  extern __shared__ double sm[];
+  double* X = sm;
+  double* sc = X + n2;
+  double* red = sc + A.rmax;
+  const int k0 = A.jket_ptr[ch], k1 = A.jket_ptr[ch + 1];
+  for (int idx = threadIdx.x; idx < n2; idx += blockDim.x) {
+    const int p = idx % nn, q = idx / nn;
+    const int gp = gfun(A, e, p), gq = gfun(A, e, q);
+    double x = 0.0;
+    if (gvalid(A, gp) && gvalid(A, gq))
+      for (int u = k0; u < k1; ++u) {
+        const int blk = A.jket_blk[u], k = blk % A.nang, l = blk / A.nang;
+        x += A.jket_coef[u] * P[(size_t)(l * A.nrad + gq) * A.nbf + (size_t)k * A.nrad + gp];
+      }
+    X[idx] = x;
+  }
+  __syncthreads();
+  const size_t le = (size_t)L * A.nel + e;
+  const double* rs = A.rs + le * n2;
+  const double* rb = A.rb + le * n2;
+  double ts = 0.0, tb = 0.0;
+  for (int idx = threadIdx.x; idx < n2; idx += blockDim.x) {
+    const int p = idx % nn, q = idx / nn;
+    const double xt = X[q + p * nn];
+    ts += rs[idx] * xt;
+    tb += rb[idx] * xt;
+  }
+  ts = block_sum(ts, red);
+  tb = block_sum(tb, red);
+  if (threadIdx.x == 0) {
+    S.jscal[((size_t)ch * A.nel + e) * 2 + 0] = ts;
+    S.jscal[((size_t)ch * A.nel + e) * 2 + 1] = tb;
+  }
+  const int r = A.rank[le];
+  const double* C = A.cholp + le * n2 * A.rmax;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int j = w; j < r; j += nw) {
+    double s = 0.0;
+    for (int q = lane; q < n2; q += 32) s += C[q + (size_t)j * n2] * X[q];
+    s = warp_sum(s);
+    if (lane == 0) sc[j] = s;
+  }
+  __syncthreads();
+  double* jin = S.jin + ((size_t)ch * A.nel + e) * n2;
+  for (int idx = threadIdx.x; idx < n2; idx += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < r; ++j) s += C[idx + (size_t)j * n2] * sc[j];
+    jin[idx] = s;
+  }
+}
+
+constexpr int JMAXTERMS = 64;
+
+__global__ void j_scatter(DevAtom A, DevScratch S, double* __restrict__ J, int accumulate) {
+  const int ij = blockIdx.x, e = blockIdx.y;
+  const int i = ij % A.nang, j = ij / A.nang;
+  const int b0 = A.jbra_ptr[ij], b1 = A.jbra_ptr[ij + 1];
+  const int nt = b1 - b0;
+  if (nt == 0) return;
+  const int nn = A.nn, n2 = nn * nn;
+  __shared__ double Ab[JMAXTERMS], As[JMAXTERMS], Ab1[JMAXTERMS], As1[JMAXTERMS];
+  for (int u = threadIdx.x; u < nt; u += blockDim.x) {
+    const int ch = A.jbra_chan[b0 + u];
+    const double* sc = S.jscal + (size_t)ch * A.nel * 2;
+    double big = 0.0, small = 0.0;
+    for (int e2 = e + 1; e2 < A.nel; ++e2) big += sc[2 * e2 + 1];
+    for (int e2 = 0; e2 < e; ++e2) small += sc[2 * e2 + 0];
+    Ab[u] = big;
+    As[u] = small;
+    if (e > 0) {
+      Ab1[u] = big + sc[2 * e + 1];
+      As1[u] = small - sc[2 * (e - 1) + 0];
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < n2; idx += blockDim.x) {
+    const int p = idx % nn, q = idx / nn;
+    // J has element-diagonal tiles only: the single entry two tiles share is
+    // the corner on the common boundary function, owned by the later tile
+    if (p == nn - 1 && q == nn - 1) continue;
+    const int gp = gfun(A, e, p), gq = gfun(A, e, q);
+    if (!gvalid(A, gp) || !gvalid(A, gq)) continue;
+    double v = 0.0;
+    for (int u = 0; u < nt; ++u) {
+      const int ch = A.jbra_chan[b0 + u], L = A.chanL[ch];
+      const size_t le = (size_t)L * A.nel + e;
+      const double* jin = S.jin + ((size_t)ch * A.nel + e) * n2;
+      v += A.jbra_coef[b0 + u] * (Ab[u] * A.rs[le * n2 + idx] + As[u] * A.rb[le * n2 + idx] + jin[idx]);
+    }
+    if (p == 0 && q == 0 && e > 0) {
+      const int c = (nn - 1) + (nn - 1) * nn;
+      for (int u = 0; u < nt; ++u) {
+        const int ch = A.jbra_chan[b0 + u], L = A.chanL[ch];
+        const size_t le = (size_t)L * A.nel + (e - 1);
+        const double* jin = S.jin + ((size_t)ch * A.nel + (e - 1)) * n2;
+        v += A.jbra_coef[b0 + u] * (Ab1[u] * A.rs[le * n2 + c] + As1[u] * A.rb[le * n2 + c] + jin[c]);
+      }
+    }
+    double* out = J + (size_t)(j * A.nrad + gq) * A.nbf + (size_t)i * A.nrad + gp;
+    if (accumulate) *out += v; else *out = v;
+  }
+}
+
+// ----------------------------------------------------------------- exchange
+__global__ void k_block_norms(DevAtom A, const double* __restrict__ P, unsigned char* active) {
+  __shared__ double red[32];
+  const int blk = blockIdx.x, i = blk % A.nang, l = blk / A.nang;
+  double s = 0.0;
+  const size_t n = (size_t)A.nrad * A.nrad;
+  for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    const size_t r = idx % A.nrad, c = idx / A.nrad;
+    const double v = P[(size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r];
+    s += v * v;
+  }
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) active[blk] = !(sqrt(s) < 10.0 * DBL_EPSILON);
+}
+
+__device__ __forceinline__ size_t halo_idx(const DevAtom& A, int a, int b, int jk, int h) {
+  return ((size_t)(a * A.nel + b) * (A.nang * A.nang) + jk) * (2 * A.nn - 1) + h;
+}
+
+// store the finished contribution y of tile (a,b), angular block jk
+__device__ __forceinline__ void k_store(const DevAtom& A, const DevScratch& S, double* K, int a, int b,
+                                        int jk, int p, int q, double y) {
+  const int nn = A.nn;
+  const int gp = gfun(A, a, p), gq = gfun(A, b, q);
+  if (!gvalid(A, gp) || !gvalid(A, gq)) return;
+  const int j = jk % A.nang, k = jk / A.nang;
+  if (p <= nn - 2 && q <= nn - 2)
+    K[(size_t)(k * A.nrad + gq) * A.nbf + (size_t)j * A.nrad + gp] = y;
+  else if (p == nn - 1)
+    S.khalo[halo_idx(A, a, b, jk, q)] = y;
+  else
+    S.khalo[halo_idx(A, a, b, jk, nn + p)] = y;
+}
+
+// recoupled tile value for thread (p,q) of element pair (a,b), entry ent
+__device__ __forceinline__ double k_recouple(const DevAtom& A, const double* __restrict__ P,
+                                             const unsigned char* act, int ent, int gp, int gq) {
+  double x = 0.0;
+  const int u0 = A.kent_ptr[ent], u1 = A.kent_ptr[ent + 1];
+  for (int u = u0; u < u1; ++u) {
+    const int blk = A.kterm_blk[u];
+    if (!act[blk]) continue;
+    const int i = blk % A.nang, l = blk / A.nang;
+    x += A.kterm_coef[u] * P[(size_t)(l * A.nrad + gq) * A.nbf + (size_t)i * A.nrad + gp];
+  }
+  return x;
+}
+
+__device__ __forceinline__ bool k_entry_active(const DevAtom& A, const unsigned char* act, int ent) {
+  for (int u = A.kent_ptr[ent]; u < A.kent_ptr[ent + 1]; ++u)
+    if (act[A.kterm_blk[u]]) return true;
+  return false;
+}
+
+__global__ void k_offdiag(DevAtom A, DevScratch S, const double* __restrict__ P, double* __restrict__ K) {
+  const int a = blockIdx.x % A.nel, b = blockIdx.x / A.nel;
+  if (a == b) return;
+  const int nn = A.nn, n2 = nn * nn, NL = A.NL, nang2 = A.nang * A.nang;
+  extern __shared__ double sm[];
+  double* Am = sm;
+  double* Bm = Am + NL * n2;
+  double* X = Bm + NL * n2;
+  double* T = X + n2;
+  unsigned char* act = reinterpret_cast<unsigned char*>(T + n2);
+  const double* srcA = (a < b) ? A.rs : A.rb;
+  const double* srcB = (a < b) ? A.rb : A.rs;
+  for (int idx = threadIdx.x; idx < NL * n2; idx += blockDim.x) {
+    const int L = idx / n2, o = idx % n2;
+    Am[idx] = srcA[((size_t)L * A.nel + a) * n2 + o];
+    Bm[idx] = srcB[((size_t)L * A.nel + b) * n2 + o];
+  }
+  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.active[idx];
+  __syncthreads();
+  const int t = threadIdx.x;
+  const bool live = t < n2;
+  const int p = live ? t % nn : 0, q = live ? t / nn : 0;
+  const int gp = gfun(A, a, p), gq = gfun(A, b, q);
+  const bool vpq = live && gvalid(A, gp) && gvalid(A, gq);
+  for (int jk = 0; jk < nang2; ++jk) {
+    double y = 0.0;
+    for (int ent = A.kjk_ptr[jk]; ent < A.kjk_ptr[jk + 1]; ++ent) {
+      if (!k_entry_active(A, act, ent)) continue;  // uniform over the CTA
+      const int L = A.kent_L[ent];
+      if (live) X[t] = vpq ? k_recouple(A, P, act, ent, gp, gq) : 0.0;
+      __syncthreads();
+      if (live) {
+        const double* Bl = Bm + L * n2;
+        double s = 0.0;
+        for (int c = 0; c < nn; ++c) s += X[p + c * nn] * Bl[q + c * nn];
+        T[t] = s;
+      }
+      __syncthreads();
+      if (live) {
+        const double* Al = Am + L * n2;
+        double s = 0.0;
+        for (int c = 0; c < nn; ++c) s += Al[p + c * nn] * T[c + q * nn];
+        y += s;
+      }
+      __syncthreads();
+    }
+    if (live) k_store(A, S, K, a, b, jk, p, q, -y);
+  }
+}
+
+__global__ void k_diag(DevAtom A, DevScratch S, const double* __restrict__ P, double* __restrict__ K) {
+  const int a = blockIdx.x, jk = blockIdx.y;
+  const int nn = A.nn, n2 = nn * nn, nang2 = A.nang * A.nang;
+  extern __shared__ double sm[];
+  double* X = sm;
+  unsigned char* act = reinterpret_cast<unsigned char*>(X + n2);
+  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.active[idx];
+  __syncthreads();
+  const int t = threadIdx.x;
+  const bool live = t < n2;
+  const int p = live ? t % nn : 0, q = live ? t / nn : 0;
+  const int gp = gfun(A, a, p), gq = gfun(A, a, q);
+  const bool vpq = live && gvalid(A, gp) && gvalid(A, gq);
+  double y = 0.0;
+  for (int ent = A.kjk_ptr[jk]; ent < A.kjk_ptr[jk + 1]; ++ent) {
+    if (!k_entry_active(A, act, ent)) continue;
+    const int L = A.kent_L[ent];
+    if (live) X[t] = vpq ? k_recouple(A, P, act, ent, gp, gq) : 0.0;
+    __syncthreads();
+    if (live) {
+      const double* Tk = A.tk + ((size_t)L * A.nel + a) * n2 * n2;
+      double s = 0.0;
+      for (int u = 0; u < n2; ++u) s += Tk[t + (size_t)u * n2] * X[u];
+      y += s;
+    }
+    __syncthreads();
+  }
+  if (live) k_store(A, S, K, a, a, jk, p, q, -y);
+}
+
+__global__ void k_fixup(DevAtom A, DevScratch S, double* __restrict__ K) {
+  const int a = blockIdx.x % A.nel, b = blockIdx.x / A.nel, jk = blockIdx.y;
+  const int nn = A.nn;
+  const int j = jk % A.nang, k = jk / A.nang;
+  for (int idx = threadIdx.x; idx < 2 * nn - 3; idx += blockDim.x) {
+    int p, q;
+    double v;
+    if (idx < nn - 1) {  // first row of tile (a,b), q in [0, nn-2]
+      if (a == 0) continue;
+      p = 0;
+      q = idx;
+      v = S.khalo[halo_idx(A, a - 1, b, jk, q)];
+      if (q == 0) {
+        if (b == 0) continue;
+        v += S.khalo[halo_idx(A, a, b - 1, jk, nn + 0)];
+        v += S.khalo[halo_idx(A, a - 1, b - 1, jk, nn - 1)];
+      }
+    } else {  // first column, p in [1, nn-2]
+      if (b == 0) continue;
+      p = idx - (nn - 1) + 1;
+      q = 0;
+      v = S.khalo[halo_idx(A, a, b - 1, jk, nn + p)];
+    }
+    const int gp = gfun(A, a, p), gq = gfun(A, b, q);
+    if (!gvalid(A, gp) || !gvalid(A, gq)) continue;
+    K[(size_t)(k * A.nrad + gq) * A.nbf + (size_t)j * A.nrad + gp] += v;
+  }
+}
+
+inline int threads_for(int n2) { return ((n2 + 31) / 32) * 32; }
+
+struct Mark {
+  Profiler* p;
+  int slot = -1;
+  cudaStream_t s;
+  Mark(Profiler* p_, int k, cudaStream_t s_) : p(p_), s(s_) {
+    if (p && p->on && p->n < p->cap) {
+      slot = p->n++;
+      p->cls[slot] = k;
+      cudaEventRecord(p->ev[2 * slot], s);
+    }
+  }
+  ~Mark() {
+    if (slot >= 0) cudaEventRecord(p->ev[2 * slot + 1], s);
+  }
+};
+
+}  // namespace
+
+cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* J,
+                                bool zero_output, cudaStream_t st, Profiler* prof) {
+  const int n2 = A.nn * A.nn, th = threads_for(n2);
+  if (zero_output) {
+    cudaError_t err = cudaMemsetAsync(J, 0, sizeof(double) * (size_t)A.nbf * A.nbf, st);
+    if (err != cudaSuccess) return err;
+  }
+  const size_t sm1 = sizeof(double) * (n2 + A.rmax + 32);
+  {
+    Mark m(prof, KC_J_CONTRACT, st);
+    j_contract<<<dim3(A.nchan, A.nel), th, sm1, st>>>(A, S, P);
+  }
+  {
+    Mark m(prof, KC_J_SCATTER, st);
+    j_scatter<<<dim3(A.nang * A.nang, A.nel), th, 0, st>>>(A, S, J, zero_output ? 0 : 1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* K,
+                                 cudaStream_t st, Profiler* prof) {
+  const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
+  {
+    Mark m(prof, KC_K_NORMS, st);
+    k_block_norms<<<nang2, 512, 0, st>>>(A, P, S.active);
+  }
+  {
+    Mark m(prof, KC_K_OFFDIAG, st);
+    const size_t smo = sizeof(double) * (2 * A.NL * n2 + 2 * n2) + nang2;
+    k_offdiag<<<A.nel * A.nel, th, smo, st>>>(A, S, P, K);
+  }
+  {
+    Mark m(prof, KC_K_DIAG, st);
+    const size_t smd = sizeof(double) * n2 + nang2;
+    k_diag<<<dim3(A.nel, nang2), th, smd, st>>>(A, S, P, K);
+  }
+  {
+    Mark m(prof, KC_K_FIXUP, st);
+    k_fixup<<<dim3(A.nel * A.nel, nang2), 64, 0, st>>>(A, S, K);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace hfg

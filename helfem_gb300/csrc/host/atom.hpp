@@ -1,0 +1,101 @@
+// Host-side (FP64) description of one atom: the finite-element radial basis,
+// the integrals HelFEM's TwoDBasisT::compute_tei caches, and the Gaunt
+// coupling lists, laid out for the device.
+//
+// Element layout (FiniteElementBasis.cpp:51-64, 305-313): every element is an
+// nn x nn "primitive" tile. Primitive p of element e is the global radial
+// function g(e,p) = e*(nn-1) + p - 1; consecutive elements share one function
+// (g(e,nn-1) == g(e+1,0)); g == -1 (element 0, p = 0) and g == Nrad (last
+// element, p = nn-1) are the functions removed by the Dirichlet conditions and
+// are stored as zero rows/columns. Per-element matrices are stored padded to
+// nn x nn, column-major.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace hfg {
+
+double gaunt_coeff(int L, int M, int l, int m, int lp);
+
+// 1-D rules and Lagrange interpolating polynomials
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);
+void gauss_lobatto(int n, std::vector<double>& x, std::vector<double>& w);
+void cheb_rule(int n, std::vector<double>& x, std::vector<double>& w);
+// d^n L_i(x)/dx^n for all nodes, out[ix + i*npts]
+void lip_eval(const std::vector<double>& x, const std::vector<double>& nodes, int nder,
+              std::vector<double>& out);
+
+struct RadialBasis {
+  int nn = 0;    // nodes (functions) per element
+  int nel = 0;
+  int nrad = 0;
+  std::vector<double> bval;   // nel+1
+  std::vector<double> nodes;  // Gauss-Lobatto nodes on [-1,1]
+  int g(int e, int p) const { return e * (nn - 1) + p - 1; }
+  bool valid(int e, int p) const { const int q = g(e, p); return q >= 0 && q < nrad; }
+  double sf(int e) const { return 0.5 * (bval[e + 1] - bval[e]); }
+  double mid(int e) const { return 0.5 * (bval[e + 1] + bval[e]); }
+  int first(int e) const { return e == 0 ? 0 : g(e, 0); }
+  int nfun(int e) const;
+  int pfirst(int e) const { return e == 0 ? 1 : 0; }  // first valid primitive
+  // B (nder 0/1) at reference points x: out[ix + p*npts] in primitive index
+  // space (invalid primitives zero)
+  void B(int e, const std::vector<double>& x, int nder, std::vector<double>& out) const;
+  // R = B/r and dR/dr (deflated analytically on element 0)
+  void R(int e, const std::vector<double>& x, std::vector<double>& out) const;
+  void dR(int e, const std::vector<double>& x, std::vector<double>& out) const;
+  // int R_a R_b r^(k+2) dr, nn x nn padded
+  std::vector<double> radial_integral(int k, int e) const;
+  std::vector<double> kinetic(int e) const;  // 1/2 int B'_a B'_b dr
+  // in-element (ab|cd)_L, (nn^2 x nn^2) padded, pair index a + b*nn
+  std::vector<double> twoe(int L, int e) const;
+};
+
+struct AtomHost {
+  int Z = 0;
+  RadialBasis rad;
+  int nquad = 0;
+  int nang = 0, nbf = 0, NL = 0, lmax = 0;
+  std::vector<int> lval, mval;
+  double chol_tol = 1e-12;
+
+  // per (L, e): padded nn x nn
+  std::vector<double> rs, rb;  // [(L*nel+e)*nn*nn]
+  // per (L, e): pivoted Cholesky factor, compact reference layout (Ni^2 x r)
+  std::vector<std::vector<double>> chol;
+  std::vector<int> chol_rank;
+  // per (L, e): padded J-ordered factor nn^2 x rmax (zero-padded columns)
+  int rmax = 0;
+  std::vector<double> cholp;  // [(L*nel+e)*nn*nn*rmax]
+  // per (L, e): exchange-ordered in-element tensor rebuilt from the factor,
+  //   Tk[(a + c*nn) + (b + d*nn)*nn^2] = sum_p Lc(a+b*nn,p) Lc(c+d*nn,p)
+  std::vector<double> tk;
+
+  // radial one-electron blocks assembled (nrad x nrad)
+  std::vector<double> Srad, Trad, Tlrad, Vrad;
+
+  // ---- Gaunt coupling lists ----------------------------------------------
+  // J: channels (L,M); ket terms (k,l,coef); bra terms per output (i,j)
+  struct Chan { int L, M; };
+  std::vector<Chan> chans;
+  std::vector<int> jket_ptr;      // [nchan+1]
+  std::vector<int> jket_blk;      // angular block index k + l*nang
+  std::vector<double> jket_coef;
+  std::vector<int> jbra_ptr;      // [nang*nang+1], output block i + j*nang
+  std::vector<int> jbra_chan;
+  std::vector<double> jbra_coef;  // includes 4pi/(2L+1)
+  // K: per output block (j + k*nang): L entries, each with (i + l*nang, coef)
+  std::vector<int> kjk_ptr;       // [nang*nang+1] -> entries
+  std::vector<int> kent_L;        // per entry
+  std::vector<int> kent_ptr;      // [nent+1] -> terms
+  std::vector<int> kterm_blk;
+  std::vector<double> kterm_coef; // includes 4pi/(2L+1)
+
+  void build(int Z, int nnodes, const std::vector<double>& bval, const std::vector<int>& lval,
+             const std::vector<int>& mval, int nquad, double chol_tol);
+  void build_couplings();
+};
+
+}  // namespace hfg

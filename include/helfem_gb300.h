@@ -1,0 +1,175 @@
+/*
+ * helfem_gb300 — C ABI of the GB300 Fock-build engine for HelFEM's atomic
+ * finite-element basis.
+ *
+ * This is the drop-in boundary. The reference exposes the path as C++ member
+ * functions (no plugin ABI); each entry point below names the reference
+ * interface it replaces. include/helfem_gb300/TwoDBasis.hpp re-exposes the
+ * reference's C++ signatures on top of these calls.
+ *
+ * Conventions
+ *   - Matrices are FP64, column-major, nbf x nbf, AO index = iang*Nrad + irad
+ *     with the angular order of the reference's angular_basis
+ *     (src/atomic/basis.cpp:179-203: |m| outer, l inner, +m before -m).
+ *   - Functions return 0 (HFG_OK) or an error code and never throw or abort.
+ *     hfg_last_error() returns a message for the last failure on the calling
+ *     thread.
+ *   - Entry points taking a `stream` expect DEVICE pointers on the current
+ *     CUDA device and enqueue work on `stream` (a cudaStream_t; NULL is the
+ *     legacy default stream). They return without synchronising.
+ *   - The *_host variants take HOST pointers, copy in and out through the
+ *     handle's own stream and return after the result is on the host (the
+ *     reference's value semantics).
+ *   - A handle keeps per-handle device scratch: calls on one handle must not
+ *     overlap in time (issue them on one stream or serialise them). Distinct
+ *     handles are independent.
+ */
+#ifndef HELFEM_GB300_H
+#define HELFEM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int hfg_status;
+enum {
+  HFG_OK = 0,
+  HFG_ERR_ARG = 1,       /* invalid argument (shape, range, null pointer)  */
+  HFG_ERR_CUDA = 2,      /* CUDA runtime / driver failure                   */
+  HFG_ERR_STATE = 3,     /* handle not ready (e.g. integrals not computed)  */
+  HFG_ERR_NOMEM = 4,     /* host or device allocation failed                */
+  HFG_ERR_INTERNAL = 5   /* anything else                                   */
+};
+
+typedef struct hfg_atom hfg_atom;
+
+/* Description of an atomic basis. Mirrors the arguments of the reference's
+ * TwoDBasisT constructor (src/atomic/TwoDBasis.h:135-142; TwoDBasis.cpp:66-94)
+ * for a point nucleus and LIP elements on Gauss-Lobatto nodes (primbas 4,
+ * libhelfem/src/PolynomialBasis.cpp:51-59). */
+typedef struct {
+  int Z;               /* nuclear charge                                    */
+  int nnodes;          /* LIP nodes per element, 3..17                       */
+  int nquad;           /* radial DFT points per element; 0 -> 5*nnodes       */
+  int nelem;           /* number of radial elements                          */
+  const double* bval;  /* nelem+1 element boundaries, bval[0] = 0            */
+  int nang;            /* number of angular functions                        */
+  const int* lval;     /* [nang] l of each angular function                  */
+  const int* mval;     /* [nang] m of each angular function                  */
+  double chol_tol;     /* pivoted-Cholesky tolerance; 0 -> 1e-12 (reference) */
+  int host_only;       /* 1: tabulate on the host only and never touch a GPU;
+                          the device entry points then fail with
+                          HFG_ERR_STATE (for CPU-side checks)             */
+} hfg_atom_desc;
+
+typedef struct {
+  int nrad;   /* radial functions: nelem*(nnodes-1)-1 */
+  int nang;
+  int nbf;    /* nang*nrad */
+  int nelem;
+  int nnodes;
+  int NL;     /* multipoles L = 0..NL-1, NL = 2*max(l)+1 */
+  int rmax;   /* largest in-element Cholesky rank */
+} hfg_atom_dims_t;
+
+/* Message for the last failure on the calling thread ("" if none). */
+const char* hfg_last_error(void);
+
+/* Fill bval with grid::get_grid (libhelfem/include/grid.h:37-101): igrid
+ * 1 linear, 2 quadratic, 3 polynomial, 4 exponential, 5 geometric.
+ * bval has nelem+1 entries. */
+hfg_status hfg_grid(double rmax, int nelem, int igrid, double zexp, double* bval);
+
+/* Angular basis of the reference (src/atomic/basis.cpp:179-203). Call with
+ * lval = mval = NULL to get the count in *nang. */
+hfg_status hfg_angular_basis(int lmax, int mmax, int* nang, int* lval, int* mval);
+
+/* Build the basis and its two-electron integral caches on the host in FP64
+ * and upload them to the current device. Replaces the TwoDBasisT
+ * constructor followed by compute_tei(bool) (src/atomic/TwoDBasis.h:180-181,
+ * TwoDBasis.cpp:708-735): disjoint r^L / r^-L-1 factors
+ * (libhelfemqc/include/CoulombExchangeFE.h:180-217) and pivoted-Cholesky
+ * factors of the in-element tensors (libhelfem/src/RadialBasis.cpp:643-716). */
+hfg_status hfg_atom_create(const hfg_atom_desc* desc, hfg_atom** out);
+hfg_status hfg_atom_destroy(hfg_atom* atom);
+hfg_status hfg_atom_get_dims(const hfg_atom* atom, hfg_atom_dims_t* dims);
+
+/* One-electron matrices, host output nbf x nbf. Replace TwoDBasisT::overlap,
+ * kinetic, nuclear (src/atomic/TwoDBasis.h:201-207; point nucleus). */
+hfg_status hfg_overlap(const hfg_atom* atom, double* S);
+hfg_status hfg_kinetic(const hfg_atom* atom, double* T);
+hfg_status hfg_nuclear(const hfg_atom* atom, double* V);
+
+/* Cached radial tables of multipole L and element iel, in the reference's
+ * compact layout (Ni x Ni; Cholesky factor Ni^2 x rank, pair index a + b*Ni,
+ * CoulombExchangeFE.h:471-477). Any output may be NULL; rbig is zero for
+ * iel = 0 (never used there). For checking against an independent
+ * tabulation. */
+hfg_status hfg_atom_radial_tables(const hfg_atom* atom, int L, int iel, int* ni, double* rsmall,
+                                  double* rbig, int* rank, double* chol);
+
+/* Gaunt coefficient coeff(L,M,l,m,lp) = int Y_L^M* Y_l^m Y_lp^(M-m), the
+ * value of GauntT<double>::coeff (src/general/gaunt.cpp:201-251). */
+hfg_status hfg_gaunt(int L, int M, int l, int m, int lp, double* value);
+
+/* ---- Fock-build hot path (device pointers, asynchronous on `stream`) ---- */
+
+/* J(P): replaces TwoDBasisT::coulomb (src/atomic/TwoDBasis.cpp:773-877).
+ * J is overwritten (zero outside the element-diagonal tiles). */
+hfg_status hfg_coulomb(hfg_atom* atom, const double* P, double* J, void* stream);
+
+/* F += J(P): the same build accumulated into an existing matrix, for
+ * Fock assembly without a separate J buffer. */
+hfg_status hfg_coulomb_acc(hfg_atom* atom, const double* P, double* F, void* stream);
+
+/* K(P) for a spin density P, returned with the reference's sign (the matrix
+ * that is ADDED to the Fock matrix): replaces TwoDBasisT::exchange
+ * (src/atomic/TwoDBasis.cpp:879-999), including its density-block screening
+ * (blocks with Frobenius norm < 10*DBL_EPSILON are skipped). K is
+ * overwritten. */
+hfg_status hfg_exchange(hfg_atom* atom, const double* P, double* K, void* stream);
+
+/* ---- host-pointer drop-ins (value semantics, synchronous) ---- */
+hfg_status hfg_coulomb_host(hfg_atom* atom, const double* P, double* J);
+hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);
+
+/* Algorithmic work of one J and one K build on this basis with every density
+ * block active (the unit counts behind roofline figures). FLOPs count one
+ * fused multiply-add as two; recoupling FLOPs are the Gaunt-weighted sums of
+ * density tiles, transform FLOPs the r_small/r_big products (off-diagonal
+ * element pairs) and the in-element tensor contraction (diagonal elements).
+ * Bytes are the minimal HBM traffic: read P, write the output. */
+typedef struct {
+  double k_offdiag_flops;  /* element pairs a != b: recoupling + A X B^T     */
+  double k_diag_flops;     /* element pairs a == b: recoupling + tensor      */
+  double k_bytes;          /* 8*nbf^2 (read P) + 8*nbf^2 (write K)           */
+  double j_flops;
+  double j_bytes;          /* element-diagonal tiles of P read, J band written */
+  int n_k_entries;         /* (jang,kang,L) transforms                        */
+  int n_k_terms;           /* recoupling terms over all entries               */
+} hfg_work_t;
+hfg_status hfg_atom_work(const hfg_atom* atom, hfg_work_t* work);
+
+/* ---- per-kernel timing (counterpart of the reference's scf_driver::FockTimer,
+ * src/general/scf_driver_common.h:69-170) ----
+ * Kernel classes: 0 J contraction, 1 J scatter, 2 K block norms,
+ * 3 K off-diagonal element pairs, 4 K diagonal elements, 5 K boundary fix-up.
+ * hfg_profile_enable(atom, capacity) brackets each of the next `capacity`
+ * launches on this handle with CUDA events on the launch stream (0 turns
+ * timing off). hfg_profile_read waits for the recorded events and returns
+ * per-class launch counts and total milliseconds; reset != 0 clears them. */
+#define HFG_NUM_KERNEL_CLASSES 6
+typedef struct {
+  int launches[HFG_NUM_KERNEL_CLASSES];
+  double ms[HFG_NUM_KERNEL_CLASSES];
+} hfg_profile_t;
+hfg_status hfg_profile_enable(hfg_atom* atom, int capacity);
+hfg_status hfg_profile_read(hfg_atom* atom, hfg_profile_t* out, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HELFEM_GB300_H */
