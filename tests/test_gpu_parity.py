@@ -29,7 +29,7 @@ CASES = [
 def test_jk_match_oracle_dense_density(case):
     torch = torch_cuda()
     A, O = make_pair(*case)
-    P = random_density(O.nbf, 7, seed=case[0], S=O.S)
+    P = random_density(O.nbf, min(7, O.nbf), seed=case[0], S=O.S)
     F = FockOracle(O)
     Jr, Kr = F.coulomb(P), F.exchange(P)
     Pd = to_dev(torch, P)
