@@ -66,6 +66,7 @@ _SIGS = {
     "hfg_coulomb": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_coulomb_acc": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_exchange": ([_P, _P, _P, _P], ctypes.c_int),
+    "hfg_coulomb_noalloc": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_atom_work": ([_P, _P], ctypes.c_int),
@@ -218,6 +219,9 @@ class Atom:
 
     def coulomb_acc(self, P, F, stream=None):
         _check(_lib.hfg_coulomb_acc(self._h, _ptr(P), _ptr(F), _stream(stream)))
+
+    def coulomb_noalloc(self, P, J, stream=None):
+        _check(_lib.hfg_coulomb_noalloc(self._h, _ptr(P), _ptr(J), _stream(stream)))
 
     def exchange(self, P, K, stream=None):
         _check(_lib.hfg_exchange(self._h, _ptr(P), _ptr(K), _stream(stream)))

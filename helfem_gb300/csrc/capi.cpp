@@ -363,6 +363,26 @@ hfg_status hfg_coulomb_acc(hfg_atom* a, const double* P, double* F, void* stream
   });
 }
 
+hfg_status hfg_coulomb_noalloc(hfg_atom* a, const double* P, double* J, void* stream) {
+  return guard([&] {
+    need(a && P && J, "hfg_coulomb_noalloc: null argument");
+    a->check_device();
+    const size_t n2 = (size_t)a->dev.nn * a->dev.nn;
+    const size_t need_jin = (size_t)a->dev.nchan * a->dev.nel * n2;
+    const size_t need_all = need_jin + (size_t)a->dev.nchan * a->dev.nel * 2;
+    if (need_all > (size_t)HFG_NOALLOC_SCRATCH_DOUBLES)
+      throw std::invalid_argument("hfg_coulomb_noalloc: atom needs " + std::to_string(need_all) +
+                                  " doubles of Coulomb scratch, the static array holds " +
+                                  std::to_string((size_t)HFG_NOALLOC_SCRATCH_DOUBLES));
+    double* base = nullptr;
+    ck(hfg::noalloc_coulomb_scratch(need_all, &base), "static Coulomb scratch");
+    hfg::DevScratch s = a->scr;
+    s.jin = base;
+    s.jscal = base + need_jin;
+    ck(hfg::launch_coulomb_fp64(a->dev, s, P, J, true, (cudaStream_t)stream, nullptr), "coulomb kernels");
+  });
+}
+
 hfg_status hfg_exchange(hfg_atom* a, const double* P, double* K, void* stream) {
   return guard([&] {
     need(a && P && K, "hfg_exchange: null argument");

@@ -57,6 +57,13 @@ struct Profiler {
   int* cls = nullptr;         // [cap]
 };
 
+// Capacity of the static scratch behind hfg_coulomb_noalloc (4 MiB).
+#define HFG_NOALLOC_SCRATCH_DOUBLES (512 * 1024)
+// Device address of that scratch on the current device; resolved once per
+// device (coulomb_noalloc.cu). cudaErrorInvalidValue if doubles_needed
+// exceeds the capacity.
+cudaError_t noalloc_coulomb_scratch(size_t doubles_needed, double** out);
+
 // launchers (jk_fp64.cu)
 cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* J,
                                 bool zero_output, cudaStream_t st, Profiler* prof = nullptr);

@@ -131,6 +131,19 @@ hfg_status hfg_coulomb_acc(hfg_atom* atom, const double* P, double* F, void* str
  * overwritten. */
 hfg_status hfg_exchange(hfg_atom* atom, const double* P, double* K, void* stream);
 
+/* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
+ * fixed 4 MiB array in the library's static device memory rather than the
+ * handle's buffers. No counterpart in the reference; it exists for callers
+ * whose per-call path cannot allocate device memory (inside CUDA stream
+ * capture, under a host framework that owns every device allocation, or in
+ * loops that must not risk an allocation's synchronisation or failure).
+ * Atoms needing more than 4 MiB of Coulomb scratch
+ * (channels * elements * (nnodes^2 + 2) doubles) are rejected with
+ * HFG_ERR_ARG. All calls share the one array: calls that overlap on the GPU
+ * race and must be serialised by the caller. The first call on each device
+ * resolves the array's device address; make it before any stream capture. */
+hfg_status hfg_coulomb_noalloc(hfg_atom* atom, const double* P, double* J, void* stream);
+
 /* ---- host-pointer drop-ins (value semantics, synchronous) ---- */
 hfg_status hfg_coulomb_host(hfg_atom* atom, const double* P, double* J);
 hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);
