@@ -34,7 +34,7 @@ METRIC = "Fock builds/s (J+K, plain FP64)"
 UNIT = "builds/s"
 WORKLOAD = ("Kr (Z=36) J+K Fock build: 40 elements r_i=61^(i/40)-1, 15-node LIP, l<=2, m<=2, "
             "Nbf=5031, L<=4, P=CC^T (18 cols, N(0,1), seed 12345, Loewdin in S)")
-KERNELS_PER_STEP = 6  # j_contract, j_scatter, k_block_norms, k_offdiag, k_diag, k_fixup
+KERNELS_PER_STEP = 5  # j_contract, j_scatter, k_block_norms, k_tiles, k_fixup
 
 
 def kr_basis():
@@ -106,7 +106,7 @@ class ClockSampler:
         try:
             self.p = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.p = None
@@ -169,8 +169,8 @@ def fp64_peak_tflops(torch) -> float:
 
 
 def profiled_traffic():
-    """Per-launch DRAM bytes of k_offdiag from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_offdiag_kr.txt")
+    """Per-launch DRAM bytes of k_tiles from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_tiles_kr.txt")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -244,7 +244,7 @@ def run_ours(args):
 
     def step():
         atom.coulomb(Pd, Jd, stream)
-        atom.exchange(Pd, Kd, stream)
+        atom.exchange(Pd, Kd, stream, symmetric=True)  # P = C C^T is symmetric
 
     for _ in range(args.warmup):
         step()
@@ -281,19 +281,19 @@ def run_ours(args):
     Ph[...] = P
     atom.coulomb_host(Ph, out=Jh)
     atom.exchange_host(Ph, out=Kh)
-    ne = max(3, min(args.steps, 10))
+    ne = args.e2e_steps
     if dist is not None:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(ne):
         atom.coulomb_host(Ph, out=Jh)
         atom.exchange_host(Ph, out=Kh)
-    te = time.perf_counter() - t0
+    te = max(time.perf_counter() - t0, 1e-30)
     if dist is not None:
         t = torch.tensor([te], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         te = float(t.item())
-    e2e = {"value": ws * ne / te, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nbf * nbf,
+    e2e = {"value": ws * ne / te if ne else None, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nbf * nbf,
            "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
            "path": "hfg_coulomb_host + hfg_exchange_host (pinned host P, J, K)"}
 
@@ -303,24 +303,28 @@ def run_ours(args):
         return
 
     work = atom.work()
-    n_off, ms_off = prof["k_offdiag"]
+    n_off, ms_off = prof["k_tiles"]
     off_ms = ms_off / max(n_off, 1)
-    achieved = work["k_offdiag_flops"] / (off_ms * 1e-3) / 1e12
+    kflops = work["k_offdiag_sym_flops"] + work["k_diag_sym_flops"]
+    achieved = kflops / (off_ms * 1e-3) / 1e12
     peak = fp64_peak_tflops(torch)
     traffic = profiled_traffic()
     hbm_peak = measured_peaks().get("hbm_gbs")
     kernel_ms = {k: (v[1] / max(v[0], 1)) for k, v in prof.items()}
     roofline = {
-        "bound": "fp64", "kernel": "k_offdiag", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        "bound": "fp64", "kernel": "k_tiles", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
         "frac": achieved / peak if peak else None,
         "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (no FP64 figure in MEASURED_PEAKS.json)",
-        "flops_per_launch": work["k_offdiag_flops"], "ms_per_launch": off_ms,
+        "flops_per_launch": kflops, "ms_per_launch": off_ms,
         "traffic": traffic,
         "hbm": {"achieved_gbs": (work["k_bytes"] / 2) / (off_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
-                "note": "k_offdiag reads P once; HBM is not its bound"},
+                "note": "k_tiles reads P once; HBM is not its bound"},
         "kernel_ms_per_launch": kernel_ms,
     }
-    cpu_rate, cpu_n, cpu_dt, cpu_threads = cpu_reference_builds(args.cpu_seconds, 1000)
+    if args.cpu_seconds > 0:
+        cpu_rate, cpu_n, cpu_dt, cpu_threads = cpu_reference_builds(args.cpu_seconds, 1000)
+    else:
+        cpu_rate, cpu_n, cpu_dt, cpu_threads = None, 0, 0.0, host_cores()
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -342,10 +346,12 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="seconds of oracle builds for cpu_baseline (0 skips it)")
+    ap.add_argument("--e2e-steps", type=int, default=10, help="host-pointer drop-in steps (0 skips)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

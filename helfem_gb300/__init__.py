@@ -66,6 +66,7 @@ _SIGS = {
     "hfg_coulomb": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_coulomb_acc": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_exchange": ([_P, _P, _P, _P], ctypes.c_int),
+    "hfg_exchange_ex": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
     "hfg_coulomb_noalloc": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
@@ -73,19 +74,21 @@ _SIGS = {
     "hfg_profile_enable": ([_P, ctypes.c_int], ctypes.c_int),
     "hfg_profile_read": ([_P, _P, ctypes.c_int], ctypes.c_int),
 }
-KERNEL_CLASSES = ("j_contract", "j_scatter", "k_block_norms", "k_offdiag", "k_diag", "k_fixup")
+KERNEL_CLASSES = ("j_contract", "j_scatter", "k_block_norms", "k_tiles", "k_fixup")
+EXCHANGE_SYMMETRIC = 1
 
 
 
 
 class _Work(ctypes.Structure):
     _fields_ = [("k_offdiag_flops", ctypes.c_double), ("k_diag_flops", ctypes.c_double),
+                ("k_offdiag_sym_flops", ctypes.c_double), ("k_diag_sym_flops", ctypes.c_double),
                 ("k_bytes", ctypes.c_double), ("j_flops", ctypes.c_double), ("j_bytes", ctypes.c_double),
                 ("n_k_entries", ctypes.c_int), ("n_k_terms", ctypes.c_int)]
 
 
 class _Prof(ctypes.Structure):
-    _fields_ = [("launches", ctypes.c_int * 6), ("ms", ctypes.c_double * 6)]
+    _fields_ = [("launches", ctypes.c_int * 5), ("ms", ctypes.c_double * 5)]
 
 
 for _name, (_args, _res) in _SIGS.items():
@@ -223,8 +226,11 @@ class Atom:
     def coulomb_noalloc(self, P, J, stream=None):
         _check(_lib.hfg_coulomb_noalloc(self._h, _ptr(P), _ptr(J), _stream(stream)))
 
-    def exchange(self, P, K, stream=None):
-        _check(_lib.hfg_exchange(self._h, _ptr(P), _ptr(K), _stream(stream)))
+    def exchange(self, P, K, stream=None, symmetric: bool = False):
+        if symmetric:
+            _check(_lib.hfg_exchange_ex(self._h, _ptr(P), _ptr(K), EXCHANGE_SYMMETRIC, _stream(stream)))
+        else:
+            _check(_lib.hfg_exchange(self._h, _ptr(P), _ptr(K), _stream(stream)))
 
     def work(self) -> dict:
         w = _Work()

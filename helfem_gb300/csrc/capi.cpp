@@ -94,7 +94,9 @@ struct hfg_atom {
   // device copies of the tables
   DBuf d_rs, d_rb, d_cholp, d_rank, d_tk, d_chanL, d_jket_ptr, d_jket_blk, d_jket_coef, d_jbra_ptr,
       d_jbra_chan, d_jbra_coef, d_kjk_ptr, d_kent_L, d_kent_ptr, d_kterm_blk, d_kterm_coef;
-  DBuf s_jin, s_jscal, s_khalo, s_active;
+  DBuf s_jin, s_jscal, s_khalo, s_bnorm;
+  DBuf d_units_all, d_units_sym, d_diag_all, d_diag_sym;
+  hfg::KUnits units;
   // staging for the host-pointer entry points (allocated on first use)
   DBuf h_in, h_out;
   hfg::Profiler prof;
@@ -179,12 +181,67 @@ struct hfg_atom {
     s_jin.alloc(sizeof(double) * A.nchan * A.nel * n2);
     s_jscal.alloc(sizeof(double) * A.nchan * A.nel * 2);
     s_khalo.alloc(sizeof(double) * (size_t)A.nel * A.nel * A.nang * A.nang * (2 * A.nn - 1));
-    s_active.alloc((size_t)A.nang * A.nang);
+    s_bnorm.alloc(sizeof(double) * (size_t)A.nang * A.nang * NORM_SPLIT);
     scr.jin = s_jin.as<double>();
     scr.jscal = s_jscal.as<double>();
     scr.khalo = s_khalo.as<double>();
-    scr.active = s_active.as<unsigned char>();
+    scr.bnorm = s_bnorm.as<double>();
+    build_units();
     on_device = true;
+  }
+
+  // Exchange work units: element pairs split into balanced ranges of output
+  // angular blocks (enough units to keep every SM busy to the end), then
+  // one unit per (diagonal element, output block); off-diagonal units first
+  // so the short diagonal ones fill the tail.
+  void build_units() {
+    const hfg::AtomHost& H = host;
+    const int nel = H.rad.nel, nang2 = H.nang * H.nang;
+    std::vector<int> cnt(nang2);
+    long tot = 0;
+    for (int jk = 0; jk < nang2; ++jk) {
+      cnt[jk] = H.kjk_ptr[jk + 1] - H.kjk_ptr[jk];
+      tot += cnt[jk];
+    }
+    auto ranges = [&](int nsplit) {
+      std::vector<int> cut(1, 0);
+      long acc = 0;
+      int s = 1;
+      for (int jk = 0; jk < nang2; ++jk) {
+        acc += cnt[jk];
+        if (s < nsplit && acc * nsplit >= tot * s) { cut.push_back(jk + 1); ++s; }
+      }
+      if (cut.back() != nang2) cut.push_back(nang2);
+      return cut;
+    };
+    auto make = [&](bool sym, std::vector<int>& dj) {
+      std::vector<int4> u;
+      const long npairs = sym ? (long)nel * (nel - 1) / 2 : (long)nel * (nel - 1);
+      int nsplit = (int)std::min<long>(std::max<long>(1, (2432 + npairs - 1) / std::max<long>(npairs, 1)), 8);
+      nsplit = std::min(nsplit, nang2);
+      const std::vector<int> cut = ranges(nsplit);
+      for (int a = 0; a < nel; ++a)
+        for (int b = 0; b < nel; ++b) {
+          if (a == b || (sym && b < a)) continue;
+          for (size_t s = 0; s + 1 < cut.size(); ++s)
+            if (cut[s + 1] > cut[s]) u.push_back(make_int4(a, b, cut[s], cut[s + 1]));
+        }
+      dj.clear();
+      for (int k = 0; k < H.nang; ++k)
+        for (int j = 0; j < H.nang; ++j)
+          if (!sym || j <= k) dj.push_back(j + k * H.nang);
+      for (int a = 0; a < nel; ++a)
+        for (int w = 0; w < (int)dj.size(); ++w) u.push_back(make_int4(a, a, w, w + 1));
+      return u;
+    };
+    std::vector<int> dja, djs;
+    std::vector<int4> ua = make(false, dja), us = make(true, djs);
+    units.all = d_units_all.upload(ua);
+    units.n_all = (int)ua.size();
+    units.sym = d_units_sym.upload(us);
+    units.n_sym = (int)us.size();
+    units.diag_all = d_diag_all.upload(dja);
+    units.diag_sym = d_diag_sym.upload(djs);
   }
 
   void staging() {
@@ -384,10 +441,17 @@ hfg_status hfg_coulomb_noalloc(hfg_atom* a, const double* P, double* J, void* st
 }
 
 hfg_status hfg_exchange(hfg_atom* a, const double* P, double* K, void* stream) {
+  return hfg_exchange_ex(a, P, K, 0, stream);
+}
+
+hfg_status hfg_exchange_ex(hfg_atom* a, const double* P, double* K, int flags, void* stream) {
   return guard([&] {
     need(a && P && K, "hfg_exchange: null argument");
+    need((flags & ~HFG_EXCHANGE_SYMMETRIC) == 0, "hfg_exchange_ex: unknown flags");
     a->check_device();
-    ck(hfg::launch_exchange_fp64(a->dev, a->scr, P, K, (cudaStream_t)stream, &a->prof), "exchange kernels");
+    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P, K, (flags & HFG_EXCHANGE_SYMMETRIC) != 0,
+                                 (cudaStream_t)stream, &a->prof),
+       "exchange kernels");
   });
 }
 
@@ -401,7 +465,9 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb) {
   if (coulomb)
     ck(hfg::launch_coulomb_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof), "coulomb");
   else
-    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), st, &a->prof), "exchange");
+    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(), false, st,
+                                 &a->prof),
+       "exchange");
   ck(cudaMemcpyAsync(out, a->h_out.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
   ck(cudaStreamSynchronize(st), "stream sync");
 }
@@ -438,6 +504,18 @@ hfg_status hfg_atom_work(const hfg_atom* a, hfg_work_t* w) {
     w->n_k_terms = (int)H.kterm_blk.size();
     w->k_offdiag_flops = nent * off_prod + 2.0 * nterm * off_pair;
     w->k_diag_flops = nent * diag_prod + 2.0 * nterm * diag_pair;
+    // symmetric mode: pairs a < b, diagonal blocks j <= k
+    double sent = 0.0, sterm = 0.0;
+    for (int k = 0; k < H.nang; ++k)
+      for (int j = 0; j <= k; ++j) {
+        const int jk = j + k * H.nang;
+        for (int e = H.kjk_ptr[jk]; e < H.kjk_ptr[jk + 1]; ++e) {
+          sent += 1.0;
+          sterm += H.kent_ptr[e + 1] - H.kent_ptr[e];
+        }
+      }
+    w->k_offdiag_sym_flops = 0.5 * w->k_offdiag_flops;
+    w->k_diag_sym_flops = sent * diag_prod + 2.0 * sterm * diag_pair;
     w->k_bytes = 16.0 * (double)H.nbf * H.nbf;
     double jf = 0.0;
     for (size_t ch = 0; ch < H.chans.size(); ++ch) {

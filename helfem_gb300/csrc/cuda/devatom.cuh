@@ -41,7 +41,23 @@ struct DevScratch {
   double* jin;          // [nchan*nel*nn*nn]
   double* jscal;        // [nchan*nel*2]
   double* khalo;        // [nel*nel*nang*nang*(2nn-1)]
-  unsigned char* active;// [nang*nang]
+  double* bnorm;        // [nang*nang*NORM_SPLIT] partial squared block norms
+};
+
+// Column bands per angular block in the density-norm pass
+#define NORM_SPLIT 16
+
+// Exchange work units (int4: a, b, lo, hi), built once per atom on the host.
+// a != b: element pair, output blocks jk in [lo, hi) (natural order);
+// a == b: diagonal element, output blocks diag_jk[lo..hi).
+struct KUnits {
+  const int4* all = nullptr;   // every ordered pair and every jk
+  int n_all = 0;
+  const int4* sym = nullptr;   // a < b pairs, j <= k diagonal blocks
+  int n_sym = 0;
+  const int* diag_all = nullptr;  // 0..nang^2-1
+  const int* diag_sym = nullptr;  // jk with j <= k
+  const int* diag_jk_src(bool symmetric) const { return symmetric ? diag_sym : diag_all; }
 };
 
 __host__ __device__ inline int gfun(const DevAtom& A, int e, int p) { return e * (A.nn - 1) + p - 1; }
@@ -49,7 +65,7 @@ __host__ __device__ inline int gfun(const DevAtom& A, int e, int p) { return e *
 // Optional per-kernel timing (the engine's counterpart of the reference's
 // FockTimer): when enabled, every kernel launch is bracketed by a pair of
 // pre-created events on its stream; records are read back after the work.
-enum KernelClass { KC_J_CONTRACT = 0, KC_J_SCATTER, KC_K_NORMS, KC_K_OFFDIAG, KC_K_DIAG, KC_K_FIXUP, KC_COUNT };
+enum KernelClass { KC_J_CONTRACT = 0, KC_J_SCATTER, KC_K_NORMS, KC_K_TILES, KC_K_FIXUP, KC_COUNT };
 struct Profiler {
   bool on = false;
   int cap = 0, n = 0;
@@ -67,7 +83,7 @@ cudaError_t noalloc_coulomb_scratch(size_t doubles_needed, double** out);
 // launchers (jk_fp64.cu)
 cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* J,
                                 bool zero_output, cudaStream_t st, Profiler* prof = nullptr);
-cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* K,
-                                 cudaStream_t st, Profiler* prof = nullptr);
+cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
+                                 double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr);
 
 }  // namespace hfg

@@ -13,11 +13,13 @@
 // K restates TwoDBasisT::exchange (TwoDBasis.cpp:879-999) with
 // assemble_K_FE_one_multipole_cached_chol (CoulombExchangeFE.h:484-530):
 //   k_block_norms : density-block screening, ||P_il||_F < 10 eps skipped.
-//   k_offdiag     : one CTA per element pair (a != b) for every output angular
-//                   block: recouple the (a,b) tiles of P, then A_L X B_L^T
-//                   with A/B = r_small/r_big by element order.
-//   k_diag        : diagonal element tiles through the exchange-ordered
-//                   in-element tensor (equal to sum_p M_p X M_p^T).
+//   k_tiles       : work units of (element pair, range of output angular
+//                   blocks). Off-diagonal pairs: recouple the (a,b) tiles of
+//                   P, then A_L X B_L^T with A/B = r_small/r_big by element
+//                   order. Diagonal elements: the exchange-ordered
+//                   in-element tensor (equal to sum_p M_p X M_p^T). With a
+//                   symmetric density only half of the tiles are computed and
+//                   each is also written transposed (K_kj(b,a) = K_jk(a,b)^T).
 //   k_fixup       : adds the contributions of neighbouring tiles on the
 //                   shared boundary functions, in a fixed order (no atomics,
 //                   bitwise reproducible).
@@ -156,25 +158,41 @@ __global__ void j_scatter(DevAtom A, DevScratch S, double* __restrict__ J, int a
 }
 
 // ----------------------------------------------------------------- exchange
-__global__ void k_block_norms(DevAtom A, const double* __restrict__ P, unsigned char* active) {
+// Partial Frobenius norms of the angular blocks of P: grid (nang^2, NORM_SPLIT),
+// each CTA sums a band of columns; consumers add the partials in a fixed
+// order and apply the reference's 10*DBL_EPSILON screen.
+__global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* __restrict__ part) {
   __shared__ double red[32];
   const int blk = blockIdx.x, i = blk % A.nang, l = blk / A.nang;
+  const int c0 = (int)((long)A.nrad * blockIdx.y / NORM_SPLIT);
+  const int c1 = (int)((long)A.nrad * (blockIdx.y + 1) / NORM_SPLIT);
   double s = 0.0;
-  const size_t n = (size_t)A.nrad * A.nrad;
+  const size_t n = (size_t)A.nrad * (c1 - c0);
   for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
-    const size_t r = idx % A.nrad, c = idx / A.nrad;
+    const size_t r = idx % A.nrad, c = c0 + idx / A.nrad;
     const double v = P[(size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r];
     s += v * v;
   }
   s = block_sum(s, red);
-  if (threadIdx.x == 0) active[blk] = !(sqrt(s) < 10.0 * DBL_EPSILON);
+  if (threadIdx.x == 0) part[blk * NORM_SPLIT + blockIdx.y] = s;
+}
+
+__device__ __forceinline__ void load_active(const DevAtom& A, const DevScratch& S, unsigned char* act) {
+  const int nang2 = A.nang * A.nang;
+  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[idx * NORM_SPLIT + c];
+    act[idx] = !(sqrt(s) < 10.0 * DBL_EPSILON);
+  }
 }
 
 __device__ __forceinline__ size_t halo_idx(const DevAtom& A, int a, int b, int jk, int h) {
   return ((size_t)(a * A.nel + b) * (A.nang * A.nang) + jk) * (2 * A.nn - 1) + h;
 }
 
-// store the finished contribution y of tile (a,b), angular block jk
+// store the finished contribution y of tile (a,b), angular block jk, at
+// local position (p,q): owned entries go to K, the shared last row/column to
+// the halo buffer (added by k_fixup)
 __device__ __forceinline__ void k_store(const DevAtom& A, const DevScratch& S, double* K, int a, int b,
                                         int jk, int p, int q, double y) {
   const int nn = A.nn;
@@ -209,84 +227,84 @@ __device__ __forceinline__ bool k_entry_active(const DevAtom& A, const unsigned 
   return false;
 }
 
-__global__ void k_offdiag(DevAtom A, DevScratch S, const double* __restrict__ P, double* __restrict__ K) {
-  const int a = blockIdx.x % A.nel, b = blockIdx.x / A.nel;
-  if (a == b) return;
+// One work unit = one element pair (a,b) and a range of output angular
+// blocks. a != b: off-diagonal pair, jk over [lo,hi) in natural order,
+// contribution A_L X B_L^T. a == b: diagonal element, jk = diag_jk[lo..hi),
+// contribution Tk X. In symmetric mode (P = P^T) only a < b pairs and j <= k
+// diagonal blocks are units; each also writes the transposed partner tile
+// (k,j,b,a), since K_kj(b,a) = K_jk(a,b)^T.
+__global__ void __launch_bounds__(320) k_tiles(DevAtom A, DevScratch S, const int4* __restrict__ units,
+                                               const int* __restrict__ diag_jk, int symmetric,
+                                               const double* __restrict__ P, double* __restrict__ K) {
+  const int4 u = units[blockIdx.x];
+  const int a = u.x, b = u.y;
   const int nn = A.nn, n2 = nn * nn, NL = A.NL, nang2 = A.nang * A.nang;
   extern __shared__ double sm[];
-  double* Am = sm;
-  double* Bm = Am + NL * n2;
-  double* X = Bm + NL * n2;
+  double* X = sm;
   double* T = X + n2;
-  unsigned char* act = reinterpret_cast<unsigned char*>(T + n2);
-  const double* srcA = (a < b) ? A.rs : A.rb;
-  const double* srcB = (a < b) ? A.rb : A.rs;
-  for (int idx = threadIdx.x; idx < NL * n2; idx += blockDim.x) {
-    const int L = idx / n2, o = idx % n2;
-    Am[idx] = srcA[((size_t)L * A.nel + a) * n2 + o];
-    Bm[idx] = srcB[((size_t)L * A.nel + b) * n2 + o];
+  double* Am = T + n2;
+  double* Bm = Am + NL * n2;
+  unsigned char* act = reinterpret_cast<unsigned char*>(Bm + NL * n2);
+  const bool diag = (a == b);
+  if (!diag) {
+    const double* srcA = (a < b) ? A.rs : A.rb;
+    const double* srcB = (a < b) ? A.rb : A.rs;
+    for (int idx = threadIdx.x; idx < NL * n2; idx += blockDim.x) {
+      const int L = idx / n2, o = idx % n2;
+      Am[idx] = srcA[((size_t)L * A.nel + a) * n2 + o];
+      Bm[idx] = srcB[((size_t)L * A.nel + b) * n2 + o];
+    }
   }
-  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.active[idx];
+  load_active(A, S, act);
   __syncthreads();
   const int t = threadIdx.x;
   const bool live = t < n2;
   const int p = live ? t % nn : 0, q = live ? t / nn : 0;
   const int gp = gfun(A, a, p), gq = gfun(A, b, q);
   const bool vpq = live && gvalid(A, gp) && gvalid(A, gq);
-  for (int jk = 0; jk < nang2; ++jk) {
+  for (int w = u.z; w < u.w; ++w) {
+    const int jk = diag ? diag_jk[w] : w;
     double y = 0.0;
     for (int ent = A.kjk_ptr[jk]; ent < A.kjk_ptr[jk + 1]; ++ent) {
       if (!k_entry_active(A, act, ent)) continue;  // uniform over the CTA
       const int L = A.kent_L[ent];
       if (live) X[t] = vpq ? k_recouple(A, P, act, ent, gp, gq) : 0.0;
       __syncthreads();
-      if (live) {
-        const double* Bl = Bm + L * n2;
-        double s = 0.0;
-        for (int c = 0; c < nn; ++c) s += X[p + c * nn] * Bl[q + c * nn];
-        T[t] = s;
-      }
-      __syncthreads();
-      if (live) {
-        const double* Al = Am + L * n2;
-        double s = 0.0;
-        for (int c = 0; c < nn; ++c) s += Al[p + c * nn] * T[c + q * nn];
-        y += s;
+      if (diag) {
+        if (live) {
+          const double* Tk = A.tk + ((size_t)L * A.nel + a) * n2 * n2;
+          double s = 0.0;
+          for (int v = 0; v < n2; ++v) s += Tk[t + (size_t)v * n2] * X[v];
+          y += s;
+        }
+      } else {
+        if (live) {
+          const double* Bl = Bm + L * n2;
+          double s = 0.0;
+          for (int c = 0; c < nn; ++c) s += X[p + c * nn] * Bl[q + c * nn];
+          T[t] = s;
+        }
+        __syncthreads();
+        if (live) {
+          const double* Al = Am + L * n2;
+          double s = 0.0;
+          for (int c = 0; c < nn; ++c) s += Al[p + c * nn] * T[c + q * nn];
+          y += s;
+        }
       }
       __syncthreads();
     }
     if (live) k_store(A, S, K, a, b, jk, p, q, -y);
-  }
-}
-
-__global__ void k_diag(DevAtom A, DevScratch S, const double* __restrict__ P, double* __restrict__ K) {
-  const int a = blockIdx.x, jk = blockIdx.y;
-  const int nn = A.nn, n2 = nn * nn, nang2 = A.nang * A.nang;
-  extern __shared__ double sm[];
-  double* X = sm;
-  unsigned char* act = reinterpret_cast<unsigned char*>(X + n2);
-  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.active[idx];
-  __syncthreads();
-  const int t = threadIdx.x;
-  const bool live = t < n2;
-  const int p = live ? t % nn : 0, q = live ? t / nn : 0;
-  const int gp = gfun(A, a, p), gq = gfun(A, a, q);
-  const bool vpq = live && gvalid(A, gp) && gvalid(A, gq);
-  double y = 0.0;
-  for (int ent = A.kjk_ptr[jk]; ent < A.kjk_ptr[jk + 1]; ++ent) {
-    if (!k_entry_active(A, act, ent)) continue;
-    const int L = A.kent_L[ent];
-    if (live) X[t] = vpq ? k_recouple(A, P, act, ent, gp, gq) : 0.0;
-    __syncthreads();
-    if (live) {
-      const double* Tk = A.tk + ((size_t)L * A.nel + a) * n2 * n2;
-      double s = 0.0;
-      for (int u = 0; u < n2; ++u) s += Tk[t + (size_t)u * n2] * X[u];
-      y += s;
+    const int j = jk % A.nang, k = jk / A.nang;
+    if (symmetric && (!diag || j != k)) {
+      // transposed partner: stage through shared memory so that consecutive
+      // threads write consecutive rows of the column-major output
+      if (live) X[t] = -y;
+      __syncthreads();
+      if (live) k_store(A, S, K, b, a, k + j * A.nang, p, q, X[q + p * nn]);
+      __syncthreads();
     }
-    __syncthreads();
   }
-  if (live) k_store(A, S, K, a, a, jk, p, q, -y);
 }
 
 __global__ void k_fixup(DevAtom A, DevScratch S, double* __restrict__ K) {
@@ -357,22 +375,19 @@ cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const dou
   return cudaGetLastError();
 }
 
-cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* K,
-                                 cudaStream_t st, Profiler* prof) {
+cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
+                                 double* K, bool symmetric, cudaStream_t st, Profiler* prof) {
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
-    k_block_norms<<<nang2, 512, 0, st>>>(A, P, S.active);
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm);
   }
   {
-    Mark m(prof, KC_K_OFFDIAG, st);
-    const size_t smo = sizeof(double) * (2 * A.NL * n2 + 2 * n2) + nang2;
-    k_offdiag<<<A.nel * A.nel, th, smo, st>>>(A, S, P, K);
-  }
-  {
-    Mark m(prof, KC_K_DIAG, st);
-    const size_t smd = sizeof(double) * n2 + nang2;
-    k_diag<<<dim3(A.nel, nang2), th, smd, st>>>(A, S, P, K);
+    Mark m(prof, KC_K_TILES, st);
+    const size_t smem = sizeof(double) * (2 * n2 + 2 * A.NL * n2) + nang2;
+    const int nunits = symmetric ? U.n_sym : U.n_all;
+    k_tiles<<<nunits, th, smem, st>>>(A, S, symmetric ? U.sym : U.all, U.diag_jk_src(symmetric), symmetric ? 1 : 0,
+                                      P, K);
   }
   {
     Mark m(prof, KC_K_FIXUP, st);

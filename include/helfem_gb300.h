@@ -131,6 +131,14 @@ hfg_status hfg_coulomb_acc(hfg_atom* atom, const double* P, double* F, void* str
  * overwritten. */
 hfg_status hfg_exchange(hfg_atom* atom, const double* P, double* K, void* stream);
 
+/* hfg_exchange with options. HFG_EXCHANGE_SYMMETRIC: the caller guarantees
+ * P = P^T (every density matrix is); K is then symmetric and only half of
+ * the element-pair tiles are computed, each written with its transposed
+ * partner (about half the FP64 work). The result for a non-symmetric P is
+ * undefined under this flag. */
+#define HFG_EXCHANGE_SYMMETRIC 1
+hfg_status hfg_exchange_ex(hfg_atom* atom, const double* P, double* K, int flags, void* stream);
+
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
  * fixed 4 MiB array in the library's static device memory rather than the
  * handle's buffers. No counterpart in the reference; it exists for callers
@@ -157,6 +165,8 @@ hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);
 typedef struct {
   double k_offdiag_flops;  /* element pairs a != b: recoupling + A X B^T     */
   double k_diag_flops;     /* element pairs a == b: recoupling + tensor      */
+  double k_offdiag_sym_flops; /* the same under HFG_EXCHANGE_SYMMETRIC       */
+  double k_diag_sym_flops;
   double k_bytes;          /* 8*nbf^2 (read P) + 8*nbf^2 (write K)           */
   double j_flops;
   double j_bytes;          /* element-diagonal tiles of P read, J band written */
@@ -168,12 +178,12 @@ hfg_status hfg_atom_work(const hfg_atom* atom, hfg_work_t* work);
 /* ---- per-kernel timing (counterpart of the reference's scf_driver::FockTimer,
  * src/general/scf_driver_common.h:69-170) ----
  * Kernel classes: 0 J contraction, 1 J scatter, 2 K block norms,
- * 3 K off-diagonal element pairs, 4 K diagonal elements, 5 K boundary fix-up.
+ * 3 K element-pair tiles, 4 K boundary fix-up.
  * hfg_profile_enable(atom, capacity) brackets each of the next `capacity`
  * launches on this handle with CUDA events on the launch stream (0 turns
  * timing off). hfg_profile_read waits for the recorded events and returns
  * per-class launch counts and total milliseconds; reset != 0 clears them. */
-#define HFG_NUM_KERNEL_CLASSES 6
+#define HFG_NUM_KERNEL_CLASSES 5
 typedef struct {
   int launches[HFG_NUM_KERNEL_CLASSES];
   double ms[HFG_NUM_KERNEL_CLASSES];

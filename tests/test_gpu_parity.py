@@ -35,13 +35,16 @@ def test_jk_match_oracle_dense_density(case):
     Pd = to_dev(torch, P)
     Jd = torch.full_like(Pd, np.nan)
     Kd = torch.full_like(Pd, np.nan)
+    Ks = torch.full_like(Pd, np.nan)
     A.coulomb(Pd, Jd)
     A.exchange(Pd, Kd)
+    A.exchange(Pd, Ks, symmetric=True)
     torch.cuda.synchronize()
-    J, K = from_dev(Jd), from_dev(Kd)
-    assert np.isfinite(J).all() and np.isfinite(K).all()
+    J, K, KS = from_dev(Jd), from_dev(Kd), from_dev(Ks)
+    assert np.isfinite(J).all() and np.isfinite(K).all() and np.isfinite(KS).all()
     assert relerr(J, Jr) < TOL
     assert relerr(K, Kr) < TOL
+    assert relerr(KS, Kr) < TOL
 
 
 def test_block_diagonal_density_screening():
@@ -57,10 +60,14 @@ def test_block_diagonal_density_screening():
     F = FockOracle(O)
     Pd = to_dev(torch, P)
     Kd = torch.empty_like(Pd)
+    Ks = torch.empty_like(Pd)
     Jd = torch.empty_like(Pd)
     A.exchange(Pd, Kd)
+    A.exchange(Pd, Ks, symmetric=True)
     A.coulomb(Pd, Jd)
-    assert relerr(from_dev(Kd), F.exchange(P)) < TOL
+    Kr = F.exchange(P)
+    assert relerr(from_dev(Kd), Kr) < TOL
+    assert relerr(from_dev(Ks), Kr) < TOL
     assert relerr(from_dev(Jd), F.coulomb(P)) < TOL
 
 
@@ -118,13 +125,15 @@ def test_kr_full_size_properties():
     P = random_density(n, 18, seed=12345, S=S)
     Q = random_density(n, 4, seed=7)
     Pd, Qd = to_dev(torch, P), to_dev(torch, Q)
-    K1, K2, K3 = (torch.empty_like(Pd) for _ in range(3))
+    K1, K2, K3, K4 = (torch.empty_like(Pd) for _ in range(4))
     A.exchange(Pd, K1)
     A.exchange(Qd, K2)
     A.exchange(0.5 * Pd - 2.0 * Qd, K3)
+    A.exchange(Pd, K4, symmetric=True)
     lin = K3 - (0.5 * K1 - 2.0 * K2)
     assert float(lin.abs().max()) < 1e-11 * float(K1.abs().max())
     assert float((K1 - K1.T).abs().max()) < 1e-12 * float(K1.abs().max())
+    assert float((K4 - K1).abs().max()) < 1e-12 * float(K1.abs().max())
     assert float((Pd * K1).sum()) < 0.0
     J1 = torch.empty_like(Pd)
     A.coulomb(Pd, J1)
