@@ -71,10 +71,21 @@ _SIGS = {
     "hfg_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_atom_work": ([_P, _P], ctypes.c_int),
+    "hfg_dft_grid": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
+    "hfg_xc_host": ([_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, ctypes.c_double], ctypes.c_int),
     "hfg_profile_enable": ([_P, ctypes.c_int], ctypes.c_int),
     "hfg_profile_read": ([_P, _P, ctypes.c_int], ctypes.c_int),
 }
 KERNEL_CLASSES = ("j_contract", "j_scatter", "k_block_norms", "k_tiles", "k_fixup")
+XC_IDS = {"lda_x": 1, "lda_c_vwn": 7, "lda_c_pw": 12, "gga_x_pbe": 101, "gga_c_pbe": 130}
+
+
+def parse_xc(method: str):
+    """'lda_x-lda_c_vwn' style names -> (x_id, c_id) (dftfuncs.cpp:94-143)."""
+    parts = [p for p in method.split("-") if p]
+    ids = [XC_IDS[p] for p in parts]
+    return (ids + [0, 0])[:2]
 EXCHANGE_SYMMETRIC = 1
 
 
@@ -236,6 +247,29 @@ class Atom:
         w = _Work()
         _check(_lib.hfg_atom_work(self._h, ctypes.byref(w)))
         return {n: getattr(w, n) for n, _ in _Work._fields_}
+
+    # ---- XC ----
+    def dft_grid(self, ldft: int = 0, mdft: int = 0):
+        _check(_lib.hfg_dft_grid(self._h, ldft, mdft))
+
+    def xc(self, x_func, c_func, Pa, Ha, Pb=None, Hb=None, energies=None, thr=1e-12, stream=None):
+        _check(_lib.hfg_xc(self._h, x_func, c_func, _ptr(Pa), _ptr(Pb) if Pb is not None else None,
+                           _ptr(Ha), _ptr(Hb) if Hb is not None else None,
+                           _ptr(energies) if energies is not None else None, thr, _stream(stream)))
+
+    def xc_host(self, x_func, c_func, Pa, Pb=None, thr=1e-12):
+        """Returns (Ha, Hb or None, Exc, Nel)."""
+        Pa = np.asfortranarray(Pa, dtype=np.float64)
+        Ha = np.zeros_like(Pa, order="F")
+        Pb_ = Hb = None
+        if Pb is not None:
+            Pb_ = np.asfortranarray(Pb, dtype=np.float64)
+            Hb = np.zeros_like(Pa, order="F")
+        exc, nel = ctypes.c_double(), ctypes.c_double()
+        _check(_lib.hfg_xc_host(self._h, x_func, c_func, _dptr(Pa), _dptr(Pb_) if Pb_ is not None else None,
+                                _dptr(Ha), _dptr(Hb) if Hb is not None else None,
+                                ctypes.byref(exc), ctypes.byref(nel), thr))
+        return Ha, Hb, exc.value, nel.value
 
     # ---- per-kernel timing ----
     def profile_enable(self, capacity: int = 4096):

@@ -98,7 +98,12 @@ struct hfg_atom {
   DBuf d_units_all, d_units_sym, d_diag_all, d_diag_sym;
   hfg::KUnits units;
   // staging for the host-pointer entry points (allocated on first use)
-  DBuf h_in, h_out;
+  DBuf h_in, h_out, h_in2, h_out2, h_e;
+  // DFT grid (built on first use or by hfg_dft_grid)
+  hfg::DevXC xc{};
+  hfg::XcScratch xs{};
+  bool xc_ready = false;
+  DBuf x_wang, x_isin, x_W, x_Wt, x_Wp, x_r, x_wr, x_R, x_dR, xs_D, xs_Dr, xs_F, xs_U, xs_ep;
   hfg::Profiler prof;
   std::vector<cudaEvent_t> prof_ev;
   std::vector<int> prof_cls;
@@ -242,6 +247,34 @@ struct hfg_atom {
     units.n_sym = (int)us.size();
     units.diag_all = d_diag_all.upload(dja);
     units.diag_sym = d_diag_sym.upload(djs);
+  }
+
+  void setup_xc(int ldft, int mdft) {
+    host.build_dft_grid(ldft, mdft);
+    const hfg::AtomHost& H = host;
+    xc.nquad = H.nquad;
+    xc.nap = H.nap;
+    xc.wang = x_wang.upload(H.xc_wang);
+    xc.isin = x_isin.upload(H.xc_isin);
+    xc.W = x_W.upload(H.xc_W);
+    xc.Wt = x_Wt.upload(H.xc_Wt);
+    xc.Wp = x_Wp.upload(H.xc_Wp);
+    xc.r = x_r.upload(H.xc_r);
+    xc.wr = x_wr.upload(H.xc_wr);
+    xc.R = x_R.upload(H.xc_R);
+    xc.dR = x_dR.upload(H.xc_dR);
+    const size_t nel = H.rad.nel, nq = H.nquad, nab = (size_t)H.nang * H.nang, nap = H.nap;
+    xs_D.alloc(sizeof(double) * 2 * nel * nab * nq);
+    xs_Dr.alloc(sizeof(double) * 2 * nel * nab * nq);
+    xs_F.alloc(sizeof(double) * 8 * nel * nq * nap);
+    xs_U.alloc(sizeof(double) * 8 * nel * nab * nq);
+    xs_ep.alloc(sizeof(double) * 2 * nel * nq);
+    xs.D = xs_D.as<double>();
+    xs.Dr = xs_Dr.as<double>();
+    xs.F = xs_F.as<double>();
+    xs.U = xs_U.as<double>();
+    xs.epart = xs_ep.as<double>();
+    xc_ready = true;
   }
 
   void staging() {
@@ -527,6 +560,66 @@ hfg_status hfg_atom_work(const hfg_atom* a, hfg_work_t* w) {
     jf += 6.0 * (double)H.jbra_chan.size() * S2;
     w->j_flops = jf;
     w->j_bytes = 16.0 * (double)H.nang * H.nang * S2;
+  });
+}
+
+hfg_status hfg_dft_grid(hfg_atom* a, int ldft, int mdft) {
+  return guard([&] {
+    need(a != nullptr && ldft >= 0 && mdft >= 0, "hfg_dft_grid: bad arguments");
+    a->check_device();
+    a->setup_xc(ldft, mdft);
+  });
+}
+
+static void check_xc_args(int x_func, int c_func) {
+  need(hfg::xc_func_supported(x_func) && hfg::xc_func_supported(c_func),
+       "hfg_xc: unsupported functional id (supported: 1 lda_x, 7 lda_c_vwn, 12 lda_c_pw, 101 gga_x_pbe, "
+       "130 gga_c_pbe)");
+}
+
+hfg_status hfg_xc(hfg_atom* a, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha, double* Hb,
+                  double* energies, double thr, void* stream) {
+  return guard([&] {
+    need(a && Pa && Ha, "hfg_xc: null argument");
+    need(!Pb || Hb, "hfg_xc: an unrestricted call needs Hb");
+    check_xc_args(x_func, c_func);
+    a->check_device();
+    if (!a->xc_ready) a->setup_xc(0, 0);
+    ck(hfg::launch_xc_fp64(a->dev, a->xc, a->xs, x_func, c_func, Pa, Pb, Ha, Hb, energies, thr,
+                           (cudaStream_t)stream),
+       "xc kernels");
+  });
+}
+
+hfg_status hfg_xc_host(hfg_atom* a, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
+                       double* Hb, double* Exc, double* Nel, double thr) {
+  return guard([&] {
+    need(a && Pa && Ha, "hfg_xc_host: null argument");
+    need(!Pb || Hb, "hfg_xc_host: an unrestricted call needs Hb");
+    check_xc_args(x_func, c_func);
+    a->check_device();
+    if (!a->xc_ready) a->setup_xc(0, 0);
+    a->staging();
+    const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
+    if (Pb) {
+      if (a->h_in2.n != bytes) a->h_in2.alloc(bytes);
+      if (a->h_out2.n != bytes) a->h_out2.alloc(bytes);
+    }
+    if (a->h_e.n == 0) a->h_e.alloc(2 * sizeof(double));
+    cudaStream_t st = a->own_stream;
+    ck(cudaMemcpyAsync(a->h_in.p, Pa, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+    if (Pb) ck(cudaMemcpyAsync(a->h_in2.p, Pb, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+    ck(hfg::launch_xc_fp64(a->dev, a->xc, a->xs, x_func, c_func, a->h_in.as<double>(),
+                           Pb ? a->h_in2.as<double>() : nullptr, a->h_out.as<double>(),
+                           Pb ? a->h_out2.as<double>() : nullptr, a->h_e.as<double>(), thr, st),
+       "xc kernels");
+    double e[2];
+    ck(cudaMemcpyAsync(Ha, a->h_out.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
+    if (Pb) ck(cudaMemcpyAsync(Hb, a->h_out2.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
+    ck(cudaMemcpyAsync(e, a->h_e.p, sizeof(e), cudaMemcpyDeviceToHost, st), "D2H copy");
+    ck(cudaStreamSynchronize(st), "stream sync");
+    if (Exc) *Exc = e[0];
+    if (Nel) *Nel = e[1];
   });
 }
 

@@ -73,6 +73,34 @@ struct Profiler {
   int* cls = nullptr;         // [cap]
 };
 
+// Device tables of the atomic DFT grid (host layout in host/atom.hpp)
+struct DevXC {
+  int nquad = 0, nap = 0;
+  const double* wang = nullptr;  // [nap]
+  const double* isin = nullptr;  // [nap]
+  const double* W = nullptr;     // [(alpha + beta*nang)*nap + a]
+  const double* Wt = nullptr;
+  const double* Wp = nullptr;
+  const double* r = nullptr;     // [e*nquad + q]
+  const double* wr = nullptr;    // radial weight times r^2
+  const double* R = nullptr;     // [(e*nquad + q)*nn + p]
+  const double* dR = nullptr;
+};
+struct XcScratch {
+  double* D;      // [2][nel][nang^2][nquad]
+  double* Dr;     // same
+  double* F;      // [2][4][nel][nquad][nap]
+  double* U;      // [2][4][nel][nang^2][nquad]
+  double* epart;  // [nel*nquad][2]
+};
+bool xc_func_supported(int id);
+bool xc_func_is_gga(int id);
+// Pb == nullptr: restricted (Pa is the total density, Ha the potential);
+// energies (device, may be null) receives {Exc, Nel}
+cudaError_t launch_xc_fp64(const DevAtom& A, const DevXC& X, const XcScratch& S, int xid, int cid,
+                           const double* Pa, const double* Pb, double* Ha, double* Hb, double* energies,
+                           double thr, cudaStream_t st);
+
 // Capacity of the static scratch behind hfg_coulomb_noalloc (4 MiB).
 #define HFG_NOALLOC_SCRATCH_DOUBLES (512 * 1024)
 // Device address of that scratch on the current device; resolved once per

@@ -93,9 +93,29 @@ struct AtomHost {
   std::vector<int> kterm_blk;
   std::vector<double> kterm_coef; // includes 4pi/(2L+1)
 
+  // ---- DFT grid (src/atomic/dftgrid.cpp:470-576, angular.cpp:21-70) -----
+  // per element: nquad Chebyshev radial points; angular product rule of
+  // ldft cos(theta) Chebyshev points x mdft uniform phi points (nap total)
+  int ldft = 0, mdft = 0, nap = 0;
+  std::vector<double> xc_wang;     // [nap] angular weights
+  std::vector<double> xc_isin;     // [nap] 1/sin(theta)
+  // real angular tables, [(alpha + beta*nang)*nap + a]:
+  //   W   = Re[Y_alpha conj(Y_beta)]
+  //   Wt  = Re[dY_alpha/dtheta conj(Y_beta)]
+  //   Wp  = Re[(i m_alpha) Y_alpha conj(Y_beta)]
+  std::vector<double> xc_W, xc_Wt, xc_Wp;
+  // per element e and radial point q: r, total radial weight wrad*r^2,
+  // R and dR/dr of the nn primitives: [(e*nquad + q)*nn + p]
+  std::vector<double> xc_r, xc_wr, xc_R, xc_dR;
+  void build_dft_grid(int ldft, int mdft);
+
   void build(int Z, int nnodes, const std::vector<double>& bval, const std::vector<int>& lval,
              const std::vector<int>& mval, int nquad, double chol_tol);
   void build_couplings();
 };
+
+// normalised Y_l^m(theta, phi) with the Condon-Shortley phase (value of the
+// reference's ::spherical_harmonics, src/general/spherical_harmonics.cpp)
+void ylm(int l, int m, double cth, double phi, double& re, double& im);
 
 }  // namespace hfg

@@ -152,6 +152,25 @@ hfg_status hfg_exchange_ex(hfg_atom* atom, const double* P, double* K, int flags
  * resolves the array's device address; make it before any stream capture. */
 hfg_status hfg_coulomb_noalloc(hfg_atom* atom, const double* P, double* J, void* stream);
 
+/* ---- XC potential on the atomic DFT grid ----
+ * Replaces DFTGrid::eval_Fxc (src/atomic/dftgrid.h:156-159,
+ * src/atomic/dftgrid.cpp:591-712) with functionals restated from the papers
+ * (libxc ids: 1 lda_x, 7 lda_c_vwn (VWN5), 12 lda_c_pw (PW92), 101 gga_x_pbe,
+ * 130 gga_c_pbe; 0 = none). External functional parameters are not
+ * supported. Restricted: Pb == NULL, Pa is the total density and Ha the XC
+ * potential matrix. Unrestricted: spin densities Pa, Pb -> Ha, Hb. Ha/Hb are
+ * overwritten. `energies` (device, 2 doubles, may be NULL) receives
+ * {Exc, electron count on the grid}. thr is the density threshold
+ * (reference default 1e-12). */
+/* (Re)build the grid: ldft cos(theta) points x mdft phi points per element
+ * (0 -> the reference defaults 4*lmax+12, 4*mmax+12; src/atomic/main.cpp:329-331).
+ * Called implicitly with the defaults by the first XC call. */
+hfg_status hfg_dft_grid(hfg_atom* atom, int ldft, int mdft);
+hfg_status hfg_xc(hfg_atom* atom, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
+                  double* Hb, double* energies, double thr, void* stream);
+hfg_status hfg_xc_host(hfg_atom* atom, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
+                       double* Hb, double* Exc, double* Nel, double thr);
+
 /* ---- host-pointer drop-ins (value semantics, synchronous) ---- */
 hfg_status hfg_coulomb_host(hfg_atom* atom, const double* P, double* J);
 hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);

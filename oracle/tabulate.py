@@ -391,7 +391,7 @@ def theta_lm(l: int, m: int, x: np.ndarray) -> np.ndarray:
         return np.zeros_like(x)
     if m >= 0:
         return _assoc_legendre_norm(l, m, x)
-    return ((-1) ** m) * _assoc_legendre_norm(l, -m, x)
+    return ((-1) ** abs(int(m))) * _assoc_legendre_norm(l, -m, x)
 
 
 def _pi_decimal():
