@@ -74,6 +74,7 @@ _SIGS = {
     "hfg_dft_grid": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
     "hfg_xc_host": ([_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, ctypes.c_double], ctypes.c_int),
+    "hfg_scf_run": ([_P, _P, _P, _D, _P], ctypes.c_int),
     "hfg_profile_enable": ([_P, ctypes.c_int], ctypes.c_int),
     "hfg_profile_read": ([_P, _P, ctypes.c_int], ctypes.c_int),
 }
@@ -96,6 +97,19 @@ class _Work(ctypes.Structure):
                 ("k_offdiag_sym_flops", ctypes.c_double), ("k_diag_sym_flops", ctypes.c_double),
                 ("k_bytes", ctypes.c_double), ("j_flops", ctypes.c_double), ("j_bytes", ctypes.c_double),
                 ("n_k_entries", ctypes.c_int), ("n_k_terms", ctypes.c_int)]
+
+
+class _ScfDesc(ctypes.Structure):
+    _fields_ = [("nela", ctypes.c_int), ("nelb", ctypes.c_int), ("restricted", ctypes.c_int),
+                ("symmetry", ctypes.c_int), ("x_func", ctypes.c_int), ("c_func", ctypes.c_int),
+                ("kfrac", ctypes.c_double), ("maxiter", ctypes.c_int), ("e_tol", ctypes.c_double),
+                ("diis_tol", ctypes.c_double), ("fixed_occ", _I), ("n_fixed_blocks", ctypes.c_int),
+                ("dftthr", ctypes.c_double)]
+
+
+class _ScfRes(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("Etot", "Ekin", "Enuc", "Ecoul", "Exx", "Exc", "Nel_grid")] + \
+               [("iterations", ctypes.c_int), ("converged", ctypes.c_int)]
 
 
 class _Prof(ctypes.Structure):
@@ -270,6 +284,28 @@ class Atom:
                                 _dptr(Ha), _dptr(Hb) if Hb is not None else None,
                                 ctypes.byref(exc), ctypes.byref(nel), thr))
         return Ha, Hb, exc.value, nel.value
+
+    # ---- SCF ----
+    def scf(self, nela: int, nelb: int, method: str = "hf", restricted: bool = True, symmetry: int = 1,
+            fixed_occ=None, maxiter: int = 0, e_tol: float = 0.0, diis_tol: float = 0.0, stream=None) -> dict:
+        """Atomic SCF on the device. fixed_occ: dict m -> (n_alpha, n_beta) (symmetry 1)."""
+        x, c = (0, 0) if method.lower() == "hf" else parse_xc(method)
+        occ = None
+        nfix = 0
+        if fixed_occ is not None:
+            ms = sorted(set(int(m) for m in self.mval))
+            occ = np.array([v for m in ms for v in fixed_occ.get(m, (0, 0))], dtype=np.int32)
+            nfix = len(ms)
+        d = _ScfDesc(nela, nelb, int(restricted), symmetry, x, c, -1.0, maxiter, e_tol, diis_tol,
+                     occ.ctypes.data_as(_I) if occ is not None else None, nfix, 0.0)
+        r = _ScfRes()
+        nspin = 1 if restricted else 2
+        eps = np.zeros(self.nbf * nspin)
+        _check(_lib.hfg_scf_run(self._h, ctypes.byref(d), ctypes.byref(r), _dptr(eps),
+                                _stream(stream) if stream is not None else None))
+        out = {n: getattr(r, n) for n, _ in _ScfRes._fields_}
+        out["orbital_energies"] = eps
+        return out
 
     # ---- per-kernel timing ----
     def profile_enable(self, capacity: int = 4096):

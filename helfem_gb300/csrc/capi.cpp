@@ -1,294 +1,14 @@
 // C ABI of the engine (declarations and contract in include/helfem_gb300.h).
 // Every entry point converts exceptions and CUDA errors into status codes and
 // a thread-local message; nothing throws across the boundary.
-#include "helfem_gb300.h"
+#include "handle.hpp"
 
-#include <cuda_runtime.h>
-
-#include <cmath>
-#include <cstring>
-#include <memory>
-#include <new>
-#include <stdexcept>
-#include <string>
-#include <vector>
-
-#include "cuda/devatom.cuh"
-#include "host/atom.hpp"
-
-namespace {
-
+namespace hfg_abi {
 thread_local std::string g_err;
-
-struct CudaError : std::runtime_error {
-  using std::runtime_error::runtime_error;
-};
-
-void ck(cudaError_t e, const char* what) {
-  if (e != cudaSuccess)
-    throw CudaError(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
 }
-
-template <class F>
-hfg_status guard(F&& f) {
-  try {
-    f();
-    g_err.clear();
-    return HFG_OK;
-  } catch (const std::invalid_argument& e) {
-    g_err = e.what();
-    return HFG_ERR_ARG;
-  } catch (const CudaError& e) {
-    g_err = e.what();
-    return HFG_ERR_CUDA;
-  } catch (const std::bad_alloc&) {
-    g_err = "host allocation failed";
-    return HFG_ERR_NOMEM;
-  } catch (const std::logic_error& e) {
-    g_err = e.what();
-    return HFG_ERR_STATE;
-  } catch (const std::exception& e) {
-    g_err = e.what();
-    return HFG_ERR_INTERNAL;
-  } catch (...) {
-    g_err = "unknown error";
-    return HFG_ERR_INTERNAL;
-  }
-}
-
-// RAII device allocation
-struct DBuf {
-  void* p = nullptr;
-  size_t n = 0;
-  DBuf() = default;
-  DBuf(const DBuf&) = delete;
-  DBuf& operator=(const DBuf&) = delete;
-  ~DBuf() { if (p) cudaFree(p); }
-  void alloc(size_t bytes) {
-    if (p) { cudaFree(p); p = nullptr; }
-    n = bytes;
-    if (bytes == 0) return;
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
-    ck(e, "cudaMalloc");
-  }
-  template <class T>
-  T* upload(const std::vector<T>& v) {
-    alloc(std::max<size_t>(1, v.size()) * sizeof(T));
-    if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
-    return static_cast<T*>(p);
-  }
-  template <class T>
-  T* as() const { return static_cast<T*>(p); }
-};
-
-}  // namespace
-
-struct hfg_atom {
-  hfg::AtomHost host;
-  int device = 0;
-  bool on_device = false;
-  cudaStream_t own_stream = nullptr;
-  hfg::DevAtom dev{};
-  hfg::DevScratch scr{};
-  // device copies of the tables
-  DBuf d_rs, d_rb, d_cholp, d_rank, d_tk, d_chanL, d_jket_ptr, d_jket_blk, d_jket_coef, d_jbra_ptr,
-      d_jbra_chan, d_jbra_coef, d_kjk_ptr, d_kent_L, d_kent_ptr, d_kterm_blk, d_kterm_coef;
-  DBuf s_jin, s_jscal, s_khalo, s_bnorm;
-  DBuf d_units_all, d_units_sym, d_diag_all, d_diag_sym;
-  hfg::KUnits units;
-  // staging for the host-pointer entry points (allocated on first use)
-  DBuf h_in, h_out, h_in2, h_out2, h_e;
-  // DFT grid (built on first use or by hfg_dft_grid)
-  hfg::DevXC xc{};
-  hfg::XcScratch xs{};
-  bool xc_ready = false;
-  DBuf x_wang, x_isin, x_W, x_Wt, x_Wp, x_r, x_wr, x_R, x_dR, xs_D, xs_Dr, xs_F, xs_U, xs_ep;
-  hfg::Profiler prof;
-  std::vector<cudaEvent_t> prof_ev;
-  std::vector<int> prof_cls;
-
-  ~hfg_atom() {
-    free_profiler();
-    if (own_stream) cudaStreamDestroy(own_stream);
-  }
-
-  void free_profiler() {
-    for (cudaEvent_t e : prof_ev) cudaEventDestroy(e);
-    prof_ev.clear();
-    prof_cls.clear();
-    prof = hfg::Profiler();
-  }
-
-  void enable_profiler(int cap) {
-    free_profiler();
-    if (cap <= 0) return;
-    prof_ev.resize(2 * (size_t)cap);
-    for (auto& e : prof_ev) ck(cudaEventCreate(&e), "cudaEventCreate");
-    prof_cls.assign(cap, 0);
-    prof.ev = prof_ev.data();
-    prof.cls = prof_cls.data();
-    prof.cap = cap;
-    prof.n = 0;
-    prof.on = true;
-  }
-
-  void check_device() const {
-    if (!on_device) throw std::logic_error("handle was created host-only; device entry points are unavailable");
-    int d = -1;
-    ck(cudaGetDevice(&d), "cudaGetDevice");
-    if (d != device) throw std::invalid_argument("handle used on a different CUDA device than it was created on");
-  }
-
-  void upload() {
-    using namespace hfg;
-    const AtomHost& H = host;
-    ck(cudaGetDevice(&device), "cudaGetDevice");
-    ck(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    DevAtom& A = dev;
-    A.nn = H.rad.nn;
-    A.nel = H.rad.nel;
-    A.nrad = H.rad.nrad;
-    A.nang = H.nang;
-    A.nbf = H.nbf;
-    A.NL = H.NL;
-    A.rmax = H.rmax;
-    A.rs = d_rs.upload(H.rs);
-    A.rb = d_rb.upload(H.rb);
-    A.cholp = d_cholp.upload(H.cholp);
-    A.rank = d_rank.upload(H.chol_rank);
-    A.tk = d_tk.upload(H.tk);
-    std::vector<int> chanL;
-    for (auto& c : H.chans) chanL.push_back(c.L);
-    A.nchan = (int)H.chans.size();
-    A.chanL = d_chanL.upload(chanL);
-    A.jket_ptr = d_jket_ptr.upload(H.jket_ptr);
-    A.jket_blk = d_jket_blk.upload(H.jket_blk);
-    A.jket_coef = d_jket_coef.upload(H.jket_coef);
-    A.jbra_ptr = d_jbra_ptr.upload(H.jbra_ptr);
-    A.jbra_chan = d_jbra_chan.upload(H.jbra_chan);
-    A.jbra_coef = d_jbra_coef.upload(H.jbra_coef);
-    A.kjk_ptr = d_kjk_ptr.upload(H.kjk_ptr);
-    A.kent_L = d_kent_L.upload(H.kent_L);
-    A.kent_ptr = d_kent_ptr.upload(H.kent_ptr);
-    A.kterm_blk = d_kterm_blk.upload(H.kterm_blk);
-    A.kterm_coef = d_kterm_coef.upload(H.kterm_coef);
-    int mx = 0;
-    for (int jk = 0; jk < H.nang * H.nang; ++jk) {
-      int n = 0;
-      for (int e = H.kjk_ptr[jk]; e < H.kjk_ptr[jk + 1]; ++e) n += H.kent_ptr[e + 1] - H.kent_ptr[e];
-      mx = std::max(mx, n);
-    }
-    A.max_terms_per_jk = mx;
-    for (int ij = 0; ij < H.nang * H.nang; ++ij)
-      if (H.jbra_ptr[ij + 1] - H.jbra_ptr[ij] > 64) throw std::invalid_argument("too many Coulomb bra terms");
-    const size_t n2 = (size_t)A.nn * A.nn;
-    s_jin.alloc(sizeof(double) * A.nchan * A.nel * n2);
-    s_jscal.alloc(sizeof(double) * A.nchan * A.nel * 2);
-    s_khalo.alloc(sizeof(double) * (size_t)A.nel * A.nel * A.nang * A.nang * (2 * A.nn - 1));
-    s_bnorm.alloc(sizeof(double) * (size_t)A.nang * A.nang * NORM_SPLIT);
-    scr.jin = s_jin.as<double>();
-    scr.jscal = s_jscal.as<double>();
-    scr.khalo = s_khalo.as<double>();
-    scr.bnorm = s_bnorm.as<double>();
-    build_units();
-    on_device = true;
-  }
-
-  // Exchange work units: element pairs split into balanced ranges of output
-  // angular blocks (enough units to keep every SM busy to the end), then
-  // one unit per (diagonal element, output block); off-diagonal units first
-  // so the short diagonal ones fill the tail.
-  void build_units() {
-    const hfg::AtomHost& H = host;
-    const int nel = H.rad.nel, nang2 = H.nang * H.nang;
-    std::vector<int> cnt(nang2);
-    long tot = 0;
-    for (int jk = 0; jk < nang2; ++jk) {
-      cnt[jk] = H.kjk_ptr[jk + 1] - H.kjk_ptr[jk];
-      tot += cnt[jk];
-    }
-    auto ranges = [&](int nsplit) {
-      std::vector<int> cut(1, 0);
-      long acc = 0;
-      int s = 1;
-      for (int jk = 0; jk < nang2; ++jk) {
-        acc += cnt[jk];
-        if (s < nsplit && acc * nsplit >= tot * s) { cut.push_back(jk + 1); ++s; }
-      }
-      if (cut.back() != nang2) cut.push_back(nang2);
-      return cut;
-    };
-    auto make = [&](bool sym, std::vector<int>& dj) {
-      std::vector<int4> u;
-      const long npairs = sym ? (long)nel * (nel - 1) / 2 : (long)nel * (nel - 1);
-      int nsplit = (int)std::min<long>(std::max<long>(1, (2432 + npairs - 1) / std::max<long>(npairs, 1)), 8);
-      nsplit = std::min(nsplit, nang2);
-      const std::vector<int> cut = ranges(nsplit);
-      for (int a = 0; a < nel; ++a)
-        for (int b = 0; b < nel; ++b) {
-          if (a == b || (sym && b < a)) continue;
-          for (size_t s = 0; s + 1 < cut.size(); ++s)
-            if (cut[s + 1] > cut[s]) u.push_back(make_int4(a, b, cut[s], cut[s + 1]));
-        }
-      dj.clear();
-      for (int k = 0; k < H.nang; ++k)
-        for (int j = 0; j < H.nang; ++j)
-          if (!sym || j <= k) dj.push_back(j + k * H.nang);
-      for (int a = 0; a < nel; ++a)
-        for (int w = 0; w < (int)dj.size(); ++w) u.push_back(make_int4(a, a, w, w + 1));
-      return u;
-    };
-    std::vector<int> dja, djs;
-    std::vector<int4> ua = make(false, dja), us = make(true, djs);
-    units.all = d_units_all.upload(ua);
-    units.n_all = (int)ua.size();
-    units.sym = d_units_sym.upload(us);
-    units.n_sym = (int)us.size();
-    units.diag_all = d_diag_all.upload(dja);
-    units.diag_sym = d_diag_sym.upload(djs);
-  }
-
-  void setup_xc(int ldft, int mdft) {
-    host.build_dft_grid(ldft, mdft);
-    const hfg::AtomHost& H = host;
-    xc.nquad = H.nquad;
-    xc.nap = H.nap;
-    xc.wang = x_wang.upload(H.xc_wang);
-    xc.isin = x_isin.upload(H.xc_isin);
-    xc.W = x_W.upload(H.xc_W);
-    xc.Wt = x_Wt.upload(H.xc_Wt);
-    xc.Wp = x_Wp.upload(H.xc_Wp);
-    xc.r = x_r.upload(H.xc_r);
-    xc.wr = x_wr.upload(H.xc_wr);
-    xc.R = x_R.upload(H.xc_R);
-    xc.dR = x_dR.upload(H.xc_dR);
-    const size_t nel = H.rad.nel, nq = H.nquad, nab = (size_t)H.nang * H.nang, nap = H.nap;
-    xs_D.alloc(sizeof(double) * 2 * nel * nab * nq);
-    xs_Dr.alloc(sizeof(double) * 2 * nel * nab * nq);
-    xs_F.alloc(sizeof(double) * 8 * nel * nq * nap);
-    xs_U.alloc(sizeof(double) * 8 * nel * nab * nq);
-    xs_ep.alloc(sizeof(double) * 2 * nel * nq);
-    xs.D = xs_D.as<double>();
-    xs.Dr = xs_Dr.as<double>();
-    xs.F = xs_F.as<double>();
-    xs.U = xs_U.as<double>();
-    xs.epart = xs_ep.as<double>();
-    xc_ready = true;
-  }
-
-  void staging() {
-    const size_t bytes = sizeof(double) * (size_t)host.nbf * host.nbf;
-    if (h_in.n != bytes) h_in.alloc(bytes);
-    if (h_out.n != bytes) h_out.alloc(bytes);
-  }
-};
+using hfg_abi::g_err;
 
 namespace {
-
-void need(bool c, const char* msg) {
-  if (!c) throw std::invalid_argument(msg);
-}
 
 void write_full(const hfg_atom* a, const std::vector<double>& rad, double scale, const std::vector<double>* lrad,
                 double* out) {

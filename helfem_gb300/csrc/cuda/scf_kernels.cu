@@ -1,0 +1,82 @@
+// Small device kernels of the SCF driver: gathering a symmetry block out of
+// an AO matrix, scattering a block density back, the DIIS commutator in the
+// orthonormal basis and elementwise Fock assembly.
+#include "scf_kernels.cuh"
+
+namespace hfg {
+namespace {
+
+// angular-block indexed gather: Mk[r + c*nk] = M[ang[r/nrad]*nrad + r%nrad, ang[c/nrad]*nrad + c%nrad]
+__global__ void gather_block(const double* __restrict__ M, int nbf, int nrad, const int* __restrict__ ang, int nk,
+                             double* __restrict__ Mk) {
+  const size_t n = (size_t)nk * nk;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(idx % nk), c = (int)(idx / nk);
+    const size_t R = (size_t)ang[r / nrad] * nrad + r % nrad;
+    const size_t C = (size_t)ang[c / nrad] * nrad + c % nrad;
+    Mk[idx] = M[R + C * nbf];
+  }
+}
+
+__global__ void scatter_add_block(double* __restrict__ M, int nbf, int nrad, const int* __restrict__ ang, int nk,
+                                  const double* __restrict__ Mk, double alpha) {
+  const size_t n = (size_t)nk * nk;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(idx % nk), c = (int)(idx / nk);
+    const size_t R = (size_t)ang[r / nrad] * nrad + r % nrad;
+    const size_t C = (size_t)ang[c / nrad] * nrad + c % nrad;
+    M[R + C * nbf] += alpha * Mk[idx];
+  }
+}
+
+// E = G - G^T where G = W diag(occ) V^T  (W = F' V_occ): the commutator F'D' - D'F'
+__global__ void antisym(const double* __restrict__ G, int n, double* __restrict__ E) {
+  const size_t nn = (size_t)n * n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < nn; idx += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(idx % n), c = (int)(idx / n);
+    E[idx] = G[idx] - G[c + (size_t)r * n];
+  }
+}
+
+// out = a + b + c (+ d), any of c, d may be null
+__global__ void add4(double* __restrict__ out, const double* __restrict__ a, const double* __restrict__ b,
+                     const double* __restrict__ c, const double* __restrict__ d, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double v = a[i] + b[i];
+    if (c) v += c[i];
+    if (d) v += d[i];
+    out[i] = v;
+  }
+}
+
+// columns scaled: Y[:, j] = X[:, j] * s[j]
+__global__ void scale_cols(const double* __restrict__ X, int n, int m, const double* __restrict__ s,
+                           double* __restrict__ Y) {
+  const size_t nn = (size_t)n * m;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < nn; idx += (size_t)gridDim.x * blockDim.x)
+    Y[idx] = X[idx] * s[idx / n];
+}
+
+inline int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
+
+}  // namespace
+
+void k_gather_block(const double* M, int nbf, int nrad, const int* ang, int nk, double* Mk, cudaStream_t st) {
+  gather_block<<<grid_for((size_t)nk * nk), 256, 0, st>>>(M, nbf, nrad, ang, nk, Mk);
+}
+void k_scatter_add_block(double* M, int nbf, int nrad, const int* ang, int nk, const double* Mk, double alpha,
+                         cudaStream_t st) {
+  scatter_add_block<<<grid_for((size_t)nk * nk), 256, 0, st>>>(M, nbf, nrad, ang, nk, Mk, alpha);
+}
+void k_antisym(const double* G, int n, double* E, cudaStream_t st) {
+  antisym<<<grid_for((size_t)n * n), 256, 0, st>>>(G, n, E);
+}
+void k_add4(double* out, const double* a, const double* b, const double* c, const double* d, size_t n,
+            cudaStream_t st) {
+  add4<<<grid_for(n), 256, 0, st>>>(out, a, b, c, d, n);
+}
+void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cudaStream_t st) {
+  scale_cols<<<grid_for((size_t)n * m), 256, 0, st>>>(X, n, m, s, Y);
+}
+
+}  // namespace hfg

@@ -1,0 +1,19 @@
+// Launchers of the SCF driver's small device kernels (scf_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstddef>
+
+namespace hfg {
+
+void k_gather_block(const double* M, int nbf, int nrad, const int* ang, int nk, double* Mk, cudaStream_t st);
+void k_scatter_add_block(double* M, int nbf, int nrad, const int* ang, int nk, const double* Mk, double alpha,
+                         cudaStream_t st);
+void k_antisym(const double* G, int n, double* E, cudaStream_t st);
+void k_add4(double* out, const double* a, const double* b, const double* c, const double* d, size_t n,
+            cudaStream_t st);
+void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cudaStream_t st);
+
+}  // namespace hfg

@@ -1,0 +1,475 @@
+// Atomic SCF on the device: the Fock-builder loop of the reference's atomic
+// driver (src/atomic/main.cpp:369-470) with its per-symmetry-block
+// orthonormalisation and diagonalisation (src/general/scf_driver_common.h:
+// 176-187, 406-445, 459-520; src/general/scf_helpers.cpp:41-50).
+//
+// The reference hands convergence to OpenOrbitalOptimizer (DIIS, ODA, CG);
+// converged energies do not depend on the accelerator, so this driver uses
+// Pulay DIIS on the orthonormal-basis Fock blocks with Aufbau occupations
+// across blocks (or fixed per-block counts, the reference's --readocc).
+//
+// Everything large stays on the device: P, J, K, Vxc, F (nbf x nbf), the
+// orthonormal blocks and the DIIS history. Two structural facts cut the FP64
+// work of the diagonalisation step on GB300 (FP64 ~1/64 of FP32):
+//  * S is block diagonal with one radial block per angular function, so the
+//    block orthonormaliser is I (x) X_rad with X_rad = invh(S_rad); the
+//    transform X^T F X is two strided-batched nrad-sized GEMMs per block
+//    instead of two dense block GEMMs;
+//  * only occupied orbitals are back-transformed and used for P.
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <numeric>
+
+#include "cuda/scf_kernels.cuh"
+#include "handle.hpp"
+
+namespace {
+
+void cb(cublasStatus_t s, const char* what) {
+  if (s != CUBLAS_STATUS_SUCCESS) throw hfg_abi::CudaError(std::string(what) + ": cuBLAS status " + std::to_string((int)s));
+}
+void cs(cusolverStatus_t s, const char* what) {
+  if (s != CUSOLVER_STATUS_SUCCESS)
+    throw hfg_abi::CudaError(std::string(what) + ": cuSOLVER status " + std::to_string((int)s));
+}
+
+struct Handles {
+  cublasHandle_t bl = nullptr;
+  cusolverDnHandle_t so = nullptr;
+  ~Handles() {
+    if (bl) cublasDestroy(bl);
+    if (so) cusolverDnDestroy(so);
+  }
+};
+
+struct Block {
+  int key = 0;                // m (symmetry 1) or angular index (symmetry 2)
+  std::vector<int> ang;       // angular functions in the block
+  int nk = 0;                 // ang.size() * nrad
+  DBuf d_ang;
+  size_t off = 0;             // offset of the block in a flattened block vector
+};
+
+// symmetric eigensolve of an n x n device matrix in place (eigenvectors)
+struct Eigh {
+  DBuf work, info;
+  int lwork = 0;
+  void run(cusolverDnHandle_t h, double* A, int n, double* w) {
+    int lw = 0;
+    cs(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, A, n, w, &lw),
+       "syevd buffer size");
+    if (lw > lwork) {
+      work.alloc(sizeof(double) * (size_t)lw);
+      lwork = lw;
+    }
+    if (!info.p) info.alloc(sizeof(int));
+    cs(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, A, n, w, work.as<double>(), lwork,
+                        info.as<int>()),
+       "syevd");
+  }
+};
+
+}  // namespace
+
+extern "C" hfg_status hfg_scf_run(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, double* orbital_energies,
+                                  void* stream) {
+  return guard([&] {
+    need(a && d && res, "hfg_scf_run: null argument");
+    a->check_device();
+    const hfg::AtomHost& H = a->host;
+    const int nbf = H.nbf, nrad = H.rad.nrad, nang = H.nang;
+    const bool restricted = d->restricted != 0;
+    const int nspin = restricted ? 1 : 2;
+    need(d->nela >= 0 && d->nelb >= 0 && d->nela + d->nelb > 0, "hfg_scf_run: no electrons");
+    need(d->symmetry == 1 || d->symmetry == 2, "hfg_scf_run: symmetry must be 1 (per m) or 2 (per l,m)");
+    const bool have_xc = d->x_func != 0 || d->c_func != 0;
+    need(hfg::xc_func_supported(d->x_func) && hfg::xc_func_supported(d->c_func), "hfg_scf_run: unsupported functional");
+    const double kfrac = d->kfrac >= 0 ? d->kfrac : (have_xc ? 0.0 : 1.0);
+    const int maxiter = d->maxiter > 0 ? d->maxiter : 200;
+    const double etol = d->e_tol > 0 ? d->e_tol : 1e-10;
+    const double dtol = d->diis_tol > 0 ? d->diis_tol : 1e-7;
+    const double thr = d->dftthr > 0 ? d->dftthr : 1e-12;
+    cudaStream_t st = stream ? (cudaStream_t)stream : a->own_stream;
+    if (have_xc && !a->xc_ready) a->setup_xc(0, 0);
+
+    Handles hd;
+    cb(cublasCreate(&hd.bl), "cublasCreate");
+    cb(cublasSetStream(hd.bl, st), "cublasSetStream");
+    cs(cusolverDnCreate(&hd.so), "cusolverDnCreate");
+    cs(cusolverDnSetStream(hd.so, st), "cusolverDnSetStream");
+
+    // ---- symmetry blocks (TwoDBasis.cpp:218-232: unique m ascending) ----
+    std::vector<Block> blocks;
+    if (d->symmetry == 1) {
+      std::map<int, std::vector<int>> bym;
+      for (int i = 0; i < nang; ++i) bym[H.mval[i]].push_back(i);
+      for (auto& kv : bym) {
+        Block b;
+        b.key = kv.first;
+        b.ang = kv.second;
+        blocks.push_back(std::move(b));
+      }
+    } else {
+      for (int i = 0; i < nang; ++i) {
+        Block b;
+        b.key = i;
+        b.ang = {i};
+        blocks.push_back(std::move(b));
+      }
+    }
+    const int nblk = (int)blocks.size();
+    size_t Lblk = 0;
+    int nkmax = 0;
+    for (auto& b : blocks) {
+      b.nk = (int)b.ang.size() * nrad;
+      b.off = Lblk;
+      Lblk += (size_t)b.nk * b.nk;
+      nkmax = std::max(nkmax, b.nk);
+      b.d_ang.upload(b.ang);
+    }
+    if (d->fixed_occ) need(d->n_fixed_blocks == nblk, "hfg_scf_run: fixed_occ needs one (alpha, beta) pair per block");
+
+    // ---- radial orthonormaliser X = invh(S_rad) (utils.cpp:120-159) ----
+    const size_t nr2 = (size_t)nrad * nrad, nb2 = (size_t)nbf * nbf;
+    DBuf dX, dtmp, dw;
+    {
+      std::vector<double> S(H.Srad), dn(nrad);
+      for (int i = 0; i < nrad; ++i) dn[i] = 1.0 / std::sqrt(S[i + (size_t)i * nrad]);
+      for (int c = 0; c < nrad; ++c)
+        for (int r = 0; r < nrad; ++r) S[r + (size_t)c * nrad] *= dn[r] * dn[c];
+      DBuf dS;
+      double* Sd = dS.upload(S);
+      dw.alloc(sizeof(double) * nrad);
+      Eigh eg;
+      eg.run(hd.so, Sd, nrad, dw.as<double>());
+      std::vector<double> U(nr2), lam(nrad);
+      ck(cudaMemcpyAsync(U.data(), Sd, sizeof(double) * nr2, cudaMemcpyDeviceToHost, st), "D2H");
+      ck(cudaMemcpyAsync(lam.data(), dw.p, sizeof(double) * nrad, cudaMemcpyDeviceToHost, st), "D2H");
+      ck(cudaStreamSynchronize(st), "sync");
+      need(lam[0] > 0, "hfg_scf_run: overlap matrix is not positive definite");
+      std::vector<double> X(nr2, 0.0), Ul(nr2);
+      for (int k = 0; k < nrad; ++k) {
+        const double f = 1.0 / std::sqrt(lam[k]);
+        for (int r = 0; r < nrad; ++r) Ul[r + (size_t)k * nrad] = U[r + (size_t)k * nrad] * f;
+      }
+      // X = diag(dn) U diag(lam^-1/2) U^T, formed on the host (nrad^3, once)
+      for (int c = 0; c < nrad; ++c)
+        for (int k = 0; k < nrad; ++k) {
+          const double u = U[c + (size_t)k * nrad];
+          for (int r = 0; r < nrad; ++r) X[r + (size_t)c * nrad] += Ul[r + (size_t)k * nrad] * u;
+        }
+      for (int c = 0; c < nrad; ++c)
+        for (int r = 0; r < nrad; ++r) X[r + (size_t)c * nrad] *= dn[r];
+      dX.upload(X);
+    }
+
+    // ---- one-electron matrices on the device ----
+    std::vector<double> hT(nb2, 0.0), hV(nb2, 0.0);
+    for (int ia = 0; ia < nang; ++ia) {
+      const double lf = (double)H.lval[ia] * (H.lval[ia] + 1);
+      for (int c = 0; c < nrad; ++c)
+        for (int r = 0; r < nrad; ++r) {
+          const size_t o = (size_t)(ia * nrad + c) * nbf + ia * nrad + r, q = r + (size_t)c * nrad;
+          hT[o] = H.Trad[q] + lf * H.Tlrad[q];
+          hV[o] = -(double)H.Z * H.Vrad[q];
+        }
+    }
+    DBuf dT, dV, dH, dP, dPs[2], dJ, dK[2], dXC[2], dF[2], dE;
+    double* T = dT.upload(hT);
+    double* V = dV.upload(hV);
+    hT.clear();
+    hV.clear();
+    dH.alloc(sizeof(double) * nb2);
+    hfg::k_add4(dH.as<double>(), T, V, nullptr, nullptr, nb2, st);
+    dP.alloc(sizeof(double) * nb2);
+    dJ.alloc(sizeof(double) * nb2);
+    dE.alloc(sizeof(double) * 2);
+    for (int s = 0; s < 2; ++s) {
+      dPs[s].alloc(sizeof(double) * nb2);
+      dF[s].alloc(sizeof(double) * nb2);
+      if (kfrac != 0.0) dK[s].alloc(sizeof(double) * nb2);
+      if (have_xc) dXC[s].alloc(sizeof(double) * nb2);
+    }
+
+    // ---- per-iteration block buffers ----
+    const size_t Ltot = Lblk * nspin;
+    DBuf dFo, dEo, dFk, dT1, dVec, dW, dG, dCo, deps;
+    dFo.alloc(sizeof(double) * Ltot);  // orthonormal Fock blocks (current)
+    dEo.alloc(sizeof(double) * Ltot);  // DIIS errors (current)
+    dFk.alloc(sizeof(double) * (size_t)nkmax * nkmax);
+    dT1.alloc(sizeof(double) * (size_t)nkmax * nkmax);
+    dVec.alloc(sizeof(double) * Ltot);  // eigenvectors, per spin and block
+    dW.alloc(sizeof(double) * (size_t)nkmax * nkmax);
+    dG.alloc(sizeof(double) * (size_t)nkmax * nkmax);
+    dCo.alloc(sizeof(double) * (size_t)nkmax * nkmax);
+    deps.alloc(sizeof(double) * (size_t)nbf * nspin);
+    const int nhist = 8;
+    std::vector<DBuf> hF(nhist), hE(nhist);
+    for (int i = 0; i < nhist; ++i) {
+      hF[i].alloc(sizeof(double) * Ltot);
+      hE[i].alloc(sizeof(double) * Ltot);
+    }
+    Eigh eg;
+    const double one = 1.0, zero = 0.0;
+
+    // X^T M_k X for block k of AO matrix M into out (nk x nk)
+    auto to_ortho = [&](const double* M, const Block& b, double* out) {
+      hfg::k_gather_block(M, nbf, nrad, b.d_ang.as<int>(), b.nk, dFk.as<double>(), st);
+      const int p = (int)b.ang.size(), nk = b.nk;
+      cb(cublasDgemmStridedBatched(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, nk, nrad, nrad, &one, dFk.as<double>(), nk,
+                                   (long long)nrad * nk, dX.as<double>(), nrad, 0, &zero, dT1.as<double>(), nk,
+                                   (long long)nrad * nk, p),
+         "F X");
+      cb(cublasDgemmStridedBatched(hd.bl, CUBLAS_OP_T, CUBLAS_OP_N, nrad, nk, nrad, &one, dX.as<double>(), nrad, 0,
+                                   dT1.as<double>(), nk, nrad, &zero, out, nk, nrad, p),
+         "X^T F X");
+    };
+
+    // orbitals: eps (all blocks, per spin), occupations
+    std::vector<double> eps((size_t)nbf * nspin);
+    std::vector<std::vector<std::vector<double>>> occ(nspin, std::vector<std::vector<double>>(nblk));
+
+    auto diagonalise = [&](const double* Fo_all, int s) {
+      double* Vs = dVec.as<double>() + Lblk * s;
+      ck(cudaMemcpyAsync(Vs, Fo_all + Lblk * s, sizeof(double) * Lblk, cudaMemcpyDeviceToDevice, st), "copy");
+      size_t eo = 0;
+      for (auto& b : blocks) {
+        eg.run(hd.so, Vs + b.off, b.nk, deps.as<double>() + (size_t)nbf * s + eo);
+        eo += b.nk;
+      }
+    };
+
+    auto occupy = [&]() {
+      ck(cudaMemcpyAsync(eps.data(), deps.p, sizeof(double) * eps.size(), cudaMemcpyDeviceToHost, st), "D2H eps");
+      ck(cudaStreamSynchronize(st), "sync");
+      const double maxocc = restricted ? 2.0 : 1.0;
+      for (int s = 0; s < nspin; ++s) {
+        size_t eo = 0;
+        std::vector<std::pair<double, std::pair<int, int>>> all;
+        for (int k = 0; k < nblk; ++k) {
+          occ[s][k].assign(blocks[k].nk, 0.0);
+          for (int i = 0; i < blocks[k].nk; ++i) all.push_back({eps[(size_t)nbf * s + eo + i], {k, i}});
+          eo += blocks[k].nk;
+        }
+        if (d->fixed_occ) {
+          for (int k = 0; k < nblk; ++k) {
+            double left = restricted ? d->fixed_occ[2 * k] + d->fixed_occ[2 * k + 1] : d->fixed_occ[2 * k + s];
+            for (int i = 0; i < blocks[k].nk && left > 0; ++i) {
+              occ[s][k][i] = std::min(maxocc, left);
+              left -= occ[s][k][i];
+            }
+          }
+        } else {
+          std::stable_sort(all.begin(), all.end(), [](auto& x, auto& y) { return x.first < y.first; });
+          double left = restricted ? (double)(d->nela + d->nelb) : (s == 0 ? d->nela : d->nelb);
+          for (auto& e : all) {
+            if (left <= 0) break;
+            const double o = std::min(maxocc, left);
+            occ[s][e.second.first][e.second.second] = o;
+            left -= o;
+          }
+        }
+      }
+    };
+
+    // P_s = sum_k C_occ diag(occ) C_occ^T, C = (I (x) X) V
+    auto build_density = [&]() {
+      for (int s = 0; s < nspin; ++s) {
+        double* P = dPs[s].as<double>();
+        ck(cudaMemsetAsync(P, 0, sizeof(double) * nb2, st), "memset");
+        for (int k = 0; k < nblk; ++k) {
+          const Block& b = blocks[k];
+          int nocc = 0;
+          while (nocc < b.nk && occ[s][k][nocc] > 0) ++nocc;
+          if (nocc == 0) continue;
+          const double* Vk = dVec.as<double>() + Lblk * s + b.off;
+          const int p = (int)b.ang.size(), nk = b.nk;
+          // C_occ = (I x X) V_occ : nk x nocc
+          cb(cublasDgemmStridedBatched(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, nrad, nocc, nrad, &one, dX.as<double>(), nrad,
+                                       0, Vk, nk, nrad, &zero, dCo.as<double>(), nk, nrad, p),
+             "X V");
+          std::vector<double> o(occ[s][k].begin(), occ[s][k].begin() + nocc);
+          DBuf dO;
+          dO.upload(o);
+          hfg::k_scale_cols(dCo.as<double>(), nk, nocc, dO.as<double>(), dW.as<double>(), st);
+          cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_T, nk, nk, nocc, &one, dW.as<double>(), nk, dCo.as<double>(),
+                         nk, &zero, dG.as<double>(), nk),
+             "C occ C^T");
+          hfg::k_scatter_add_block(P, nbf, nrad, b.d_ang.as<int>(), nk, dG.as<double>(), 1.0, st);
+        }
+      }
+      if (restricted) {
+        // P is the total density; the spin density for K is P/2
+        ck(cudaMemcpyAsync(dP.p, dPs[0].p, sizeof(double) * nb2, cudaMemcpyDeviceToDevice, st), "copy");
+        const double half = 0.5;
+        cb(cublasDscal(hd.bl, (int)std::min<size_t>(nb2, 0x7fffffff), &half, dPs[0].as<double>(), 1), "scal");
+        if (nb2 > 0x7fffffff) throw std::invalid_argument("basis too large for this driver");
+      } else {
+        hfg::k_add4(dP.as<double>(), dPs[0].as<double>(), dPs[1].as<double>(), nullptr, nullptr, nb2, st);
+      }
+    };
+
+    auto dot = [&](const double* x, const double* y) {
+      double r = 0.0;
+      cb(cublasDdot(hd.bl, (int)nb2, x, 1, y, 1, &r), "ddot");
+      return r;
+    };
+
+    // ---- core-Hamiltonian guess (iguess 0) ----
+    for (int s = 0; s < nspin; ++s)
+      for (auto& b : blocks) to_ortho(dH.as<double>(), b, dFo.as<double>() + Lblk * s + b.off);
+    for (int s = 0; s < nspin; ++s) diagonalise(dFo.as<double>(), s);
+    occupy();
+    build_density();
+
+    double Eold = 0.0;
+    int it = 0, nh = 0;
+    bool converged = false;
+    double Ekin = 0, Enuc = 0, Ecoul = 0, Exx = 0, Exc = 0, Ngrid = 0, Etot = 0;
+    for (it = 1; it <= maxiter; ++it) {
+      // ---- Fock build (main.cpp:386-446) ----
+      ck(hfg::launch_coulomb_fp64(a->dev, a->scr, dP.as<double>(), dJ.as<double>(), true, st, &a->prof), "J");
+      if (kfrac != 0.0)
+        for (int s = 0; s < nspin; ++s)
+          ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, dPs[s].as<double>(), dK[s].as<double>(), true, st,
+                                       &a->prof),
+             "K");
+      if (have_xc)
+        ck(hfg::launch_xc_fp64(a->dev, a->xc, a->xs, d->x_func, d->c_func,
+                               restricted ? dP.as<double>() : dPs[0].as<double>(),
+                               restricted ? nullptr : dPs[1].as<double>(), dXC[0].as<double>(),
+                               restricted ? nullptr : dXC[1].as<double>(), dE.as<double>(), thr, st),
+           "XC");
+      for (int s = 0; s < nspin; ++s) {
+        if (kfrac != 0.0 && kfrac != 1.0) {
+          cb(cublasDscal(hd.bl, (int)nb2, &kfrac, dK[s].as<double>(), 1), "scal K");
+        }
+        hfg::k_add4(dF[s].as<double>(), dH.as<double>(), dJ.as<double>(),
+                    kfrac != 0.0 ? dK[s].as<double>() : nullptr, have_xc ? dXC[s].as<double>() : nullptr, nb2, st);
+      }
+      Ekin = dot(dP.as<double>(), T);
+      Enuc = dot(dP.as<double>(), V);
+      Ecoul = 0.5 * dot(dP.as<double>(), dJ.as<double>());
+      Exx = 0.0;
+      if (kfrac != 0.0) {
+        Exx = 0.5 * dot(dPs[0].as<double>(), dK[0].as<double>());
+        Exx = restricted ? 2.0 * Exx : Exx + 0.5 * dot(dPs[1].as<double>(), dK[1].as<double>());
+      }
+      if (have_xc) {
+        double e[2];
+        ck(cudaMemcpyAsync(e, dE.p, sizeof(e), cudaMemcpyDeviceToHost, st), "D2H");
+        ck(cudaStreamSynchronize(st), "sync");
+        Exc = e[0];
+        Ngrid = e[1];
+      }
+      Etot = Ekin + Enuc + Ecoul + Exx + Exc;
+
+      // ---- orthonormal Fock blocks and DIIS errors F'D' - D'F' ----
+      double emax = 0.0;
+      for (int s = 0; s < nspin; ++s)
+        for (int k = 0; k < nblk; ++k) {
+          const Block& b = blocks[k];
+          double* Fo = dFo.as<double>() + Lblk * s + b.off;
+          double* Eo = dEo.as<double>() + Lblk * s + b.off;
+          to_ortho(dF[s].as<double>(), b, Fo);
+          int nocc = 0;
+          while (nocc < b.nk && occ[s][k][nocc] > 0) ++nocc;
+          if (nocc == 0) {
+            ck(cudaMemsetAsync(Eo, 0, sizeof(double) * b.nk * b.nk, st), "memset");
+            continue;
+          }
+          const double* Vk = dVec.as<double>() + Lblk * s + b.off;
+          // W = F' V_occ diag(occ);  G = W V_occ^T;  E = G - G^T
+          cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, b.nk, nocc, b.nk, &one, Fo, b.nk, Vk, b.nk, &zero,
+                         dW.as<double>(), b.nk),
+             "F' V");
+          std::vector<double> o(occ[s][k].begin(), occ[s][k].begin() + nocc);
+          DBuf dO;
+          dO.upload(o);
+          hfg::k_scale_cols(dW.as<double>(), b.nk, nocc, dO.as<double>(), dCo.as<double>(), st);
+          cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_T, b.nk, b.nk, nocc, &one, dCo.as<double>(), b.nk, Vk, b.nk,
+                         &zero, dG.as<double>(), b.nk),
+             "G");
+          hfg::k_antisym(dG.as<double>(), b.nk, Eo, st);
+        }
+      {
+        int imax = 0;
+        cb(cublasIdamax(hd.bl, (int)Ltot, dEo.as<double>(), 1, &imax), "idamax");
+        ck(cudaMemcpyAsync(&emax, dEo.as<double>() + (imax - 1), sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        ck(cudaStreamSynchronize(st), "sync");
+        emax = std::fabs(emax);
+      }
+      if (it > 1 && std::fabs(Etot - Eold) < etol && emax < dtol) {
+        converged = true;
+        break;
+      }
+      Eold = Etot;
+
+      // ---- DIIS extrapolation ----
+      const int slot = (nh < nhist) ? nh : (it - 1) % nhist;
+      ck(cudaMemcpyAsync(hF[slot].p, dFo.p, sizeof(double) * Ltot, cudaMemcpyDeviceToDevice, st), "copy");
+      ck(cudaMemcpyAsync(hE[slot].p, dEo.p, sizeof(double) * Ltot, cudaMemcpyDeviceToDevice, st), "copy");
+      if (nh < nhist) ++nh;
+      std::vector<double> B((size_t)(nh + 1) * (nh + 1), -1.0), rhs(nh + 1, 0.0);
+      B[(size_t)nh * (nh + 1) + nh] = 0.0;
+      rhs[nh] = -1.0;
+      for (int i = 0; i < nh; ++i)
+        for (int j = 0; j <= i; ++j) {
+          double r = 0.0;
+          cb(cublasDdot(hd.bl, (int)Ltot, hE[i].as<double>(), 1, hE[j].as<double>(), 1, &r), "ddot");
+          B[i + (size_t)j * (nh + 1)] = B[j + (size_t)i * (nh + 1)] = r;
+        }
+      // small dense solve (Gaussian elimination with partial pivoting)
+      std::vector<double> c(rhs);
+      {
+        const int n = nh + 1;
+        std::vector<double> M(B);
+        bool ok = true;
+        for (int col = 0; col < n && ok; ++col) {
+          int piv = col;
+          for (int r = col + 1; r < n; ++r)
+            if (std::fabs(M[r + (size_t)col * n]) > std::fabs(M[piv + (size_t)col * n])) piv = r;
+          if (std::fabs(M[piv + (size_t)col * n]) < 1e-300) { ok = false; break; }
+          for (int k = 0; k < n; ++k) std::swap(M[col + (size_t)k * n], M[piv + (size_t)k * n]);
+          std::swap(c[col], c[piv]);
+          for (int r = col + 1; r < n; ++r) {
+            const double f = M[r + (size_t)col * n] / M[col + (size_t)col * n];
+            for (int k = col; k < n; ++k) M[r + (size_t)k * n] -= f * M[col + (size_t)k * n];
+            c[r] -= f * c[col];
+          }
+        }
+        if (ok) {
+          for (int r = n - 1; r >= 0; --r) {
+            double v = c[r];
+            for (int k = r + 1; k < n; ++k) v -= M[r + (size_t)k * n] * c[k];
+            c[r] = v / M[r + (size_t)r * n];
+          }
+        } else {
+          std::fill(c.begin(), c.end(), 0.0);
+          c[slot] = 1.0;
+        }
+      }
+      ck(cudaMemsetAsync(dFo.p, 0, sizeof(double) * Ltot, st), "memset");
+      for (int i = 0; i < nh; ++i)
+        cb(cublasDaxpy(hd.bl, (int)Ltot, &c[i], hF[i].as<double>(), 1, dFo.as<double>(), 1), "axpy");
+      for (int s = 0; s < nspin; ++s) diagonalise(dFo.as<double>(), s);
+      occupy();
+      build_density();
+    }
+    ck(cudaStreamSynchronize(st), "sync");
+    res->Etot = Etot;
+    res->Ekin = Ekin;
+    res->Enuc = Enuc;
+    res->Ecoul = Ecoul;
+    res->Exx = Exx;
+    res->Exc = Exc;
+    res->Nel_grid = Ngrid;
+    res->iterations = std::min(it, maxiter);
+    res->converged = converged ? 1 : 0;
+    if (orbital_energies) std::memcpy(orbital_energies, eps.data(), sizeof(double) * eps.size());
+  });
+}

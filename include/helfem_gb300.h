@@ -194,6 +194,39 @@ typedef struct {
 } hfg_work_t;
 hfg_status hfg_atom_work(const hfg_atom* atom, hfg_work_t* work);
 
+/* ---- atomic SCF on the device ----
+ * The Fock-builder loop of the reference's atomic driver
+ * (src/atomic/main.cpp:369-470) with per-symmetry-block orthonormalisation
+ * and diagonalisation (src/general/scf_driver_common.h:176-187, 406-520) and
+ * the energy decomposition (main.cpp:410-446). Convergence: Pulay DIIS in
+ * the orthonormal basis (the reference delegates to OpenOrbitalOptimizer;
+ * converged energies do not depend on the accelerator). Core-Hamiltonian
+ * guess. Energies in hartree. */
+typedef struct {
+  int nela, nelb;          /* alpha / beta electrons                          */
+  int restricted;          /* 1: closed-shell P (max occupation 2)            */
+  int symmetry;            /* 1: blocks per m (reference default), 2: per (l,m) */
+  int x_func, c_func;      /* XC functional ids (0, 0 = Hartree-Fock)         */
+  double kfrac;            /* exact-exchange fraction; < 0 -> 1 for HF, 0 for DFT */
+  int maxiter;             /* 0 -> 200                                        */
+  double e_tol;            /* |dE| convergence; 0 -> 1e-10                    */
+  double diis_tol;         /* max |F'D' - D'F'|; 0 -> 1e-7                    */
+  const int* fixed_occ;    /* NULL: Aufbau; else [n_fixed_blocks][2] (alpha, beta)
+                              electrons per block, blocks in ascending m (the
+                              reference's --readocc)                           */
+  int n_fixed_blocks;
+  double dftthr;           /* density threshold; 0 -> 1e-12                   */
+} hfg_scf_desc;
+typedef struct {
+  double Etot, Ekin, Enuc, Ecoul, Exx, Exc, Nel_grid;
+  int iterations, converged;
+} hfg_scf_result;
+/* orbital_energies (host, may be NULL): nbf per spin, blocks concatenated in
+ * block order, ascending within a block. Runs on `stream` (NULL: the
+ * handle's stream) and returns when converged or out of iterations. */
+hfg_status hfg_scf_run(hfg_atom* atom, const hfg_scf_desc* desc, hfg_scf_result* result,
+                       double* orbital_energies, void* stream);
+
 /* ---- per-kernel timing (counterpart of the reference's scf_driver::FockTimer,
  * src/general/scf_driver_common.h:69-170) ----
  * Kernel classes: 0 J contraction, 1 J scatter, 2 K block norms,
