@@ -30,7 +30,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "Fock builds/s (J+K, plain FP64)"
+METRIC = "Fock builds/s (J+K)"
 UNIT = "builds/s"
 WORKLOAD = ("Kr (Z=36) J+K Fock build: 40 elements r_i=61^(i/40)-1, 15-node LIP, l<=2, m<=2, "
             "Nbf=5031, L<=4, P=CC^T (18 cols, N(0,1), seed 12345, Loewdin in S)")
@@ -168,6 +168,29 @@ def fp64_peak_tflops(torch) -> float:
     return best
 
 
+def fp32_peak_tflops(torch) -> float:
+    """cuBLAS SGEMM with TF32 disabled: the FP32-pipe denominator."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        a @ b
+        torch.cuda.synchronize()
+        best = 0.0
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+        return best
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 def profiled_traffic():
     """Per-launch DRAM bytes of k_tiles from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_tiles_kr.txt")
@@ -242,9 +265,36 @@ def run_ours(args):
     Jd, Kd = torch.empty_like(Pd), torch.empty_like(Pd)
     stream = torch.cuda.current_stream()
 
-    def step():
+    split = not args.plain
+
+    def step(split_k=split):
         atom.coulomb(Pd, Jd, stream)
-        atom.exchange(Pd, Kd, stream, symmetric=True)  # P = C C^T is symmetric
+        atom.exchange(Pd, Kd, stream, symmetric=True, split=split_k)  # P = C C^T is symmetric
+
+    # plain FP64 beside the split form: rate and the split error on this density
+    plain = None
+    if split:
+        K64 = torch.empty_like(Pd)
+        for _ in range(args.warmup):
+            step(False)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(args.steps):
+            step(False)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        K64.copy_(Kd)
+        step(True)
+        torch.cuda.synchronize()
+        dK = Kd - K64
+        plain = {"value": args.steps / (p0.elapsed_time(p1) * 1e-3), "unit": UNIT,
+                 "ms_per_step": p0.elapsed_time(p1) / args.steps,
+                 "split_error_vs_fp64": {
+                     "k_max_rel": float(dK.abs().max() / K64.abs().max()),
+                     "exchange_energy_abs_eh": abs(0.5 * float((Pd * dK).sum())),
+                     "exchange_energy_eh": 0.5 * float((Pd * K64).sum())}}
+        del K64, dK
 
     for _ in range(args.warmup):
         step()
@@ -280,14 +330,14 @@ def run_ours(args):
     Ph, Jh, Kh = pinned(), pinned(), pinned()
     Ph[...] = P
     atom.coulomb_host(Ph, out=Jh)
-    atom.exchange_host(Ph, out=Kh)
+    atom.exchange_host(Ph, out=Kh, symmetric=True, split=split)
     ne = args.e2e_steps
     if dist is not None:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(ne):
         atom.coulomb_host(Ph, out=Jh)
-        atom.exchange_host(Ph, out=Kh)
+        atom.exchange_host(Ph, out=Kh, symmetric=True, split=split)
     te = max(time.perf_counter() - t0, 1e-30)
     if dist is not None:
         t = torch.tensor([te], device="cuda", dtype=torch.float64)
@@ -295,7 +345,7 @@ def run_ours(args):
         te = float(t.item())
     e2e = {"value": ws * ne / te if ne else None, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nbf * nbf,
            "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
-           "path": "hfg_coulomb_host + hfg_exchange_host (pinned host P, J, K)"}
+           "path": "hfg_coulomb_host + hfg_exchange_host_ex (pinned host P, J, K; same K form as value)"}
 
     if rank != 0:
         if dist is not None:
@@ -306,21 +356,35 @@ def run_ours(args):
     n_off, ms_off = prof["k_tiles"]
     off_ms = ms_off / max(n_off, 1)
     kflops = work["k_offdiag_sym_flops"] + work["k_diag_sym_flops"]
-    achieved = kflops / (off_ms * 1e-3) / 1e12
+    achieved = kflops / (off_ms * 1e-3) / 1e12  # FP64-equivalent algorithmic FLOPs
     peak = fp64_peak_tflops(torch)
+    fp32 = fp32_peak_tflops(torch)
     traffic = profiled_traffic()
     hbm_peak = measured_peaks().get("hbm_gbs")
     kernel_ms = {k: (v[1] / max(v[0], 1)) for k, v in prof.items()}
-    roofline = {
-        "bound": "fp64", "kernel": "k_tiles", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-        "frac": achieved / peak if peak else None,
-        "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (no FP64 figure in MEASURED_PEAKS.json)",
+    if split:
+        # ~12 FP32 instructions per FP64-equivalent FMA (TwoProd + TwoSum), 2 FLOPs per FMA
+        fp32_rate = achieved * 12.0 / 2.0 * 2.0
+        roofline = {
+            "bound": "fp32", "kernel": "k_tiles_split", "achieved": fp32_rate, "peak": fp32, "unit": "TFLOP/s",
+            "frac": fp32_rate / fp32 if fp32 else None,
+            "achieved_fp64_equivalent_tflops": achieved,
+            "fp64_peak_tflops": peak,
+            "peak_source": "measured in this run: cuBLAS SGEMM 8192^3 with TF32 off (FP32 pipe)",
+            "achieved_note": "FP32 rate = FP64-equivalent algorithmic FLOP rate x 12 FP32 instructions per "
+                             "emulated multiply-add",
+        }
+    else:
+        roofline = {"bound": "fp64", "kernel": "k_tiles", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak if peak else None,
+                    "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (no FP64 figure in MEASURED_PEAKS.json)"}
+    roofline.update({
         "flops_per_launch": kflops, "ms_per_launch": off_ms,
         "traffic": traffic,
         "hbm": {"achieved_gbs": (work["k_bytes"] / 2) / (off_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
-                "note": "k_tiles reads P once; HBM is not its bound"},
+                "note": "the tile kernel reads P once; HBM is not its bound"},
         "kernel_ms_per_launch": kernel_ms,
-    }
+    })
     if args.cpu_seconds > 0:
         cpu_rate, cpu_n, cpu_dt, cpu_threads = cpu_reference_builds(args.cpu_seconds, 1000)
     else:
@@ -332,6 +396,8 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "nbf": nbf, "parallelism": f"replicas x{ws}",
                    "inputs_vs_l2": "P is 202 MB > 129 MB L2: no flush needed"},
         "roofline": roofline,
+        "form": "split precision (FP32-pair contraction, FP64 recombination)" if split else "plain FP64",
+        "plain_fp64": plain,
         "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_n} full-size Kr J+K builds in {cpu_dt:.1f} s (oracle, OpenMP)"},
         "e2e": e2e,
@@ -352,6 +418,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="seconds of oracle builds for cpu_baseline (0 skips it)")
     ap.add_argument("--e2e-steps", type=int, default=10, help="host-pointer drop-in steps (0 skips)")
+    ap.add_argument("--plain", action="store_true", help="time the plain FP64 form only")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -70,6 +70,7 @@ _SIGS = {
     "hfg_coulomb_noalloc": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
+    "hfg_exchange_host_ex": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_atom_work": ([_P, _P], ctypes.c_int),
     "hfg_dft_grid": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
@@ -88,6 +89,7 @@ def parse_xc(method: str):
     ids = [XC_IDS[p] for p in parts]
     return (ids + [0, 0])[:2]
 EXCHANGE_SYMMETRIC = 1
+EXCHANGE_SPLIT = 2
 
 
 
@@ -251,9 +253,10 @@ class Atom:
     def coulomb_noalloc(self, P, J, stream=None):
         _check(_lib.hfg_coulomb_noalloc(self._h, _ptr(P), _ptr(J), _stream(stream)))
 
-    def exchange(self, P, K, stream=None, symmetric: bool = False):
-        if symmetric:
-            _check(_lib.hfg_exchange_ex(self._h, _ptr(P), _ptr(K), EXCHANGE_SYMMETRIC, _stream(stream)))
+    def exchange(self, P, K, stream=None, symmetric: bool = False, split: bool = False):
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        if flags:
+            _check(_lib.hfg_exchange_ex(self._h, _ptr(P), _ptr(K), flags, _stream(stream)))
         else:
             _check(_lib.hfg_exchange(self._h, _ptr(P), _ptr(K), _stream(stream)))
 
@@ -324,9 +327,14 @@ class Atom:
         _check(_lib.hfg_coulomb_host(self._h, _dptr(P), _dptr(J)))
         return J
 
-    def exchange_host(self, P: np.ndarray, out: np.ndarray = None) -> np.ndarray:
+    def exchange_host(self, P: np.ndarray, out: np.ndarray = None, symmetric: bool = False,
+                      split: bool = False) -> np.ndarray:
         P = np.asfortranarray(P, dtype=np.float64)
         K = np.zeros_like(P, order="F") if out is None else out
         assert K.flags.f_contiguous and K.shape == P.shape
-        _check(_lib.hfg_exchange_host(self._h, _dptr(P), _dptr(K)))
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        if flags:
+            _check(_lib.hfg_exchange_host_ex(self._h, _dptr(P), _dptr(K), flags))
+        else:
+            _check(_lib.hfg_exchange_host(self._h, _dptr(P), _dptr(K)))
         return K

@@ -200,37 +200,63 @@ hfg_status hfg_exchange(hfg_atom* a, const double* P, double* K, void* stream) {
 hfg_status hfg_exchange_ex(hfg_atom* a, const double* P, double* K, int flags, void* stream) {
   return guard([&] {
     need(a && P && K, "hfg_exchange: null argument");
-    need((flags & ~HFG_EXCHANGE_SYMMETRIC) == 0, "hfg_exchange_ex: unknown flags");
+    need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "hfg_exchange_ex: unknown flags");
     a->check_device();
-    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P, K, (flags & HFG_EXCHANGE_SYMMETRIC) != 0,
-                                 (cudaStream_t)stream, &a->prof),
-       "exchange kernels");
+    const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
+    if (flags & HFG_EXCHANGE_SPLIT) {
+      const size_t bytes = sizeof(float2) * (size_t)a->host.nbf * a->host.nbf;
+      if (a->s_p2.n != bytes) {
+        a->s_p2.alloc(bytes);
+        a->scr.p2 = a->s_p2.as<float2>();
+      }
+      ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
+         "exchange kernels (split)");
+    } else {
+      ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
+         "exchange kernels");
+    }
   });
 }
 
-static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb) {
+static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, int flags) {
   need(a && P && out, "null argument");
+  need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "unknown flags");
   a->check_device();
   a->staging();
   const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
   cudaStream_t st = a->own_stream;
   ck(cudaMemcpyAsync(a->h_in.p, P, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
-  if (coulomb)
-    ck(hfg::launch_coulomb_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof), "coulomb");
-  else
-    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(), false, st,
-                                 &a->prof),
+  if (coulomb) {
+    ck(hfg::launch_coulomb_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof),
+       "coulomb");
+  } else if (flags & HFG_EXCHANGE_SPLIT) {
+    const size_t b2 = sizeof(float2) * (size_t)a->host.nbf * a->host.nbf;
+    if (a->s_p2.n != b2) {
+      a->s_p2.alloc(b2);
+      a->scr.p2 = a->s_p2.as<float2>();
+    }
+    ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
+                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof),
+       "exchange (split)");
+  } else {
+    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
+                                 (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof),
        "exchange");
+  }
   ck(cudaMemcpyAsync(out, a->h_out.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
   ck(cudaStreamSynchronize(st), "stream sync");
 }
 
 hfg_status hfg_coulomb_host(hfg_atom* a, const double* P, double* J) {
-  return guard([&] { host_call(a, P, J, true); });
+  return guard([&] { host_call(a, P, J, true, 0); });
 }
 
 hfg_status hfg_exchange_host(hfg_atom* a, const double* P, double* K) {
-  return guard([&] { host_call(a, P, K, false); });
+  return guard([&] { host_call(a, P, K, false, 0); });
+}
+
+hfg_status hfg_exchange_host_ex(hfg_atom* a, const double* P, double* K, int flags) {
+  return guard([&] { host_call(a, P, K, false, flags); });
 }
 
 hfg_status hfg_atom_work(const hfg_atom* a, hfg_work_t* w) {

@@ -34,6 +34,12 @@ struct DevAtom {
   const int* kterm_blk;
   const double* kterm_coef;
   int max_terms_per_jk; // bound on terms of one output block
+  // split-precision copies: every FP64 value v stored as float2 (hi, lo) with
+  // hi = fl32(v), lo = fl32(v - hi)
+  const float2* rs2 = nullptr;
+  const float2* rb2 = nullptr;
+  const float2* tk2 = nullptr;
+  const float2* kterm_coef2 = nullptr;
 };
 
 // Scratch owned by the atom handle (sizes fixed at creation)
@@ -42,6 +48,7 @@ struct DevScratch {
   double* jscal;        // [nchan*nel*2]
   double* khalo;        // [nel*nel*nang*nang*(2nn-1)]
   double* bnorm;        // [nang*nang*NORM_SPLIT] partial squared block norms
+  float2* p2;           // [nbf*nbf] split copy of the density (split path)
 };
 
 // Column bands per angular block in the density-norm pass
@@ -113,5 +120,8 @@ cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const dou
                                 bool zero_output, cudaStream_t st, Profiler* prof = nullptr);
 cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr);
+// split-precision exchange (float-float on the FP32 pipe, FP64 recombination)
+cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
+                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr);
 
 }  // namespace hfg

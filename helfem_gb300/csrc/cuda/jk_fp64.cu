@@ -161,7 +161,8 @@ __global__ void j_scatter(DevAtom A, DevScratch S, double* __restrict__ J, int a
 // Partial Frobenius norms of the angular blocks of P: grid (nang^2, NORM_SPLIT),
 // each CTA sums a band of columns; consumers add the partials in a fixed
 // order and apply the reference's 10*DBL_EPSILON screen.
-__global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* __restrict__ part) {
+__global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* __restrict__ part,
+                              float2* __restrict__ p2) {
   __shared__ double red[32];
   const int blk = blockIdx.x, i = blk % A.nang, l = blk / A.nang;
   const int c0 = (int)((long)A.nrad * blockIdx.y / NORM_SPLIT);
@@ -170,8 +171,13 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   const size_t n = (size_t)A.nrad * (c1 - c0);
   for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
     const size_t r = idx % A.nrad, c = c0 + idx / A.nrad;
-    const double v = P[(size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r];
+    const size_t o = (size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r;
+    const double v = P[o];
     s += v * v;
+    if (p2) {
+      const float hi = __double2float_rn(v);
+      p2[o] = make_float2(hi, __double2float_rn(v - (double)hi));
+    }
   }
   s = block_sum(s, red);
   if (threadIdx.x == 0) part[blk * NORM_SPLIT + blockIdx.y] = s;
@@ -307,6 +313,123 @@ __global__ void __launch_bounds__(320) k_tiles(DevAtom A, DevScratch S, const in
   }
 }
 
+// ---------------------------------------------------------------------------
+// Split-precision tiles. Every FP64 operand is held as an unevaluated sum of
+// two floats (hi + lo, ~48 significant bits). Products are made exact with an
+// FMA (TwoProd), sums carry their rounding error (TwoSum), so the FP32 pipe -
+// 64x the FP64 pipe on GB300 - does the contraction; the result is recombined
+// in FP64 once per output element.
+struct ffv {
+  float hi, lo;
+};
+
+// The explicitly rounded intrinsics keep the compiler from contracting the
+// error-free transformations into FMAs (which would break their exactness).
+__device__ __forceinline__ ffv ff_norm(float s, float e) {  // fast two-sum, |s| >= |e|
+  const float t = __fadd_rn(s, e);
+  return {t, __fsub_rn(e, __fsub_rn(t, s))};
+}
+
+// acc + x*y: TwoProd via FMA, TwoSum for the high words, low words summed
+// and renormalised once per call
+__device__ __forceinline__ ffv ff_fma(ffv acc, float2 x, float2 y) {
+  const float p = __fmul_rn(x.x, y.x);
+  float pe = fmaf(x.x, y.x, -p);
+  pe = fmaf(x.x, y.y, pe);
+  pe = fmaf(x.y, y.x, pe);
+  const float s = __fadd_rn(acc.hi, p);
+  const float bb = __fsub_rn(s, acc.hi);
+  const float e = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  return ff_norm(s, __fadd_rn(e, __fadd_rn(acc.lo, pe)));
+}
+
+__device__ __forceinline__ float2 ff2(ffv v) { return make_float2(v.hi, v.lo); }
+__device__ __forceinline__ double ff_to_d(ffv v) { return (double)v.hi + (double)v.lo; }
+
+__device__ __forceinline__ ffv k_recouple_ff(const DevAtom& A, const DevScratch& S, const unsigned char* act,
+                                             int ent, int gp, int gq) {
+  ffv x = {0.f, 0.f};
+  const int u0 = A.kent_ptr[ent], u1 = A.kent_ptr[ent + 1];
+  for (int u = u0; u < u1; ++u) {
+    const int blk = A.kterm_blk[u];
+    if (!act[blk]) continue;
+    const int i = blk % A.nang, l = blk / A.nang;
+    x = ff_fma(x, A.kterm_coef2[u], S.p2[(size_t)(l * A.nrad + gq) * A.nbf + (size_t)i * A.nrad + gp]);
+  }
+  return x;
+}
+
+__global__ void __launch_bounds__(320) k_tiles_split(DevAtom A, DevScratch S, const int4* __restrict__ units,
+                                                     const int* __restrict__ diag_jk, int symmetric,
+                                                     double* __restrict__ K) {
+  const int4 u = units[blockIdx.x];
+  const int a = u.x, b = u.y;
+  const int nn = A.nn, n2 = nn * nn, NL = A.NL;
+  extern __shared__ float2 sm2[];
+  float2* X = sm2;
+  float2* T = X + n2;
+  float2* Am = T + n2;
+  float2* Bm = Am + NL * n2;
+  double* Y = reinterpret_cast<double*>(Bm + NL * n2);
+  unsigned char* act = reinterpret_cast<unsigned char*>(Y + n2);
+  const bool diag = (a == b);
+  if (!diag) {
+    const float2* srcA = (a < b) ? A.rs2 : A.rb2;
+    const float2* srcB = (a < b) ? A.rb2 : A.rs2;
+    for (int idx = threadIdx.x; idx < NL * n2; idx += blockDim.x) {
+      const int L = idx / n2, o = idx % n2;
+      Am[idx] = srcA[((size_t)L * A.nel + a) * n2 + o];
+      Bm[idx] = srcB[((size_t)L * A.nel + b) * n2 + o];
+    }
+  }
+  load_active(A, S, act);
+  __syncthreads();
+  const int t = threadIdx.x;
+  const bool live = t < n2;
+  const int p = live ? t % nn : 0, q = live ? t / nn : 0;
+  const int gp = gfun(A, a, p), gq = gfun(A, b, q);
+  const bool vpq = live && gvalid(A, gp) && gvalid(A, gq);
+  for (int w = u.z; w < u.w; ++w) {
+    const int jk = diag ? diag_jk[w] : w;
+    double y = 0.0;
+    for (int ent = A.kjk_ptr[jk]; ent < A.kjk_ptr[jk + 1]; ++ent) {
+      if (!k_entry_active(A, act, ent)) continue;
+      const int L = A.kent_L[ent];
+      if (live) X[t] = vpq ? ff2(k_recouple_ff(A, S, act, ent, gp, gq)) : make_float2(0.f, 0.f);
+      __syncthreads();
+      ffv acc = {0.f, 0.f};
+      if (diag) {
+        if (live) {
+          const float2* Tk = A.tk2 + ((size_t)L * A.nel + a) * n2 * n2;
+          for (int v = 0; v < n2; ++v) acc = ff_fma(acc, Tk[t + (size_t)v * n2], X[v]);
+        }
+      } else {
+        if (live) {
+          const float2* Bl = Bm + L * n2;
+          ffv s = {0.f, 0.f};
+          for (int c = 0; c < nn; ++c) s = ff_fma(s, X[p + c * nn], Bl[q + c * nn]);
+          T[t] = ff2(s);
+        }
+        __syncthreads();
+        if (live) {
+          const float2* Al = Am + L * n2;
+          for (int c = 0; c < nn; ++c) acc = ff_fma(acc, Al[p + c * nn], T[c + q * nn]);
+        }
+      }
+      y += ff_to_d(acc);  // FP64 recombination, once per output and multipole
+      __syncthreads();
+    }
+    if (live) k_store(A, S, K, a, b, jk, p, q, -y);
+    const int j = jk % A.nang, k = jk / A.nang;
+    if (symmetric && (!diag || j != k)) {
+      if (live) Y[t] = -y;
+      __syncthreads();
+      if (live) k_store(A, S, K, b, a, k + j * A.nang, p, q, Y[q + p * nn]);
+      __syncthreads();
+    }
+  }
+}
+
 __global__ void k_fixup(DevAtom A, DevScratch S, double* __restrict__ K) {
   const int a = blockIdx.x % A.nel, b = blockIdx.x / A.nel, jk = blockIdx.y;
   const int nn = A.nn;
@@ -380,7 +503,7 @@ cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KU
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
-    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm);
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, nullptr);
   }
   {
     Mark m(prof, KC_K_TILES, st);
@@ -388,6 +511,27 @@ cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KU
     const int nunits = symmetric ? U.n_sym : U.n_all;
     k_tiles<<<nunits, th, smem, st>>>(A, S, symmetric ? U.sym : U.all, U.diag_jk_src(symmetric), symmetric ? 1 : 0,
                                       P, K);
+  }
+  {
+    Mark m(prof, KC_K_FIXUP, st);
+    k_fixup<<<dim3(A.nel * A.nel, nang2), 64, 0, st>>>(A, S, K);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
+                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof) {
+  const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
+  {
+    Mark m(prof, KC_K_NORMS, st);
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2);
+  }
+  {
+    Mark m(prof, KC_K_TILES, st);
+    const size_t smem = sizeof(float2) * (2 * n2 + 2 * A.NL * n2) + sizeof(double) * n2 + nang2;
+    const int nunits = symmetric ? U.n_sym : U.n_all;
+    k_tiles_split<<<nunits, th, smem, st>>>(A, S, symmetric ? U.sym : U.all, U.diag_jk_src(symmetric),
+                                            symmetric ? 1 : 0, K);
   }
   {
     Mark m(prof, KC_K_FIXUP, st);

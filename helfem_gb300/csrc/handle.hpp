@@ -113,7 +113,8 @@ struct hfg_atom {
   // device copies of the tables
   DBuf d_rs, d_rb, d_cholp, d_rank, d_tk, d_chanL, d_jket_ptr, d_jket_blk, d_jket_coef, d_jbra_ptr,
       d_jbra_chan, d_jbra_coef, d_kjk_ptr, d_kent_L, d_kent_ptr, d_kterm_blk, d_kterm_coef;
-  DBuf s_jin, s_jscal, s_khalo, s_bnorm;
+  DBuf s_jin, s_jscal, s_khalo, s_bnorm, s_p2;
+  DBuf d_rs2, d_rb2, d_tk2, d_kcoef2;
   DBuf d_units_all, d_units_sym, d_diag_all, d_diag_sym;
   hfg::KUnits units;
   // staging for the host-pointer entry points (allocated on first use)
@@ -210,6 +211,19 @@ struct hfg_atom {
     scr.jscal = s_jscal.as<double>();
     scr.khalo = s_khalo.as<double>();
     scr.bnorm = s_bnorm.as<double>();
+    scr.p2 = nullptr;  // allocated on the first split-precision call
+    auto split = [](const std::vector<double>& v) {
+      std::vector<float2> o(v.size());
+      for (size_t i = 0; i < v.size(); ++i) {
+        const float hi = (float)v[i];
+        o[i] = make_float2(hi, (float)(v[i] - (double)hi));
+      }
+      return o;
+    };
+    A.rs2 = d_rs2.upload(split(H.rs));
+    A.rb2 = d_rb2.upload(split(H.rb));
+    A.tk2 = d_tk2.upload(split(H.tk));
+    A.kterm_coef2 = d_kcoef2.upload(split(H.kterm_coef));
     build_units();
     on_device = true;
   }

@@ -137,6 +137,13 @@ hfg_status hfg_exchange(hfg_atom* atom, const double* P, double* K, void* stream
  * partner (about half the FP64 work). The result for a non-symmetric P is
  * undefined under this flag. */
 #define HFG_EXCHANGE_SYMMETRIC 1
+/* HFG_EXCHANGE_SPLIT: split-precision form. Each FP64 density element and
+ * integral is split into two FP32 pieces (hi + lo, ~48 significant bits);
+ * the contractions run on the FP32 pipe with error-free products and sums
+ * and are recombined in FP64 (relative error ~1e-14 against FP64; reported
+ * by the tests and the benchmark). Allocates an nbf^2 float2 density copy
+ * on the first call. */
+#define HFG_EXCHANGE_SPLIT 2
 hfg_status hfg_exchange_ex(hfg_atom* atom, const double* P, double* K, int flags, void* stream);
 
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
@@ -174,6 +181,8 @@ hfg_status hfg_xc_host(hfg_atom* atom, int x_func, int c_func, const double* Pa,
 /* ---- host-pointer drop-ins (value semantics, synchronous) ---- */
 hfg_status hfg_coulomb_host(hfg_atom* atom, const double* P, double* J);
 hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);
+/* hfg_exchange_host with the hfg_exchange_ex flags (symmetric / split). */
+hfg_status hfg_exchange_host_ex(hfg_atom* atom, const double* P, double* K, int flags);
 
 /* Algorithmic work of one J and one K build on this basis with every density
  * block active (the unit counts behind roofline figures). FLOPs count one

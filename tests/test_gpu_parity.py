@@ -139,3 +139,45 @@ def test_kr_full_size_properties():
     A.coulomb(Pd, J1)
     assert float((J1 - J1.T).abs().max()) < 1e-12 * float(J1.abs().max())
     assert float((Pd * J1).sum()) > 0.0
+
+
+SPLIT_TOL = 1e-12  # split-precision K against the FP64 oracle (observed ~1e-14)
+
+
+@pytest.mark.parametrize("case", CASES[:5], ids=lambda c: f"Z{c[0]}_l{c[1]}m{c[2]}_e{c[3]}_n{c[4]}")
+def test_split_exchange_error(case):
+    """Split-precision K (FP32-pair contraction, FP64 recombination): the
+    error against the FP64 oracle is stated per result and bounded here."""
+    torch = torch_cuda()
+    A, O = make_pair(*case)
+    P = random_density(O.nbf, min(7, O.nbf), seed=case[0] + 100, S=O.S)
+    Kr = FockOracle(O).exchange(P)
+    Pd = to_dev(torch, P)
+    for sym in (False, True):
+        Kd = torch.full_like(Pd, np.nan)
+        A.exchange(Pd, Kd, symmetric=sym, split=True)
+        K = from_dev(Kd)
+        err = relerr(K, Kr)
+        print(f"split K {case} symmetric={sym}: max rel err {err:.2e}")
+        assert np.isfinite(K).all() and err < SPLIT_TOL
+
+
+def test_split_exchange_energy_error_full_size():
+    """Kr benchmark basis: exchange-energy error of the split form against
+    plain FP64 on the device, |dE| well below the 1e-8 Eh bar."""
+    torch = torch_cuda()
+    from oracle import tabulate as tab
+    import helfem_gb300 as hg
+    b = tab.get_grid(60.0, 40, 4, 1.0)
+    lv, mv = hg.angular_basis(2, 2)
+    A = hg.Atom(36, b, lv, mv)
+    P = random_density(A.nbf, 18, seed=12345, S=A.overlap())
+    Pd = to_dev(torch, P)
+    K64, K32 = torch.empty_like(Pd), torch.empty_like(Pd)
+    A.exchange(Pd, K64, symmetric=True)
+    A.exchange(Pd, K32, symmetric=True, split=True)
+    dE = 0.5 * float((Pd * (K32 - K64)).sum())
+    E = 0.5 * float((Pd * K64).sum())
+    rel = float((K32 - K64).abs().max() / K64.abs().max())
+    print(f"Kr split K: max rel err {rel:.2e}, exchange energy {E:.10f}, dE {dE:.2e}")
+    assert abs(dE) < 1e-9 and rel < SPLIT_TOL

@@ -64,5 +64,5 @@ def test_orbital_energies_match_oracle():
     A = tab.build_atom(2, 15, tab.get_grid(40.0, 5, 4, 2.0), 0, 0)
     o = oscf.run_scf(A, 1, 1, "hf", True)
     e_gpu = np.sort(r["orbital_energies"])[:3]
-    e_ora = np.sort(np.concatenate(o.eps))[:3]
+    e_ora = np.sort(np.concatenate(o.eps[0]))[:3]
     assert np.abs(e_gpu - e_ora).max() < 1e-7, (e_gpu, e_ora)
