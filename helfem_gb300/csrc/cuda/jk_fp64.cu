@@ -158,6 +158,24 @@ __global__ void j_scatter(DevAtom A, DevScratch S, double* __restrict__ J, int a
 }
 
 // ----------------------------------------------------------------- exchange
+// Split an FP64 value into float hi + lo using integer operations only (the
+// FP64 pipe is the scarce unit on GB300): hi carries the top 24 significand
+// bits (truncated), lo the next 29 bits rounded to 24; |hi + lo - v| <=
+// 2^-47 |v|. Values below 2^-126 and non-finite inputs map to (0, 0) and
+// (v, 0) respectively.
+__device__ __forceinline__ float2 split_bits(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0x7FF) return make_float2((float)v, 0.f);
+  const int E = e - 1023;
+  if (E < -126) return make_float2(0.f, 0.f);
+  const unsigned long long S = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const float sgn = (b >> 63) ? -1.f : 1.f;
+  const float hi = sgn * ldexpf(__uint2float_rn((unsigned)(S >> 29)), E - 23);
+  const float lo = sgn * ldexpf(__uint2float_rn((unsigned)(S & 0x1FFFFFFFull)), E - 52);
+  return make_float2(hi, lo);
+}
+
 // Partial Frobenius norms of the angular blocks of P: grid (nang^2, NORM_SPLIT),
 // each CTA sums a band of columns; consumers add the partials in a fixed
 // order and apply the reference's 10*DBL_EPSILON screen.
@@ -168,17 +186,23 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   const int c0 = (int)((long)A.nrad * blockIdx.y / NORM_SPLIT);
   const int c1 = (int)((long)A.nrad * (blockIdx.y + 1) / NORM_SPLIT);
   double s = 0.0;
+  float sf = 0.f;
   const size_t n = (size_t)A.nrad * (c1 - c0);
   for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
     const size_t r = idx % A.nrad, c = c0 + idx / A.nrad;
     const size_t o = (size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r;
     const double v = P[o];
-    s += v * v;
     if (p2) {
-      const float hi = __double2float_rn(v);
-      p2[o] = make_float2(hi, __double2float_rn(v - (double)hi));
+      // split path: integer-only split (no FP64-pipe instructions) and an
+      // FP32 norm of the high words for the screen
+      const float2 h = split_bits(v);
+      p2[o] = h;
+      sf = fmaf(h.x, h.x, sf);
+    } else {
+      s += v * v;
     }
   }
+  if (p2) s = (double)sf;
   s = block_sum(s, red);
   if (threadIdx.x == 0) part[blk * NORM_SPLIT + blockIdx.y] = s;
 }
@@ -330,8 +354,9 @@ __device__ __forceinline__ ffv ff_norm(float s, float e) {  // fast two-sum, |s|
   return {t, __fsub_rn(e, __fsub_rn(t, s))};
 }
 
-// acc + x*y: TwoProd via FMA, TwoSum for the high words, low words summed
-// and renormalised once per call
+// acc + x*y: TwoProd via FMA, TwoSum for the high words; the low words
+// (product and sum errors) accumulate in acc.lo, which stays small against
+// acc.hi over the short contractions here and is renormalised on read
 __device__ __forceinline__ ffv ff_fma(ffv acc, float2 x, float2 y) {
   const float p = __fmul_rn(x.x, y.x);
   float pe = fmaf(x.x, y.x, -p);
@@ -340,10 +365,19 @@ __device__ __forceinline__ ffv ff_fma(ffv acc, float2 x, float2 y) {
   const float s = __fadd_rn(acc.hi, p);
   const float bb = __fsub_rn(s, acc.hi);
   const float e = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-  return ff_norm(s, __fadd_rn(e, __fadd_rn(acc.lo, pe)));
+  return {s, __fadd_rn(acc.lo, __fadd_rn(e, pe))};
 }
 
-__device__ __forceinline__ float2 ff2(ffv v) { return make_float2(v.hi, v.lo); }
+// normalised every call: for the long (nn^2-term) in-element contraction
+__device__ __forceinline__ ffv ff_fma_n(ffv acc, float2 x, float2 y) {
+  const ffv r = ff_fma(acc, x, y);
+  return ff_norm(r.hi, r.lo);
+}
+
+__device__ __forceinline__ float2 ff2(ffv v) {
+  const ffv n = ff_norm(v.hi, v.lo);
+  return make_float2(n.hi, n.lo);
+}
 __device__ __forceinline__ double ff_to_d(ffv v) { return (double)v.hi + (double)v.lo; }
 
 __device__ __forceinline__ ffv k_recouple_ff(const DevAtom& A, const DevScratch& S, const unsigned char* act,
@@ -401,7 +435,7 @@ __global__ void __launch_bounds__(320) k_tiles_split(DevAtom A, DevScratch S, co
       if (diag) {
         if (live) {
           const float2* Tk = A.tk2 + ((size_t)L * A.nel + a) * n2 * n2;
-          for (int v = 0; v < n2; ++v) acc = ff_fma(acc, Tk[t + (size_t)v * n2], X[v]);
+          for (int v = 0; v < n2; ++v) acc = ff_fma_n(acc, Tk[t + (size_t)v * n2], X[v]);
         }
       } else {
         if (live) {
