@@ -76,6 +76,11 @@ _SIGS = {
     "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
     "hfg_xc_host": ([_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, ctypes.c_double], ctypes.c_int),
     "hfg_scf_run": ([_P, _P, _P, _D, _P], ctypes.c_int),
+    "hfg_engine_create": ([ctypes.c_int, ctypes.c_double, ctypes.POINTER(_P)], ctypes.c_int),
+    "hfg_engine_submit": ([_P, _P, _P, ctypes.POINTER(ctypes.c_ulonglong)], ctypes.c_int),
+    "hfg_engine_wait": ([_P, ctypes.c_ulonglong, ctypes.c_double, _P], ctypes.c_int),
+    "hfg_engine_stats": ([_P, _I, _I, _D], ctypes.c_int),
+    "hfg_engine_destroy": ([_P], ctypes.c_int),
     "hfg_profile_enable": ([_P, ctypes.c_int], ctypes.c_int),
     "hfg_profile_read": ([_P, _P, ctypes.c_int], ctypes.c_int),
 }
@@ -106,12 +111,18 @@ class _ScfDesc(ctypes.Structure):
                 ("symmetry", ctypes.c_int), ("x_func", ctypes.c_int), ("c_func", ctypes.c_int),
                 ("kfrac", ctypes.c_double), ("maxiter", ctypes.c_int), ("e_tol", ctypes.c_double),
                 ("diis_tol", ctypes.c_double), ("fixed_occ", _I), ("n_fixed_blocks", ctypes.c_int),
-                ("dftthr", ctypes.c_double)]
+                ("dftthr", ctypes.c_double), ("frac_aufbau", ctypes.c_int)]
 
 
 class _ScfRes(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("Etot", "Ekin", "Enuc", "Ecoul", "Exx", "Exc", "Nel_grid")] + \
                [("iterations", ctypes.c_int), ("converged", ctypes.c_int)]
+
+
+class _JobRes(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("scf", _ScfRes), ("queue_ms", ctypes.c_double),
+                ("setup_ms", ctypes.c_double), ("scf_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("footprint_bytes", ctypes.c_double), ("error", ctypes.c_char * 256)]
 
 
 class _Prof(ctypes.Structure):
@@ -290,7 +301,8 @@ class Atom:
 
     # ---- SCF ----
     def scf(self, nela: int, nelb: int, method: str = "hf", restricted: bool = True, symmetry: int = 1,
-            fixed_occ=None, maxiter: int = 0, e_tol: float = 0.0, diis_tol: float = 0.0, stream=None) -> dict:
+            fixed_occ=None, maxiter: int = 0, e_tol: float = 0.0, diis_tol: float = 0.0, stream=None,
+            frac_aufbau: bool = False) -> dict:
         """Atomic SCF on the device. fixed_occ: dict m -> (n_alpha, n_beta) (symmetry 1)."""
         x, c = (0, 0) if method.lower() == "hf" else parse_xc(method)
         occ = None
@@ -300,7 +312,7 @@ class Atom:
             occ = np.array([v for m in ms for v in fixed_occ.get(m, (0, 0))], dtype=np.int32)
             nfix = len(ms)
         d = _ScfDesc(nela, nelb, int(restricted), symmetry, x, c, -1.0, maxiter, e_tol, diis_tol,
-                     occ.ctypes.data_as(_I) if occ is not None else None, nfix, 0.0)
+                     occ.ctypes.data_as(_I) if occ is not None else None, nfix, 0.0, int(frac_aufbau))
         r = _ScfRes()
         nspin = 1 if restricted else 2
         eps = np.zeros(self.nbf * nspin)
@@ -338,3 +350,62 @@ class Atom:
         else:
             _check(_lib.hfg_exchange_host(self._h, _dptr(P), _dptr(K)))
         return K
+
+
+def _scf_desc(nela, nelb, method="hf", restricted=True, symmetry=1, fixed=None, nblocks=0, e_tol=0.0,
+              diis_tol=0.0, maxiter=0, frac_aufbau=False):
+    x, c = (0, 0) if method.lower() == "hf" else parse_xc(method)
+    return _ScfDesc(nela, nelb, int(restricted), symmetry, x, c, -1.0, maxiter, e_tol, diis_tol,
+                    fixed.ctypes.data_as(_I) if fixed is not None else None, nblocks, 0.0, int(frac_aufbau))
+
+
+class Engine:
+    """Concurrent atomic SCF solves (hfg_engine_*): submit() returns a job id
+    at once; wait() returns the result dict (energies, timings)."""
+
+    def __init__(self, n_workers: int = 4, hbm_budget_gb: float = 180.0):
+        h = _P()
+        _check(_lib.hfg_engine_create(n_workers, hbm_budget_gb, ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, Z, bval, lval, mval, nela, nelb, method="hf", restricted=True, nnodes=15, symmetry=1,
+               fixed_occ=None, e_tol=0.0, diis_tol=0.0, frac_aufbau=False) -> int:
+        bval = np.ascontiguousarray(bval, dtype=np.float64)
+        lval = np.ascontiguousarray(lval, dtype=np.int32)
+        mval = np.ascontiguousarray(mval, dtype=np.int32)
+        ad = _Desc(int(Z), nnodes, 0, len(bval) - 1, _dptr(bval), len(lval), lval.ctypes.data_as(_I),
+                   mval.ctypes.data_as(_I), 0.0, 0)
+        occ, nfix = None, 0
+        if fixed_occ is not None:
+            ms = sorted(set(int(m) for m in mval))
+            occ = np.array([v for m in ms for v in fixed_occ.get(m, (0, 0))], dtype=np.int32)
+            nfix = len(ms)
+        sd = _scf_desc(nela, nelb, method, restricted, symmetry, occ, nfix, e_tol, diis_tol,
+                       frac_aufbau=frac_aufbau)
+        jid = ctypes.c_ulonglong()
+        _check(_lib.hfg_engine_submit(self._h, ctypes.byref(ad), ctypes.byref(sd), ctypes.byref(jid)))
+        return jid.value
+
+    def wait(self, job_id: int, timeout_s: float = -1.0) -> dict:
+        r = _JobRes()
+        _check(_lib.hfg_engine_wait(self._h, job_id, timeout_s, ctypes.byref(r)))
+        out = {n: getattr(r.scf, n) for n, _ in _ScfRes._fields_}
+        out.update(status=r.status, queue_ms=r.queue_ms, setup_ms=r.setup_ms, scf_ms=r.scf_ms,
+                   total_ms=r.total_ms, footprint_bytes=r.footprint_bytes, error=r.error.decode())
+        return out
+
+    def stats(self):
+        q, r, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(_lib.hfg_engine_stats(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(g)))
+        return {"queued": q.value, "running": r.value, "in_use_gb": g.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _check(_lib.hfg_engine_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -3,8 +3,26 @@
 // a thread-local message; nothing throws across the boundary.
 #include "handle.hpp"
 
+#include <mutex>
+
 namespace hfg_abi {
 thread_local std::string g_err;
+thread_local cudaStream_t t_alloc_stream = nullptr;
+
+void retain_pool_memory() {
+  static std::mutex mu;
+  static std::vector<char> done(64, 0);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    unsigned long long thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = 1;
+}
 }
 using hfg_abi::g_err;
 
@@ -162,6 +180,7 @@ hfg_status hfg_coulomb(hfg_atom* a, const double* P, double* J, void* stream) {
     need(a && P && J, "hfg_coulomb: null argument");
     a->check_device();
     ck(hfg::launch_coulomb_fp64(a->dev, a->scr, P, J, true, (cudaStream_t)stream, &a->prof), "coulomb kernels");
+    a->mark_use((cudaStream_t)stream);
   });
 }
 
@@ -170,6 +189,7 @@ hfg_status hfg_coulomb_acc(hfg_atom* a, const double* P, double* F, void* stream
     need(a && P && F, "hfg_coulomb_acc: null argument");
     a->check_device();
     ck(hfg::launch_coulomb_fp64(a->dev, a->scr, P, F, false, (cudaStream_t)stream, &a->prof), "coulomb kernels");
+    a->mark_use((cudaStream_t)stream);
   });
 }
 
@@ -190,6 +210,7 @@ hfg_status hfg_coulomb_noalloc(hfg_atom* a, const double* P, double* J, void* st
     s.jin = base;
     s.jscal = base + need_jin;
     ck(hfg::launch_coulomb_fp64(a->dev, s, P, J, true, (cudaStream_t)stream, nullptr), "coulomb kernels");
+    a->mark_use((cudaStream_t)stream);
   });
 }
 
@@ -206,8 +227,10 @@ hfg_status hfg_exchange_ex(hfg_atom* a, const double* P, double* K, int flags, v
     if (flags & HFG_EXCHANGE_SPLIT) {
       const size_t bytes = sizeof(float2) * (size_t)a->host.nbf * a->host.nbf;
       if (a->s_p2.n != bytes) {
+        hfg_abi::AllocStream alloc_on(a->own_stream);
         a->s_p2.alloc(bytes);
         a->scr.p2 = a->s_p2.as<float2>();
+        ck(cudaStreamSynchronize(a->own_stream), "sync");
       }
       ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
          "exchange kernels (split)");
@@ -215,6 +238,7 @@ hfg_status hfg_exchange_ex(hfg_atom* a, const double* P, double* K, int flags, v
       ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
          "exchange kernels");
     }
+    a->mark_use((cudaStream_t)stream);
   });
 }
 
@@ -232,6 +256,7 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
   } else if (flags & HFG_EXCHANGE_SPLIT) {
     const size_t b2 = sizeof(float2) * (size_t)a->host.nbf * a->host.nbf;
     if (a->s_p2.n != b2) {
+      hfg_abi::AllocStream alloc_on(a->own_stream);
       a->s_p2.alloc(b2);
       a->scr.p2 = a->s_p2.as<float2>();
     }
@@ -334,6 +359,7 @@ hfg_status hfg_xc(hfg_atom* a, int x_func, int c_func, const double* Pa, const d
     ck(hfg::launch_xc_fp64(a->dev, a->xc, a->xs, x_func, c_func, Pa, Pb, Ha, Hb, energies, thr,
                            (cudaStream_t)stream),
        "xc kernels");
+    a->mark_use((cudaStream_t)stream);
   });
 }
 
@@ -347,11 +373,14 @@ hfg_status hfg_xc_host(hfg_atom* a, int x_func, int c_func, const double* Pa, co
     if (!a->xc_ready) a->setup_xc(0, 0);
     a->staging();
     const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
-    if (Pb) {
-      if (a->h_in2.n != bytes) a->h_in2.alloc(bytes);
-      if (a->h_out2.n != bytes) a->h_out2.alloc(bytes);
+    {
+      hfg_abi::AllocStream alloc_on(a->own_stream);
+      if (Pb) {
+        if (a->h_in2.n != bytes) a->h_in2.alloc(bytes);
+        if (a->h_out2.n != bytes) a->h_out2.alloc(bytes);
+      }
+      if (a->h_e.n == 0) a->h_e.alloc(2 * sizeof(double));
     }
-    if (a->h_e.n == 0) a->h_e.alloc(2 * sizeof(double));
     cudaStream_t st = a->own_stream;
     ck(cudaMemcpyAsync(a->h_in.p, Pa, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
     if (Pb) ck(cudaMemcpyAsync(a->h_in2.p, Pb, bytes, cudaMemcpyHostToDevice, st), "H2D copy");

@@ -60,41 +60,80 @@ hfg_status guard(F&& f) {
   }
 }
 
+// Stream-ordered allocation: while an AllocStream guard is alive on a
+// thread, device buffers created on that thread are allocated with
+// cudaMallocAsync on its stream and later freed with cudaFreeAsync on the
+// same stream, from the device's default pool with its release threshold
+// raised so freed memory stays cached. Concurrent solves on different
+// streams then never pay the device-wide synchronisation of
+// cudaMalloc/cudaFree.
+extern thread_local cudaStream_t t_alloc_stream;
+void retain_pool_memory();  // once per device
+
+struct AllocStream {
+  cudaStream_t prev;
+  explicit AllocStream(cudaStream_t s) : prev(t_alloc_stream) {
+    retain_pool_memory();
+    t_alloc_stream = s;
+  }
+  ~AllocStream() { t_alloc_stream = prev; }
+};
+
 // RAII device allocation
 struct DBuf {
   void* p = nullptr;
   size_t n = 0;
+  cudaStream_t st = nullptr;  // stream of a stream-ordered allocation
+  bool async = false;
   DBuf() = default;
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
-  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), st(o.st), async(o.async) { o.p = nullptr; o.n = 0; }
   DBuf& operator=(DBuf&& o) noexcept {
     if (this != &o) {
-      if (p) cudaFree(p);
-      p = o.p; n = o.n;
+      release();
+      p = o.p; n = o.n; st = o.st; async = o.async;
       o.p = nullptr; o.n = 0;
     }
     return *this;
   }
-  ~DBuf() { if (p) cudaFree(p); }
+  ~DBuf() { release(); }
+  void release() {
+    if (!p) return;
+    if (async) cudaFreeAsync(p, st); else cudaFree(p);
+    p = nullptr;
+  }
   void alloc(size_t bytes) {
-    if (p) { cudaFree(p); p = nullptr; }
+    release();
     n = bytes;
     if (bytes == 0) return;
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
-    ck(e, "cudaMalloc");
+    st = t_alloc_stream;
+    async = st != nullptr;
+    cudaError_t e = async ? cudaMallocAsync(&p, bytes, st) : cudaMalloc(&p, bytes);
+    if (e == cudaErrorMemoryAllocation) { p = nullptr; throw std::bad_alloc(); }
+    ck(e, "device allocation");
   }
+  // copies from pageable host memory: the call returns once the source has
+  // been staged, so the host vector may be released right after
   template <class T>
   T* upload(const std::vector<T>& v) {
     alloc(std::max<size_t>(1, v.size()) * sizeof(T));
-    if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+    if (!v.empty())
+      ck(async ? cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st)
+               : cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice),
+         "upload");
     return static_cast<T*>(p);
   }
   template <class T>
   T* as() const { return static_cast<T*>(p); }
 };
 
+// owns a stream; declared first in a struct so it outlives the buffers that
+// free on it
+struct StreamHolder {
+  cudaStream_t s = nullptr;
+  ~StreamHolder() { if (s) cudaStreamDestroy(s); }
+};
 
 }  // namespace hfg_abi
 
@@ -104,6 +143,7 @@ using hfg_abi::need;
 using hfg_abi::guard;
 
 struct hfg_atom {
+  hfg_abi::StreamHolder stream_holder;  // destroyed last
   hfg::AtomHost host;
   int device = 0;
   bool on_device = false;
@@ -128,9 +168,19 @@ struct hfg_atom {
   std::vector<cudaEvent_t> prof_ev;
   std::vector<int> prof_cls;
 
+  // last use of the handle's buffers on a caller stream; destruction orders
+  // the stream-ordered frees after it
+  cudaEvent_t last_use = nullptr;
+  void mark_use(cudaStream_t st) {
+    if (last_use) cudaEventRecord(last_use, st);
+  }
+
   ~hfg_atom() {
     free_profiler();
-    if (own_stream) cudaStreamDestroy(own_stream);
+    if (last_use) {
+      if (own_stream) cudaStreamWaitEvent(own_stream, last_use, 0);
+      cudaEventDestroy(last_use);
+    }
   }
 
   void free_profiler() {
@@ -164,7 +214,11 @@ struct hfg_atom {
     using namespace hfg;
     const AtomHost& H = host;
     ck(cudaGetDevice(&device), "cudaGetDevice");
-    ck(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!own_stream) {
+      ck(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      stream_holder.s = own_stream;
+    }
+    hfg_abi::AllocStream alloc_on(own_stream);
     DevAtom& A = dev;
     A.nn = H.rad.nn;
     A.nel = H.rad.nel;
@@ -212,6 +266,7 @@ struct hfg_atom {
     scr.khalo = s_khalo.as<double>();
     scr.bnorm = s_bnorm.as<double>();
     scr.p2 = nullptr;  // allocated on the first split-precision call
+    ck(cudaEventCreateWithFlags(&last_use, cudaEventDisableTiming), "cudaEventCreate");
     auto split = [](const std::vector<double>& v) {
       std::vector<float2> o(v.size());
       for (size_t i = 0; i < v.size(); ++i) {
@@ -225,6 +280,7 @@ struct hfg_atom {
     A.tk2 = d_tk2.upload(split(H.tk));
     A.kterm_coef2 = d_kcoef2.upload(split(H.kterm_coef));
     build_units();
+    ck(cudaStreamSynchronize(own_stream), "sync after upload");
     on_device = true;
   }
 
@@ -283,6 +339,7 @@ struct hfg_atom {
   }
 
   void setup_xc(int ldft, int mdft) {
+    hfg_abi::AllocStream alloc_on(own_stream);
     host.build_dft_grid(ldft, mdft);
     const hfg::AtomHost& H = host;
     xc.nquad = H.nquad;
@@ -307,10 +364,12 @@ struct hfg_atom {
     xs.F = xs_F.as<double>();
     xs.U = xs_U.as<double>();
     xs.epart = xs_ep.as<double>();
+    ck(cudaStreamSynchronize(own_stream), "sync after grid upload");
     xc_ready = true;
   }
 
   void staging() {
+    hfg_abi::AllocStream alloc_on(own_stream);
     const size_t bytes = sizeof(double) * (size_t)host.nbf * host.nbf;
     if (h_in.n != bytes) h_in.alloc(bytes);
     if (h_out.n != bytes) h_out.alloc(bytes);

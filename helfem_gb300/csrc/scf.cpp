@@ -75,9 +75,11 @@ struct Eigh {
 
 }  // namespace
 
-extern "C" hfg_status hfg_scf_run(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, double* orbital_energies,
-                                  void* stream) {
-  return guard([&] {
+// The SCF proper; throws on failure. bl/so: handles already bound to the
+// stream (the engine's workers keep one pair each).
+void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, double* orbital_energies,
+                  cudaStream_t stream, cublasHandle_t bl_in, cusolverDnHandle_t so_in) {
+  {
     need(a && d && res, "hfg_scf_run: null argument");
     a->check_device();
     const hfg::AtomHost& H = a->host;
@@ -95,12 +97,12 @@ extern "C" hfg_status hfg_scf_run(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_re
     const double thr = d->dftthr > 0 ? d->dftthr : 1e-12;
     cudaStream_t st = stream ? (cudaStream_t)stream : a->own_stream;
     if (have_xc && !a->xc_ready) a->setup_xc(0, 0);
+    hfg_abi::AllocStream alloc_on(st);  // every buffer below is stream-ordered on st
 
-    Handles hd;
-    cb(cublasCreate(&hd.bl), "cublasCreate");
-    cb(cublasSetStream(hd.bl, st), "cublasSetStream");
-    cs(cusolverDnCreate(&hd.so), "cusolverDnCreate");
-    cs(cusolverDnSetStream(hd.so, st), "cusolverDnSetStream");
+    struct {
+      cublasHandle_t bl;
+      cusolverDnHandle_t so;
+    } hd{bl_in, so_in};
 
     // ---- symmetry blocks (TwoDBasis.cpp:218-232: unique m ascending) ----
     std::vector<Block> blocks;
@@ -266,11 +268,15 @@ extern "C" hfg_status hfg_scf_run(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_re
         } else {
           std::stable_sort(all.begin(), all.end(), [](auto& x, auto& y) { return x.first < y.first; });
           double left = restricted ? (double)(d->nela + d->nelb) : (s == 0 ? d->nela : d->nelb);
-          for (auto& e : all) {
-            if (left <= 0) break;
-            const double o = std::min(maxocc, left);
-            occ[s][e.second.first][e.second.second] = o;
-            left -= o;
+          for (size_t i = 0; i < all.size() && left > 0;) {
+            size_t j = i + 1;
+            if (d->frac_aufbau)  // degenerate group at this level
+              while (j < all.size() && all[j].first - all[i].first < 1e-5 * (1.0 + std::fabs(all[i].first))) ++j;
+            const double cap = maxocc * (double)(j - i);
+            const double o = (left >= cap) ? maxocc : left / (double)(j - i);
+            for (size_t q = i; q < j; ++q) occ[s][all[q].second.first][all[q].second.second] = o;
+            left -= o * (double)(j - i);
+            i = j;
           }
         }
       }
@@ -461,6 +467,7 @@ extern "C" hfg_status hfg_scf_run(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_re
       build_density();
     }
     ck(cudaStreamSynchronize(st), "sync");
+    a->mark_use(st);
     res->Etot = Etot;
     res->Ekin = Ekin;
     res->Enuc = Enuc;
@@ -471,5 +478,20 @@ extern "C" hfg_status hfg_scf_run(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_re
     res->iterations = std::min(it, maxiter);
     res->converged = converged ? 1 : 0;
     if (orbital_energies) std::memcpy(orbital_energies, eps.data(), sizeof(double) * eps.size());
+  }
+}
+
+extern "C" hfg_status hfg_scf_run(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, double* orbital_energies,
+                                  void* stream) {
+  return guard([&] {
+    need(a != nullptr, "hfg_scf_run: null argument");
+    a->check_device();
+    cudaStream_t st = stream ? (cudaStream_t)stream : a->own_stream;
+    Handles hd;
+    cb(cublasCreate(&hd.bl), "cublasCreate");
+    cb(cublasSetStream(hd.bl, st), "cublasSetStream");
+    cs(cusolverDnCreate(&hd.so), "cusolverDnCreate");
+    cs(cusolverDnSetStream(hd.so, st), "cusolverDnSetStream");
+    hfg_scf_impl(a, d, res, orbital_energies, st, hd.bl, hd.so);
   });
 }

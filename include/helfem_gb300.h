@@ -225,6 +225,10 @@ typedef struct {
                               reference's --readocc)                           */
   int n_fixed_blocks;
   double dftthr;           /* density threshold; 0 -> 1e-12                   */
+  int frac_aufbau;         /* 1: electrons that only partly fill a degenerate
+                              frontier shell are shared equally over it
+                              (spherically averaged open shells); 0: integer
+                              Aufbau as the reference                         */
 } hfg_scf_desc;
 typedef struct {
   double Etot, Ekin, Enuc, Ecoul, Exx, Exc, Nel_grid;
@@ -235,6 +239,35 @@ typedef struct {
  * handle's stream) and returns when converged or out of iterations. */
 hfg_status hfg_scf_run(hfg_atom* atom, const hfg_scf_desc* desc, hfg_scf_result* result,
                        double* orbital_energies, void* stream);
+
+/* ---- batched / serving runtime ----
+ * Many atomic SCF solves on one GPU: worker threads, one CUDA stream each,
+ * run whole solves (host tabulation, upload, device SCF) concurrently.
+ * A queued job starts when its estimated device footprint fits in the HBM
+ * budget still free (first fitting job in arrival order). The reference has
+ * no counterpart (one atom per process); this serves the batched and
+ * streaming configurations. */
+typedef struct hfg_engine hfg_engine;
+typedef struct {
+  int status;               /* 0 queued, 1 running, 2 done, 3 failed          */
+  hfg_scf_result scf;
+  double queue_ms;          /* submit -> start                                 */
+  double setup_ms;          /* host tabulation + upload                        */
+  double scf_ms;            /* device SCF                                      */
+  double total_ms;          /* submit -> result                                */
+  double footprint_bytes;   /* admission estimate                              */
+  char error[256];          /* failure message (status 3)                      */
+} hfg_job_result;
+hfg_status hfg_engine_create(int n_workers, double hbm_budget_gb, hfg_engine** out);
+/* copies the descriptions (and their arrays); returns at once */
+hfg_status hfg_engine_submit(hfg_engine* e, const hfg_atom_desc* atom, const hfg_scf_desc* scf,
+                             unsigned long long* job_id);
+/* waits up to timeout_s (< 0: no limit); a finished job's result is returned
+ * once and then forgotten; status < 2 means it is still pending */
+hfg_status hfg_engine_wait(hfg_engine* e, unsigned long long job_id, double timeout_s, hfg_job_result* out);
+hfg_status hfg_engine_stats(hfg_engine* e, int* queued, int* running, double* in_use_gb);
+/* cancels queued jobs, waits for running ones */
+hfg_status hfg_engine_destroy(hfg_engine* e);
 
 /* ---- per-kernel timing (counterpart of the reference's scf_driver::FockTimer,
  * src/general/scf_driver_common.h:69-170) ----

@@ -1,0 +1,81 @@
+"""The batched / serving runtime: concurrent solves give the same results as
+solves run alone, memory admission holds jobs back, failures are reported
+per job without disturbing the others."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import helfem_gb300 as hg
+from helfem_gb300 import workloads as wl
+from gpu_util import torch_cuda
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+CI = {c["name"]: c for c in json.load(open(os.path.join(HERE, "golden", "ci_energies.json")))}
+
+
+def ci_job(Z, lmax, mmax, method, restricted, nela, nelb, fixed=None):
+    b = wl.grid(40.0, 5)
+    lv, mv = wl.angular(lmax, mmax)
+    return dict(Z=Z, bval=b, lval=lv, mval=mv, nela=nela, nelb=nelb, method=method, restricted=restricted,
+                fixed_occ=fixed)
+
+
+JOBS = {
+    "atomic-He-hf-r": ci_job(2, 0, 0, "hf", True, 1, 1),
+    "atomic-Be-lda-u": ci_job(4, 0, 0, "lda_x-lda_c_vwn", False, 2, 2),
+    "atomic-He-gga-r": ci_job(2, 0, 0, "gga_x_pbe-gga_c_pbe", True, 1, 1),
+    "atomic-O-3P-p0-hf": ci_job(8, 1, 1, "hf", False, 5, 3, {0: (3, 3), 1: (1, 0), -1: (1, 0)}),
+    "atomic-Ne-hf-r": ci_job(10, 1, 1, "hf", True, 5, 5),
+    "atomic-H-hf-u": ci_job(1, 0, 0, "hf", False, 1, 0),
+}
+
+
+def test_engine_mix_equals_alone_and_reference():
+    torch_cuda()
+    eng = hg.Engine(n_workers=4, hbm_budget_gb=40.0)
+    ids = {}
+    for rep in range(2):  # each job twice, interleaved
+        for name, j in JOBS.items():
+            ids[(name, rep)] = eng.submit(j["Z"], j["bval"], j["lval"], j["mval"], j["nela"], j["nelb"],
+                                          j["method"], j["restricted"], fixed_occ=j["fixed_occ"])
+    res = {k: eng.wait(v) for k, v in ids.items()}
+    eng.close()
+    for (name, rep), r in res.items():
+        assert r["status"] == 2, r
+        assert abs(r["Etot"] - CI[name]["total"]) < 1e-8, (name, r["Etot"])
+    for name, j in JOBS.items():
+        a = hg.Atom(j["Z"], j["bval"], j["lval"], j["mval"])
+        alone = a.scf(j["nela"], j["nelb"], j["method"], restricted=j["restricted"], fixed_occ=j["fixed_occ"])
+        for rep in range(2):
+            assert abs(res[(name, rep)]["Etot"] - alone["Etot"]) < 1e-10
+
+
+def test_engine_admission_and_failure():
+    torch_cuda()
+    # budget fits about one small job at a time: jobs queue, all complete
+    eng = hg.Engine(n_workers=4, hbm_budget_gb=0.12)
+    j = JOBS["atomic-Ne-hf-r"]
+    ok = [eng.submit(j["Z"], j["bval"], j["lval"], j["mval"], 5, 5, "hf", True) for _ in range(4)]
+    bad = eng.submit(2, j["bval"], [0], [0], 0, 0, "hf", True)  # no electrons: fails on its own
+    res = [eng.wait(i) for i in ok]
+    rb = eng.wait(bad)
+    eng.close()
+    assert rb["status"] == 3 and "electrons" in rb["error"]
+    assert all(r["status"] == 2 for r in res)
+    assert len(set(round(r["Etot"], 12) for r in res)) == 1
+    assert max(r["queue_ms"] for r in res) > 0.5 * min(r["scf_ms"] + r["setup_ms"] for r in res)
+
+
+def test_fractional_aufbau_open_shell_converges():
+    torch_cuda()
+    jobs = wl.batch_atoms(4, seed=3, zmax=18, nel_range=(6, 8), nodes=(10,))
+    eng = hg.Engine(n_workers=4, hbm_budget_gb=40.0)
+    ids = [eng.submit(j["Z"], j["bval"], j["lval"], j["mval"], j["nela"], j["nelb"], j["method"],
+                      j["restricted"], nnodes=j["nnodes"], symmetry=2, frac_aufbau=True) for j in jobs]
+    res = [eng.wait(i) for i in ids]
+    eng.close()
+    for j, r in zip(jobs, res):
+        assert r["status"] == 2 and r["converged"], (j["Z"], r)
