@@ -111,7 +111,7 @@ class _ScfDesc(ctypes.Structure):
                 ("symmetry", ctypes.c_int), ("x_func", ctypes.c_int), ("c_func", ctypes.c_int),
                 ("kfrac", ctypes.c_double), ("maxiter", ctypes.c_int), ("e_tol", ctypes.c_double),
                 ("diis_tol", ctypes.c_double), ("fixed_occ", _I), ("n_fixed_blocks", ctypes.c_int),
-                ("dftthr", ctypes.c_double), ("frac_aufbau", ctypes.c_int)]
+                ("dftthr", ctypes.c_double), ("frac_aufbau", ctypes.c_int), ("split_exchange", ctypes.c_int)]
 
 
 class _ScfRes(ctypes.Structure):
@@ -302,7 +302,7 @@ class Atom:
     # ---- SCF ----
     def scf(self, nela: int, nelb: int, method: str = "hf", restricted: bool = True, symmetry: int = 1,
             fixed_occ=None, maxiter: int = 0, e_tol: float = 0.0, diis_tol: float = 0.0, stream=None,
-            frac_aufbau: bool = False) -> dict:
+            frac_aufbau: bool = False, split: bool = False) -> dict:
         """Atomic SCF on the device. fixed_occ: dict m -> (n_alpha, n_beta) (symmetry 1)."""
         x, c = (0, 0) if method.lower() == "hf" else parse_xc(method)
         occ = None
@@ -312,7 +312,8 @@ class Atom:
             occ = np.array([v for m in ms for v in fixed_occ.get(m, (0, 0))], dtype=np.int32)
             nfix = len(ms)
         d = _ScfDesc(nela, nelb, int(restricted), symmetry, x, c, -1.0, maxiter, e_tol, diis_tol,
-                     occ.ctypes.data_as(_I) if occ is not None else None, nfix, 0.0, int(frac_aufbau))
+                     occ.ctypes.data_as(_I) if occ is not None else None, nfix, 0.0, int(frac_aufbau),
+                     int(split))
         r = _ScfRes()
         nspin = 1 if restricted else 2
         eps = np.zeros(self.nbf * nspin)
@@ -353,10 +354,11 @@ class Atom:
 
 
 def _scf_desc(nela, nelb, method="hf", restricted=True, symmetry=1, fixed=None, nblocks=0, e_tol=0.0,
-              diis_tol=0.0, maxiter=0, frac_aufbau=False):
+              diis_tol=0.0, maxiter=0, frac_aufbau=False, split=False):
     x, c = (0, 0) if method.lower() == "hf" else parse_xc(method)
     return _ScfDesc(nela, nelb, int(restricted), symmetry, x, c, -1.0, maxiter, e_tol, diis_tol,
-                    fixed.ctypes.data_as(_I) if fixed is not None else None, nblocks, 0.0, int(frac_aufbau))
+                    fixed.ctypes.data_as(_I) if fixed is not None else None, nblocks, 0.0, int(frac_aufbau),
+                    int(split))
 
 
 class Engine:
@@ -369,7 +371,7 @@ class Engine:
         self._h = h
 
     def submit(self, Z, bval, lval, mval, nela, nelb, method="hf", restricted=True, nnodes=15, symmetry=1,
-               fixed_occ=None, e_tol=0.0, diis_tol=0.0, frac_aufbau=False) -> int:
+               fixed_occ=None, e_tol=0.0, diis_tol=0.0, frac_aufbau=False, split=False) -> int:
         bval = np.ascontiguousarray(bval, dtype=np.float64)
         lval = np.ascontiguousarray(lval, dtype=np.int32)
         mval = np.ascontiguousarray(mval, dtype=np.int32)
@@ -381,7 +383,7 @@ class Engine:
             occ = np.array([v for m in ms for v in fixed_occ.get(m, (0, 0))], dtype=np.int32)
             nfix = len(ms)
         sd = _scf_desc(nela, nelb, method, restricted, symmetry, occ, nfix, e_tol, diis_tol,
-                       frac_aufbau=frac_aufbau)
+                       frac_aufbau=frac_aufbau, split=split)
         jid = ctypes.c_ulonglong()
         _check(_lib.hfg_engine_submit(self._h, ctypes.byref(ad), ctypes.byref(sd), ctypes.byref(jid)))
         return jid.value

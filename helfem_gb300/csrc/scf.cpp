@@ -217,6 +217,13 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     }
     Eigh eg;
     const double one = 1.0, zero = 0.0;
+    // split-precision exchange needs a float2 copy of the density
+    DBuf dP2;
+    hfg::DevScratch scr_split = a->scr;
+    if (d->split_exchange && kfrac != 0.0) {
+      dP2.alloc(sizeof(float2) * nb2);
+      scr_split.p2 = dP2.as<float2>();
+    }
 
     // X^T M_k X for block k of AO matrix M into out (nk x nk)
     auto to_ortho = [&](const double* M, const Block& b, double* out) {
@@ -340,10 +347,16 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       // ---- Fock build (main.cpp:386-446) ----
       ck(hfg::launch_coulomb_fp64(a->dev, a->scr, dP.as<double>(), dJ.as<double>(), true, st, &a->prof), "J");
       if (kfrac != 0.0)
-        for (int s = 0; s < nspin; ++s)
-          ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, dPs[s].as<double>(), dK[s].as<double>(), true, st,
-                                       &a->prof),
-             "K");
+        for (int s = 0; s < nspin; ++s) {
+          if (d->split_exchange)
+            ck(hfg::launch_exchange_split(a->dev, scr_split, a->units, dPs[s].as<double>(), dK[s].as<double>(), true,
+                                          st, &a->prof),
+               "K (split)");
+          else
+            ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, dPs[s].as<double>(), dK[s].as<double>(), true,
+                                         st, &a->prof),
+               "K");
+        }
       if (have_xc)
         ck(hfg::launch_xc_fp64(a->dev, a->xc, a->xs, d->x_func, d->c_func,
                                restricted ? dP.as<double>() : dPs[0].as<double>(),

@@ -229,6 +229,7 @@ typedef struct {
                               frontier shell are shared equally over it
                               (spherically averaged open shells); 0: integer
                               Aufbau as the reference                         */
+  int split_exchange;      /* 1: exchange in the split-precision form          */
 } hfg_scf_desc;
 typedef struct {
   double Etot, Ekin, Enuc, Ecoul, Exx, Exc, Nel_grid;
