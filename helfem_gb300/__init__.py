@@ -116,7 +116,10 @@ class _ScfDesc(ctypes.Structure):
 
 class _ScfRes(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("Etot", "Ekin", "Enuc", "Ecoul", "Exx", "Exc", "Nel_grid")] + \
-               [("iterations", ctypes.c_int), ("converged", ctypes.c_int)]
+               [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("phase_ms", ctypes.c_double * 6)]
+
+
+PHASES = ("fock", "energies", "ortho_errors", "diis", "eigh_occupy", "density")
 
 
 class _JobRes(ctypes.Structure):
@@ -319,7 +322,8 @@ class Atom:
         eps = np.zeros(self.nbf * nspin)
         _check(_lib.hfg_scf_run(self._h, ctypes.byref(d), ctypes.byref(r), _dptr(eps),
                                 _stream(stream) if stream is not None else None))
-        out = {n: getattr(r, n) for n, _ in _ScfRes._fields_}
+        out = {n: getattr(r, n) for n, _ in _ScfRes._fields_ if n != "phase_ms"}
+        out["phase_ms"] = dict(zip(PHASES, list(r.phase_ms)))
         out["orbital_energies"] = eps
         return out
 
@@ -391,7 +395,8 @@ class Engine:
     def wait(self, job_id: int, timeout_s: float = -1.0) -> dict:
         r = _JobRes()
         _check(_lib.hfg_engine_wait(self._h, job_id, timeout_s, ctypes.byref(r)))
-        out = {n: getattr(r.scf, n) for n, _ in _ScfRes._fields_}
+        out = {n: getattr(r.scf, n) for n, _ in _ScfRes._fields_ if n != "phase_ms"}
+        out["phase_ms"] = dict(zip(PHASES, list(r.scf.phase_ms)))
         out.update(status=r.status, queue_ms=r.queue_ms, setup_ms=r.setup_ms, scf_ms=r.scf_ms,
                    total_ms=r.total_ms, footprint_bytes=r.footprint_bytes, error=r.error.decode())
         return out

@@ -20,6 +20,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <map>
 #include <numeric>
@@ -70,6 +71,19 @@ struct Eigh {
     cs(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, A, n, w, work.as<double>(), lwork,
                         info.as<int>()),
        "syevd");
+  }
+};
+
+// Host wall-clock per SCF phase; every phase ends at a point where the host
+// waits for the device anyway (a blocking dot product, the eigenvalue copy),
+// so the split costs no extra synchronisation.
+struct PhaseTimer {
+  double ms[7] = {0, 0, 0, 0, 0, 0, 0};
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void lap(int k) {
+    const auto n = std::chrono::steady_clock::now();
+    ms[k] += std::chrono::duration<double, std::milli>(n - t).count();
+    t = n;
   }
 };
 
@@ -343,6 +357,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     int it = 0, nh = 0;
     bool converged = false;
     double Ekin = 0, Enuc = 0, Ecoul = 0, Exx = 0, Exc = 0, Ngrid = 0, Etot = 0;
+    PhaseTimer pt;
     for (it = 1; it <= maxiter; ++it) {
       // ---- Fock build (main.cpp:386-446) ----
       ck(hfg::launch_coulomb_fp64(a->dev, a->scr, dP.as<double>(), dJ.as<double>(), true, st, &a->prof), "J");
@@ -371,6 +386,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
                     kfrac != 0.0 ? dK[s].as<double>() : nullptr, have_xc ? dXC[s].as<double>() : nullptr, nb2, st);
       }
       Ekin = dot(dP.as<double>(), T);
+      pt.lap(0);  // Fock build (J, K, XC, assembly) + first blocking dot
       Enuc = dot(dP.as<double>(), V);
       Ecoul = 0.5 * dot(dP.as<double>(), dJ.as<double>());
       Exx = 0.0;
@@ -386,6 +402,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         Ngrid = e[1];
       }
       Etot = Ekin + Enuc + Ecoul + Exx + Exc;
+      pt.lap(1);  // energies
 
       // ---- orthonormal Fock blocks and DIIS errors F'D' - D'F' ----
       double emax = 0.0;
@@ -422,6 +439,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         ck(cudaStreamSynchronize(st), "sync");
         emax = std::fabs(emax);
       }
+      pt.lap(2);  // orthonormal blocks + DIIS errors
       if (it > 1 && std::fabs(Etot - Eold) < etol && emax < dtol) {
         converged = true;
         break;
@@ -475,9 +493,13 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       ck(cudaMemsetAsync(dFo.p, 0, sizeof(double) * Ltot, st), "memset");
       for (int i = 0; i < nh; ++i)
         cb(cublasDaxpy(hd.bl, (int)Ltot, &c[i], hF[i].as<double>(), 1, dFo.as<double>(), 1), "axpy");
+      pt.lap(3);  // DIIS extrapolation
       for (int s = 0; s < nspin; ++s) diagonalise(dFo.as<double>(), s);
       occupy();
+      pt.lap(4);  // eigensolves + occupations
       build_density();
+      ck(cudaStreamSynchronize(st), "sync");
+      pt.lap(5);  // density
     }
     ck(cudaStreamSynchronize(st), "sync");
     a->mark_use(st);
@@ -489,6 +511,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     res->Exc = Exc;
     res->Nel_grid = Ngrid;
     res->iterations = std::min(it, maxiter);
+    for (int k = 0; k < 6; ++k) res->phase_ms[k] = pt.ms[k];
     res->converged = converged ? 1 : 0;
     if (orbital_energies) std::memcpy(orbital_energies, eps.data(), sizeof(double) * eps.size());
   }

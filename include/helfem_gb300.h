@@ -234,6 +234,10 @@ typedef struct {
 typedef struct {
   double Etot, Ekin, Enuc, Ecoul, Exx, Exc, Nel_grid;
   int iterations, converged;
+  /* wall milliseconds per phase over all iterations: 0 Fock build, 1 energies,
+   * 2 orthonormal blocks + DIIS errors, 3 DIIS extrapolation,
+   * 4 eigensolves + occupations, 5 density */
+  double phase_ms[6];
 } hfg_scf_result;
 /* orbital_energies (host, may be NULL): nbf per spin, blocks concatenated in
  * block order, ascending within a block. Runs on `stream` (NULL: the
