@@ -424,7 +424,7 @@ def run_engine_batch(jobs, n_workers, budget_gb, split):
     eng = hg.Engine(n_workers=n_workers, hbm_budget_gb=budget_gb)
     t0 = time.perf_counter()
     ids = [eng.submit(j["Z"], j["bval"], j["lval"], j["mval"], j["nela"], j["nelb"], j["method"], j["restricted"],
-                      nnodes=j["nnodes"], symmetry=2, frac_aufbau=True, split=split) for j in jobs]
+                      nnodes=j["nnodes"], symmetry=2, split=split, l_occ=j["l_occ"]) for j in jobs]
     res = [eng.wait(i) for i in ids]
     wall = time.perf_counter() - t0
     eng.close()
@@ -455,7 +455,7 @@ def run_scf_batch(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{len(jobs)} seeded atoms: Z 1-86, {10}-{args.nel_max} elements, nodes "
                                "{10,13,15,17}, Rmax 40-80, lmax by occupied shells, HF / LDA(Slater+PW92) 50/50, "
-                               "restricted, fractional Aufbau, per-(l,m) blocks, to 1e-10 Eh",
+                               "restricted, Madelung occupations per l (spherically averaged), per-(l,m) blocks, to 1e-10 Eh",
                    "workers": args.workers, "hbm_budget_gb": 180.0},
         "converged": len(ok), "iterations_mean": float(np.mean([r["iterations"] for r in res])),
         "latency_ms": {"p50": _percentile(lat, 0.5), "p99": _percentile(lat, 0.99)},
@@ -489,7 +489,7 @@ def run_serve(args):
             if dt > 0:
                 time.sleep(dt)
             ids.append(eng.submit(j["Z"], j["bval"], j["lval"], j["mval"], j["nela"], j["nelb"], j["method"],
-                                  j["restricted"], nnodes=j["nnodes"], symmetry=2, frac_aufbau=True, split=True))
+                                  j["restricted"], nnodes=j["nnodes"], symmetry=2, split=True, l_occ=j["l_occ"]))
         res = [eng.wait(i) for i in ids]
     wall = time.perf_counter() - t0
     eng.close()

@@ -111,7 +111,8 @@ class _ScfDesc(ctypes.Structure):
                 ("symmetry", ctypes.c_int), ("x_func", ctypes.c_int), ("c_func", ctypes.c_int),
                 ("kfrac", ctypes.c_double), ("maxiter", ctypes.c_int), ("e_tol", ctypes.c_double),
                 ("diis_tol", ctypes.c_double), ("fixed_occ", _I), ("n_fixed_blocks", ctypes.c_int),
-                ("dftthr", ctypes.c_double), ("frac_aufbau", ctypes.c_int), ("split_exchange", ctypes.c_int)]
+                ("dftthr", ctypes.c_double), ("frac_aufbau", ctypes.c_int), ("split_exchange", ctypes.c_int),
+                ("l_occ", _D), ("n_l_occ", ctypes.c_int)]
 
 
 class _ScfRes(ctypes.Structure):
@@ -305,8 +306,9 @@ class Atom:
     # ---- SCF ----
     def scf(self, nela: int, nelb: int, method: str = "hf", restricted: bool = True, symmetry: int = 1,
             fixed_occ=None, maxiter: int = 0, e_tol: float = 0.0, diis_tol: float = 0.0, stream=None,
-            frac_aufbau: bool = False, split: bool = False) -> dict:
-        """Atomic SCF on the device. fixed_occ: dict m -> (n_alpha, n_beta) (symmetry 1)."""
+            frac_aufbau: bool = False, split: bool = False, l_occ=None) -> dict:
+        """Atomic SCF on the device. fixed_occ: dict m -> (n_alpha, n_beta) (symmetry 1);
+        l_occ: [lmax+1][2] alpha/beta electrons per l shared equally over m (symmetry 2)."""
         x, c = (0, 0) if method.lower() == "hf" else parse_xc(method)
         occ = None
         nfix = 0
@@ -314,9 +316,11 @@ class Atom:
             ms = sorted(set(int(m) for m in self.mval))
             occ = np.array([v for m in ms for v in fixed_occ.get(m, (0, 0))], dtype=np.int32)
             nfix = len(ms)
+        lo = None if l_occ is None else np.ascontiguousarray(np.asarray(l_occ, dtype=np.float64).ravel())
         d = _ScfDesc(nela, nelb, int(restricted), symmetry, x, c, -1.0, maxiter, e_tol, diis_tol,
                      occ.ctypes.data_as(_I) if occ is not None else None, nfix, 0.0, int(frac_aufbau),
-                     int(split))
+                     int(split), lo.ctypes.data_as(_D) if lo is not None else None,
+                     len(lo) // 2 if lo is not None else 0)
         r = _ScfRes()
         nspin = 1 if restricted else 2
         eps = np.zeros(self.nbf * nspin)
@@ -358,11 +362,12 @@ class Atom:
 
 
 def _scf_desc(nela, nelb, method="hf", restricted=True, symmetry=1, fixed=None, nblocks=0, e_tol=0.0,
-              diis_tol=0.0, maxiter=0, frac_aufbau=False, split=False):
+              diis_tol=0.0, maxiter=0, frac_aufbau=False, split=False, l_occ=None):
     x, c = (0, 0) if method.lower() == "hf" else parse_xc(method)
     return _ScfDesc(nela, nelb, int(restricted), symmetry, x, c, -1.0, maxiter, e_tol, diis_tol,
                     fixed.ctypes.data_as(_I) if fixed is not None else None, nblocks, 0.0, int(frac_aufbau),
-                    int(split))
+                    int(split), l_occ.ctypes.data_as(_D) if l_occ is not None else None,
+                    len(l_occ) // 2 if l_occ is not None else 0)
 
 
 class Engine:
@@ -375,7 +380,7 @@ class Engine:
         self._h = h
 
     def submit(self, Z, bval, lval, mval, nela, nelb, method="hf", restricted=True, nnodes=15, symmetry=1,
-               fixed_occ=None, e_tol=0.0, diis_tol=0.0, frac_aufbau=False, split=False) -> int:
+               fixed_occ=None, e_tol=0.0, diis_tol=0.0, frac_aufbau=False, split=False, l_occ=None) -> int:
         bval = np.ascontiguousarray(bval, dtype=np.float64)
         lval = np.ascontiguousarray(lval, dtype=np.int32)
         mval = np.ascontiguousarray(mval, dtype=np.int32)
@@ -386,8 +391,9 @@ class Engine:
             ms = sorted(set(int(m) for m in mval))
             occ = np.array([v for m in ms for v in fixed_occ.get(m, (0, 0))], dtype=np.int32)
             nfix = len(ms)
+        lo = None if l_occ is None else np.ascontiguousarray(np.asarray(l_occ, dtype=np.float64).ravel())
         sd = _scf_desc(nela, nelb, method, restricted, symmetry, occ, nfix, e_tol, diis_tol,
-                       frac_aufbau=frac_aufbau, split=split)
+                       frac_aufbau=frac_aufbau, split=split, l_occ=lo)
         jid = ctypes.c_ulonglong()
         _check(_lib.hfg_engine_submit(self._h, ctypes.byref(ad), ctypes.byref(sd), ctypes.byref(jid)))
         return jid.value

@@ -45,6 +45,7 @@ struct Job {
   // owned copies of the caller's arrays
   std::vector<double> bval;
   std::vector<int> lval, mval, fixed;
+  std::vector<double> l_occ;
   hfg_atom_desc atom{};
   hfg_scf_desc scf{};
   size_t footprint = 0;
@@ -204,6 +205,11 @@ hfg_status hfg_engine_submit(hfg_engine* e, const hfg_atom_desc* atom, const hfg
     if (scf->fixed_occ) {
       j->fixed.assign(scf->fixed_occ, scf->fixed_occ + 2 * scf->n_fixed_blocks);
       j->scf.fixed_occ = j->fixed.data();
+    }
+    if (scf->l_occ) {
+      need(scf->n_l_occ >= 1 && scf->n_l_occ <= 64, "hfg_engine_submit: bad l_occ size");
+      j->l_occ.assign(scf->l_occ, scf->l_occ + 2 * scf->n_l_occ);
+      j->scf.l_occ = j->l_occ.data();
     }
     j->footprint = hfg_job_footprint(j->atom, j->scf);
     j->t_submit = Clock::now();

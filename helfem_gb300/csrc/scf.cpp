@@ -148,6 +148,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       b.d_ang.upload(b.ang);
     }
     if (d->fixed_occ) need(d->n_fixed_blocks == nblk, "hfg_scf_run: fixed_occ needs one (alpha, beta) pair per block");
+    if (d->l_occ) need(d->symmetry == 2 && d->n_l_occ >= 1, "hfg_scf_run: l_occ needs symmetry 2");
 
     // ---- radial orthonormaliser X = invh(S_rad) (utils.cpp:120-159) ----
     const size_t nr2 = (size_t)nrad * nrad, nb2 = (size_t)nbf * nbf;
@@ -261,7 +262,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     // (one call for every block of a size; ~3-7x faster than one syevd per
     // block on GB300). Spherical solves (per-(l,m) blocks with fractional
     // Aufbau) diagonalise one block per l and copy it to the other m.
-    const bool spherical = d->symmetry == 2 && d->frac_aufbau && !d->fixed_occ;
+    const bool spherical = d->symmetry == 2 && ((d->frac_aufbau && !d->fixed_occ) || d->l_occ);
     std::vector<int> rep(nblk);  // block whose eigenpairs block k uses
     for (int k = 0; k < nblk; ++k) {
       rep[k] = k;
@@ -337,7 +338,18 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
           for (int i = 0; i < blocks[k].nk; ++i) all.push_back({eps[(size_t)nbf * s + eo + i], {k, i}});
           eo += blocks[k].nk;
         }
-        if (d->fixed_occ) {
+        if (d->l_occ) {
+          for (int k = 0; k < nblk; ++k) {
+            const int l = H.lval[blocks[k].ang[0]];
+            double left = 0.0;
+            if (l < d->n_l_occ)
+              left = (restricted ? d->l_occ[2 * l] + d->l_occ[2 * l + 1] : d->l_occ[2 * l + s]) / (2.0 * l + 1.0);
+            for (int i = 0; i < blocks[k].nk && left > 1e-14; ++i) {
+              occ[s][k][i] = std::min(maxocc, left);
+              left -= occ[s][k][i];
+            }
+          }
+        } else if (d->fixed_occ) {
           for (int k = 0; k < nblk; ++k) {
             double left = restricted ? d->fixed_occ[2 * k] + d->fixed_occ[2 * k + 1] : d->fixed_occ[2 * k + s];
             for (int i = 0; i < blocks[k].nk && left > 0; ++i) {
@@ -410,8 +422,11 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     };
 
     // ---- core-Hamiltonian guess (iguess 0) ----
+    ck(cudaMemsetAsync(dFo.p, 0, sizeof(double) * Ltot, st), "memset");
+    ck(cudaMemsetAsync(dEo.p, 0, sizeof(double) * Ltot, st), "memset");
     for (int s = 0; s < nspin; ++s)
-      for (auto& b : blocks) to_ortho(dH.as<double>(), b, dFo.as<double>() + Lblk * s + b.off);
+      for (int k = 0; k < nblk; ++k)
+        if (rep[k] == k) to_ortho(dH.as<double>(), blocks[k], dFo.as<double>() + Lblk * s + blocks[k].off);
     for (int s = 0; s < nspin; ++s) diagonalise(dFo.as<double>(), s);
     occupy();
     build_density();
@@ -471,6 +486,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       double emax = 0.0;
       for (int s = 0; s < nspin; ++s)
         for (int k = 0; k < nblk; ++k) {
+          if (rep[k] != k) continue;  // identical to its representative (spherical solves)
           const Block& b = blocks[k];
           double* Fo = dFo.as<double>() + Lblk * s + b.off;
           double* Eo = dEo.as<double>() + Lblk * s + b.off;

@@ -6,9 +6,10 @@ in a range, nodes per element from {10, 13, 15, 17}, Rmax uniform in
 50/50. Stream: Poisson arrivals; Z in 1..zmax with charge -1..+3,
 spin-restricted or unrestricted, HF / LDA / PBE, 15-node elements.
 
-Open shells are solved with fractional Aufbau over the degenerate frontier
-shell (spherically averaged densities), which makes per-(l,m) symmetry
-blocks exact and the solves robust.
+Occupations are fixed per angular momentum from Madelung-order filling of
+each spin and shared equally over the 2l+1 m components (spherically
+averaged open shells), which makes per-(l,m) symmetry blocks exact and the
+solves robust.
 """
 from __future__ import annotations
 
@@ -28,6 +29,21 @@ def occupied_lmax(nel: int) -> int:
         lmax = max(lmax, l)
         left -= 2 * (2 * l + 1)
     return lmax
+
+
+def l_occupations(nela: int, nelb: int, lmax: int) -> np.ndarray:
+    """Alpha/beta electrons per l from Madelung-order filling of each spin,
+    [lmax+1][2]; used as spherically averaged fixed occupations."""
+    out = np.zeros((lmax + 1, 2))
+    for s, n in enumerate((nela, nelb)):
+        left = n
+        for _, l in _ORDER:
+            if left <= 0:
+                break
+            take = min(left, 2 * l + 1)
+            out[l, s] += take
+            left -= take
+    return out
 
 
 def grid(rmax: float, nelem: int, zexp: float = 2.0) -> np.ndarray:
@@ -62,8 +78,9 @@ def batch_atoms(n: int, seed: int = 2024, zmax: int = 86, nel_range=(10, 60), no
         rmax = float(rng.uniform(*rmax_range))
         method = "hf" if rng.random() < 0.5 else "lda_x-lda_c_pw"
         lv, mv = angular(lmax, lmax)
-        out.append(dict(Z=Z, nela=(Z + 1) // 2, nelb=Z // 2, restricted=True, method=method, nnodes=nn,
-                        bval=grid(rmax, nelem), lval=lv, mval=mv))
+        nela, nelb = (Z + 1) // 2, Z // 2
+        out.append(dict(Z=Z, nela=nela, nelb=nelb, restricted=True, method=method, nnodes=nn,
+                        bval=grid(rmax, nelem), lval=lv, mval=mv, l_occ=l_occupations(nela, nelb, lmax)))
     return out
 
 
@@ -79,6 +96,7 @@ def stream_atoms(n: int, seed: int = 7, zmax: int = 86, nel_range=(10, 80)):
         method = ["hf", "lda_x-lda_c_vwn", "gga_x_pbe-gga_c_pbe"][int(rng.integers(0, 3))]
         restricted = bool(rng.random() < 0.5)
         lv, mv = angular(lmax, lmax)
-        out.append(dict(Z=Z, nela=(nel + 1) // 2, nelb=nel // 2, restricted=restricted, method=method, nnodes=15,
-                        bval=grid(40.0, nelem), lval=lv, mval=mv))
+        nela, nelb = (nel + 1) // 2, nel // 2
+        out.append(dict(Z=Z, nela=nela, nelb=nelb, restricted=restricted, method=method, nnodes=15,
+                        bval=grid(40.0, nelem), lval=lv, mval=mv, l_occ=l_occupations(nela, nelb, lmax)))
     return out

@@ -230,6 +230,11 @@ typedef struct {
                               (spherically averaged open shells); 0: integer
                               Aufbau as the reference                         */
   int split_exchange;      /* 1: exchange in the split-precision form          */
+  const double* l_occ;     /* NULL, or (symmetry 2) [n_l_occ][2] alpha/beta
+                              electrons per l, shared equally over its 2l+1
+                              m blocks and filled lowest-first within a block
+                              (spherically averaged fixed occupations)      */
+  int n_l_occ;
 } hfg_scf_desc;
 typedef struct {
   double Etot, Ekin, Enuc, Ecoul, Exx, Exc, Nel_grid;

@@ -90,3 +90,12 @@ def test_errors_are_status_codes():
     with pytest.raises(hg.HfgError) as e:
         A.coulomb(1 << 20, 1 << 21, 0)
     assert e.value.status == hg.HFG_ERR_STATE
+
+
+def test_madelung_l_occupations():
+    from helfem_gb300 import workloads as wl
+    occ = wl.l_occupations(13, 13, 2)  # Fe: [Ar] 4s2 3d6 restricted-averaged -> 13 per spin
+    assert occ.tolist() == [[4, 4], [6, 6], [3, 3]]
+    occ = wl.l_occupations(5, 3, 1)  # O
+    assert occ.tolist() == [[2, 2], [3, 1]]
+    assert wl.l_occupations(1, 0, 0).tolist() == [[1, 0]]

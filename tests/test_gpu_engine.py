@@ -79,3 +79,22 @@ def test_fractional_aufbau_open_shell_converges():
     eng.close()
     for j, r in zip(jobs, res):
         assert r["status"] == 2 and r["converged"], (j["Z"], r)
+
+
+def test_spherical_l_occupations_match_fractional_aufbau():
+    """Per-l fixed occupations shared over m give the fractional-Aufbau
+    solution wherever Aufbau fills the same shells (light open shells)."""
+    torch_cuda()
+    jobs = wl.batch_atoms(4, seed=3, zmax=18, nel_range=(6, 8), nodes=(10,))
+    eng = hg.Engine(n_workers=4, hbm_budget_gb=40.0)
+    ids = []
+    for j in jobs:
+        for kw in (dict(frac_aufbau=True), dict(l_occ=j["l_occ"])):
+            ids.append(eng.submit(j["Z"], j["bval"], j["lval"], j["mval"], j["nela"], j["nelb"], j["method"],
+                                  j["restricted"], nnodes=j["nnodes"], symmetry=2, **kw))
+    res = [eng.wait(i) for i in ids]
+    eng.close()
+    for i, j in enumerate(jobs):
+        fa, lo = res[2 * i], res[2 * i + 1]
+        assert fa["status"] == 2 and lo["status"] == 2 and lo["converged"], (j["Z"], fa, lo)
+        assert abs(fa["Etot"] - lo["Etot"]) < 1e-8, (j["Z"], fa["Etot"], lo["Etot"])
