@@ -191,9 +191,9 @@ def fp32_peak_tflops(torch) -> float:
         torch.backends.cuda.matmul.allow_tf32 = prev
 
 
-def profiled_traffic():
-    """Per-launch DRAM bytes of k_tiles from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_tiles_kr.txt")
+def profiled_traffic(kernel="k_tiles"):
+    """Per-launch DRAM bytes of the exchange tile kernel from its committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", kernel + "_kr.txt")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -359,7 +359,7 @@ def run_ours(args):
     achieved = kflops / (off_ms * 1e-3) / 1e12  # FP64-equivalent algorithmic FLOPs
     peak = fp64_peak_tflops(torch)
     fp32 = fp32_peak_tflops(torch)
-    traffic = profiled_traffic()
+    traffic = profiled_traffic("k_tiles_split" if split else "k_tiles")
     hbm_peak = measured_peaks().get("hbm_gbs")
     kernel_ms = {k: (v[1] / max(v[0], 1)) for k, v in prof.items()}
     if split:
