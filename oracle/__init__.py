@@ -24,20 +24,27 @@ from . import tabulate  # noqa: F401
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "_build", "libfock_ref.so")
+_DLIB = os.path.join(_HERE, "_build", "libdfock_ref.so")
 _lock = threading.Lock()
 _lib = None
+_dlib = None
+
+
+def _compile(src_name: str, out: str, force: bool) -> str:
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    src = os.path.join(_HERE, src_name)
+    if force or not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        tmp = out + f".tmp{os.getpid()}"
+        subprocess.check_call(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
+                               src, "-o", tmp])
+        os.replace(tmp, out)
+    return out
 
 
 def build(force: bool = False) -> str:
-    """Compile the C++ oracle (plain g++, OpenMP)."""
-    os.makedirs(os.path.dirname(_LIB), exist_ok=True)
-    src = os.path.join(_HERE, "fock_ref.cpp")
-    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
-        tmp = _LIB + f".tmp{os.getpid()}"
-        subprocess.check_call(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
-                               src, "-o", tmp])
-        os.replace(tmp, _LIB)
-    return _LIB
+    """Compile the C++ oracles (plain g++, OpenMP): atomic and diatomic."""
+    _compile("dfock_ref.cpp", _DLIB, force)
+    return _compile("fock_ref.cpp", _LIB, force)
 
 
 class _OraAtom(ctypes.Structure):
@@ -139,3 +146,88 @@ class FockOracle:
         K = np.zeros((self.nbf, self.nbf), order="F")
         lib().ora_exchange(ctypes.byref(self.s), P.ctypes.data, K.ctypes.data)
         return K
+
+
+# ---------------------------------------------------------------------------
+# Diatomic (prolate spheroidal) basis
+# ---------------------------------------------------------------------------
+
+
+class _OraDiatomic(ctypes.Structure):
+    _fields_ = [
+        ("nrad", ctypes.c_int), ("nang", ctypes.c_int), ("nel", ctypes.c_int), ("nn", ctypes.c_int),
+        ("nlm", ctypes.c_int), ("Lmax", ctypes.c_int), ("mmax", ctypes.c_int), ("Rhalf", ctypes.c_double),
+        ("lval", ctypes.c_void_p), ("mval", ctypes.c_void_p), ("first", ctypes.c_void_p), ("ni", ctypes.c_void_p),
+        ("lm_L", ctypes.c_void_p), ("lm_M", ctypes.c_void_p),
+        ("P0", ctypes.c_void_p), ("P2", ctypes.c_void_p), ("Q0", ctypes.c_void_p), ("Q2", ctypes.c_void_p),
+        ("cdB", ctypes.c_void_p), ("cdB_off", ctypes.c_void_p), ("cds", ctypes.c_void_p),
+        ("cds_off", ctypes.c_void_p), ("cd_rank", ctypes.c_void_p),
+        ("coef", ctypes.c_void_p), ("modc", ctypes.c_void_p),
+    ]
+
+
+def dlib():
+    global _dlib
+    with _lock:
+        if _dlib is None:
+            _dlib = ctypes.CDLL(_compile("dfock_ref.cpp", _DLIB, False))
+            _dlib.ora_dexchange.argtypes = [ctypes.POINTER(_OraDiatomic), ctypes.c_void_p, ctypes.c_void_p]
+            _dlib.ora_dexchange.restype = None
+            _dlib.ora_num_threads_d.restype = ctypes.c_int
+    return _dlib
+
+
+class DiatomicOracle:
+    """J (numpy) and K (compiled, OpenMP) of a diatomic basis from
+    ``diatomic.build_diatomic`` tables; inputs and outputs are pure-basis
+    (boundary-removed) matrices, as the reference's coulomb/exchange take."""
+
+    def __init__(self, D):
+        from . import diatomic as dia
+        self.D = D
+        nel, nlm, nn = D.nel, len(D.lm), D.nnodes
+        keep = []
+
+        def arr(x, dt):
+            a = np.ascontiguousarray(np.asarray(x, dtype=dt))
+            keep.append(a)
+            return a.ctypes.data
+
+        pads = {}
+        for name in ("P0", "P2", "Q0", "Q2"):
+            buf = np.zeros((nlm, nel, nn, nn))
+            src = getattr(D, name)
+            for i in range(nlm):
+                for e in range(nel):
+                    m = src[i][e]
+                    buf[i, e, :m.shape[0], :m.shape[1]] = m.T  # row-major (c, r) -> column-major tile
+            pads[name] = buf
+        cb, cs, boff, soff, rank = [], [], [], [], []
+        ob = os_ = 0
+        for i in range(nlm):
+            for e in range(nel):
+                B = D.cdB[i][e]
+                boff.append(ob); cb.append(B.ravel(order="F")); ob += B.size
+                soff.append(os_); cs.append(D.cds[i][e]); os_ += D.cds[i][e].size
+                rank.append(B.shape[1])
+        co, mo, Lmax, mmax = dia.gaunt_tables(D)
+        self.s = _OraDiatomic(
+            D.nrad, D.nang, nel, nn, nlm, Lmax, mmax, D.Rhalf,
+            arr(D.lval, np.int32), arr(D.mval, np.int32), arr(D.first, np.int32), arr(D.ni, np.int32),
+            arr([L for L, _ in D.lm], np.int32), arr([M for _, M in D.lm], np.int32),
+            arr(pads["P0"], np.float64), arr(pads["P2"], np.float64), arr(pads["Q0"], np.float64),
+            arr(pads["Q2"], np.float64),
+            arr(np.concatenate(cb) if cb else np.zeros(1), np.float64), arr(boff, np.int64),
+            arr(np.concatenate(cs) if cs else np.zeros(1), np.float64), arr(soff, np.int64),
+            arr(rank, np.int32), arr(co, np.float64), arr(mo, np.float64))
+        self._keep = keep
+
+    def coulomb(self, Ppure: np.ndarray) -> np.ndarray:
+        from . import diatomic as dia
+        return dia.coulomb(self.D, np.asarray(Ppure, dtype=np.float64))
+
+    def exchange(self, Ppure: np.ndarray) -> np.ndarray:
+        Pd = np.asfortranarray(self.D.expand(np.asarray(Ppure, dtype=np.float64)))
+        Kd = np.zeros_like(Pd, order="F")
+        dlib().ora_dexchange(ctypes.byref(self.s), Pd.ctypes.data, Kd.ctypes.data)
+        return self.D.remove(Kd)

@@ -41,7 +41,10 @@ class SCFResult:
 
 
 def sym_blocks(atom: tab.AtomTables):
-    """Per-m blocks, unique m ascending (TwoDBasis.cpp:218-232, symmetry=1)."""
+    """Per-m blocks, unique m ascending (TwoDBasis.cpp:218-232, symmetry=1;
+    diatomic: basis.cpp:906-918 over the pure functions)."""
+    if hasattr(atom, "sym_blocks"):
+        return atom.sym_blocks()
     n = atom.nrad
     out = []
     for m in sorted(set(int(x) for x in atom.mval)):
