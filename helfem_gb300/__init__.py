@@ -83,6 +83,22 @@ _SIGS = {
     "hfg_engine_destroy": ([_P], ctypes.c_int),
     "hfg_profile_enable": ([_P, ctypes.c_int], ctypes.c_int),
     "hfg_profile_read": ([_P, _P, ctypes.c_int], ctypes.c_int),
+    "hfg_diatomic_create": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
+    "hfg_diatomic_destroy": ([_P], ctypes.c_int),
+    "hfg_diatomic_get_dims": ([_P, _P], ctypes.c_int),
+    "hfg_diatomic_pure_indices": ([_P, _I], ctypes.c_int),
+    "hfg_diatomic_overlap": ([_P, _D], ctypes.c_int),
+    "hfg_diatomic_kinetic": ([_P, _D], ctypes.c_int),
+    "hfg_diatomic_nuclear": ([_P, _D], ctypes.c_int),
+    "hfg_diatomic_one_electron_block": ([_P, ctypes.c_int, ctypes.c_int, _D, _I], ctypes.c_int),
+    "hfg_diatomic_tables": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _I, _D, _D], ctypes.c_int),
+    "hfg_legendre_pq": ([ctypes.c_int, ctypes.c_int, ctypes.c_double, _D, _D], ctypes.c_int),
+    "hfg_gaunt_mod": ([ctypes.c_int] * 6 + [_D], ctypes.c_int),
+    "hfg_diatomic_coulomb": ([_P, _P, _P, _P], ctypes.c_int),
+    "hfg_diatomic_exchange": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
+    "hfg_diatomic_coulomb_host": ([_P, _D, _D], ctypes.c_int),
+    "hfg_diatomic_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
+    "hfg_diatomic_work": ([_P, _P, _P], ctypes.c_int),
 }
 KERNEL_CLASSES = ("j_contract", "j_scatter", "k_block_norms", "k_tiles", "k_fixup")
 XC_IDS = {"lda_x": 1, "lda_c_vwn": 7, "lda_c_pw": 12, "gga_x_pbe": 101, "gga_c_pbe": 130}
@@ -422,3 +438,173 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# Diatomic molecules (prolate spheroidal coordinates)
+# ---------------------------------------------------------------------------
+
+
+class _DDesc(ctypes.Structure):
+    _fields_ = [("Z1", ctypes.c_int), ("Z2", ctypes.c_int), ("Rhalf", ctypes.c_double), ("nnodes", ctypes.c_int),
+                ("nelem", ctypes.c_int), ("bval", _D), ("nang", ctypes.c_int), ("lval", _I), ("mval", _I),
+                ("cd_thresh", ctypes.c_double), ("host_only", ctypes.c_int)]
+
+
+class _DDims(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("nrad", "nang", "nel", "nnodes", "ndummy", "nbf", "nlm", "Lmax",
+                                             "rmax", "nchan", "nent")]
+
+
+class _DWork(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("k_offdiag_flops", "k_diag_flops", "k_recouple_flops", "n_entries",
+                                                "k_offdiag_sym_flops", "k_diag_sym_flops",
+                                                "k_recouple_sym_flops", "n_entries_sym")]
+
+
+def lm_to_l_m(lmmax):
+    """Angular basis of a diatomic from lmax per |m| (the reference's
+    lm_to_l_m, src/diatomic/basis.cpp:456-471)."""
+    lv, mv = [], []
+    for mabs, lmx in enumerate(lmmax):
+        for l in range(mabs, int(lmx) + 1):
+            lv.append(l)
+            mv.append(mabs)
+            if mabs > 0:
+                lv.append(l)
+                mv.append(-mabs)
+    return np.array(lv, np.int32), np.array(mv, np.int32)
+
+
+def legendre_pq(Lmax: int, Mmax: int, mu: float):
+    """P[M, L], Q[M, L] of cosh(mu) (Hobson convention), the product's own
+    evaluation."""
+    P = np.zeros((Mmax + 1) * (Lmax + 1))
+    Q = np.zeros_like(P)
+    _check(_lib.hfg_legendre_pq(Lmax, Mmax, mu, _dptr(P), _dptr(Q)))
+    return P.reshape(Mmax + 1, Lmax + 1), Q.reshape(Mmax + 1, Lmax + 1)
+
+
+def gaunt_mod(lj, mj, L, M, li, mi) -> float:
+    v = ctypes.c_double()
+    _check(_lib.hfg_gaunt_mod(lj, mj, L, M, li, mi, ctypes.byref(v)))
+    return v.value
+
+
+class Diatomic:
+    """One diatomic basis (the reference's diatomic TwoDBasis after
+    compute_tei): Z1 at one end of the bond and Z2 at the other, half bond
+    length Rhalf, LIP elements in mu with boundaries ``bval`` and angular
+    functions (lval, mval). Matrices are over the pure basis."""
+
+    def __init__(self, Z1: int, Z2: int, Rhalf: float, bval, lval, mval, nnodes: int = 15,
+                 cd_thresh: float = 1e-12, host_only: bool = False):
+        self._bval = np.ascontiguousarray(bval, dtype=np.float64)
+        self._lval = np.ascontiguousarray(lval, dtype=np.int32)
+        self._mval = np.ascontiguousarray(mval, dtype=np.int32)
+        d = _DDesc(Z1, Z2, Rhalf, nnodes, len(self._bval) - 1, _dptr(self._bval), len(self._lval),
+                   self._lval.ctypes.data_as(_I), self._mval.ctypes.data_as(_I), cd_thresh, int(host_only))
+        h = _P()
+        _check(_lib.hfg_diatomic_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        dims = _DDims()
+        _check(_lib.hfg_diatomic_get_dims(h, ctypes.byref(dims)))
+        self.dims = {n: getattr(dims, n) for n, _ in _DDims._fields_}
+        self.nbf = dims.nbf
+        self.nrad = dims.nrad
+        self.nang = dims.nang
+        self.ndummy = dims.ndummy
+        self.Z1, self.Z2, self.Rhalf = Z1, Z2, Rhalf
+        self.lval, self.mval = self._lval, self._mval
+
+    @classmethod
+    def from_grid(cls, Z1, Z2, Rbond, nelem, lmmax, Rmax=40.0, igrid=4, zexp=1.0, nnodes=15, **kw):
+        """The reference's diatomic driver set-up (src/diatomic/main.cpp:
+        195-217): mu_max = arccosh(Rmax / Rhalf), element grid in mu."""
+        import math
+        Rhalf = 0.5 * Rbond
+        bval = get_grid(math.acosh(Rmax / Rhalf), nelem, igrid, zexp)
+        lv, mv = lm_to_l_m(lmmax)
+        return cls(Z1, Z2, Rhalf, bval, lv, mv, nnodes=nnodes, **kw)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.hfg_diatomic_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pure_indices(self) -> np.ndarray:
+        idx = np.zeros(self.nbf, dtype=np.int32)
+        _check(_lib.hfg_diatomic_pure_indices(self._h, idx.ctypes.data_as(_I)))
+        return idx
+
+    def _one(self, fn):
+        M = np.zeros((self.nbf, self.nbf), order="F")
+        _check(fn(self._h, _dptr(M)))
+        return M
+
+    def overlap(self):
+        return self._one(_lib.hfg_diatomic_overlap)
+
+    def kinetic(self):
+        return self._one(_lib.hfg_diatomic_kinetic)
+
+    def nuclear(self):
+        return self._one(_lib.hfg_diatomic_nuclear)
+
+    def one_electron_block(self, which: str, m: int) -> np.ndarray:
+        w = {"S": 0, "T": 1, "V": 2}[which]
+        n = ctypes.c_int()
+        _check(_lib.hfg_diatomic_one_electron_block(self._h, w, m, None, ctypes.byref(n)))
+        M = np.zeros((n.value, n.value), order="F")
+        _check(_lib.hfg_diatomic_one_electron_block(self._h, w, m, _dptr(M), ctypes.byref(n)))
+        return M
+
+    def tables(self, which: int, ilm: int, iel: int):
+        """(L, |M|, padded table) for which 0..3 (P0, P2, Q0, Q2), or
+        (L, |M|, factor, sigma) for which 4."""
+        L, M, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        nn = self.dims["nnodes"]
+        _check(_lib.hfg_diatomic_tables(self._h, which, ilm, iel, ctypes.byref(L), ctypes.byref(M),
+                                        ctypes.byref(r), None, None))
+        if which < 4:
+            out = np.zeros((nn, nn), order="F")
+            _check(_lib.hfg_diatomic_tables(self._h, which, ilm, iel, None, None, None, _dptr(out), None))
+            return L.value, M.value, out
+        out = np.zeros((2 * nn * nn, r.value), order="F")
+        sg = np.zeros(r.value)
+        _check(_lib.hfg_diatomic_tables(self._h, which, ilm, iel, None, None, None, _dptr(out), _dptr(sg)))
+        return L.value, M.value, out, sg
+
+    # ---- hot path: device pointers ----
+    def coulomb(self, P, J, stream=None):
+        _check(_lib.hfg_diatomic_coulomb(self._h, _ptr(P), _ptr(J), _stream(stream)))
+
+    def exchange(self, P, K, symmetric: bool = False, stream=None):
+        _check(_lib.hfg_diatomic_exchange(self._h, _ptr(P), _ptr(K), EXCHANGE_SYMMETRIC if symmetric else 0,
+                                          _stream(stream)))
+
+    # ---- hot path: host arrays (drop-in value semantics) ----
+    def coulomb_host(self, P: np.ndarray, out: np.ndarray = None) -> np.ndarray:
+        P = np.asfortranarray(P, dtype=np.float64)
+        J = np.zeros_like(P, order="F") if out is None else out
+        _check(_lib.hfg_diatomic_coulomb_host(self._h, _dptr(P), _dptr(J)))
+        return J
+
+    def exchange_host(self, P: np.ndarray, out: np.ndarray = None, symmetric: bool = False) -> np.ndarray:
+        P = np.asfortranarray(P, dtype=np.float64)
+        K = np.zeros_like(P, order="F") if out is None else out
+        _check(_lib.hfg_diatomic_exchange_host(self._h, _dptr(P), _dptr(K),
+                                               EXCHANGE_SYMMETRIC if symmetric else 0))
+        return K
+
+    def work(self, act: np.ndarray = None) -> dict:
+        w = _DWork()
+        a = None if act is None else np.ascontiguousarray(act, dtype=np.uint8)
+        _check(_lib.hfg_diatomic_work(self._h, None if a is None else a.ctypes.data, ctypes.byref(w)))
+        return {n: getattr(w, n) for n, _ in _DWork._fields_}

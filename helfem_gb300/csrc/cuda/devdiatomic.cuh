@@ -1,0 +1,75 @@
+// Device-resident diatomic context shared by the diatomic Fock-build kernels.
+//
+// Radial layout: element e owns an nn x nn primitive tile; primitive p is the
+// global function g(e,p) = e*(nn-1) + p, valid for g < nrad. Dummy AO index
+// = iang*nrad + irad (nd = nang*nrad); matrices are column-major FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace hfg {
+
+struct DevDiatomic {
+  int nn, nel, nrad, nang, nd, nlm, rmax, Lmax, mmax, nM;
+  // per (ilm, e) padded nn x nn tiles
+  const double* p0;
+  const double* p2;
+  const double* q0;
+  const double* q2;
+  const double* cdB;     // [(ilm*nel+e)*2nn^2*rmax]
+  const double* cds;     // [(ilm*nel+e)*rmax]
+  const int* cdrank;     // [ilm*nel+e]
+  const double* tx;      // [((ilm*nel+e)*4 + ab)*(nn^2)^2] exchange-ordered in-element kernel
+  const double* lmfac;   // [ilm] 4 pi Rhalf^5 (L-|M|)!/(L+|M|)! (sign (-1)^M applied at use)
+  // angular coupling table: (a, L, M) -> (b, c0 = cos^2 coupling, c2 = Gaunt)
+  const int* al_ptr;
+  const int* al_b;
+  const double* al_c0;
+  const double* al_c2;
+  // Coulomb channels and bra lists
+  int nchan;
+  const int* ch_L;
+  const int* ch_M;
+  const int* ch_ilm;
+  const double* ch_fac;
+  const int* jbra_ptr;
+  const int* jbra_chan;
+  const double* jbra_c0;
+  const double* jbra_c2;
+  // exchange entries
+  int nent;
+  const int* kjk_ptr;    // [nang^2+1]
+  const int* kent_L;
+  const int* kent_Ma;
+  const int* kent_ilm;
+  const int* kent_jk;    // [nent] owning output block
+  // element pairs: off-diagonal ordered pairs (a != b) and a < b pairs
+  const int2* pairs_all;
+  int npairs_all;
+  const int2* pairs_sym;
+  int npairs_sym;
+};
+
+struct DevDiatomicScratch {
+  double* jin;            // [nchan*nel*2*nn^2]
+  double* jscal;          // [nchan*nel*4]
+  double* khalo;          // [nel*nel*nang^2*(2nn-1)]
+  double* bnorm;          // [nang^2*DNORM_SPLIT]
+  unsigned char* act;     // [nang^2] density block above the screen
+  unsigned char* ent_act; // [nent]
+  unsigned char* jk_act;  // [nang^2]
+  int* jk_list;           // [2*nang^2]: active output blocks, then those with j <= k
+  int* counts;            // [2]
+};
+
+#define DNORM_SPLIT 8
+
+cudaError_t launch_diatomic_expand(const double* P, int nbf, const int* pure, double* Pd, int nd, cudaStream_t st);
+cudaError_t launch_diatomic_gather(const double* Fd, int nd, const int* pure, int nbf, double* F, cudaStream_t st);
+cudaError_t launch_diatomic_tx(const DevDiatomic& D, double* tx, cudaStream_t st);
+cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd, double* Jd,
+                                    cudaStream_t st);
+cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
+                                     double* Kd, bool symmetric, cudaStream_t st);
+
+}  // namespace hfg

@@ -1,0 +1,546 @@
+// Plain-FP64 Coulomb (J) and exchange (K) builds for the diatomic basis.
+//
+// J restates diatomic TwoDBasis::coulomb (src/diatomic/basis.cpp:1621-1815):
+//   dj_contract : per signed (L,M) channel and element, the two Gaunt-weighted
+//                 ket sums over the element-diagonal tile (channel 0 with the
+//                 cos^2-weighted coupling, channel 2 with the plain one), the
+//                 four disjoint traces tr(P0 X0), tr(Q0 X0), tr(P2 X2),
+//                 tr(Q2 X2) times LMfac, and the in-element contraction
+//                 LMfac B diag(sigma) B' [x0; x2].
+//   dj_scatter  : per output angular block and element, the O(Nel) prefix
+//                 sums of the traces (the reference's O(Nel^2) loop) with the
+//                 channel signs (+ for 00, 22; - for 02, 20) and the bra sum.
+// K restates diatomic TwoDBasis::exchange (basis.cpp:1817-2061):
+//   dk_norms / dk_act : density-block screening (||P_il|| < 10 eps skipped).
+//   dk_entry_act      : which (output block, (L,|M|)) entries see an active
+//                       density block; dk_compact lists the active output
+//                       blocks on the device.
+//   dk_tiles          : persistent CTAs over (element pair, active output
+//                       block) items. Each entry recouples the four radial
+//                       matrices R00, R02, R20, R22 from the density with the
+//                       product couplings (the j-side coupling times the
+//                       k-side one, summed in that order), then
+//                       off-diagonal pairs: K -= I0 (R00 J0' + R02 J2') +
+//                       I2 (R20 J0' + R22 J2') with I/J the P- or Q-type
+//                       integrals by element order; in-element blocks: the
+//                       exchange-ordered kernel rebuilt from the factor.
+//   dk_fixup          : the shared-boundary contributions of neighbouring
+//                       tiles, added in a fixed order (bitwise reproducible).
+#include <algorithm>
+#include <cfloat>
+
+#include "devdiatomic.cuh"
+
+namespace hfg {
+namespace {
+
+__device__ __forceinline__ double dwarp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ double dblock_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = dwarp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < nw; ++i) s += red[i];
+  __syncthreads();
+  return s;
+}
+
+__device__ __forceinline__ int dgf(const DevDiatomic& D, int e, int p) { return e * (D.nn - 1) + p; }
+__device__ __forceinline__ int al_idx(const DevDiatomic& D, int a, int L, int M) {
+  return (a * (D.Lmax + 1) + L) * D.nM + M + 2 * D.mmax;
+}
+
+// ------------------------------------------------------- boundary handling
+__global__ void d_expand(const double* __restrict__ P, int nbf, const int* __restrict__ pure, double* __restrict__ Pd,
+                         int nd) {
+  const size_t n = (size_t)nbf * nbf;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(idx % nbf), c = (int)(idx / nbf);
+    Pd[(size_t)pure[r] + (size_t)pure[c] * nd] = P[idx];
+  }
+}
+
+__global__ void d_gather(const double* __restrict__ Fd, int nd, const int* __restrict__ pure, int nbf,
+                         double* __restrict__ F) {
+  const size_t n = (size_t)nbf * nbf;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(idx % nbf), c = (int)(idx / nbf);
+    F[idx] = Fd[(size_t)pure[r] + (size_t)pure[c] * nd];
+  }
+}
+
+// exchange-ordered in-element kernel from the sign-carrying factor:
+//   tx_ab[(p,q),(i,l)] = s_ab sum_r sigma_r M_a^r(i,p) M_b^r(q,l),
+// M_a^r the channel-a half of factor column r as an nn x nn matrix and
+// s_ab = +1 for 00, 22 and -1 for 02, 20
+__global__ void d_build_tx(DevDiatomic D, double* __restrict__ tx) {
+  const int blk = blockIdx.x, ab = blk & 3, le = blk >> 2;
+  const int a = ab >> 1, b = ab & 1;
+  const double sgn = (a == b) ? 1.0 : -1.0;
+  const int nn = D.nn, n2 = nn * nn, N = 2 * n2;
+  const int r = D.cdrank[le];
+  const double* B = D.cdB + (size_t)le * N * D.rmax;
+  const double* s = D.cds + (size_t)le * D.rmax;
+  double* out = tx + (size_t)blk * n2 * n2;
+  for (int idx = threadIdx.x; idx < n2 * n2; idx += blockDim.x) {
+    const int t = idx % n2, v = idx / n2;
+    const int p = t % nn, q = t / nn, i = v % nn, l = v / nn;
+    const int ra = a * n2 + i + p * nn, rb = b * n2 + q + l * nn;
+    double acc = 0.0;
+    for (int k = 0; k < r; ++k) acc += s[k] * B[ra + (size_t)k * N] * B[rb + (size_t)k * N];
+    out[idx] = sgn * acc;
+  }
+}
+
+// ------------------------------------------------------------------ Coulomb
+__global__ void dj_contract(DevDiatomic D, DevDiatomicScratch S, const double* __restrict__ Pd) {
+  const int ch = blockIdx.x, e = blockIdx.y;
+  const int nn = D.nn, n2 = nn * nn, L = D.ch_L[ch], M = D.ch_M[ch], ilm = D.ch_ilm[ch];
+  const double fac = D.ch_fac[ch];
+  extern __shared__ double sm[];
+  double* X = sm;             // [2*n2]
+  double* cv = X + 2 * n2;    // [rmax]
+  double* red = cv + D.rmax;  // [32]
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+    const int p = t % nn, q = t / nn;
+    const int gp = dgf(D, e, p), gq = dgf(D, e, q);
+    double x0 = 0.0, x2 = 0.0;
+    if (gp < D.nrad && gq < D.nrad)
+      for (int k = 0; k < D.nang; ++k) {
+        const int ix = al_idx(D, k, L, M);
+        for (int u = D.al_ptr[ix]; u < D.al_ptr[ix + 1]; ++u) {
+          const int l = D.al_b[u];
+          const double v = Pd[(size_t)(l * D.nrad + gq) * D.nd + (size_t)k * D.nrad + gp];
+          x0 += D.al_c0[u] * v;
+          x2 += D.al_c2[u] * v;
+        }
+      }
+    X[t] = x0;
+    X[n2 + t] = x2;
+  }
+  __syncthreads();
+  const size_t le = (size_t)ilm * D.nel + e;
+  const double* P0 = D.p0 + le * n2;
+  const double* P2 = D.p2 + le * n2;
+  const double* Q0 = D.q0 + le * n2;
+  const double* Q2 = D.q2 + le * n2;
+  double ts0 = 0.0, tb0 = 0.0, ts2 = 0.0, tb2 = 0.0;
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+    const int p = t % nn, q = t / nn, tt = q + p * nn;  // tr(A X) = sum A(p,q) X(q,p)
+    ts0 += P0[t] * X[tt];
+    tb0 += Q0[t] * X[tt];
+    ts2 += P2[t] * X[n2 + tt];
+    tb2 += Q2[t] * X[n2 + tt];
+  }
+  ts0 = dblock_sum(ts0, red);
+  tb0 = dblock_sum(tb0, red);
+  ts2 = dblock_sum(ts2, red);
+  tb2 = dblock_sum(tb2, red);
+  if (threadIdx.x == 0) {
+    double* sc = S.jscal + ((size_t)ch * D.nel + e) * 4;
+    sc[0] = fac * ts0;
+    sc[1] = fac * tb0;
+    sc[2] = fac * ts2;
+    sc[3] = fac * tb2;
+  }
+  const int r = D.cdrank[le], N = 2 * n2;
+  const double* B = D.cdB + le * N * D.rmax;
+  const double* sg = D.cds + le * D.rmax;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int j = w; j < r; j += nw) {
+    double s = 0.0;
+    for (int v = lane; v < N; v += 32) s += B[v + (size_t)j * N] * X[v];
+    s = dwarp_sum(s);
+    if (lane == 0) cv[j] = s * sg[j];
+  }
+  __syncthreads();
+  double* jin = S.jin + ((size_t)ch * D.nel + e) * N;
+  for (int v = threadIdx.x; v < N; v += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < r; ++j) s += B[v + (size_t)j * N] * cv[j];
+    jin[v] = fac * s;
+  }
+}
+
+constexpr int DJMAXTERMS = 64;
+
+__global__ void dj_scatter(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Jd) {
+  const int ij = blockIdx.x, e = blockIdx.y;
+  const int i = ij % D.nang, j = ij / D.nang;
+  const int b0 = D.jbra_ptr[ij], b1 = D.jbra_ptr[ij + 1];
+  const int nt = b1 - b0;
+  if (nt == 0) return;
+  const int nn = D.nn, n2 = nn * nn;
+  __shared__ double Bg[DJMAXTERMS], Sm[DJMAXTERMS], Bg1[DJMAXTERMS], Sm1[DJMAXTERMS];
+  for (int u = threadIdx.x; u < nt; u += blockDim.x) {
+    const double* sc = S.jscal + (size_t)D.jbra_chan[b0 + u] * D.nel * 4;
+    double big = 0.0, small = 0.0;
+    for (int e2 = e + 1; e2 < D.nel; ++e2) big += sc[4 * e2 + 1] - sc[4 * e2 + 3];
+    for (int e2 = 0; e2 < e; ++e2) small += sc[4 * e2 + 0] - sc[4 * e2 + 2];
+    Bg[u] = big;
+    Sm[u] = small;
+    if (e > 0) {
+      Bg1[u] = big + (sc[4 * e + 1] - sc[4 * e + 3]);
+      Sm1[u] = small - (sc[4 * (e - 1) + 0] - sc[4 * (e - 1) + 2]);
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+    const int p = t % nn, q = t / nn;
+    // the corner on the boundary function shared with the next element is
+    // owned by that element's tile
+    if (p == nn - 1 && q == nn - 1) continue;
+    const int gp = dgf(D, e, p), gq = dgf(D, e, q);
+    if (gp >= D.nrad || gq >= D.nrad) continue;
+    double v = 0.0;
+    for (int u = 0; u < nt; ++u) {
+      const int ch = D.jbra_chan[b0 + u];
+      const size_t le = (size_t)D.ch_ilm[ch] * D.nel + e;
+      const double* jin = S.jin + ((size_t)ch * D.nel + e) * 2 * n2;
+      const double j0 = Bg[u] * D.p0[le * n2 + t] + Sm[u] * D.q0[le * n2 + t] + jin[t];
+      const double j2 = -Bg[u] * D.p2[le * n2 + t] - Sm[u] * D.q2[le * n2 + t] + jin[n2 + t];
+      v += D.jbra_c0[b0 + u] * j0 + D.jbra_c2[b0 + u] * j2;
+    }
+    if (p == 0 && q == 0 && e > 0) {
+      const int c = (nn - 1) + (nn - 1) * nn;
+      for (int u = 0; u < nt; ++u) {
+        const int ch = D.jbra_chan[b0 + u];
+        const size_t le = (size_t)D.ch_ilm[ch] * D.nel + (e - 1);
+        const double* jin = S.jin + ((size_t)ch * D.nel + (e - 1)) * 2 * n2;
+        const double j0 = Bg1[u] * D.p0[le * n2 + c] + Sm1[u] * D.q0[le * n2 + c] + jin[c];
+        const double j2 = -Bg1[u] * D.p2[le * n2 + c] - Sm1[u] * D.q2[le * n2 + c] + jin[n2 + c];
+        v += D.jbra_c0[b0 + u] * j0 + D.jbra_c2[b0 + u] * j2;
+      }
+    }
+    Jd[(size_t)(j * D.nrad + gq) * D.nd + (size_t)i * D.nrad + gp] = v;
+  }
+}
+
+// ----------------------------------------------------------------- exchange
+__global__ void dk_norms(DevDiatomic D, const double* __restrict__ Pd, double* __restrict__ part) {
+  __shared__ double red[32];
+  const int blk = blockIdx.x, i = blk % D.nang, l = blk / D.nang;
+  const int c0 = (int)((long)D.nrad * blockIdx.y / DNORM_SPLIT);
+  const int c1 = (int)((long)D.nrad * (blockIdx.y + 1) / DNORM_SPLIT);
+  double s = 0.0;
+  const size_t n = (size_t)D.nrad * (c1 - c0);
+  for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    const size_t r = idx % D.nrad, c = c0 + idx / D.nrad;
+    const double v = Pd[(size_t)(l * D.nrad + c) * D.nd + (size_t)i * D.nrad + r];
+    s += v * v;
+  }
+  s = dblock_sum(s, red);
+  if (threadIdx.x == 0) part[blk * DNORM_SPLIT + blockIdx.y] = s;
+}
+
+__global__ void dk_act(DevDiatomic D, DevDiatomicScratch S) {
+  const int n = D.nang * D.nang;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < DNORM_SPLIT; ++c) s += S.bnorm[idx * DNORM_SPLIT + c];
+    S.act[idx] = !(sqrt(s) < 10.0 * DBL_EPSILON);
+  }
+}
+
+__global__ void dk_entry_act(DevDiatomic D, DevDiatomicScratch S) {
+  for (int ent = blockIdx.x * blockDim.x + threadIdx.x; ent < D.nent; ent += gridDim.x * blockDim.x) {
+    const int jk = D.kent_jk[ent], j = jk % D.nang, k = jk / D.nang;
+    const int L = D.kent_L[ent], Ma = D.kent_Ma[ent];
+    bool any = false;
+    for (int sgn = 0; sgn < (Ma ? 2 : 1) && !any; ++sgn) {
+      const int M = sgn ? -Ma : Ma;
+      const int xj = al_idx(D, j, L, M), xk = al_idx(D, k, L, M);
+      for (int uj = D.al_ptr[xj]; uj < D.al_ptr[xj + 1] && !any; ++uj) {
+        const int i = D.al_b[uj];
+        for (int uk = D.al_ptr[xk]; uk < D.al_ptr[xk + 1]; ++uk)
+          if (S.act[i + D.al_b[uk] * D.nang]) { any = true; break; }
+      }
+    }
+    S.ent_act[ent] = any ? 1 : 0;
+  }
+}
+
+// one CTA: flags and compacted lists of the active output blocks (all, and
+// those with j <= k for the symmetric mode), in ascending jk order
+__global__ void dk_compact(DevDiatomic D, DevDiatomicScratch S) {
+  __shared__ int ca[1024], cs[1024];
+  const int n = D.nang * D.nang, nt = blockDim.x;
+  const int chunk = (n + nt - 1) / nt;
+  const int lo = min(n, (int)threadIdx.x * chunk), hi = min(n, lo + chunk);
+  int na = 0, ns = 0;
+  for (int jk = lo; jk < hi; ++jk) {
+    bool a = false;
+    for (int ent = D.kjk_ptr[jk]; ent < D.kjk_ptr[jk + 1]; ++ent)
+      if (S.ent_act[ent]) { a = true; break; }
+    S.jk_act[jk] = a ? 1 : 0;
+    if (a) {
+      ++na;
+      if (jk % D.nang <= jk / D.nang) ++ns;
+    }
+  }
+  ca[threadIdx.x] = na;
+  cs[threadIdx.x] = ns;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int sa = 0, ss = 0;
+    for (int t = 0; t < nt; ++t) {
+      const int a = ca[t], s = cs[t];
+      ca[t] = sa;
+      cs[t] = ss;
+      sa += a;
+      ss += s;
+    }
+    S.counts[0] = sa;
+    S.counts[1] = ss;
+  }
+  __syncthreads();
+  int oa = ca[threadIdx.x], os = cs[threadIdx.x];
+  for (int jk = lo; jk < hi; ++jk)
+    if (S.jk_act[jk]) {
+      S.jk_list[oa++] = jk;
+      if (jk % D.nang <= jk / D.nang) S.jk_list[n + os++] = jk;
+    }
+}
+
+__device__ __forceinline__ size_t dhalo_idx(const DevDiatomic& D, int a, int b, int jk, int h) {
+  return ((size_t)(a * D.nel + b) * (D.nang * D.nang) + jk) * (2 * D.nn - 1) + h;
+}
+
+__device__ __forceinline__ void dk_store(const DevDiatomic& D, const DevDiatomicScratch& S, double* Kd, int a, int b,
+                                         int jk, int p, int q, double y) {
+  const int nn = D.nn;
+  const int gp = dgf(D, a, p), gq = dgf(D, b, q);
+  if (gp >= D.nrad || gq >= D.nrad) return;
+  const int j = jk % D.nang, k = jk / D.nang;
+  if (p <= nn - 2 && q <= nn - 2)
+    Kd[(size_t)(k * D.nrad + gq) * D.nd + (size_t)j * D.nrad + gp] = y;
+  else if (p == nn - 1)
+    S.khalo[dhalo_idx(D, a, b, jk, q)] = y;
+  else
+    S.khalo[dhalo_idx(D, a, b, jk, nn + p)] = y;
+}
+
+// Persistent CTAs over work items. Item w < n_off: element pair
+// pairs[w / n_act], output block jk_list[w % n_act]; the rest: diagonal
+// element e, output block from the (symmetric: j <= k) list. In symmetric
+// mode (P = P^T) only a < b pairs are items and each also writes the
+// transposed partner tile, K_kj(b,a) = K_jk(a,b)^T.
+__global__ void __launch_bounds__(320) dk_tiles(DevDiatomic D, DevDiatomicScratch S, const double* __restrict__ Pd,
+                                                double* __restrict__ Kd, int symmetric) {
+  const int nn = D.nn, n2 = nn * nn, nang2 = D.nang * D.nang;
+  const int n_act = S.counts[0], n_dact = symmetric ? S.counts[1] : S.counts[0];
+  const int* dlist = symmetric ? S.jk_list + nang2 : S.jk_list;
+  const int2* pairs = symmetric ? D.pairs_sym : D.pairs_all;
+  const long npairs = symmetric ? D.npairs_sym : D.npairs_all;
+  const long n_off = npairs * n_act, total = n_off + (long)D.nel * n_dact;
+  extern __shared__ double sm[];
+  double* X = sm;            // [4*n2]: R00, R02, R20, R22 tiles
+  double* T = X + 4 * n2;    // [2*n2]
+  double* Im = T + 2 * n2;   // [2*n2] row-element integrals (channel 0, 2)
+  double* Jm = Im + 2 * n2;  // [2*n2] column-element integrals
+  unsigned char* act = reinterpret_cast<unsigned char*>(Jm + 2 * n2);
+  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.act[idx];
+  __syncthreads();
+  const int t = threadIdx.x;
+  const bool live = t < n2;
+  const int p = live ? t % nn : 0, q = live ? t / nn : 0;
+  for (long w = blockIdx.x; w < total; w += gridDim.x) {
+    int a, b, jk;
+    if (w < n_off) {
+      const int2 pr = pairs[w / n_act];
+      a = pr.x;
+      b = pr.y;
+      jk = S.jk_list[w % n_act];
+    } else {
+      const long w2 = w - n_off;
+      a = b = (int)(w2 / n_dact);
+      jk = dlist[w2 % n_dact];
+    }
+    const bool diag = (a == b);
+    const int j = jk % D.nang, k = jk / D.nang;
+    const int gp = dgf(D, a, p), gq = dgf(D, b, q);
+    const bool vpq = live && gp < D.nrad && gq < D.nrad;
+    double y = 0.0;
+    for (int ent = D.kjk_ptr[jk]; ent < D.kjk_ptr[jk + 1]; ++ent) {
+      if (!S.ent_act[ent]) continue;  // uniform over the CTA
+      const int L = D.kent_L[ent], Ma = D.kent_Ma[ent], ilm = D.kent_ilm[ent];
+      double x00 = 0.0, x02 = 0.0, x20 = 0.0, x22 = 0.0;
+      if (vpq) {
+        for (int sgn = 0; sgn < (Ma ? 2 : 1); ++sgn) {
+          const int M = sgn ? -Ma : Ma;
+          const int xj = al_idx(D, j, L, M), xk = al_idx(D, k, L, M);
+          const int k0 = D.al_ptr[xk], k1 = D.al_ptr[xk + 1];
+          for (int uj = D.al_ptr[xj]; uj < D.al_ptr[xj + 1]; ++uj) {
+            const int i = D.al_b[uj];
+            const double* Pi = Pd + (size_t)i * D.nrad + gp;
+            double u0 = 0.0, u2 = 0.0;
+            for (int uk = k0; uk < k1; ++uk) {
+              const int l = D.al_b[uk];
+              if (!act[i + l * D.nang]) continue;
+              const double v = Pi[(size_t)(l * D.nrad + gq) * D.nd];
+              u0 += D.al_c0[uk] * v;
+              u2 += D.al_c2[uk] * v;
+            }
+            const double c0 = D.al_c0[uj], c2 = D.al_c2[uj];
+            x00 += c0 * u0;
+            x02 += c0 * u2;
+            x20 += c2 * u0;
+            x22 += c2 * u2;
+          }
+        }
+      }
+      const double fac = (Ma & 1) ? -D.lmfac[ilm] : D.lmfac[ilm];
+      if (live) {
+        X[t] = fac * x00;
+        X[n2 + t] = -fac * x02;
+        X[2 * n2 + t] = -fac * x20;
+        X[3 * n2 + t] = fac * x22;
+        if (!diag) {
+          const size_t la = ((size_t)ilm * D.nel + a) * n2 + t, lb = ((size_t)ilm * D.nel + b) * n2 + t;
+          Im[t] = (a < b) ? D.p0[la] : D.q0[la];
+          Im[n2 + t] = (a < b) ? D.p2[la] : D.q2[la];
+          Jm[t] = (a < b) ? D.q0[lb] : D.p0[lb];
+          Jm[n2 + t] = (a < b) ? D.q2[lb] : D.p2[lb];
+        }
+      }
+      __syncthreads();
+      if (diag) {
+        if (live) {
+          const double* tx = D.tx + ((size_t)ilm * D.nel + a) * 4 * n2 * n2;
+          double s = 0.0;
+          for (int ab = 0; ab < 4; ++ab) {
+            const double* txb = tx + (size_t)ab * n2 * n2;
+            const double* Xb = X + ab * n2;
+            for (int v = 0; v < n2; ++v) s += txb[t + (size_t)v * n2] * Xb[v];
+          }
+          y += s;
+        }
+      } else {
+        if (live) {
+          double s0 = 0.0, s2 = 0.0;
+          for (int c = 0; c < nn; ++c) {
+            const double j0 = Jm[q + c * nn], j2 = Jm[n2 + q + c * nn];
+            s0 += X[p + c * nn] * j0 + X[n2 + p + c * nn] * j2;
+            s2 += X[2 * n2 + p + c * nn] * j0 + X[3 * n2 + p + c * nn] * j2;
+          }
+          T[t] = s0;
+          T[n2 + t] = s2;
+        }
+        __syncthreads();
+        if (live) {
+          double s = 0.0;
+          for (int c = 0; c < nn; ++c) s += Im[p + c * nn] * T[c + q * nn] + Im[n2 + p + c * nn] * T[n2 + c + q * nn];
+          y += s;
+        }
+      }
+      __syncthreads();
+    }
+    if (live) dk_store(D, S, Kd, a, b, jk, p, q, -y);
+    if (symmetric && (!diag || j != k)) {
+      if (live) X[t] = -y;
+      __syncthreads();
+      if (live) dk_store(D, S, Kd, b, a, k + j * D.nang, p, q, X[q + p * nn]);
+      __syncthreads();
+    }
+  }
+}
+
+// Shared-boundary fix-up: entry (p,q) of tile (a,b) in its first row or
+// column also receives the last row of the tile above (a-1,b), the last
+// column of the tile to the left (a,b-1) and, at the corner, the last corner
+// of (a-1,b-1). Unlike the atomic basis, element 0 keeps its first function
+// (mu = 0), so the first row of a = 0 tiles and the first column of b = 0
+// tiles are real entries too.
+__global__ void dk_fixup(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd) {
+  const int jk = blockIdx.y;
+  if (!S.jk_act[jk]) return;
+  const int a = blockIdx.x % D.nel, b = blockIdx.x / D.nel;
+  const int nn = D.nn;
+  const int j = jk % D.nang, k = jk / D.nang;
+  for (int idx = threadIdx.x; idx < 2 * nn - 3; idx += blockDim.x) {
+    const int p = idx < nn - 1 ? 0 : idx - (nn - 1) + 1;  // first row q in [0, nn-2], then first column
+    const int q = idx < nn - 1 ? idx : 0;
+    double v = 0.0;
+    bool any = false;
+    if (p == 0 && a > 0) {
+      v += S.khalo[dhalo_idx(D, a - 1, b, jk, q)];
+      any = true;
+    }
+    if (q == 0 && b > 0) {
+      v += S.khalo[dhalo_idx(D, a, b - 1, jk, nn + p)];
+      any = true;
+    }
+    if (p == 0 && q == 0 && a > 0 && b > 0) v += S.khalo[dhalo_idx(D, a - 1, b - 1, jk, nn - 1)];
+    if (!any) continue;
+    const int gp = dgf(D, a, p), gq = dgf(D, b, q);
+    if (gp >= D.nrad || gq >= D.nrad) continue;
+    Kd[(size_t)(k * D.nrad + gq) * D.nd + (size_t)j * D.nrad + gp] += v;
+  }
+}
+
+inline int dthreads(int n2) { return ((n2 + 31) / 32) * 32; }
+inline int dgrid(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 32); }
+
+}  // namespace
+
+cudaError_t launch_diatomic_expand(const double* P, int nbf, const int* pure, double* Pd, int nd, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(Pd, 0, sizeof(double) * (size_t)nd * nd, st);
+  if (e != cudaSuccess) return e;
+  d_expand<<<dgrid((size_t)nbf * nbf), 256, 0, st>>>(P, nbf, pure, Pd, nd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diatomic_gather(const double* Fd, int nd, const int* pure, int nbf, double* F, cudaStream_t st) {
+  d_gather<<<dgrid((size_t)nbf * nbf), 256, 0, st>>>(Fd, nd, pure, nbf, F);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diatomic_tx(const DevDiatomic& D, double* tx, cudaStream_t st) {
+  d_build_tx<<<D.nlm * D.nel * 4, 256, 0, st>>>(D, tx);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd, double* Jd,
+                                    cudaStream_t st) {
+  const int n2 = D.nn * D.nn, th = dthreads(n2);
+  cudaError_t e = cudaMemsetAsync(Jd, 0, sizeof(double) * (size_t)D.nd * D.nd, st);
+  if (e != cudaSuccess) return e;
+  const size_t sm1 = sizeof(double) * (2 * n2 + D.rmax + 32);
+  dj_contract<<<dim3(D.nchan, D.nel), th, sm1, st>>>(D, S, Pd);
+  dj_scatter<<<dim3(D.nang * D.nang, D.nel), th, 0, st>>>(D, S, Jd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd, double* Kd,
+                                     bool symmetric, cudaStream_t st) {
+  const int n2 = D.nn * D.nn, th = dthreads(n2), nang2 = D.nang * D.nang;
+  cudaError_t e = cudaMemsetAsync(Kd, 0, sizeof(double) * (size_t)D.nd * D.nd, st);
+  if (e != cudaSuccess) return e;
+  dk_norms<<<dim3(nang2, DNORM_SPLIT), 256, 0, st>>>(D, Pd, S.bnorm);
+  dk_act<<<(nang2 + 255) / 256, 256, 0, st>>>(D, S);
+  dk_entry_act<<<(D.nent + 127) / 128 > 0 ? (D.nent + 127) / 128 : 1, 128, 0, st>>>(D, S);
+  dk_compact<<<1, 1024, 0, st>>>(D, S);
+  int dev = 0, nsm = 152, per = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = sizeof(double) * 10 * n2 + nang2;
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(dk_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dk_tiles, th, smem);
+  if (e != cudaSuccess) return e;
+  const int grid = nsm * std::max(per, 1);
+  dk_tiles<<<grid, th, smem, st>>>(D, S, Pd, Kd, symmetric ? 1 : 0);
+  dk_fixup<<<dim3(D.nel * D.nel, nang2), 64, 0, st>>>(D, S, Kd);
+  return cudaGetLastError();
+}
+
+}  // namespace hfg

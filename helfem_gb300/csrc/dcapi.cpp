@@ -1,0 +1,357 @@
+// C ABI of the diatomic Fock build (declarations and contract in
+// include/helfem_gb300.h). The handle owns the host tabulation, the device
+// tables and the per-call scratch; every entry point converts exceptions
+// and CUDA errors into status codes.
+#include <algorithm>
+#include <cstring>
+
+#include "cuda/devdiatomic.cuh"
+#include "handle.hpp"
+#include "host/diatomic.hpp"
+
+struct hfg_diatomic {
+  hfg_abi::StreamHolder stream_holder;  // destroyed last
+  hfg::DiatomicHost host;
+  int device = 0;
+  bool on_device = false;
+  cudaStream_t own_stream = nullptr;
+  hfg::DevDiatomic dev{};
+  hfg::DevDiatomicScratch scr{};
+  DBuf d_p0, d_p2, d_q0, d_q2, d_cdB, d_cds, d_cdrank, d_tx, d_lmfac, d_al_ptr, d_al_b, d_al_c0, d_al_c2, d_chL,
+      d_chM, d_chilm, d_chfac, d_jbra_ptr, d_jbra_chan, d_jbra_c0, d_jbra_c2, d_kjk_ptr, d_kentL, d_kentMa,
+      d_kentilm, d_kentjk, d_pairs_all, d_pairs_sym, d_pure;
+  DBuf s_jin, s_jscal, s_khalo, s_bnorm, s_act, s_entact, s_jkact, s_jklist, s_counts, s_Pd, s_Fd;
+  DBuf h_in, h_out;
+  cudaEvent_t last_use = nullptr;
+
+  ~hfg_diatomic() {
+    if (last_use) {
+      if (own_stream) cudaStreamWaitEvent(own_stream, last_use, 0);
+      cudaEventDestroy(last_use);
+    }
+  }
+  void mark_use(cudaStream_t st) {
+    if (last_use) cudaEventRecord(last_use, st);
+  }
+  void check_device() const {
+    if (!on_device) throw std::logic_error("handle was created host-only; device entry points are unavailable");
+    int d = -1;
+    ck(cudaGetDevice(&d), "cudaGetDevice");
+    if (d != device) throw std::invalid_argument("handle used on a different CUDA device than it was created on");
+  }
+
+  void upload() {
+    using namespace hfg;
+    const DiatomicHost& H = host;
+    ck(cudaGetDevice(&device), "cudaGetDevice");
+    ck(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    stream_holder.s = own_stream;
+    hfg_abi::AllocStream alloc_on(own_stream);
+    DevDiatomic& D = dev;
+    D.nn = H.nn;
+    D.nel = H.nel;
+    D.nrad = H.nrad;
+    D.nang = H.nang;
+    D.nd = H.ndummy;
+    D.nlm = H.nlm;
+    D.rmax = H.rmax;
+    D.Lmax = H.Lmax;
+    D.mmax = H.mmax;
+    D.nM = H.nM;
+    D.p0 = d_p0.upload(H.p0);
+    D.p2 = d_p2.upload(H.p2);
+    D.q0 = d_q0.upload(H.q0);
+    D.q2 = d_q2.upload(H.q2);
+    D.cdB = d_cdB.upload(H.cd_B);
+    D.cds = d_cds.upload(H.cd_s);
+    D.cdrank = d_cdrank.upload(H.cd_rank);
+    std::vector<double> lmf(H.nlm);
+    for (int i = 0; i < H.nlm; ++i) {
+      const int L = H.lm_L[i], Ma = H.lm_M[i];
+      double fr = 1.0;
+      for (int p = L + Ma; p > L - Ma; --p) fr *= p;
+      lmf[i] = 4.0 * M_PI * std::pow(H.Rhalf, 5) / fr;
+    }
+    D.lmfac = d_lmfac.upload(lmf);
+    D.al_ptr = d_al_ptr.upload(H.al_ptr);
+    D.al_b = d_al_b.upload(H.al_b);
+    D.al_c0 = d_al_c0.upload(H.al_c0);
+    D.al_c2 = d_al_c2.upload(H.al_c2);
+    D.nchan = (int)H.ch_L.size();
+    D.ch_L = d_chL.upload(H.ch_L);
+    D.ch_M = d_chM.upload(H.ch_M);
+    D.ch_ilm = d_chilm.upload(H.ch_ilm);
+    D.ch_fac = d_chfac.upload(H.ch_fac);
+    D.jbra_ptr = d_jbra_ptr.upload(H.jbra_ptr);
+    D.jbra_chan = d_jbra_chan.upload(H.jbra_chan);
+    D.jbra_c0 = d_jbra_c0.upload(H.jbra_c0);
+    D.jbra_c2 = d_jbra_c2.upload(H.jbra_c2);
+    for (int ij = 0; ij < H.nang * H.nang; ++ij)
+      if (H.jbra_ptr[ij + 1] - H.jbra_ptr[ij] > 64) throw std::invalid_argument("too many Coulomb bra terms");
+    D.nent = (int)H.kent_L.size();
+    D.kjk_ptr = d_kjk_ptr.upload(H.kjk_ptr);
+    D.kent_L = d_kentL.upload(H.kent_L);
+    D.kent_Ma = d_kentMa.upload(H.kent_Ma);
+    D.kent_ilm = d_kentilm.upload(H.kent_ilm);
+    std::vector<int> kjk(D.nent);
+    for (int jk = 0; jk < H.nang * H.nang; ++jk)
+      for (int e = H.kjk_ptr[jk]; e < H.kjk_ptr[jk + 1]; ++e) kjk[e] = jk;
+    D.kent_jk = d_kentjk.upload(kjk);
+    std::vector<int2> pa, ps;
+    for (int b = 0; b < H.nel; ++b)
+      for (int a = 0; a < H.nel; ++a) {
+        if (a == b) continue;
+        pa.push_back(make_int2(a, b));
+        if (a < b) ps.push_back(make_int2(a, b));
+      }
+    D.pairs_all = d_pairs_all.upload(pa);
+    D.npairs_all = (int)pa.size();
+    D.pairs_sym = d_pairs_sym.upload(ps);
+    D.npairs_sym = (int)ps.size();
+    d_pure.upload(H.pure);
+    const size_t n2 = (size_t)H.nn * H.nn, nang2 = (size_t)H.nang * H.nang, nd = (size_t)H.ndummy;
+    d_tx.alloc(sizeof(double) * (size_t)H.nlm * H.nel * 4 * n2 * n2);
+    D.tx = d_tx.as<double>();
+    ck(hfg::launch_diatomic_tx(D, d_tx.as<double>(), own_stream), "in-element kernel build");
+    s_jin.alloc(sizeof(double) * (size_t)D.nchan * H.nel * 2 * n2);
+    s_jscal.alloc(sizeof(double) * (size_t)D.nchan * H.nel * 4);
+    s_khalo.alloc(sizeof(double) * (size_t)H.nel * H.nel * nang2 * (2 * H.nn - 1));
+    s_bnorm.alloc(sizeof(double) * nang2 * DNORM_SPLIT);
+    s_act.alloc(nang2);
+    s_entact.alloc(std::max<size_t>(1, D.nent));
+    s_jkact.alloc(nang2);
+    s_jklist.alloc(sizeof(int) * 2 * nang2);
+    s_counts.alloc(sizeof(int) * 2);
+    s_Pd.alloc(sizeof(double) * nd * nd);
+    s_Fd.alloc(sizeof(double) * nd * nd);
+    scr.jin = s_jin.as<double>();
+    scr.jscal = s_jscal.as<double>();
+    scr.khalo = s_khalo.as<double>();
+    scr.bnorm = s_bnorm.as<double>();
+    scr.act = s_act.as<unsigned char>();
+    scr.ent_act = s_entact.as<unsigned char>();
+    scr.jk_act = s_jkact.as<unsigned char>();
+    scr.jk_list = s_jklist.as<int>();
+    scr.counts = s_counts.as<int>();
+    ck(cudaEventCreateWithFlags(&last_use, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaStreamSynchronize(own_stream), "sync after upload");
+    on_device = true;
+  }
+
+  // J or K of a pure-basis density (device pointers) on stream st
+  void build(const double* P, double* F, bool exchange, bool symmetric, cudaStream_t st) {
+    check_device();
+    const hfg::DiatomicHost& H = host;
+    ck(hfg::launch_diatomic_expand(P, H.nbf, d_pure.as<int>(), s_Pd.as<double>(), H.ndummy, st), "expand");
+    if (exchange)
+      ck(hfg::launch_diatomic_exchange(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st), "exchange");
+    else
+      ck(hfg::launch_diatomic_coulomb(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), st), "coulomb");
+    ck(hfg::launch_diatomic_gather(s_Fd.as<double>(), H.ndummy, d_pure.as<int>(), H.nbf, F, st), "gather");
+    mark_use(st);
+  }
+
+  void build_host(const double* P, double* F, bool exchange, bool symmetric) {
+    check_device();
+    hfg_abi::AllocStream alloc_on(own_stream);
+    const size_t bytes = sizeof(double) * (size_t)host.nbf * host.nbf;
+    if (h_in.n != bytes) h_in.alloc(bytes);
+    if (h_out.n != bytes) h_out.alloc(bytes);
+    ck(cudaMemcpyAsync(h_in.p, P, bytes, cudaMemcpyHostToDevice, own_stream), "copy in");
+    build(h_in.as<double>(), h_out.as<double>(), exchange, symmetric, own_stream);
+    ck(cudaMemcpyAsync(F, h_out.p, bytes, cudaMemcpyDeviceToHost, own_stream), "copy out");
+    ck(cudaStreamSynchronize(own_stream), "sync");
+  }
+};
+
+namespace {
+cudaStream_t to_stream(void* s) { return static_cast<cudaStream_t>(s); }
+}  // namespace
+
+extern "C" {
+
+hfg_status hfg_diatomic_create(const hfg_diatomic_desc* desc, hfg_diatomic** out) {
+  return guard([&] {
+    need(desc != nullptr && out != nullptr, "hfg_diatomic_create: null argument");
+    need(desc->bval && desc->lval && desc->mval && desc->nelem >= 2 && desc->nang >= 1,
+         "hfg_diatomic_create: bad description");
+    need(desc->nang <= 255, "hfg_diatomic_create: at most 255 angular functions");
+    std::unique_ptr<hfg_diatomic> d(new hfg_diatomic());
+    std::vector<double> bval(desc->bval, desc->bval + desc->nelem + 1);
+    std::vector<int> lv(desc->lval, desc->lval + desc->nang), mv(desc->mval, desc->mval + desc->nang);
+    d->host.build(desc->Z1, desc->Z2, desc->Rhalf, desc->nnodes, bval, lv, mv, desc->cd_thresh);
+    if (!desc->host_only) d->upload();
+    *out = d.release();
+  });
+}
+
+hfg_status hfg_diatomic_destroy(hfg_diatomic* d) {
+  return guard([&] { delete d; });
+}
+
+hfg_status hfg_diatomic_get_dims(const hfg_diatomic* d, hfg_diatomic_dims_t* dims) {
+  return guard([&] {
+    need(d && dims, "hfg_diatomic_get_dims: null argument");
+    const hfg::DiatomicHost& H = d->host;
+    dims->nrad = H.nrad;
+    dims->nang = H.nang;
+    dims->nel = H.nel;
+    dims->nnodes = H.nn;
+    dims->ndummy = H.ndummy;
+    dims->nbf = H.nbf;
+    dims->nlm = H.nlm;
+    dims->Lmax = H.Lmax;
+    dims->rmax = H.rmax;
+    dims->nchan = (int)H.ch_L.size();
+    dims->nent = (int)H.kent_L.size();
+  });
+}
+
+hfg_status hfg_diatomic_pure_indices(const hfg_diatomic* d, int* idx) {
+  return guard([&] {
+    need(d && idx, "hfg_diatomic_pure_indices: null argument");
+    std::copy(d->host.pure.begin(), d->host.pure.end(), idx);
+  });
+}
+
+static hfg_status one_e(const hfg_diatomic* d, double* out, int which) {
+  return guard([&] {
+    need(d && out, "hfg_diatomic one-electron: null argument");
+    std::vector<double> M;
+    if (which == 0) d->host.overlap(M);
+    else if (which == 1) d->host.kinetic(M);
+    else d->host.nuclear(M);
+    std::copy(M.begin(), M.end(), out);
+  });
+}
+hfg_status hfg_diatomic_overlap(const hfg_diatomic* d, double* S) { return one_e(d, S, 0); }
+hfg_status hfg_diatomic_kinetic(const hfg_diatomic* d, double* T) { return one_e(d, T, 1); }
+hfg_status hfg_diatomic_nuclear(const hfg_diatomic* d, double* V) { return one_e(d, V, 2); }
+
+hfg_status hfg_diatomic_one_electron_block(const hfg_diatomic* d, int which, int mblock, double* out, int* n) {
+  return guard([&] {
+    need(d && n && which >= 0 && which <= 2, "hfg_diatomic_one_electron_block: bad arguments");
+    std::vector<double> M;
+    int nb = 0;
+    d->host.one_electron_block(which, mblock, M, nb);
+    *n = nb;
+    if (out) std::copy(M.begin(), M.end(), out);
+  });
+}
+
+hfg_status hfg_diatomic_tables(const hfg_diatomic* d, int which, int ilm, int iel, int* L, int* M, int* rank,
+                               double* out, double* sigma) {
+  return guard([&] {
+    need(d != nullptr, "hfg_diatomic_tables: null handle");
+    const hfg::DiatomicHost& H = d->host;
+    need(ilm >= 0 && ilm < H.nlm && iel >= 0 && iel < H.nel && which >= 0 && which <= 4,
+         "hfg_diatomic_tables: index out of range");
+    if (L) *L = H.lm_L[ilm];
+    if (M) *M = H.lm_M[ilm];
+    const size_t le = (size_t)ilm * H.nel + iel, n2 = (size_t)H.nn * H.nn;
+    if (rank) *rank = H.cd_rank[le];
+    if (!out) return;
+    if (which < 4) {
+      const std::vector<double>* src[4] = {&H.p0, &H.p2, &H.q0, &H.q2};
+      std::copy(src[which]->begin() + le * n2, src[which]->begin() + (le + 1) * n2, out);
+    } else {
+      const size_t N = 2 * n2, r = H.cd_rank[le];
+      std::copy(H.cd_B.begin() + le * N * H.rmax, H.cd_B.begin() + le * N * H.rmax + N * r, out);
+      if (sigma) std::copy(H.cd_s.begin() + le * H.rmax, H.cd_s.begin() + le * H.rmax + r, sigma);
+    }
+  });
+}
+
+hfg_status hfg_legendre_pq(int Lmax, int Mmax, double mu, double* P, double* Q) {
+  return guard([&] {
+    need(P && Q && Lmax >= 0 && Mmax >= 0 && mu > 0, "hfg_legendre_pq: bad arguments");
+    hfg::legendre_pq(Lmax, Mmax, mu, P, Q);
+  });
+}
+
+hfg_status hfg_gaunt_mod(int lj, int mj, int L, int M, int li, int mi, double* value) {
+  return guard([&] {
+    need(value != nullptr, "hfg_gaunt_mod: null argument");
+    if (mj != M + mi) { *value = 0.0; return; }
+    const double c0 = 2.0 / 3.0 * std::sqrt(M_PI), c2 = 4.0 / 15.0 * std::sqrt(5.0 * M_PI);
+    double v = c0 * hfg::gaunt_coeff(L, M, 0, 0, L) * hfg::gaunt_coeff(lj, mj, li, mi, L);
+    for (int Lp = std::max(std::max(L - 2, 0), std::abs(M)); Lp <= L + 2; ++Lp)
+      v += c2 * hfg::gaunt_coeff(Lp, M, 2, 0, L) * hfg::gaunt_coeff(lj, mj, li, mi, Lp);
+    *value = v;
+  });
+}
+
+hfg_status hfg_diatomic_coulomb(hfg_diatomic* d, const double* P, double* J, void* stream) {
+  return guard([&] {
+    need(d && P && J, "hfg_diatomic_coulomb: null argument");
+    d->build(P, J, false, false, to_stream(stream));
+  });
+}
+
+hfg_status hfg_diatomic_exchange(hfg_diatomic* d, const double* P, double* K, int flags, void* stream) {
+  return guard([&] {
+    need(d && P && K, "hfg_diatomic_exchange: null argument");
+    need((flags & ~HFG_EXCHANGE_SYMMETRIC) == 0, "hfg_diatomic_exchange: unsupported flags");
+    d->build(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0, to_stream(stream));
+  });
+}
+
+hfg_status hfg_diatomic_coulomb_host(hfg_diatomic* d, const double* P, double* J) {
+  return guard([&] {
+    need(d && P && J, "hfg_diatomic_coulomb_host: null argument");
+    d->build_host(P, J, false, false);
+  });
+}
+
+hfg_status hfg_diatomic_exchange_host(hfg_diatomic* d, const double* P, double* K, int flags) {
+  return guard([&] {
+    need(d && P && K, "hfg_diatomic_exchange_host: null argument");
+    need((flags & ~HFG_EXCHANGE_SYMMETRIC) == 0, "hfg_diatomic_exchange_host: unsupported flags");
+    d->build_host(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0);
+  });
+}
+
+hfg_status hfg_diatomic_work(const hfg_diatomic* d, const unsigned char* act, hfg_diatomic_work_t* w) {
+  return guard([&] {
+    need(d && w, "hfg_diatomic_work: null argument");
+    const hfg::DiatomicHost& H = d->host;
+    std::memset(w, 0, sizeof(*w));
+    const int nang = H.nang, nel = H.nel;
+    // padded tiles, as computed: per (element pair, entry) the two stages of
+    // off-diagonal products cost 12 nn^3 flops; per (element, entry) the four
+    // exchange-ordered in-element blocks 8 nn^4; the recoupling about 4 flops
+    // per (density term, tile element)
+    const double n2 = (double)H.nn * H.nn, nn3 = n2 * H.nn, npo = (double)nel * (nel - 1);
+    for (int k = 0; k < nang; ++k)
+      for (int j = 0; j < nang; ++j) {
+        const int jk = j + k * nang;
+        for (int ent = H.kjk_ptr[jk]; ent < H.kjk_ptr[jk + 1]; ++ent) {
+          const int L = H.kent_L[ent], Ma = H.kent_Ma[ent];
+          double terms = 0.0;
+          for (int sg = 0; sg < (Ma ? 2 : 1); ++sg) {
+            const int M = sg ? -Ma : Ma;
+            const int xj = H.al_index(j, L, M), xk = H.al_index(k, L, M);
+            for (int uj = H.al_ptr[xj]; uj < H.al_ptr[xj + 1]; ++uj)
+              for (int uk = H.al_ptr[xk]; uk < H.al_ptr[xk + 1]; ++uk)
+                if (!act || act[H.al_b[uj] + H.al_b[uk] * nang]) terms += 1.0;
+          }
+          if (terms == 0.0) continue;
+          const double off = 12.0 * nn3 * npo, dia = 8.0 * n2 * n2 * nel;
+          const double roff = 4.0 * terms * n2 * npo, rdia = 4.0 * terms * n2 * nel;
+          w->k_offdiag_flops += off;
+          w->k_diag_flops += dia;
+          w->k_recouple_flops += roff + rdia;
+          w->n_entries += 1.0;
+          w->k_offdiag_sym_flops += 0.5 * off;
+          w->k_recouple_sym_flops += 0.5 * roff;
+          if (j <= k) {
+            w->k_diag_sym_flops += dia;
+            w->k_recouple_sym_flops += rdia;
+            w->n_entries_sym += 1.0;
+          }
+        }
+      }
+  });
+}
+
+}  // extern "C"

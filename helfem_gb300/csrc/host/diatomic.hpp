@@ -1,0 +1,88 @@
+// Host-side (FP64) description of one diatomic molecule in prolate
+// spheroidal coordinates (mu, nu, phi): the finite-element basis in mu, the
+// integrals HelFEM's diatomic TwoDBasis::compute_tei caches, the angular
+// coupling tables and the one-electron radial blocks, laid out for the
+// device.
+//
+// Radial layout (src/diatomic/basis.cpp:522-540): element e owns an nn x nn
+// primitive tile; primitive p is the global function g(e,p) = e*(nn-1) + p,
+// valid for g < nrad = nel*(nn-1) (the mu = 0 function is kept, the mu_max
+// one dropped). The "dummy" basis is nang*nrad functions (AO index
+// iang*nrad + irad); the pure basis drops the mu = 0 function of every m != 0
+// shell (basis.cpp:712-736).
+#pragma once
+
+#include <vector>
+
+namespace hfg {
+
+// P[M*(Lmax+1) + L], Q[...] of x = cosh(mu), Hobson convention (no
+// Condon-Shortley phase), for 0 <= M <= Mmax, 0 <= L <= Lmax. Non-finite and
+// subnormal values are returned as 0.
+void legendre_pq(int Lmax, int Mmax, double mu, double* P, double* Q);
+
+struct DiatomicHost {
+  int Z1 = 0, Z2 = 0;
+  double Rhalf = 0.0;
+  int nn = 0, nel = 0, nrad = 0, nang = 0, ndummy = 0, nbf = 0;
+  std::vector<double> bval, nodes;
+  std::vector<int> lval, mval;
+  std::vector<int> pure;  // [nbf] dummy index of each pure function
+  int mmax = 0;           // max |m| of the basis
+  int Lmax = 0;           // max multipole L
+  // (L,|M|) multipoles, |M|-major then L (basis.cpp:553-620)
+  int nlm = 0;
+  std::vector<int> lm_L, lm_M;
+  int lm_index(int L, int Mabs) const;
+  // per (ilm, e), padded nn x nn column-major: int B_a B_b sinh cosh^k P (k = 0, 2)
+  // and the same with Q
+  std::vector<double> p0, p2, q0, q2;
+  // per (ilm, e): sign-carrying factor of the 2-channel in-element kernel,
+  // padded (2 nn^2 x rmax), row = channel*nn^2 + a + b*nn
+  int rmax = 0;
+  std::vector<int> cd_rank;
+  std::vector<double> cd_B, cd_s;  // cd_s: [(ilm*nel+e)*rmax]
+  double cd_thresh = 1e-12;
+  // assembled one-electron radial blocks (nrad x nrad, column-major):
+  // int B B sinh, sinh cosh, sinh cosh^2, 1/sinh, and int B' B' sinh
+  std::vector<double> I10, I11, I12, Im1, Trad;
+
+  // ---- angular coupling table ---------------------------------------------
+  // For angular function a, multipole L and signed M (|M| <= 2 mmax): the
+  // functions b with mb = ma - M that couple, with
+  //   c0 = int Y_a* cos^2(nu) Y_L^M Y_b   (the reference's mod_coeff)
+  //   c2 = int Y_a* Y_L^M Y_b             (its coeff)
+  // Serves the Coulomb ket and bra sums and the exchange recoupling.
+  int nM = 0;  // 4*mmax + 1
+  std::vector<int> al_ptr;  // [(a*(Lmax+1) + L)*nM + M + 2 mmax] (+1)
+  std::vector<int> al_b;
+  std::vector<double> al_c0, al_c2;
+  int al_index(int a, int L, int M) const { return (a * (Lmax + 1) + L) * nM + M + 2 * mmax; }
+
+  // ---- Coulomb channels (signed (L, M)) and bra lists ----------------------
+  std::vector<int> ch_L, ch_M, ch_ilm;
+  std::vector<double> ch_fac;  // (-1)^M 4 pi Rhalf^5 (L-|M|)!/(L+|M|)!
+  std::vector<int> jbra_ptr;   // [nang*nang+1] output block i + j*nang
+  std::vector<int> jbra_chan;
+  std::vector<double> jbra_c0, jbra_c2;
+  // ---- exchange entries per output block j + k*nang: (L, |M|) --------------
+  std::vector<int> kjk_ptr;    // [nang*nang+1]
+  std::vector<int> kent_L, kent_Ma, kent_ilm;
+
+  void build(int Z1, int Z2, double Rhalf, int nnodes, const std::vector<double>& bval,
+             const std::vector<int>& lval, const std::vector<int>& mval, double cd_thresh);
+  // pure-basis one-electron matrices (nbf x nbf, column-major)
+  void overlap(std::vector<double>& S) const;
+  void kinetic(std::vector<double>& T) const;
+  void nuclear(std::vector<double>& V) const;
+  // the same restricted to the pure functions with m == mblock (symmetry
+  // block, pure order): n_out functions
+  void one_electron_block(int which, int mblock, std::vector<double>& out, int& n_out) const;
+
+ private:
+  void tabulate_radial();
+  void build_couplings();
+  void dense_one_electron(int which, std::vector<double>& D) const;
+};
+
+}  // namespace hfg

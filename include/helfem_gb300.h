@@ -295,6 +295,89 @@ typedef struct {
 hfg_status hfg_profile_enable(hfg_atom* atom, int capacity);
 hfg_status hfg_profile_read(hfg_atom* atom, hfg_profile_t* out, int reset);
 
+/* ======================================================================
+ * Diatomic molecules (prolate spheroidal coordinates mu, nu, phi):
+ * src/diatomic/basis.{h,cpp}. Matrices are over the PURE basis (the
+ * reference's Nbf(): every m != 0 shell drops its mu = 0 radial function,
+ * basis.cpp:712-736), FP64 column-major, with the angular order of
+ * lm_to_l_m (basis.cpp:456-471: |m| outer, l inner, +m before -m).
+ * ====================================================================== */
+typedef struct hfg_diatomic hfg_diatomic;
+
+typedef struct {
+  int Z1, Z2;            /* nuclear charges (Z2 = 0: a dummy centre)       */
+  double Rhalf;          /* half bond length, bohr                         */
+  int nnodes;            /* LIP nodes per mu element (3..17)               */
+  int nelem;             /* mu elements                                    */
+  const double* bval;    /* nelem+1 boundaries in mu, bval[0] = 0          */
+  int nang;              /* angular functions                              */
+  const int* lval;       /* [nang]                                         */
+  const int* mval;       /* [nang]                                         */
+  double cd_thresh;      /* in-element factor threshold (<= 0: 1e-12)      */
+  int host_only;         /* 1: tabulate only, no device state              */
+} hfg_diatomic_desc;
+
+typedef struct {
+  int nrad, nang, nel, nnodes, ndummy, nbf, nlm, Lmax, rmax, nchan, nent;
+} hfg_diatomic_dims_t;
+
+/* Replaces the TwoDBasis constructor + compute_tei (basis.cpp:522-645,
+ * 1382-1548): tabulates the disjoint P/Q integrals and the sign-carrying
+ * factor of the 2-channel in-element kernel, then uploads them. */
+hfg_status hfg_diatomic_create(const hfg_diatomic_desc* desc, hfg_diatomic** out);
+hfg_status hfg_diatomic_destroy(hfg_diatomic* d);
+hfg_status hfg_diatomic_get_dims(const hfg_diatomic* d, hfg_diatomic_dims_t* dims);
+/* dummy index (iang*Nrad + irad) of each pure function, [nbf] */
+hfg_status hfg_diatomic_pure_indices(const hfg_diatomic* d, int* idx);
+
+/* One-electron matrices (host, nbf x nbf): overlap, kinetic, nuclear
+ * (basis.cpp:1033-1140, point nuclei). */
+hfg_status hfg_diatomic_overlap(const hfg_diatomic* d, double* S);
+hfg_status hfg_diatomic_kinetic(const hfg_diatomic* d, double* T);
+hfg_status hfg_diatomic_nuclear(const hfg_diatomic* d, double* V);
+/* The same restricted to one symmetry block (the pure functions with
+ * m == mblock, in pure order): which 0 = S, 1 = T, 2 = V. *n receives the
+ * block size; out may be NULL to query it. */
+hfg_status hfg_diatomic_one_electron_block(const hfg_diatomic* d, int which, int mblock, double* out, int* n);
+
+/* Cached tables of multipole index ilm (the (L,|M|) list, |M|-major) and
+ * element iel, padded nnodes x nnodes column-major (which 0..3 = P0, P2, Q0,
+ * Q2: int B_a B_b sinh cosh^k P_L^|M|(cosh mu), k = 0, 2, and the same with
+ * Q), or the in-element factor (which 4: (2 nnodes^2 x rank) with its signs
+ * in sigma). L, M, rank and sigma may be NULL. For checking against an
+ * independent tabulation. */
+hfg_status hfg_diatomic_tables(const hfg_diatomic* d, int which, int ilm, int iel, int* L, int* M, int* rank,
+                               double* out, double* sigma);
+
+/* Associated Legendre functions P_L^M(cosh mu), Q_L^M(cosh mu) (Hobson
+ * convention, src/legendre/Legendre.h), out[M*(Lmax+1) + L]. */
+hfg_status hfg_legendre_pq(int Lmax, int Mmax, double mu, double* P, double* Q);
+/* mod_coeff(lj,mj,L,M,li,mi) = int Y_lj^mj* cos^2(nu) Y_L^M Y_li^mi
+ * (src/general/gaunt.cpp:254-275). */
+hfg_status hfg_gaunt_mod(int lj, int mj, int L, int M, int li, int mi, double* value);
+
+/* J(P) over the pure basis: replaces diatomic TwoDBasis::coulomb
+ * (basis.cpp:1621-1815, boundary expansion and removal included). */
+hfg_status hfg_diatomic_coulomb(hfg_diatomic* d, const double* P, double* J, void* stream);
+/* K(P) for a spin density, with the reference's sign (added to F): replaces
+ * diatomic TwoDBasis::exchange (basis.cpp:1817-2061), including its
+ * density-block screening. flags: HFG_EXCHANGE_SYMMETRIC (P = P^T). */
+hfg_status hfg_diatomic_exchange(hfg_diatomic* d, const double* P, double* K, int flags, void* stream);
+/* host-pointer value-semantics variants */
+hfg_status hfg_diatomic_coulomb_host(hfg_diatomic* d, const double* P, double* J);
+hfg_status hfg_diatomic_exchange_host(hfg_diatomic* d, const double* P, double* K, int flags);
+
+/* Algorithmic work of one exchange build given the density-block activity
+ * (act[i + l*nang] != 0 for blocks above the screen; NULL = all active):
+ * FP64 flops of the off-diagonal element-pair contractions, of the in-element
+ * blocks and of the recoupling, and the number of (output block, multipole)
+ * entries evaluated. */
+typedef struct {
+  double k_offdiag_flops, k_diag_flops, k_recouple_flops, n_entries;
+  double k_offdiag_sym_flops, k_diag_sym_flops, k_recouple_sym_flops, n_entries_sym;
+} hfg_diatomic_work_t;
+hfg_status hfg_diatomic_work(const hfg_diatomic* d, const unsigned char* act, hfg_diatomic_work_t* w);
+
 #ifdef __cplusplus
 }
 #endif
