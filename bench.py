@@ -507,6 +507,219 @@ def run_serve(args):
     print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------- N2 diatomic
+N2_WORKLOAD = ("N2 diatomic J+K Fock build: R=2.074 bohr, 30 mu-elements to mu_max=arccosh(40/Rhalf) "
+               "(exponential grid), 15-node LIP, l<=12 for m=0..3 (Nang=79, Nrad=420, Nbf=33114), L<=26; "
+               "P from 7 seeded N(0,1) doubly occupied orbitals drawn inside m-blocks (5 sigma, 1 pi+, 1 pi-), "
+               "Loewdin-orthonormal in the block overlap; K from the spin density P/2")
+
+
+def n2_setup(hg, host_only=False):
+    d = hg.Diatomic.from_grid(7, 7, 2.074, 30, [12, 12, 12, 12], host_only=host_only)
+    idx = d.pure_indices()
+    mv = d.mval[idx // d.nrad]
+    rng = np.random.default_rng(12345)
+    P = np.zeros((d.nbf, d.nbf), order="F")
+    act = np.zeros(d.nang * d.nang, np.uint8)
+    for m, nocc in ((0, 5), (1, 1), (-1, 1)):
+        sel = np.where(mv == m)[0]
+        S = d.one_electron_block("S", m)
+        C = rng.standard_normal((len(sel), nocc))
+        w, v = np.linalg.eigh(C.T @ S @ C)
+        C = C @ (v @ np.diag(w ** -0.5) @ v.T)
+        P[np.ix_(sel, sel)] = 2.0 * (C @ C.T)
+        shells = np.where(d.mval == m)[0]
+        for i in shells:
+            for l in shells:
+                act[i + l * d.nang] = 1
+    return d, P, act
+
+
+def n2_cpu_sample(d, P, seconds):
+    """The oracle's exchange (the reference's loop structure, OpenMP) on a
+    bounded sample of output blocks, scaled to a full build by the work model;
+    plus the oracle's J on the full density."""
+    import oracle
+    from oracle import diatomic as dia
+    nel, nn = d.dims["nel"], d.dims["nnodes"]
+    nlm = d.dims["nlm"]
+    lm, P0, P2, Q0, Q2, cdB, cds = [], [], [], [], [], [], []
+    ni = [nn] * (nel - 1) + [nn - 1]
+    for i in range(nlm):
+        rows = {k: [] for k in range(4)}
+        fB, fS = [], []
+        for e in range(nel):
+            for which in range(4):
+                L, M, t = d.tables(which, i, e)
+                rows[which].append(np.asarray(t[:ni[e], :ni[e]]))
+            _, _, B, s = d.tables(4, i, e)
+            keep = np.array([a + b * nn for b in range(ni[e]) for a in range(ni[e])])
+            fB.append(np.asarray(B[np.concatenate([keep, nn * nn + keep])]))
+            fS.append(s)
+        lm.append((L, M))
+        P0.append(rows[0]); P2.append(rows[1]); Q0.append(rows[2]); Q2.append(rows[3])
+        cdB.append(fB); cds.append(fS)
+    _, LM = dia.lm_maps(d.lval, d.mval)
+    first = np.array([e * (nn - 1) for e in range(nel)])
+    bval = np.zeros(nel + 1)
+    D = dia.DiatomicTables(d.Z1, d.Z2, d.Rhalf, nn, bval, np.asarray(d.lval, int), np.asarray(d.mval, int),
+                           d.nrad, first, np.array(ni), lm, LM, P0, P2, Q0, Q2, cdB, cds)
+    F = oracle.DiatomicOracle(D)
+    Pd = np.asfortranarray(D.expand(0.5 * P))
+    nang = d.nang
+    mv = np.asarray(d.mval)
+    active = [j + k * nang for k in range(nang) for j in range(nang) if mv[j] == mv[k] and abs(mv[j]) <= 3]
+    # a spread sample of active output blocks, grown until it takes `seconds`
+    rng = np.random.default_rng(7)
+    order = list(rng.permutation(active))
+    n, spent, done = 4, 0.0, []
+    while order and spent < seconds:
+        batch, order = order[:n], order[n:]
+        t0 = time.perf_counter()
+        F.exchange_dummy_blocks(Pd, batch)
+        spent += time.perf_counter() - t0
+        done += batch
+        n *= 2
+    act = np.zeros(nang * nang, np.uint8)
+    for i in range(nang):
+        for l in range(nang):
+            act[i + l * nang] = mv[i] == mv[l] and abs(mv[i]) <= 1
+    mask = np.zeros(nang * nang, np.uint8)
+    mask[done] = 1
+    w_s = d.work(act, mask)
+    w_t = d.work(act)
+    tot = lambda w: w["k_offdiag_flops"] + w["k_diag_flops"] + w["k_recouple_flops"]
+    k_sec = spent * tot(w_t) / max(tot(w_s), 1.0)
+    return k_sec, len(done), len(active), spent, oracle.dlib().ora_num_threads_d()
+
+
+def run_n2_reference(args):
+    import helfem_gb300 as hg
+    rank, ws, local, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    d, P, _ = n2_setup(hg, host_only=True)
+    per = []
+    for i in range(args.warmup + args.steps):
+        k_sec, ns, na, spent, thr = n2_cpu_sample(d, P, max(args.cpu_seconds, 1.0) / 4)
+        if i >= args.warmup:
+            per.append(k_sec)
+    mean = sum(per) / len(per)
+    out = {"impl": "reference", "metric": METRIC, "value": 1.0 / mean, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": N2_WORKLOAD, "inputs_vs_l2": "host run (no GPU)"},
+           "cpu_baseline": {"value": 1.0 / mean, "unit": UNIT, "cores": thr, "kind": "port",
+                            "sample": "per step: oracle exchange on a sample of active output blocks, scaled "
+                                      "by the work model to one K build"},
+           "e2e": {"value": 1.0 / mean, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_n2(args):
+    import torch
+    import helfem_gb300 as hg
+
+    rank, ws, local, dist = dist_setup(args.gpus)
+    if dist is not None:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    d, P, act = n2_setup(hg)
+    nbf = d.nbf
+    Pd = torch.from_numpy(P.ravel(order="F")).cuda()
+    Pa = 0.5 * Pd
+    Jd, Kd = torch.empty_like(Pd), torch.empty_like(Pd)
+    stream = torch.cuda.current_stream()
+    evs = []
+
+    def step(timed=False):
+        if timed:
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record(stream)
+        d.coulomb(Pd, Jd, stream=stream)
+        if timed:
+            e[1].record(stream)
+        d.exchange(Pa, Kd, symmetric=True, stream=stream)
+        if timed:
+            e[2].record(stream)
+            evs.append(e)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    j_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
+    k_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
+    value = ws * args.steps / (ms * 1e-3)
+    Ecoul = 0.5 * float((Pd * Jd).sum())
+    Exx = 0.5 * float((Pa * Kd).sum()) * 2.0
+    # end to end through the host-pointer drop-ins
+    Jh = np.empty((nbf, nbf), order="F")
+    Kh = np.empty((nbf, nbf), order="F")
+    Pah = np.asfortranarray(0.5 * P)
+    ne = max(1, min(args.e2e_steps, 2))
+    t0 = time.perf_counter()
+    for _ in range(ne):
+        d.coulomb_host(P, out=Jh)
+        d.exchange_host(Pah, out=Kh, symmetric=True)
+    te = time.perf_counter() - t0
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    w = d.work(act)
+    kflops = w["k_offdiag_sym_flops"] + w["k_diag_sym_flops"] + w["k_recouple_sym_flops"]
+    peak = fp64_peak_tflops(torch)
+    achieved = kflops / (k_ms * 1e-3) / 1e12
+    cpu = None
+    if args.cpu_seconds > 0:
+        k_sec, ns, na, spent, thr = n2_cpu_sample(d, P, args.cpu_seconds)
+        cpu = {"value": 1.0 / k_sec, "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"oracle exchange on {ns} of {na} active output blocks in {spent:.1f} s, "
+                         f"scaled by the work model to one K build ({k_sec:.1f} s); J not included"}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": N2_WORKLOAD, "nbf": nbf, "ndummy": d.ndummy, "parallelism": f"replicas x{ws}",
+                   "inputs_vs_l2": "P is 8.8 GB > 129 MB L2: no flush needed"},
+        "form": "plain FP64, symmetric exchange mode",
+        "kernel_ms": {"coulomb": j_ms, "exchange": k_ms},
+        "energies_eh": {"coulomb": Ecoul, "exchange": Exx},
+        "roofline": {"bound": "fp64", "kernel": "dk_tiles (whole exchange call)", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "flops_per_launch": kflops, "ms_per_launch": k_ms,
+                     "peak_source": "measured in this run: cuBLAS DGEMM 4096^3", "traffic": None},
+        "cpu_baseline": cpu,
+        "e2e": {"value": ws * ne / te, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nbf * nbf,
+                "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
+                "path": "hfg_diatomic_coulomb_host + hfg_diatomic_exchange_host (pageable host P, J, K)"},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps * 12,  # J: expand, contract, scatter, gather; K: expand, norms, act,
+                                           # entry_act, compact, tiles, fixup, gather
+    }
+    print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -517,7 +730,7 @@ def main():
                     help="seconds of oracle builds for cpu_baseline (0 skips it)")
     ap.add_argument("--e2e-steps", type=int, default=10, help="host-pointer drop-in steps (0 skips)")
     ap.add_argument("--plain", action="store_true", help="time the plain FP64 form only")
-    ap.add_argument("--workload", default="fock", choices=["fock", "scf-batch", "serve"])
+    ap.add_argument("--workload", default="fock", choices=["fock", "scf-batch", "serve", "n2"])
     ap.add_argument("--atoms", type=int, default=32)
     ap.add_argument("--nel-max", type=int, default=30)
     ap.add_argument("--workers", type=int, default=8)
@@ -526,12 +739,16 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.impl == "reference" and args.workload == "n2":
+        run_n2_reference(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "scf-batch":
         run_scf_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "n2":
+        run_n2(args)
     else:
         run_ours(args)
 

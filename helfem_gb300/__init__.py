@@ -98,7 +98,7 @@ _SIGS = {
     "hfg_diatomic_exchange": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
     "hfg_diatomic_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_diatomic_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
-    "hfg_diatomic_work": ([_P, _P, _P], ctypes.c_int),
+    "hfg_diatomic_work": ([_P, _P, _P, _P], ctypes.c_int),
 }
 KERNEL_CLASSES = ("j_contract", "j_scatter", "k_block_norms", "k_tiles", "k_fixup")
 XC_IDS = {"lda_x": 1, "lda_c_vwn": 7, "lda_c_pw": 12, "gga_x_pbe": 101, "gga_c_pbe": 130}
@@ -603,8 +603,12 @@ class Diatomic:
                                                EXCHANGE_SYMMETRIC if symmetric else 0))
         return K
 
-    def work(self, act: np.ndarray = None) -> dict:
+    def work(self, act: np.ndarray = None, jk_mask: np.ndarray = None) -> dict:
+        """Exchange work model (flops) for a density-block activity mask
+        act[i + l*nang] and an optional output-block mask jk_mask[j + k*nang]."""
         w = _DWork()
         a = None if act is None else np.ascontiguousarray(act, dtype=np.uint8)
-        _check(_lib.hfg_diatomic_work(self._h, None if a is None else a.ctypes.data, ctypes.byref(w)))
+        m = None if jk_mask is None else np.ascontiguousarray(jk_mask, dtype=np.uint8)
+        _check(_lib.hfg_diatomic_work(self._h, None if a is None else a.ctypes.data,
+                                      None if m is None else m.ctypes.data, ctypes.byref(w)))
         return {n: getattr(w, n) for n, _ in _DWork._fields_}

@@ -311,7 +311,8 @@ hfg_status hfg_diatomic_exchange_host(hfg_diatomic* d, const double* P, double* 
   });
 }
 
-hfg_status hfg_diatomic_work(const hfg_diatomic* d, const unsigned char* act, hfg_diatomic_work_t* w) {
+hfg_status hfg_diatomic_work(const hfg_diatomic* d, const unsigned char* act, const unsigned char* jk_mask,
+                             hfg_diatomic_work_t* w) {
   return guard([&] {
     need(d && w, "hfg_diatomic_work: null argument");
     const hfg::DiatomicHost& H = d->host;
@@ -325,6 +326,7 @@ hfg_status hfg_diatomic_work(const hfg_diatomic* d, const unsigned char* act, hf
     for (int k = 0; k < nang; ++k)
       for (int j = 0; j < nang; ++j) {
         const int jk = j + k * nang;
+        if (jk_mask && !jk_mask[jk]) continue;
         for (int ent = H.kjk_ptr[jk]; ent < H.kjk_ptr[jk + 1]; ++ent) {
           const int L = H.kent_L[ent], Ma = H.kent_Ma[ent];
           double terms = 0.0;

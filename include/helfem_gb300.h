@@ -368,7 +368,8 @@ hfg_status hfg_diatomic_coulomb_host(hfg_diatomic* d, const double* P, double* J
 hfg_status hfg_diatomic_exchange_host(hfg_diatomic* d, const double* P, double* K, int flags);
 
 /* Algorithmic work of one exchange build given the density-block activity
- * (act[i + l*nang] != 0 for blocks above the screen; NULL = all active):
+ * (act[i + l*nang] != 0 for blocks above the screen; NULL = all active),
+ * restricted to the output blocks with jk_mask[j + k*nang] != 0 (NULL = all):
  * FP64 flops of the off-diagonal element-pair contractions, of the in-element
  * blocks and of the recoupling, and the number of (output block, multipole)
  * entries evaluated. */
@@ -376,7 +377,8 @@ typedef struct {
   double k_offdiag_flops, k_diag_flops, k_recouple_flops, n_entries;
   double k_offdiag_sym_flops, k_diag_sym_flops, k_recouple_sym_flops, n_entries_sym;
 } hfg_diatomic_work_t;
-hfg_status hfg_diatomic_work(const hfg_diatomic* d, const unsigned char* act, hfg_diatomic_work_t* w);
+hfg_status hfg_diatomic_work(const hfg_diatomic* d, const unsigned char* act, const unsigned char* jk_mask,
+                             hfg_diatomic_work_t* w);
 
 #ifdef __cplusplus
 }

@@ -173,6 +173,9 @@ def dlib():
             _dlib = ctypes.CDLL(_compile("dfock_ref.cpp", _DLIB, False))
             _dlib.ora_dexchange.argtypes = [ctypes.POINTER(_OraDiatomic), ctypes.c_void_p, ctypes.c_void_p]
             _dlib.ora_dexchange.restype = None
+            _dlib.ora_dexchange_blocks.argtypes = [ctypes.POINTER(_OraDiatomic), ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_void_p, ctypes.c_int]
+            _dlib.ora_dexchange_blocks.restype = None
             _dlib.ora_num_threads_d.restype = ctypes.c_int
     return _dlib
 
@@ -231,3 +234,13 @@ class DiatomicOracle:
         Kd = np.zeros_like(Pd, order="F")
         dlib().ora_dexchange(ctypes.byref(self.s), Pd.ctypes.data, Kd.ctypes.data)
         return self.D.remove(Kd)
+
+    def exchange_dummy_blocks(self, Pdummy: np.ndarray, jk) -> np.ndarray:
+        """K over the dummy basis restricted to the output blocks jk (j + k*nang),
+        from an already expanded (Fortran-ordered) density: a bounded sample
+        of the full build for CPU timing."""
+        Pd = np.asfortranarray(Pdummy, dtype=np.float64)
+        Kd = np.zeros_like(Pd, order="F")
+        jk = np.ascontiguousarray(jk, dtype=np.int32)
+        dlib().ora_dexchange_blocks(ctypes.byref(self.s), Pd.ctypes.data, Kd.ctypes.data, jk.ctypes.data, len(jk))
+        return Kd

@@ -108,14 +108,11 @@ int ora_num_threads_d() {
 #endif
 }
 
-// K over the dummy basis (ndummy = nang*nrad); P is the expanded density
-void ora_dexchange(const ora_diatomic* Dp, const double* P, double* K) {
-  const ora_diatomic& D = *Dp;
-  const int nrad = D.nrad, nang = D.nang, nel = D.nel, nn = D.nn;
+// density-block screen: act[i + l*nang] = ||P_il|| >= 10 eps
+static void block_activity(const ora_diatomic& D, const double* P, std::vector<char>& act) {
+  const int nrad = D.nrad, nang = D.nang;
   const size_t nd = (size_t)nang * nrad;
-  std::memset(K, 0, sizeof(double) * nd * nd);
-  // density-block norms, screened at 10 eps
-  std::vector<char> act((size_t)nang * nang, 0);
+  act.assign((size_t)nang * nang, 0);
 #pragma omp parallel for collapse(2) schedule(static)
   for (int l = 0; l < nang; ++l)
     for (int i = 0; i < nang; ++i) {
@@ -127,112 +124,138 @@ void ora_dexchange(const ora_diatomic* Dp, const double* P, double* K) {
         }
       act[(size_t)i + (size_t)l * nang] = !(std::sqrt(s) < 10 * DBL_EPSILON);
     }
+}
+
+// the output block (j,k) of K; R, T, T2, Ks are per-thread work arrays
+static void exchange_block(const ora_diatomic& D, const double* P, const std::vector<char>& act, int j, int k,
+                           std::vector<double>& R, std::vector<double>& T, std::vector<double>& T2,
+                           std::vector<double>& Ks, double* K) {
+  const int nrad = D.nrad, nang = D.nang, nel = D.nel, nn = D.nn;
+  const size_t nd = (size_t)nang * nrad;
+  const int lj = D.lval[j], mj = D.mval[j], lk = D.lval[k], mk = D.mval[k];
+  for (int ilm = 0; ilm < D.nlm; ++ilm) {
+    const int L = D.lm_L[ilm], Ma = D.lm_M[ilm];
+    bool any = false;
+    // recouple: every active (i,l) with mi - ml = mj - mk and |mj - mi| = Ma
+    for (int i = 0; i < nang; ++i) {
+      const int li = D.lval[i], mi = D.mval[i];
+      const int M = mj - mi;
+      if (std::abs(M) != Ma) continue;
+      for (int l = 0; l < nang; ++l) {
+        const int ll = D.lval[l], ml = D.mval[l];
+        if (mi - ml != mj - mk) continue;
+        if (!act[(size_t)i + (size_t)l * nang]) continue;
+        const int Lmin = std::max(std::max(std::abs(li - lj), std::abs(lk - ll)) - 2, std::abs(M));
+        const int Lmx = std::min(li + lj, lk + ll) + 2;
+        if (L < Lmin || L > Lmx) continue;
+        const double m1 = tab(D, D.modc, j, L, M, i), c1 = tab(D, D.coef, j, L, M, i);
+        const double m2 = tab(D, D.modc, k, L, M, l), c2 = tab(D, D.coef, k, L, M, l);
+        const double c00 = m1 * m2, c02 = -m1 * c2, c20 = -c1 * m2, c22 = c1 * c2;
+        if (c00 == 0.0 && c02 == 0.0 && c20 == 0.0 && c22 == 0.0) continue;
+        if (!any) {
+          std::fill(R.begin(), R.end(), 0.0);
+          any = true;
+        }
+        const double f = lmfac(D, L, M);
+        const double cc[4] = {f * c00, f * c02, f * c20, f * c22};
+        for (int c = 0; c < nrad; ++c)
+          for (int r = 0; r < nrad; ++r) {
+            const double v = P[((size_t)l * nrad + c) * nd + (size_t)i * nrad + r];
+            for (int ch = 0; ch < 4; ++ch) R[(size_t)ch * nrad * nrad + r + (size_t)c * nrad] += cc[ch] * v;
+          }
+      }
+    }
+    if (!any) continue;
+    const double* R00 = R.data();
+    const double* R02 = R00 + (size_t)nrad * nrad;
+    const double* R20 = R02 + (size_t)nrad * nrad;
+    const double* R22 = R20 + (size_t)nrad * nrad;
+    for (int ie = 0; ie < nel; ++ie)
+      for (int je = 0; je < nel; ++je) {
+        const int fi = D.first[ie], Ni = D.ni[ie], fj = D.first[je], Nj = D.ni[je];
+        std::fill(Ks.begin(), Ks.end(), 0.0);
+        const size_t ro = (size_t)fi + (size_t)fj * nrad;
+        if (ie != je) {
+          const size_t oi = ((size_t)ilm * nel + ie) * nn * nn, oj = ((size_t)ilm * nel + je) * nn * nn;
+          const double* i0 = (ie > je) ? D.Q0 + oi : D.P0 + oi;
+          const double* i2 = (ie > je) ? D.Q2 + oi : D.P2 + oi;
+          const double* j0 = (ie > je) ? D.P0 + oj : D.Q0 + oj;
+          const double* j2 = (ie > je) ? D.P2 + oj : D.Q2 + oj;
+          // T = R00 j0' + R02 j2';  Ks -= i0 T
+          gemm_nt(Ni, Nj, Nj, R00 + ro, nrad, j0, nn, T.data(), nn, 1.0, false);
+          gemm_nt(Ni, Nj, Nj, R02 + ro, nrad, j2, nn, T.data(), nn, 1.0, true);
+          gemm_nn(Ni, Nj, Ni, i0, nn, T.data(), nn, Ks.data(), nn, -1.0);
+          gemm_nt(Ni, Nj, Nj, R20 + ro, nrad, j0, nn, T.data(), nn, 1.0, false);
+          gemm_nt(Ni, Nj, Nj, R22 + ro, nrad, j2, nn, T.data(), nn, 1.0, true);
+          gemm_nn(Ni, Nj, Ni, i2, nn, T.data(), nn, Ks.data(), nn, -1.0);
+          for (int c = 0; c < Nj; ++c)
+            for (int r = 0; r < Ni; ++r)
+              K[((size_t)k * nrad + fj + c) * nd + (size_t)j * nrad + fi + r] += Ks[r + (size_t)c * nn];
+        } else {
+          const int64_t bo = D.cdB_off[(size_t)ilm * nel + ie];
+          const int rk = D.cd_rank[(size_t)ilm * nel + ie];
+          const double* B = D.cdB + bo;
+          const double* sg = D.cds + D.cds_off[(size_t)ilm * nel + ie];
+          const size_t n2 = (size_t)Ni * Ni;
+          for (int p = 0; p < rk; ++p) {
+            const double* M0 = B + (size_t)p * 2 * n2;  // (Ni x Ni), symmetric
+            const double* M2 = M0 + n2;
+            // contrib = M0'R00 M0' - M0'R02 M2' - M2'R20 M0' + M2'R22 M2'
+            const double* Ms[2] = {M0, M2};
+            const double* Rs[4] = {R00 + ro, R02 + ro, R20 + ro, R22 + ro};
+            const double sgn[4] = {1.0, -1.0, -1.0, 1.0};
+            for (int a = 0; a < 2; ++a)
+              for (int b = 0; b < 2; ++b) {
+                // T2 = R_ab Mb'   (Ni x Ni)
+                for (int c = 0; c < Ni; ++c)
+                  for (int r = 0; r < Ni; ++r) {
+                    double s = 0.0;
+                    for (int t = 0; t < Ni; ++t) s += Rs[2 * a + b][r + (size_t)t * nrad] * Ms[b][c + (size_t)t * Ni];
+                    T2[r + (size_t)c * nn] = s;
+                  }
+                // Ks += sigma sgn Ma' T2
+                const double w = sg[p] * sgn[2 * a + b];
+                for (int c = 0; c < Ni; ++c)
+                  for (int r = 0; r < Ni; ++r) {
+                    double s = 0.0;
+                    for (int t = 0; t < Ni; ++t) s += Ms[a][t + (size_t)r * Ni] * T2[t + (size_t)c * nn];
+                    Ks[r + (size_t)c * nn] += w * s;
+                  }
+              }
+          }
+          for (int c = 0; c < Nj; ++c)
+            for (int r = 0; r < Ni; ++r)
+              K[((size_t)k * nrad + fj + c) * nd + (size_t)j * nrad + fi + r] -= Ks[r + (size_t)c * nn];
+        }
+      }
+  }
+}
+
+// K over the dummy basis (ndummy = nang*nrad); P is the expanded density.
+// jk == nullptr: every output block; else the n blocks jk[0..n) (j + k*nang),
+// the rest of K left zero (a bounded sample for CPU timing).
+void ora_dexchange_blocks(const ora_diatomic* Dp, const double* P, double* K, const int* jk, int n) {
+  const ora_diatomic& D = *Dp;
+  const int nrad = D.nrad, nang = D.nang, nn = D.nn;
+  const size_t nd = (size_t)nang * nrad;
+  std::memset(K, 0, sizeof(double) * nd * nd);
+  std::vector<char> act;
+  block_activity(D, P, act);
+  const int nblk = jk ? n : nang * nang;
 #pragma omp parallel
   {
     std::vector<double> R((size_t)4 * nrad * nrad);
     std::vector<double> T((size_t)nn * nn), T2((size_t)nn * nn), Ks((size_t)nn * nn);
-#pragma omp for collapse(2) schedule(dynamic)
-    for (int j = 0; j < nang; ++j)
-      for (int k = 0; k < nang; ++k) {
-        const int lj = D.lval[j], mj = D.mval[j], lk = D.lval[k], mk = D.mval[k];
-        for (int ilm = 0; ilm < D.nlm; ++ilm) {
-          const int L = D.lm_L[ilm], Ma = D.lm_M[ilm];
-          bool any = false;
-          // recouple: every active (i,l) with mi - ml = mj - mk and |mj - mi| = Ma
-          for (int i = 0; i < nang; ++i) {
-            const int li = D.lval[i], mi = D.mval[i];
-            const int M = mj - mi;
-            if (std::abs(M) != Ma) continue;
-            for (int l = 0; l < nang; ++l) {
-              const int ll = D.lval[l], ml = D.mval[l];
-              if (mi - ml != mj - mk) continue;
-              if (!act[(size_t)i + (size_t)l * nang]) continue;
-              const int Lmin = std::max(std::max(std::abs(li - lj), std::abs(lk - ll)) - 2, std::abs(M));
-              const int Lmx = std::min(li + lj, lk + ll) + 2;
-              if (L < Lmin || L > Lmx) continue;
-              const double m1 = tab(D, D.modc, j, L, M, i), c1 = tab(D, D.coef, j, L, M, i);
-              const double m2 = tab(D, D.modc, k, L, M, l), c2 = tab(D, D.coef, k, L, M, l);
-              const double c00 = m1 * m2, c02 = -m1 * c2, c20 = -c1 * m2, c22 = c1 * c2;
-              if (c00 == 0.0 && c02 == 0.0 && c20 == 0.0 && c22 == 0.0) continue;
-              if (!any) {
-                std::fill(R.begin(), R.end(), 0.0);
-                any = true;
-              }
-              const double f = lmfac(D, L, M);
-              const double cc[4] = {f * c00, f * c02, f * c20, f * c22};
-              for (int c = 0; c < nrad; ++c)
-                for (int r = 0; r < nrad; ++r) {
-                  const double v = P[((size_t)l * nrad + c) * nd + (size_t)i * nrad + r];
-                  for (int ch = 0; ch < 4; ++ch) R[(size_t)ch * nrad * nrad + r + (size_t)c * nrad] += cc[ch] * v;
-                }
-            }
-          }
-          if (!any) continue;
-          const double* R00 = R.data();
-          const double* R02 = R00 + (size_t)nrad * nrad;
-          const double* R20 = R02 + (size_t)nrad * nrad;
-          const double* R22 = R20 + (size_t)nrad * nrad;
-          for (int ie = 0; ie < nel; ++ie)
-            for (int je = 0; je < nel; ++je) {
-              const int fi = D.first[ie], Ni = D.ni[ie], fj = D.first[je], Nj = D.ni[je];
-              std::fill(Ks.begin(), Ks.end(), 0.0);
-              const size_t ro = (size_t)fi + (size_t)fj * nrad;
-              if (ie != je) {
-                const size_t oi = ((size_t)ilm * nel + ie) * nn * nn, oj = ((size_t)ilm * nel + je) * nn * nn;
-                const double* i0 = (ie > je) ? D.Q0 + oi : D.P0 + oi;
-                const double* i2 = (ie > je) ? D.Q2 + oi : D.P2 + oi;
-                const double* j0 = (ie > je) ? D.P0 + oj : D.Q0 + oj;
-                const double* j2 = (ie > je) ? D.P2 + oj : D.Q2 + oj;
-                // T = R00 j0' + R02 j2';  Ks -= i0 T
-                gemm_nt(Ni, Nj, Nj, R00 + ro, nrad, j0, nn, T.data(), nn, 1.0, false);
-                gemm_nt(Ni, Nj, Nj, R02 + ro, nrad, j2, nn, T.data(), nn, 1.0, true);
-                gemm_nn(Ni, Nj, Ni, i0, nn, T.data(), nn, Ks.data(), nn, -1.0);
-                gemm_nt(Ni, Nj, Nj, R20 + ro, nrad, j0, nn, T.data(), nn, 1.0, false);
-                gemm_nt(Ni, Nj, Nj, R22 + ro, nrad, j2, nn, T.data(), nn, 1.0, true);
-                gemm_nn(Ni, Nj, Ni, i2, nn, T.data(), nn, Ks.data(), nn, -1.0);
-                for (int c = 0; c < Nj; ++c)
-                  for (int r = 0; r < Ni; ++r)
-                    K[((size_t)k * nrad + fj + c) * nd + (size_t)j * nrad + fi + r] += Ks[r + (size_t)c * nn];
-              } else {
-                const int64_t bo = D.cdB_off[(size_t)ilm * nel + ie];
-                const int rk = D.cd_rank[(size_t)ilm * nel + ie];
-                const double* B = D.cdB + bo;
-                const double* sg = D.cds + D.cds_off[(size_t)ilm * nel + ie];
-                const size_t n2 = (size_t)Ni * Ni;
-                for (int p = 0; p < rk; ++p) {
-                  const double* M0 = B + (size_t)p * 2 * n2;  // (Ni x Ni), symmetric
-                  const double* M2 = M0 + n2;
-                  // contrib = M0'R00 M0' - M0'R02 M2' - M2'R20 M0' + M2'R22 M2'
-                  const double* Ms[2] = {M0, M2};
-                  const double* Rs[4] = {R00 + ro, R02 + ro, R20 + ro, R22 + ro};
-                  const double sgn[4] = {1.0, -1.0, -1.0, 1.0};
-                  for (int a = 0; a < 2; ++a)
-                    for (int b = 0; b < 2; ++b) {
-                      // T2 = R_ab Mb'   (Ni x Ni)
-                      for (int c = 0; c < Ni; ++c)
-                        for (int r = 0; r < Ni; ++r) {
-                          double s = 0.0;
-                          for (int t = 0; t < Ni; ++t) s += Rs[2 * a + b][r + (size_t)t * nrad] * Ms[b][c + (size_t)t * Ni];
-                          T2[r + (size_t)c * nn] = s;
-                        }
-                      // Ks += sigma sgn Ma' T2
-                      const double w = sg[p] * sgn[2 * a + b];
-                      for (int c = 0; c < Ni; ++c)
-                        for (int r = 0; r < Ni; ++r) {
-                          double s = 0.0;
-                          for (int t = 0; t < Ni; ++t) s += Ms[a][t + (size_t)r * Ni] * T2[t + (size_t)c * nn];
-                          Ks[r + (size_t)c * nn] += w * s;
-                        }
-                    }
-                }
-                for (int c = 0; c < Nj; ++c)
-                  for (int r = 0; r < Ni; ++r)
-                    K[((size_t)k * nrad + fj + c) * nd + (size_t)j * nrad + fi + r] -= Ks[r + (size_t)c * nn];
-              }
-            }
-        }
-      }
+#pragma omp for schedule(dynamic)
+    for (int b = 0; b < nblk; ++b) {
+      const int jkb = jk ? jk[b] : b;
+      exchange_block(D, P, act, jkb % nang, jkb / nang, R, T, T2, Ks, K);
+    }
   }
+}
+
+void ora_dexchange(const ora_diatomic* Dp, const double* P, double* K) {
+  ora_dexchange_blocks(Dp, P, K, nullptr, 0);
 }
 
 }  // extern "C"
