@@ -1,0 +1,226 @@
+// helfem_gb300/TwoDBasis.hpp — header-only C++ shim over the C ABI that
+// re-exposes the reference's member-function signatures for the Fock-build
+// path, so that a C++ driver written against HelFEM switches by changing the
+// type it instantiates:
+//
+//   atomic   TwoDBasisT<double>::coulomb / exchange / compute_tei / overlap /
+//            kinetic / nuclear           (src/atomic/TwoDBasis.h:180-227)
+//   diatomic TwoDBasis::coulomb / exchange / compute_tei / overlap /
+//            kinetic / nuclear           (src/diatomic/basis.h:300-337)
+//   DFTGrid::eval_Fxc(x, c, P, H, Exc, Nel, thr) and the Pa/Pb overload
+//                                        (src/atomic/dftgrid.h:156-159)
+//
+// Matrix is any column-major dense type with Matrix(rows, cols), rows(),
+// cols() and data() (Eigen::MatrixXd, helfem::Matrix). Status codes come back
+// as the reference's exception types: a missing compute_tei is
+// std::logic_error("Primitive teis have not been computed!\n") as in
+// TwoDBasis.cpp:775-776, bad shapes are std::runtime_error (as
+// dftgrid_common.h:130-134 throws), bad arguments std::invalid_argument,
+// allocation failures std::bad_alloc.
+#pragma once
+
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../helfem_gb300.h"
+
+namespace helfem_gb300 {
+
+inline void check(hfg_status s) {
+  if (s == HFG_OK) return;
+  const std::string msg = hfg_last_error();
+  switch (s) {
+    case HFG_ERR_ARG: throw std::invalid_argument(msg);
+    case HFG_ERR_STATE: throw std::logic_error(msg);
+    case HFG_ERR_NOMEM: throw std::bad_alloc();
+    default: throw std::runtime_error(msg);
+  }
+}
+
+namespace detail {
+template <class Matrix>
+void require_square(const Matrix& P, size_t n, const char* who) {
+  if ((size_t)P.rows() != n || (size_t)P.cols() != n)
+    throw std::runtime_error(std::string(who) + ": density matrix has the wrong size");
+}
+inline void no_tei() { throw std::logic_error("Primitive teis have not been computed!\n"); }
+}  // namespace detail
+
+// ---------------------------------------------------------------- atomic
+template <class Matrix>
+class AtomicTwoDBasis {
+ public:
+  AtomicTwoDBasis(int Z, int nnodes, int nquad, std::vector<double> bval, std::vector<int> lval,
+                  std::vector<int> mval)
+      : Z_(Z), nnodes_(nnodes), nquad_(nquad), bval_(std::move(bval)), lval_(std::move(lval)),
+        mval_(std::move(mval)) {
+    // one-electron matrices are available before compute_tei, as in the reference
+    host_ = make(true);
+  }
+  ~AtomicTwoDBasis() = default;
+  AtomicTwoDBasis(const AtomicTwoDBasis&) = delete;
+  AtomicTwoDBasis& operator=(const AtomicTwoDBasis&) = delete;
+
+  // caches the integrals on the device; the flag is accepted for signature
+  // compatibility (both J and K tables are always built)
+  void compute_tei(bool /*exchange*/) { gpu_ = make(false); }
+
+  size_t Nbf() const { return (size_t)dims().nbf; }
+  size_t Nrad() const { return (size_t)dims().nrad; }
+  size_t Nang() const { return lval_.size(); }
+
+  Matrix overlap() const { return one(hfg_overlap); }
+  Matrix kinetic() const { return one(hfg_kinetic); }
+  Matrix nuclear() const { return one(hfg_nuclear); }
+
+  Matrix coulomb(const Matrix& P) const {
+    if (!gpu_) detail::no_tei();
+    detail::require_square(P, Nbf(), "coulomb");
+    Matrix J(P.rows(), P.cols());
+    check(hfg_coulomb_host(gpu_.get(), P.data(), J.data()));
+    return J;
+  }
+  Matrix exchange(const Matrix& P) const {
+    if (!gpu_) detail::no_tei();
+    detail::require_square(P, Nbf(), "exchange");
+    Matrix K(P.rows(), P.cols());
+    check(hfg_exchange_host(gpu_.get(), P.data(), K.data()));
+    return K;
+  }
+
+  hfg_atom* handle() const { return gpu_.get(); }
+
+ private:
+  struct Del {
+    void operator()(hfg_atom* a) const { hfg_atom_destroy(a); }
+  };
+  std::unique_ptr<hfg_atom, Del> make(bool host_only) const {
+    hfg_atom_desc d{Z_, nnodes_, nquad_, (int)bval_.size() - 1, bval_.data(), (int)lval_.size(),
+                    lval_.data(), mval_.data(), 0.0, host_only ? 1 : 0};
+    hfg_atom* a = nullptr;
+    check(hfg_atom_create(&d, &a));
+    return std::unique_ptr<hfg_atom, Del>(a);
+  }
+  hfg_atom_dims_t dims() const {
+    hfg_atom_dims_t d{};
+    check(hfg_atom_get_dims(host_.get(), &d));
+    return d;
+  }
+  Matrix one(hfg_status (*fn)(const hfg_atom*, double*)) const {
+    const size_t n = Nbf();
+    Matrix M(n, n);
+    check(fn(host_.get(), M.data()));
+    return M;
+  }
+
+  int Z_, nnodes_, nquad_;
+  std::vector<double> bval_;
+  std::vector<int> lval_, mval_;
+  std::unique_ptr<hfg_atom, Del> host_, gpu_;
+};
+
+// DFTGrid::eval_Fxc over an atomic basis (the grid is built on the device on
+// first use; Ekin of meta-GGAs is not part of this path and returns 0)
+template <class Matrix>
+class AtomicDFTGrid {
+ public:
+  explicit AtomicDFTGrid(const AtomicTwoDBasis<Matrix>* basis) : b_(basis) {}
+  void eval_Fxc(int x_func, int c_func, const Matrix& P, Matrix& H, double& Exc, double& Nel, double& Ekin,
+                double thr) const {
+    if (!b_->handle()) detail::no_tei();
+    detail::require_square(P, b_->Nbf(), "eval_Fxc");
+    H = Matrix(P.rows(), P.cols());
+    check(hfg_xc_host(b_->handle(), x_func, c_func, P.data(), nullptr, H.data(), nullptr, &Exc, &Nel, thr));
+    Ekin = 0.0;
+  }
+  void eval_Fxc(int x_func, int c_func, const Matrix& Pa, const Matrix& Pb, Matrix& Ha, Matrix& Hb, double& Exc,
+                double& Nel, double& Ekin, double thr) const {
+    if (!b_->handle()) detail::no_tei();
+    detail::require_square(Pa, b_->Nbf(), "eval_Fxc");
+    detail::require_square(Pb, b_->Nbf(), "eval_Fxc");
+    Ha = Matrix(Pa.rows(), Pa.cols());
+    Hb = Matrix(Pb.rows(), Pb.cols());
+    check(hfg_xc_host(b_->handle(), x_func, c_func, Pa.data(), Pb.data(), Ha.data(), Hb.data(), &Exc, &Nel, thr));
+    Ekin = 0.0;
+  }
+
+ private:
+  const AtomicTwoDBasis<Matrix>* b_;
+};
+
+// -------------------------------------------------------------- diatomic
+template <class Matrix>
+class DiatomicTwoDBasis {
+ public:
+  DiatomicTwoDBasis(int Z1, int Z2, double Rhalf, int nnodes, std::vector<double> bval, std::vector<int> lval,
+                    std::vector<int> mval)
+      : Z1_(Z1), Z2_(Z2), Rhalf_(Rhalf), nnodes_(nnodes), bval_(std::move(bval)), lval_(std::move(lval)),
+        mval_(std::move(mval)) {
+    host_ = make(true);
+  }
+  DiatomicTwoDBasis(const DiatomicTwoDBasis&) = delete;
+  DiatomicTwoDBasis& operator=(const DiatomicTwoDBasis&) = delete;
+
+  void compute_tei(bool /*exchange*/) { gpu_ = make(false); }
+
+  size_t Nbf() const { return (size_t)dims().nbf; }
+  size_t Ndummy() const { return (size_t)dims().ndummy; }
+  size_t Nrad() const { return (size_t)dims().nrad; }
+  size_t Nang() const { return lval_.size(); }
+
+  Matrix overlap() const { return one(hfg_diatomic_overlap); }
+  Matrix kinetic() const { return one(hfg_diatomic_kinetic); }
+  Matrix nuclear() const { return one(hfg_diatomic_nuclear); }
+
+  Matrix coulomb(const Matrix& P) const {
+    if (!gpu_) detail::no_tei();
+    detail::require_square(P, Nbf(), "coulomb");
+    Matrix J(P.rows(), P.cols());
+    check(hfg_diatomic_coulomb_host(gpu_.get(), P.data(), J.data()));
+    return J;
+  }
+  Matrix exchange(const Matrix& P) const {
+    if (!gpu_) detail::no_tei();
+    detail::require_square(P, Nbf(), "exchange");
+    Matrix K(P.rows(), P.cols());
+    check(hfg_diatomic_exchange_host(gpu_.get(), P.data(), K.data(), 0));
+    return K;
+  }
+
+  hfg_diatomic* handle() const { return gpu_.get(); }
+
+ private:
+  struct Del {
+    void operator()(hfg_diatomic* d) const { hfg_diatomic_destroy(d); }
+  };
+  std::unique_ptr<hfg_diatomic, Del> make(bool host_only) const {
+    hfg_diatomic_desc d{Z1_, Z2_, Rhalf_, nnodes_, (int)bval_.size() - 1, bval_.data(), (int)lval_.size(),
+                        lval_.data(), mval_.data(), 0.0, host_only ? 1 : 0};
+    hfg_diatomic* h = nullptr;
+    check(hfg_diatomic_create(&d, &h));
+    return std::unique_ptr<hfg_diatomic, Del>(h);
+  }
+  hfg_diatomic_dims_t dims() const {
+    hfg_diatomic_dims_t d{};
+    check(hfg_diatomic_get_dims(host_.get(), &d));
+    return d;
+  }
+  Matrix one(hfg_status (*fn)(const hfg_diatomic*, double*)) const {
+    const size_t n = Nbf();
+    Matrix M(n, n);
+    check(fn(host_.get(), M.data()));
+    return M;
+  }
+
+  int Z1_, Z2_;
+  double Rhalf_;
+  int nnodes_;
+  std::vector<double> bval_;
+  std::vector<int> lval_, mval_;
+  std::unique_ptr<hfg_diatomic, Del> host_, gpu_;
+};
+
+}  // namespace helfem_gb300

@@ -1,0 +1,74 @@
+// Exercises the C++ shim (include/helfem_gb300/TwoDBasis.hpp) the way a
+// HelFEM driver would: reference signatures, reference exception types.
+//   shim_check host   -> prints the atomic and diatomic overlap traces and
+//                        checks that coulomb() before compute_tei() throws
+//                        std::logic_error
+//   shim_check gpu    -> prints tr(P J), tr(P K) for a fixed density
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
+#include "helfem_gb300/TwoDBasis.hpp"
+
+struct Mat {  // minimal column-major matrix with the interface the shim needs
+  std::vector<double> v;
+  long r = 0, c = 0;
+  Mat() = default;
+  Mat(long r_, long c_) : v((size_t)r_ * c_, 0.0), r(r_), c(c_) {}
+  long rows() const { return r; }
+  long cols() const { return c; }
+  double* data() { return v.data(); }
+  const double* data() const { return v.data(); }
+  double& operator()(long i, long j) { return v[(size_t)i + (size_t)j * r]; }
+};
+
+static double trace_prod(const Mat& A, const Mat& B) {
+  double s = 0.0;
+  for (size_t i = 0; i < A.v.size(); ++i) s += A.v[i] * B.v[i];
+  return s;
+}
+
+int main(int argc, char** argv) {
+  const bool gpu = argc > 1 && std::strcmp(argv[1], "gpu") == 0;
+  std::vector<double> b = {0.0, 0.5, 2.0, 8.0, 40.0};
+  helfem_gb300::AtomicTwoDBasis<Mat> atom(4, 9, 0, b, {0, 1}, {0, 0});
+  Mat S = atom.overlap();
+  double tr = 0.0;
+  for (long i = 0; i < S.rows(); ++i) tr += S(i, i);
+  std::printf("atomic nbf %zu trS %.15e\n", atom.Nbf(), tr);
+  std::vector<double> bd = {0.0, 0.8, 2.0, 4.7};
+  helfem_gb300::DiatomicTwoDBasis<Mat> mol(1, 1, 0.7, 9, bd, {0, 1, 1, 1}, {0, 0, 1, -1});
+  Mat Sd = mol.overlap();
+  double trd = 0.0;
+  for (long i = 0; i < Sd.rows(); ++i) trd += Sd(i, i);
+  std::printf("diatomic nbf %zu trS %.15e\n", mol.Nbf(), trd);
+  Mat P(atom.Nbf(), atom.Nbf());
+  for (long i = 0; i < P.rows(); ++i)
+    for (long j = 0; j < P.cols(); ++j) P(i, j) = 1e-2 / (1.0 + i + j);
+  if (!gpu) {
+    try {
+      atom.coulomb(P);
+      std::printf("no exception\n");
+      return 1;
+    } catch (const std::logic_error& e) {
+      std::printf("logic_error: %s", e.what());
+    }
+    return 0;
+  }
+  atom.compute_tei(true);
+  Mat J = atom.coulomb(P), K = atom.exchange(P);
+  std::printf("atomic trPJ %.15e trPK %.15e\n", trace_prod(P, J), trace_prod(P, K));
+  mol.compute_tei(true);
+  Mat Pd(mol.Nbf(), mol.Nbf());
+  for (long i = 0; i < Pd.rows(); ++i)
+    for (long j = 0; j < Pd.cols(); ++j) Pd(i, j) = 1e-3 / (1.0 + i + j);
+  Mat Jd = mol.coulomb(Pd), Kd = mol.exchange(Pd);
+  std::printf("diatomic trPJ %.15e trPK %.15e\n", trace_prod(Pd, Jd), trace_prod(Pd, Kd));
+  try {
+    mol.coulomb(Mat(3, 3));
+  } catch (const std::runtime_error& e) {
+    std::printf("runtime_error: %s\n", e.what());
+  }
+  return 0;
+}
