@@ -32,7 +32,9 @@ struct DevAtom {
   const int* kent_L;
   const int* kent_ptr;  // [nent+1] -> terms
   const int* kterm_blk;
+  const int* kterm_off;  // density offset of the term's block: l*nrad*nbf + i*nrad
   const double* kterm_coef;
+  int nent;
   int max_terms_per_jk; // bound on terms of one output block
   // split-precision copies: every FP64 value v stored as float2 (hi, lo) with
   // hi = fl32(v), lo = fl32(v - hi)
@@ -48,6 +50,8 @@ struct DevScratch {
   double* jscal;        // [nchan*nel*2]
   double* khalo;        // [nel*nel*nang*nang*(2nn-1)]
   double* bnorm;        // [nang*nang*NORM_SPLIT] partial squared block norms
+  unsigned char* act;   // [nang*nang] density block above the screen
+  unsigned char* ent_act;  // [nent] exchange entry with an active term
   float2* p2;           // [nbf*nbf] split copy of the density (split path)
 };
 

@@ -23,6 +23,7 @@
 //   k_fixup       : adds the contributions of neighbouring tiles on the
 //                   shared boundary functions, in a fixed order (no atomics,
 //                   bitwise reproducible).
+#include <algorithm>
 #include <cfloat>
 
 #include "devatom.cuh"
@@ -207,13 +208,32 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   if (threadIdx.x == 0) part[blk * NORM_SPLIT + blockIdx.y] = s;
 }
 
-__device__ __forceinline__ void load_active(const DevAtom& A, const DevScratch& S, unsigned char* act) {
+// density-block screen (10*DBL_EPSILON, the reference's threshold) and the
+// exchange entries that see an active block, once per build
+__global__ void k_flags(DevAtom A, DevScratch S) {
   const int nang2 = A.nang * A.nang;
-  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  for (int idx = tid; idx < nang2; idx += nth) {
     double s = 0.0;
     for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[idx * NORM_SPLIT + c];
-    act[idx] = !(sqrt(s) < 10.0 * DBL_EPSILON);
+    S.act[idx] = !(sqrt(s) < 10.0 * DBL_EPSILON);
   }
+  // every thread recomputes the block flags its entries need (no grid sync)
+  for (int ent = tid; ent < A.nent; ent += nth) {
+    bool any = false;
+    for (int u = A.kent_ptr[ent]; u < A.kent_ptr[ent + 1] && !any; ++u) {
+      const int blk = A.kterm_blk[u];
+      double s = 0.0;
+      for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[blk * NORM_SPLIT + c];
+      any = !(sqrt(s) < 10.0 * DBL_EPSILON);
+    }
+    S.ent_act[ent] = any ? 1 : 0;
+  }
+}
+
+__device__ __forceinline__ void load_active(const DevAtom& A, const DevScratch& S, unsigned char* act) {
+  const int nang2 = A.nang * A.nang;
+  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.act[idx];
 }
 
 __device__ __forceinline__ size_t halo_idx(const DevAtom& A, int a, int b, int jk, int h) {
@@ -238,23 +258,16 @@ __device__ __forceinline__ void k_store(const DevAtom& A, const DevScratch& S, d
 }
 
 // recoupled tile value for thread (p,q) of element pair (a,b), entry ent
-__device__ __forceinline__ double k_recouple(const DevAtom& A, const double* __restrict__ P,
-                                             const unsigned char* act, int ent, int gp, int gq) {
+// P_base = P + gq*nbf + gp for this thread's tile entry
+__device__ __forceinline__ double k_recouple(const DevAtom& A, const double* __restrict__ Pbase,
+                                             const unsigned char* act, int ent) {
   double x = 0.0;
   const int u0 = A.kent_ptr[ent], u1 = A.kent_ptr[ent + 1];
   for (int u = u0; u < u1; ++u) {
-    const int blk = A.kterm_blk[u];
-    if (!act[blk]) continue;
-    const int i = blk % A.nang, l = blk / A.nang;
-    x += A.kterm_coef[u] * P[(size_t)(l * A.nrad + gq) * A.nbf + (size_t)i * A.nrad + gp];
+    if (!act[A.kterm_blk[u]]) continue;
+    x += A.kterm_coef[u] * Pbase[A.kterm_off[u]];
   }
   return x;
-}
-
-__device__ __forceinline__ bool k_entry_active(const DevAtom& A, const unsigned char* act, int ent) {
-  for (int u = A.kent_ptr[ent]; u < A.kent_ptr[ent + 1]; ++u)
-    if (act[A.kterm_blk[u]]) return true;
-  return false;
 }
 
 // One work unit = one element pair (a,b) and a range of output angular
@@ -295,10 +308,11 @@ __global__ void __launch_bounds__(320) k_tiles(DevAtom A, DevScratch S, const in
   for (int w = u.z; w < u.w; ++w) {
     const int jk = diag ? diag_jk[w] : w;
     double y = 0.0;
+    const double* Pbase = P + (size_t)gq * A.nbf + gp;
     for (int ent = A.kjk_ptr[jk]; ent < A.kjk_ptr[jk + 1]; ++ent) {
-      if (!k_entry_active(A, act, ent)) continue;  // uniform over the CTA
+      if (!S.ent_act[ent]) continue;  // uniform over the CTA
       const int L = A.kent_L[ent];
-      if (live) X[t] = vpq ? k_recouple(A, P, act, ent, gp, gq) : 0.0;
+      if (live) X[t] = vpq ? k_recouple(A, Pbase, act, ent) : 0.0;
       __syncthreads();
       if (diag) {
         if (live) {
@@ -380,25 +394,36 @@ __device__ __forceinline__ float2 ff2(ffv v) {
 }
 __device__ __forceinline__ double ff_to_d(ffv v) { return (double)v.hi + (double)v.lo; }
 
-__device__ __forceinline__ ffv k_recouple_ff(const DevAtom& A, const DevScratch& S, const unsigned char* act,
-                                             int ent, int gp, int gq) {
+// p2base = S.p2 + gq*nbf + gp for this thread's tile entry
+__device__ __forceinline__ ffv k_recouple_ff(const DevAtom& A, const float2* __restrict__ p2base,
+                                             const unsigned char* act, int ent) {
   ffv x = {0.f, 0.f};
   const int u0 = A.kent_ptr[ent], u1 = A.kent_ptr[ent + 1];
   for (int u = u0; u < u1; ++u) {
-    const int blk = A.kterm_blk[u];
-    if (!act[blk]) continue;
-    const int i = blk % A.nang, l = blk / A.nang;
-    x = ff_fma(x, A.kterm_coef2[u], S.p2[(size_t)(l * A.nrad + gq) * A.nbf + (size_t)i * A.nrad + gp]);
+    if (!act[A.kterm_blk[u]]) continue;
+    x = ff_fma(x, A.kterm_coef2[u], p2base[A.kterm_off[u]]);
   }
   return x;
 }
 
+// (hi, lo) + (hi, lo), renormalised: accumulates the per-multipole results
+// of one output block before the single FP64 recombination
+__device__ __forceinline__ ffv ff_add(ffv a, ffv b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return ff_norm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+
+// NN > 0: element order fixed at compile time (the element-pair contractions
+// unroll with immediate shared-memory offsets); NN = 0: any order
+template <int NN>
 __global__ void __launch_bounds__(320) k_tiles_split(DevAtom A, DevScratch S, const int4* __restrict__ units,
                                                      const int* __restrict__ diag_jk, int symmetric,
                                                      double* __restrict__ K) {
   const int4 u = units[blockIdx.x];
   const int a = u.x, b = u.y;
-  const int nn = A.nn, n2 = nn * nn, NL = A.NL;
+  const int nn = NN > 0 ? NN : A.nn, n2 = nn * nn, NL = A.NL;
   extern __shared__ float2 sm2[];
   float2* X = sm2;
   float2* T = X + n2;
@@ -423,36 +448,58 @@ __global__ void __launch_bounds__(320) k_tiles_split(DevAtom A, DevScratch S, co
   const int p = live ? t % nn : 0, q = live ? t / nn : 0;
   const int gp = gfun(A, a, p), gq = gfun(A, b, q);
   const bool vpq = live && gvalid(A, gp) && gvalid(A, gq);
+  const float2* p2base = S.p2 + (size_t)gq * A.nbf + gp;
   for (int w = u.z; w < u.w; ++w) {
     const int jk = diag ? diag_jk[w] : w;
-    double y = 0.0;
+    ffv yacc = {0.f, 0.f};
     for (int ent = A.kjk_ptr[jk]; ent < A.kjk_ptr[jk + 1]; ++ent) {
-      if (!k_entry_active(A, act, ent)) continue;
+      if (!S.ent_act[ent]) continue;  // uniform over the CTA
       const int L = A.kent_L[ent];
-      if (live) X[t] = vpq ? ff2(k_recouple_ff(A, S, act, ent, gp, gq)) : make_float2(0.f, 0.f);
+      if (live) X[t] = vpq ? ff2(k_recouple_ff(A, p2base, act, ent)) : make_float2(0.f, 0.f);
       __syncthreads();
       ffv acc = {0.f, 0.f};
       if (diag) {
         if (live) {
+          // lazy low-word accumulation, renormalised every nn terms
           const float2* Tk = A.tk2 + ((size_t)L * A.nel + a) * n2 * n2;
-          for (int v = 0; v < n2; ++v) acc = ff_fma_n(acc, Tk[t + (size_t)v * n2], X[v]);
+          for (int v0 = 0; v0 < n2; v0 += nn) {
+#pragma unroll
+            for (int c = 0; c < (NN > 0 ? NN : 1); ++c) {
+              if (NN == 0) break;
+              acc = ff_fma(acc, Tk[t + (size_t)(v0 + c) * n2], X[v0 + c]);
+            }
+            if (NN == 0)
+              for (int v = v0; v < v0 + nn; ++v) acc = ff_fma(acc, Tk[t + (size_t)v * n2], X[v]);
+            acc = ff_norm(acc.hi, acc.lo);
+          }
         }
       } else {
         if (live) {
           const float2* Bl = Bm + L * n2;
           ffv s = {0.f, 0.f};
-          for (int c = 0; c < nn; ++c) s = ff_fma(s, X[p + c * nn], Bl[q + c * nn]);
+          if (NN > 0) {
+#pragma unroll
+            for (int c = 0; c < (NN > 0 ? NN : 1); ++c) s = ff_fma(s, X[p + c * nn], Bl[q + c * nn]);
+          } else {
+            for (int c = 0; c < nn; ++c) s = ff_fma(s, X[p + c * nn], Bl[q + c * nn]);
+          }
           T[t] = ff2(s);
         }
         __syncthreads();
         if (live) {
           const float2* Al = Am + L * n2;
-          for (int c = 0; c < nn; ++c) acc = ff_fma(acc, Al[p + c * nn], T[c + q * nn]);
+          if (NN > 0) {
+#pragma unroll
+            for (int c = 0; c < (NN > 0 ? NN : 1); ++c) acc = ff_fma(acc, Al[p + c * nn], T[c + q * nn]);
+          } else {
+            for (int c = 0; c < nn; ++c) acc = ff_fma(acc, Al[p + c * nn], T[c + q * nn]);
+          }
         }
       }
-      y += ff_to_d(acc);  // FP64 recombination, once per output and multipole
+      yacc = ff_add(yacc, ff_norm(acc.hi, acc.lo));
       __syncthreads();
     }
+    const double y = ff_to_d(yacc);  // FP64 recombination, once per output element
     if (live) k_store(A, S, K, a, b, jk, p, q, -y);
     const int j = jk % A.nang, k = jk / A.nang;
     if (symmetric && (!diag || j != k)) {
@@ -538,6 +585,7 @@ cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KU
   {
     Mark m(prof, KC_K_NORMS, st);
     k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, nullptr);
+    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S);
   }
   {
     Mark m(prof, KC_K_TILES, st);
@@ -559,12 +607,14 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
   {
     Mark m(prof, KC_K_NORMS, st);
     k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2);
+    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S);
   }
   {
     Mark m(prof, KC_K_TILES, st);
     const size_t smem = sizeof(float2) * (2 * n2 + 2 * A.NL * n2) + sizeof(double) * n2 + nang2;
     const int nunits = symmetric ? U.n_sym : U.n_all;
-    k_tiles_split<<<nunits, th, smem, st>>>(A, S, symmetric ? U.sym : U.all, U.diag_jk_src(symmetric),
+    auto kern = (A.nn == 15) ? k_tiles_split<15> : k_tiles_split<0>;
+    kern<<<nunits, th, smem, st>>>(A, S, symmetric ? U.sym : U.all, U.diag_jk_src(symmetric),
                                             symmetric ? 1 : 0, K);
   }
   {

@@ -152,8 +152,8 @@ struct hfg_atom {
   hfg::DevScratch scr{};
   // device copies of the tables
   DBuf d_rs, d_rb, d_cholp, d_rank, d_tk, d_chanL, d_jket_ptr, d_jket_blk, d_jket_coef, d_jbra_ptr,
-      d_jbra_chan, d_jbra_coef, d_kjk_ptr, d_kent_L, d_kent_ptr, d_kterm_blk, d_kterm_coef;
-  DBuf s_jin, s_jscal, s_khalo, s_bnorm, s_p2;
+      d_jbra_chan, d_jbra_coef, d_kjk_ptr, d_kent_L, d_kent_ptr, d_kterm_blk, d_kterm_off, d_kterm_coef;
+  DBuf s_jin, s_jscal, s_khalo, s_bnorm, s_p2, s_act, s_entact;
   DBuf d_rs2, d_rb2, d_tk2, d_kcoef2;
   DBuf d_units_all, d_units_sym, d_diag_all, d_diag_sym;
   hfg::KUnits units;
@@ -246,6 +246,16 @@ struct hfg_atom {
     A.kent_L = d_kent_L.upload(H.kent_L);
     A.kent_ptr = d_kent_ptr.upload(H.kent_ptr);
     A.kterm_blk = d_kterm_blk.upload(H.kterm_blk);
+    {
+      need((double)H.nbf * H.nbf < 2147483647.0, "basis too large for 32-bit density offsets");
+      std::vector<int> off(H.kterm_blk.size());
+      for (size_t u = 0; u < off.size(); ++u) {
+        const int blk = H.kterm_blk[u], i = blk % H.nang, l = blk / H.nang;
+        off[u] = l * H.rad.nrad * H.nbf + i * H.rad.nrad;
+      }
+      A.kterm_off = d_kterm_off.upload(off);
+    }
+    A.nent = (int)H.kent_L.size();
     A.kterm_coef = d_kterm_coef.upload(H.kterm_coef);
     int mx = 0;
     for (int jk = 0; jk < H.nang * H.nang; ++jk) {
@@ -261,10 +271,14 @@ struct hfg_atom {
     s_jscal.alloc(sizeof(double) * A.nchan * A.nel * 2);
     s_khalo.alloc(sizeof(double) * (size_t)A.nel * A.nel * A.nang * A.nang * (2 * A.nn - 1));
     s_bnorm.alloc(sizeof(double) * (size_t)A.nang * A.nang * NORM_SPLIT);
+    s_act.alloc((size_t)A.nang * A.nang);
+    s_entact.alloc(std::max<size_t>(1, (size_t)A.nent));
     scr.jin = s_jin.as<double>();
     scr.jscal = s_jscal.as<double>();
     scr.khalo = s_khalo.as<double>();
     scr.bnorm = s_bnorm.as<double>();
+    scr.act = s_act.as<unsigned char>();
+    scr.ent_act = s_entact.as<unsigned char>();
     scr.p2 = nullptr;  // allocated on the first split-precision call
     ck(cudaEventCreateWithFlags(&last_use, cudaEventDisableTiming), "cudaEventCreate");
     auto split = [](const std::vector<double>& v) {
