@@ -632,18 +632,39 @@ def run_n2(args):
     Jd, Kd = torch.empty_like(Pd), torch.empty_like(Pd)
     stream = torch.cuda.current_stream()
     evs = []
+    split = not args.plain
 
-    def step(timed=False):
+    def step(timed=False, split_k=split):
         if timed:
             e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
             e[0].record(stream)
         d.coulomb(Pd, Jd, stream=stream)
         if timed:
             e[1].record(stream)
-        d.exchange(Pa, Kd, symmetric=True, stream=stream)
+        d.exchange(Pa, Kd, symmetric=True, stream=stream, split=split_k)
         if timed:
             e[2].record(stream)
             evs.append(e)
+
+    # plain FP64 beside the split form: its K time and the split error
+    plain = None
+    if split:
+        step(split_k=False)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        d.exchange(Pa, Kd, symmetric=True, stream=stream)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        K64 = Kd.clone()
+        d.exchange(Pa, Kd, symmetric=True, stream=stream, split=True)
+        torch.cuda.synchronize()
+        dK = Kd - K64
+        plain = {"exchange_ms": p0.elapsed_time(p1),
+                 "split_error_vs_fp64": {"k_max_rel": float(dK.abs().max() / K64.abs().max()),
+                                         "exchange_energy_abs_eh": abs(float((Pa * dK).sum())),
+                                         "exchange_energy_eh": float((Pa * K64).sum())}}
+        del K64, dK
 
     for _ in range(args.warmup):
         step()
@@ -670,15 +691,17 @@ def run_n2(args):
     value = ws * args.steps / (ms * 1e-3)
     Ecoul = 0.5 * float((Pd * Jd).sum())
     Exx = 0.5 * float((Pa * Kd).sum()) * 2.0
-    # end to end through the host-pointer drop-ins
-    Jh = np.empty((nbf, nbf), order="F")
-    Kh = np.empty((nbf, nbf), order="F")
-    Pah = np.asfortranarray(0.5 * P)
+    # end to end through the host-pointer drop-ins (pinned host buffers)
+    def pinned():
+        return torch.empty((nbf, nbf), dtype=torch.float64, pin_memory=True).numpy().T
+    Ph, Pah, Jh, Kh = pinned(), pinned(), pinned(), pinned()
+    Ph[...] = P
+    Pah[...] = 0.5 * P
     ne = max(1, min(args.e2e_steps, 2))
     t0 = time.perf_counter()
     for _ in range(ne):
-        d.coulomb_host(P, out=Jh)
-        d.exchange_host(Pah, out=Kh, symmetric=True)
+        d.coulomb_host(Ph, out=Jh)
+        d.exchange_host(Pah, out=Kh, symmetric=True, split=split)
     te = time.perf_counter() - t0
     if rank != 0:
         if dist is not None:
@@ -700,17 +723,28 @@ def run_n2(args):
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": N2_WORKLOAD, "nbf": nbf, "ndummy": d.ndummy, "parallelism": f"replicas x{ws}",
                    "inputs_vs_l2": "P is 8.8 GB > 129 MB L2: no flush needed"},
-        "form": "plain FP64, symmetric exchange mode",
+        "form": ("split precision (FP32-pair contraction, FP64 recombination)" if split else "plain FP64")
+                + ", symmetric exchange mode",
         "kernel_ms": {"coulomb": j_ms, "exchange": k_ms},
+        "plain_fp64": plain,
         "energies_eh": {"coulomb": Ecoul, "exchange": Exx},
-        "roofline": {"bound": "fp64", "kernel": "dk_tiles (whole exchange call)", "achieved": achieved,
-                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "flops_per_launch": kflops, "ms_per_launch": k_ms,
-                     "peak_source": "measured in this run: cuBLAS DGEMM 4096^3", "traffic": None},
+        "roofline": ({"bound": "fp32", "kernel": "dk_tiles_split (whole exchange call)",
+                      "achieved": achieved * 12.0, "peak": fp32_peak_tflops(torch), "unit": "TFLOP/s",
+                      "frac": achieved * 12.0 / fp32_peak_tflops(torch),
+                      "achieved_fp64_equivalent_tflops": achieved, "fp64_peak_tflops": peak,
+                      "achieved_note": "FP32 rate = FP64-equivalent algorithmic FLOP rate x 12 FP32 instructions "
+                                       "per emulated multiply-add",
+                      "flops_per_launch": kflops, "ms_per_launch": k_ms,
+                      "peak_source": "measured in this run: cuBLAS SGEMM 8192^3 with TF32 off", "traffic": None}
+                     if split else
+                     {"bound": "fp64", "kernel": "dk_tiles (whole exchange call)", "achieved": achieved,
+                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                      "flops_per_launch": kflops, "ms_per_launch": k_ms,
+                      "peak_source": "measured in this run: cuBLAS DGEMM 4096^3", "traffic": None}),
         "cpu_baseline": cpu,
         "e2e": {"value": ws * ne / te, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nbf * nbf,
                 "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
-                "path": "hfg_diatomic_coulomb_host + hfg_diatomic_exchange_host (pageable host P, J, K)"},
+                "path": "hfg_diatomic_coulomb_host + hfg_diatomic_exchange_host (pinned host P, J, K)"},
         "clocks": clk.summary(),
         "gpu_launches": args.steps * 12,  # J: expand, contract, scatter, gather; K: expand, norms, act,
                                            # entry_act, compact, tiles, fixup, gather

@@ -585,9 +585,9 @@ class Diatomic:
     def coulomb(self, P, J, stream=None):
         _check(_lib.hfg_diatomic_coulomb(self._h, _ptr(P), _ptr(J), _stream(stream)))
 
-    def exchange(self, P, K, symmetric: bool = False, stream=None):
-        _check(_lib.hfg_diatomic_exchange(self._h, _ptr(P), _ptr(K), EXCHANGE_SYMMETRIC if symmetric else 0,
-                                          _stream(stream)))
+    def exchange(self, P, K, symmetric: bool = False, stream=None, split: bool = False):
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        _check(_lib.hfg_diatomic_exchange(self._h, _ptr(P), _ptr(K), flags, _stream(stream)))
 
     # ---- hot path: host arrays (drop-in value semantics) ----
     def coulomb_host(self, P: np.ndarray, out: np.ndarray = None) -> np.ndarray:
@@ -596,11 +596,12 @@ class Diatomic:
         _check(_lib.hfg_diatomic_coulomb_host(self._h, _dptr(P), _dptr(J)))
         return J
 
-    def exchange_host(self, P: np.ndarray, out: np.ndarray = None, symmetric: bool = False) -> np.ndarray:
+    def exchange_host(self, P: np.ndarray, out: np.ndarray = None, symmetric: bool = False,
+                      split: bool = False) -> np.ndarray:
         P = np.asfortranarray(P, dtype=np.float64)
         K = np.zeros_like(P, order="F") if out is None else out
-        _check(_lib.hfg_diatomic_exchange_host(self._h, _dptr(P), _dptr(K),
-                                               EXCHANGE_SYMMETRIC if symmetric else 0))
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        _check(_lib.hfg_diatomic_exchange_host(self._h, _dptr(P), _dptr(K), flags))
         return K
 
     def work(self, act: np.ndarray = None, jk_mask: np.ndarray = None) -> dict:

@@ -48,6 +48,20 @@ struct DevDiatomic {
   int npairs_all;
   const int2* pairs_sym;
   int npairs_sym;
+  // split-precision copies: each FP64 value v as float2 (hi, lo), hi = fl32(v)
+  const float2* p0s = nullptr;
+  const float2* p2s = nullptr;
+  const float2* q0s = nullptr;
+  const float2* q2s = nullptr;
+  const float2* txs = nullptr;
+  const float2* al_c0s = nullptr;
+  const float2* al_c2s = nullptr;
+  const float2* lmfacs = nullptr;
+  // P_L^|M| grows as e^{L mu} and Q_L^|M| decays as e^{-(L+1) mu}: beyond the
+  // FP32 range at large L and mu. The split tables hold P * 2^-k and
+  // Q * 2^+k with k = kexp[ilm*nel+e] (the exponent of the element's largest
+  // P entry); an element pair (inner a, outer b) restores 2^(k_a - k_b) <= 1.
+  const int* kexp = nullptr;
 };
 
 struct DevDiatomicScratch {
@@ -60,6 +74,7 @@ struct DevDiatomicScratch {
   unsigned char* jk_act;  // [nang^2]
   int* jk_list;           // [2*nang^2]: active output blocks, then those with j <= k
   int* counts;            // [2]
+  float2* pd2;            // [nd*nd] split copy of the density (split path)
 };
 
 #define DNORM_SPLIT 8
@@ -71,5 +86,10 @@ cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScrat
                                     cudaStream_t st);
 cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
                                      double* Kd, bool symmetric, cudaStream_t st);
+// split-precision exchange (float-float on the FP32 pipe, FP64 recombination)
+cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
+                                           double* Kd, bool symmetric, cudaStream_t st);
+// txs[i] = split(tx[i])
+cudaError_t launch_diatomic_split_tx(const double* tx, float2* txs, size_t n, cudaStream_t st);
 
 }  // namespace hfg

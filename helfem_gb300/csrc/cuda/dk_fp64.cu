@@ -30,6 +30,7 @@
 #include <cfloat>
 
 #include "devdiatomic.cuh"
+#include "ff.cuh"
 
 namespace hfg {
 namespace {
@@ -224,7 +225,8 @@ __global__ void dj_scatter(DevDiatomic D, DevDiatomicScratch S, double* __restri
 }
 
 // ----------------------------------------------------------------- exchange
-__global__ void dk_norms(DevDiatomic D, const double* __restrict__ Pd, double* __restrict__ part) {
+__global__ void dk_norms(DevDiatomic D, const double* __restrict__ Pd, double* __restrict__ part,
+                         float2* __restrict__ pd2) {
   __shared__ double red[32];
   const int blk = blockIdx.x, i = blk % D.nang, l = blk / D.nang;
   const int c0 = (int)((long)D.nrad * blockIdx.y / DNORM_SPLIT);
@@ -233,8 +235,10 @@ __global__ void dk_norms(DevDiatomic D, const double* __restrict__ Pd, double* _
   const size_t n = (size_t)D.nrad * (c1 - c0);
   for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
     const size_t r = idx % D.nrad, c = c0 + idx / D.nrad;
-    const double v = Pd[(size_t)(l * D.nrad + c) * D.nd + (size_t)i * D.nrad + r];
+    const size_t o = (size_t)(l * D.nrad + c) * D.nd + (size_t)i * D.nrad + r;
+    const double v = Pd[o];
     s += v * v;
+    if (pd2) pd2[o] = split_bits(v);
   }
   s = dblock_sum(s, red);
   if (threadIdx.x == 0) part[blk * DNORM_SPLIT + blockIdx.y] = s;
@@ -452,6 +456,156 @@ __global__ void __launch_bounds__(320) dk_tiles(DevDiatomic D, DevDiatomicScratc
   }
 }
 
+// Split-precision tiles: dk_tiles with every operand a (hi, lo) float pair,
+// TwoProd/TwoSum products on the FP32 pipe, the per-multipole results summed
+// as float pairs and recombined in FP64 once per output element.
+template <int NN>
+__global__ void __launch_bounds__(320) dk_tiles_split(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd,
+                                                      int symmetric) {
+  const int nn = NN > 0 ? NN : D.nn, n2 = nn * nn, nang2 = D.nang * D.nang;
+  const int n_act = S.counts[0], n_dact = symmetric ? S.counts[1] : S.counts[0];
+  const int* dlist = symmetric ? S.jk_list + nang2 : S.jk_list;
+  const int2* pairs = symmetric ? D.pairs_sym : D.pairs_all;
+  const long npairs = symmetric ? D.npairs_sym : D.npairs_all;
+  const long n_off = npairs * n_act, total = n_off + (long)D.nel * n_dact;
+  extern __shared__ float2 sm2[];
+  float2* X = sm2;           // [4*n2]
+  float2* T = X + 4 * n2;    // [2*n2]
+  float2* Im = T + 2 * n2;   // [2*n2]
+  float2* Jm = Im + 2 * n2;  // [2*n2]
+  double* Y = reinterpret_cast<double*>(Jm + 2 * n2);
+  unsigned char* act = reinterpret_cast<unsigned char*>(Y + n2);
+  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.act[idx];
+  __syncthreads();
+  const int t = threadIdx.x;
+  const bool live = t < n2;
+  const int p = live ? t % nn : 0, q = live ? t / nn : 0;
+  for (long w = blockIdx.x; w < total; w += gridDim.x) {
+    int a, b, jk;
+    if (w < n_off) {
+      const int2 pr = pairs[w / n_act];
+      a = pr.x;
+      b = pr.y;
+      jk = S.jk_list[w % n_act];
+    } else {
+      const long w2 = w - n_off;
+      a = b = (int)(w2 / n_dact);
+      jk = dlist[w2 % n_dact];
+    }
+    const bool diag = (a == b);
+    const int j = jk % D.nang, k = jk / D.nang;
+    const int gp = dgf(D, a, p), gq = dgf(D, b, q);
+    const bool vpq = live && gp < D.nrad && gq < D.nrad;
+    const float2* pbase = S.pd2 + (size_t)gq * D.nd + gp;
+    ffv yacc = {0.f, 0.f};
+    for (int ent = D.kjk_ptr[jk]; ent < D.kjk_ptr[jk + 1]; ++ent) {
+      if (!S.ent_act[ent]) continue;  // uniform over the CTA
+      const int L = D.kent_L[ent], Ma = D.kent_Ma[ent], ilm = D.kent_ilm[ent];
+      ffv x00 = {0.f, 0.f}, x02 = {0.f, 0.f}, x20 = {0.f, 0.f}, x22 = {0.f, 0.f};
+      if (vpq) {
+        for (int sgn = 0; sgn < (Ma ? 2 : 1); ++sgn) {
+          const int M = sgn ? -Ma : Ma;
+          const int xj = al_idx(D, j, L, M), xk = al_idx(D, k, L, M);
+          const int k0 = D.al_ptr[xk], k1 = D.al_ptr[xk + 1];
+          for (int uj = D.al_ptr[xj]; uj < D.al_ptr[xj + 1]; ++uj) {
+            const int i = D.al_b[uj];
+            ffv u0 = {0.f, 0.f}, u2 = {0.f, 0.f};
+            for (int uk = k0; uk < k1; ++uk) {
+              const int l = D.al_b[uk];
+              if (!act[i + l * D.nang]) continue;
+              const float2 v = pbase[(size_t)(l * D.nrad) * D.nd + (size_t)i * D.nrad];
+              u0 = ff_fma(u0, D.al_c0s[uk], v);
+              u2 = ff_fma(u2, D.al_c2s[uk], v);
+            }
+            const float2 U0 = ff2(u0), U2 = ff2(u2), c0 = D.al_c0s[uj], c2 = D.al_c2s[uj];
+            x00 = ff_fma(x00, c0, U0);
+            x02 = ff_fma(x02, c0, U2);
+            x20 = ff_fma(x20, c2, U0);
+            x22 = ff_fma(x22, c2, U2);
+          }
+        }
+      }
+      if (live) {
+        float2 fac = D.lmfacs[ilm];
+        if (Ma & 1) fac = make_float2(-fac.x, -fac.y);
+        const ffv z = {0.f, 0.f};
+        const float2 f00 = ff2(ff_fma(z, fac, ff2(x00))), f02 = ff2(ff_fma(z, fac, ff2(x02)));
+        const float2 f20 = ff2(ff_fma(z, fac, ff2(x20))), f22 = ff2(ff_fma(z, fac, ff2(x22)));
+        X[t] = f00;
+        X[n2 + t] = make_float2(-f02.x, -f02.y);
+        X[2 * n2 + t] = make_float2(-f20.x, -f20.y);
+        X[3 * n2 + t] = f22;
+        if (!diag) {
+          const size_t la = ((size_t)ilm * D.nel + a) * n2 + t, lb = ((size_t)ilm * D.nel + b) * n2 + t;
+          Im[t] = (a < b) ? D.p0s[la] : D.q0s[la];
+          Im[n2 + t] = (a < b) ? D.p2s[la] : D.q2s[la];
+          Jm[t] = (a < b) ? D.q0s[lb] : D.p0s[lb];
+          Jm[n2 + t] = (a < b) ? D.q2s[lb] : D.p2s[lb];
+        }
+      }
+      __syncthreads();
+      ffv acc = {0.f, 0.f};
+      if (diag) {
+        if (live) {
+          const float2* tx = D.txs + ((size_t)ilm * D.nel + a) * 4 * n2 * n2;
+          for (int ab = 0; ab < 4; ++ab) {
+            const float2* txb = tx + (size_t)ab * n2 * n2;
+            const float2* Xb = X + ab * n2;
+            for (int v0 = 0; v0 < n2; v0 += nn) {
+              for (int v = v0; v < v0 + nn; ++v) acc = ff_fma(acc, txb[t + (size_t)v * n2], Xb[v]);
+              acc = ff_norm(acc.hi, acc.lo);
+            }
+          }
+        }
+      } else {
+        if (live) {
+          ffv s0 = {0.f, 0.f}, s2 = {0.f, 0.f};
+#pragma unroll
+          for (int c = 0; c < (NN > 0 ? NN : 17); ++c) {
+            if (NN == 0 && c >= nn) break;
+            const float2 j0 = Jm[q + c * nn], j2 = Jm[n2 + q + c * nn];
+            s0 = ff_fma(s0, X[p + c * nn], j0);
+            s0 = ff_fma(s0, X[n2 + p + c * nn], j2);
+            s2 = ff_fma(s2, X[2 * n2 + p + c * nn], j0);
+            s2 = ff_fma(s2, X[3 * n2 + p + c * nn], j2);
+          }
+          T[t] = ff2(s0);
+          T[n2 + t] = ff2(s2);
+        }
+        __syncthreads();
+        if (live) {
+#pragma unroll
+          for (int c = 0; c < (NN > 0 ? NN : 17); ++c) {
+            if (NN == 0 && c >= nn) break;
+            acc = ff_fma(acc, Im[p + c * nn], T[c + q * nn]);
+            acc = ff_fma(acc, Im[n2 + p + c * nn], T[n2 + c + q * nn]);
+          }
+          // undo the tables' power-of-two scaling: 2^(k_inner - k_outer) <= 1
+          const int ka = D.kexp[(size_t)ilm * D.nel + a], kb = D.kexp[(size_t)ilm * D.nel + b];
+          const int dk = (a < b) ? ka - kb : kb - ka;
+          acc.hi = ldexpf(acc.hi, dk);
+          acc.lo = ldexpf(acc.lo, dk);
+        }
+      }
+      yacc = ff_add(yacc, ff_norm(acc.hi, acc.lo));
+      __syncthreads();
+    }
+    const double y = ff_to_d(yacc);
+    if (live) dk_store(D, S, Kd, a, b, jk, p, q, -y);
+    if (symmetric && (!diag || j != k)) {
+      if (live) Y[t] = -y;
+      __syncthreads();
+      if (live) dk_store(D, S, Kd, b, a, k + j * D.nang, p, q, Y[q + p * nn]);
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void d_split(const double* __restrict__ x, float2* __restrict__ y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = split_bits(x[i]);
+}
+
 // Shared-boundary fix-up: entry (p,q) of tile (a,b) in its first row or
 // column also receives the last row of the tile above (a-1,b), the last
 // column of the tile to the left (a,b-1) and, at the corner, the last corner
@@ -459,12 +613,11 @@ __global__ void __launch_bounds__(320) dk_tiles(DevDiatomic D, DevDiatomicScratc
 // (mu = 0), so the first row of a = 0 tiles and the first column of b = 0
 // tiles are real entries too.
 __global__ void dk_fixup(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd) {
-  const int jk = blockIdx.y;
-  if (!S.jk_act[jk]) return;
   const int a = blockIdx.x % D.nel, b = blockIdx.x / D.nel;
-  const int nn = D.nn;
-  const int j = jk % D.nang, k = jk / D.nang;
-  for (int idx = threadIdx.x; idx < 2 * nn - 3; idx += blockDim.x) {
+  const int nn = D.nn, per = 2 * nn - 3, n_act = S.counts[0];
+  for (long w = threadIdx.x; w < (long)per * n_act; w += blockDim.x) {
+    const int idx = (int)(w % per), jk = S.jk_list[w / per];
+    const int j = jk % D.nang, k = jk / D.nang;
     const int p = idx < nn - 1 ? 0 : idx - (nn - 1) + 1;  // first row q in [0, nn-2], then first column
     const int q = idx < nn - 1 ? idx : 0;
     double v = 0.0;
@@ -523,7 +676,7 @@ cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScra
   const int n2 = D.nn * D.nn, th = dthreads(n2), nang2 = D.nang * D.nang;
   cudaError_t e = cudaMemsetAsync(Kd, 0, sizeof(double) * (size_t)D.nd * D.nd, st);
   if (e != cudaSuccess) return e;
-  dk_norms<<<dim3(nang2, DNORM_SPLIT), 256, 0, st>>>(D, Pd, S.bnorm);
+  dk_norms<<<dim3(nang2, DNORM_SPLIT), 256, 0, st>>>(D, Pd, S.bnorm, nullptr);
   dk_act<<<(nang2 + 255) / 256, 256, 0, st>>>(D, S);
   dk_entry_act<<<(D.nent + 127) / 128 > 0 ? (D.nent + 127) / 128 : 1, 128, 0, st>>>(D, S);
   dk_compact<<<1, 1024, 0, st>>>(D, S);
@@ -539,7 +692,37 @@ cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScra
   if (e != cudaSuccess) return e;
   const int grid = nsm * std::max(per, 1);
   dk_tiles<<<grid, th, smem, st>>>(D, S, Pd, Kd, symmetric ? 1 : 0);
-  dk_fixup<<<dim3(D.nel * D.nel, nang2), 64, 0, st>>>(D, S, Kd);
+  dk_fixup<<<D.nel * D.nel, 256, 0, st>>>(D, S, Kd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diatomic_split_tx(const double* tx, float2* txs, size_t n, cudaStream_t st) {
+  d_split<<<dgrid(n), 256, 0, st>>>(tx, txs, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
+                                           double* Kd, bool symmetric, cudaStream_t st) {
+  const int n2 = D.nn * D.nn, th = dthreads(n2), nang2 = D.nang * D.nang;
+  cudaError_t e = cudaMemsetAsync(Kd, 0, sizeof(double) * (size_t)D.nd * D.nd, st);
+  if (e != cudaSuccess) return e;
+  dk_norms<<<dim3(nang2, DNORM_SPLIT), 256, 0, st>>>(D, Pd, S.bnorm, S.pd2);
+  dk_act<<<(nang2 + 255) / 256, 256, 0, st>>>(D, S);
+  dk_entry_act<<<(D.nent + 127) / 128 > 0 ? (D.nent + 127) / 128 : 1, 128, 0, st>>>(D, S);
+  dk_compact<<<1, 1024, 0, st>>>(D, S);
+  int dev = 0, nsm = 152, per = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = sizeof(float2) * 10 * n2 + sizeof(double) * n2 + nang2;
+  auto kern = (D.nn == 15) ? dk_tiles_split<15> : dk_tiles_split<0>;
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, th, smem);
+  if (e != cudaSuccess) return e;
+  kern<<<nsm * std::max(per, 1), th, smem, st>>>(D, S, Kd, symmetric ? 1 : 0);
+  dk_fixup<<<D.nel * D.nel, 256, 0, st>>>(D, S, Kd);
   return cudaGetLastError();
 }
 

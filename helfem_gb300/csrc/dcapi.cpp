@@ -21,8 +21,10 @@ struct hfg_diatomic {
       d_chM, d_chilm, d_chfac, d_jbra_ptr, d_jbra_chan, d_jbra_c0, d_jbra_c2, d_kjk_ptr, d_kentL, d_kentMa,
       d_kentilm, d_kentjk, d_pairs_all, d_pairs_sym, d_pure;
   DBuf s_jin, s_jscal, s_khalo, s_bnorm, s_act, s_entact, s_jkact, s_jklist, s_counts, s_Pd, s_Fd;
+  DBuf d_p0s, d_p2s, d_q0s, d_q2s, d_txs, d_alc0s, d_alc2s, d_lmfacs, d_kexp, s_pd2;  // split-precision path
   DBuf h_in, h_out;
   cudaEvent_t last_use = nullptr;
+  std::vector<double> lmfac_host;
 
   ~hfg_diatomic() {
     if (last_use) {
@@ -73,6 +75,7 @@ struct hfg_diatomic {
       lmf[i] = 4.0 * M_PI * std::pow(H.Rhalf, 5) / fr;
     }
     D.lmfac = d_lmfac.upload(lmf);
+    lmfac_host = lmf;
     D.al_ptr = d_al_ptr.upload(H.al_ptr);
     D.al_b = d_al_b.upload(H.al_b);
     D.al_c0 = d_al_c0.upload(H.al_c0);
@@ -112,6 +115,7 @@ struct hfg_diatomic {
     const size_t n2 = (size_t)H.nn * H.nn, nang2 = (size_t)H.nang * H.nang, nd = (size_t)H.ndummy;
     d_tx.alloc(sizeof(double) * (size_t)H.nlm * H.nel * 4 * n2 * n2);
     D.tx = d_tx.as<double>();
+    scr.pd2 = nullptr;
     ck(hfg::launch_diatomic_tx(D, d_tx.as<double>(), own_stream), "in-element kernel build");
     s_jin.alloc(sizeof(double) * (size_t)D.nchan * H.nel * 2 * n2);
     s_jscal.alloc(sizeof(double) * (size_t)D.nchan * H.nel * 4);
@@ -138,12 +142,63 @@ struct hfg_diatomic {
     on_device = true;
   }
 
+  // split tables and the split density buffer, on the first split-precision call
+  void ensure_split() {
+    if (dev.txs) return;
+    hfg_abi::AllocStream alloc_on(own_stream);
+    auto split = [](const std::vector<double>& v) {
+      std::vector<float2> o(v.size());
+      for (size_t i = 0; i < v.size(); ++i) {
+        const float hi = (float)v[i];
+        o[i] = make_float2(hi, (float)(v[i] - (double)hi));
+      }
+      return o;
+    };
+    const hfg::DiatomicHost& H = host;
+    // per-(multipole, element) power-of-two rescaling into the FP32 range
+    const size_t n2 = (size_t)H.nn * H.nn, ntile = (size_t)H.nlm * H.nel;
+    std::vector<int> kexp(ntile, 0);
+    std::vector<double> p0(H.p0), p2(H.p2), q0(H.q0), q2(H.q2);
+    for (size_t t = 0; t < ntile; ++t) {
+      double mx = 0.0;
+      for (size_t i = 0; i < n2; ++i) mx = std::max(mx, std::max(std::fabs(H.p0[t * n2 + i]), std::fabs(H.p2[t * n2 + i])));
+      int e = 0;
+      if (mx > 0.0) std::frexp(mx, &e);
+      kexp[t] = e;
+      for (size_t i = 0; i < n2; ++i) {
+        p0[t * n2 + i] = std::ldexp(p0[t * n2 + i], -e);
+        p2[t * n2 + i] = std::ldexp(p2[t * n2 + i], -e);
+        q0[t * n2 + i] = std::ldexp(q0[t * n2 + i], e);
+        q2[t * n2 + i] = std::ldexp(q2[t * n2 + i], e);
+      }
+    }
+    dev.kexp = d_kexp.upload(kexp);
+    dev.p0s = d_p0s.upload(split(p0));
+    dev.p2s = d_p2s.upload(split(p2));
+    dev.q0s = d_q0s.upload(split(q0));
+    dev.q2s = d_q2s.upload(split(q2));
+    dev.al_c0s = d_alc0s.upload(split(H.al_c0));
+    dev.al_c2s = d_alc2s.upload(split(H.al_c2));
+    dev.lmfacs = d_lmfacs.upload(split(lmfac_host));
+    const size_t ntx = d_tx.n / sizeof(double);
+    d_txs.alloc(sizeof(float2) * ntx);
+    ck(hfg::launch_diatomic_split_tx(d_tx.as<double>(), d_txs.as<float2>(), ntx, own_stream), "split tables");
+    s_pd2.alloc(sizeof(float2) * (size_t)H.ndummy * H.ndummy);
+    scr.pd2 = s_pd2.as<float2>();
+    ck(cudaStreamSynchronize(own_stream), "sync after split tables");
+    dev.txs = d_txs.as<float2>();
+  }
+
   // J or K of a pure-basis density (device pointers) on stream st
-  void build(const double* P, double* F, bool exchange, bool symmetric, cudaStream_t st) {
+  void build(const double* P, double* F, bool exchange, bool symmetric, cudaStream_t st, bool split = false) {
     check_device();
     const hfg::DiatomicHost& H = host;
+    if (split) ensure_split();
     ck(hfg::launch_diatomic_expand(P, H.nbf, d_pure.as<int>(), s_Pd.as<double>(), H.ndummy, st), "expand");
-    if (exchange)
+    if (exchange && split)
+      ck(hfg::launch_diatomic_exchange_split(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st),
+         "exchange (split)");
+    else if (exchange)
       ck(hfg::launch_diatomic_exchange(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st), "exchange");
     else
       ck(hfg::launch_diatomic_coulomb(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), st), "coulomb");
@@ -151,14 +206,14 @@ struct hfg_diatomic {
     mark_use(st);
   }
 
-  void build_host(const double* P, double* F, bool exchange, bool symmetric) {
+  void build_host(const double* P, double* F, bool exchange, bool symmetric, bool split = false) {
     check_device();
     hfg_abi::AllocStream alloc_on(own_stream);
     const size_t bytes = sizeof(double) * (size_t)host.nbf * host.nbf;
     if (h_in.n != bytes) h_in.alloc(bytes);
     if (h_out.n != bytes) h_out.alloc(bytes);
     ck(cudaMemcpyAsync(h_in.p, P, bytes, cudaMemcpyHostToDevice, own_stream), "copy in");
-    build(h_in.as<double>(), h_out.as<double>(), exchange, symmetric, own_stream);
+    build(h_in.as<double>(), h_out.as<double>(), exchange, symmetric, own_stream, split);
     ck(cudaMemcpyAsync(F, h_out.p, bytes, cudaMemcpyDeviceToHost, own_stream), "copy out");
     ck(cudaStreamSynchronize(own_stream), "sync");
   }
@@ -291,8 +346,8 @@ hfg_status hfg_diatomic_coulomb(hfg_diatomic* d, const double* P, double* J, voi
 hfg_status hfg_diatomic_exchange(hfg_diatomic* d, const double* P, double* K, int flags, void* stream) {
   return guard([&] {
     need(d && P && K, "hfg_diatomic_exchange: null argument");
-    need((flags & ~HFG_EXCHANGE_SYMMETRIC) == 0, "hfg_diatomic_exchange: unsupported flags");
-    d->build(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0, to_stream(stream));
+    need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "hfg_diatomic_exchange: unsupported flags");
+    d->build(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0, to_stream(stream), (flags & HFG_EXCHANGE_SPLIT) != 0);
   });
 }
 
@@ -306,8 +361,9 @@ hfg_status hfg_diatomic_coulomb_host(hfg_diatomic* d, const double* P, double* J
 hfg_status hfg_diatomic_exchange_host(hfg_diatomic* d, const double* P, double* K, int flags) {
   return guard([&] {
     need(d && P && K, "hfg_diatomic_exchange_host: null argument");
-    need((flags & ~HFG_EXCHANGE_SYMMETRIC) == 0, "hfg_diatomic_exchange_host: unsupported flags");
-    d->build_host(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0);
+    need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0,
+         "hfg_diatomic_exchange_host: unsupported flags");
+    d->build_host(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0, (flags & HFG_EXCHANGE_SPLIT) != 0);
   });
 }
 

@@ -361,7 +361,9 @@ hfg_status hfg_gaunt_mod(int lj, int mj, int L, int M, int li, int mi, double* v
 hfg_status hfg_diatomic_coulomb(hfg_diatomic* d, const double* P, double* J, void* stream);
 /* K(P) for a spin density, with the reference's sign (added to F): replaces
  * diatomic TwoDBasis::exchange (basis.cpp:1817-2061), including its
- * density-block screening. flags: HFG_EXCHANGE_SYMMETRIC (P = P^T). */
+ * density-block screening. flags: HFG_EXCHANGE_SYMMETRIC (P = P^T),
+ * HFG_EXCHANGE_SPLIT (split precision as for atoms; the first split call
+ * allocates float-pair copies of the tables and an ndummy^2 density copy). */
 hfg_status hfg_diatomic_exchange(hfg_diatomic* d, const double* P, double* K, int flags, void* stream);
 /* host-pointer value-semantics variants */
 hfg_status hfg_diatomic_coulomb_host(hfg_diatomic* d, const double* P, double* J);

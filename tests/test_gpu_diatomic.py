@@ -18,6 +18,11 @@ from gpu_util import from_dev, relerr, to_dev, torch_cuda
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-10
+# split-precision exchange against the FP64 oracle: the four channel products
+# cancel (cosh^2 - cos^2 volume element), which amplifies the ~2^-47 relative
+# error of the float pairs; energy-weighted error bounded tighter
+SPLIT_TOL = 1e-11
+SPLIT_E_TOL = 1e-12
 
 CASES = [
     # Z1, Z2, Rbond, nelem, lmax per |m|
@@ -71,11 +76,21 @@ def test_diatomic_jk_match_oracle(case):
         Jd = torch.full_like(Pd, np.nan)
         Kd = torch.full_like(Pd, np.nan)
         Ks = torch.full_like(Pd, np.nan)
+        Kp = torch.full_like(Pd, np.nan)
+        Kq = torch.full_like(Pd, np.nan)
         d.coulomb(Pd, Jd)
         d.exchange(Pd, Kd)
         d.exchange(Pd, Ks, symmetric=True)
+        d.exchange(Pd, Kp, symmetric=True, split=True)
+        d.exchange(Pd, Kq, split=True)
         torch.cuda.synchronize()
         J, K, KS = from_dev(Jd), from_dev(Kd), from_dev(Ks)
+        KP, KQ = from_dev(Kp), from_dev(Kq)
+        # split precision: stated error bound against the FP64 oracle
+        for M in (KP, KQ):
+            assert np.isfinite(M).all()
+            assert relerr(M, Kr) < SPLIT_TOL, (blockdiag, relerr(M, Kr))
+            assert abs(np.sum(P * (M - Kr))) <= SPLIT_E_TOL * abs(np.sum(P * Kr))
         assert np.isfinite(J).all() and np.isfinite(K).all() and np.isfinite(KS).all()
         assert relerr(J, Jr) < TOL, (blockdiag, relerr(J, Jr))
         assert relerr(K, Kr) < TOL, (blockdiag, relerr(K, Kr))
@@ -157,3 +172,10 @@ def test_n2_full_size_properties():
     d.exchange(Pd, Kg)
     torch.cuda.synchronize()
     assert float((Kg - out["1"][1]).abs().max()) <= 1e-12 * float(Kg.abs().max())
+    # split precision at full size (P_L, Q_L beyond the FP32 range are rescaled)
+    Kp = torch.empty_like(Pd)
+    d.exchange(Pd, Kp, symmetric=True, split=True)
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(Kp).all())
+    assert float((Kp - Kg).abs().max()) <= SPLIT_TOL * float(Kg.abs().max())
+    assert abs(float((Pd * (Kp - Kg)).sum())) <= SPLIT_E_TOL * abs(float((Pd * Kg).sum()))
