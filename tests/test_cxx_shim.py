@@ -45,7 +45,7 @@ def numbers(out, prefix):
     """Values following 'name value' pairs on the line starting with prefix."""
     for line in out.splitlines():
         if line.startswith(prefix):
-            toks = line[len(prefix):].split()
+            toks = line.split()[1:]
             return {toks[i]: float(toks[i + 1]) for i in range(0, len(toks) - 1, 2)}
     raise AssertionError(f"{prefix} missing in {out}")
 
@@ -58,14 +58,14 @@ def test_shim_gpu(tmp_path):
     i, j = np.meshgrid(np.arange(a.nbf), np.arange(a.nbf), indexing="ij")
     P = 1e-2 / (1.0 + i + j)
     r = numbers(out, "atomic trPJ")
-    tj = float(out.split("atomic trPJ")[1].split()[0])
+    tj = r["trPJ"]
     assert abs(tj - np.sum(P * a.coulomb_host(P))) < 1e-12 * abs(tj)
     assert abs(r["trPK"] - np.sum(P * a.exchange_host(P))) < 1e-12 * abs(r["trPK"])
     d = hg.Diatomic(1, 1, 0.7, [0.0, 0.8, 2.0, 4.7], [0, 1, 1, 1], [0, 0, 1, -1], nnodes=9)
     i, j = np.meshgrid(np.arange(d.nbf), np.arange(d.nbf), indexing="ij")
     Pd = 1e-3 / (1.0 + i + j)
     rd = numbers(out, "diatomic trPJ")
-    tjd = float(out.split("diatomic trPJ")[1].split()[0])
+    tjd = rd["trPJ"]
     assert abs(tjd - np.sum(Pd * d.coulomb_host(Pd))) < 1e-12 * abs(tjd)
     assert abs(rd["trPK"] - np.sum(Pd * d.exchange_host(Pd))) < 1e-12 * abs(rd["trPK"])
     assert "runtime_error" in out
