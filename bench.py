@@ -530,8 +530,8 @@ N2_WORKLOAD = ("N2 diatomic J+K Fock build: R=2.074 bohr, 30 mu-elements to mu_m
                "Loewdin-orthonormal in the block overlap; K from the spin density P/2")
 
 
-def n2_setup(hg, host_only=False):
-    d = hg.Diatomic.from_grid(7, 7, 2.074, 30, [12, 12, 12, 12], host_only=host_only)
+def n2_setup(hg, host_only=False, nelem=30, lmax=12):
+    d = hg.Diatomic.from_grid(7, 7, 2.074, nelem, [lmax] * 4, host_only=host_only)
     idx = d.pure_indices()
     mv = d.mval[idx // d.nrad]
     rng = np.random.default_rng(12345)
@@ -641,7 +641,7 @@ def run_n2(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    d, P, act = n2_setup(hg)
+    d, P, act = n2_setup(hg, nelem=args.n2_elements, lmax=args.n2_lmax)
     nbf = d.nbf
     Pd = torch.from_numpy(P.ravel(order="F")).cuda()
     Pa = 0.5 * Pd
@@ -737,7 +737,8 @@ def run_n2(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": N2_WORKLOAD, "nbf": nbf, "ndummy": d.ndummy, "parallelism": f"replicas x{ws}",
+        "config": {"workload": N2_WORKLOAD if (args.n2_elements, args.n2_lmax) == (30, 12) else
+                   f"reduced N2 case: {args.n2_elements} mu-elements, l<={args.n2_lmax} (profiling)", "nbf": nbf, "ndummy": d.ndummy, "parallelism": f"replicas x{ws}",
                    "inputs_vs_l2": "P is 8.8 GB > 129 MB L2: no flush needed"},
         "form": ("split precision (FP32-pair contraction, FP64 recombination)" if split else "plain FP64")
                 + ", symmetric exchange mode",
@@ -786,6 +787,8 @@ def main():
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--n2-elements", type=int, default=30, help="N2 workload: mu-elements (30 = the benchmark)")
+    ap.add_argument("--n2-lmax", type=int, default=12, help="N2 workload: l_max for m = 0..3 (12 = the benchmark)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
