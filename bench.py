@@ -329,23 +329,22 @@ def run_ours(args):
         return torch.empty((nbf, nbf), dtype=torch.float64, pin_memory=True).numpy().T
     Ph, Jh, Kh = pinned(), pinned(), pinned()
     Ph[...] = P
-    atom.coulomb_host(Ph, out=Jh)
-    atom.exchange_host(Ph, out=Kh, symmetric=True, split=split)
+    atom.jk_host(Ph, J=Jh, K=Kh, symmetric=True, split=split)
     ne = args.e2e_steps
     if dist is not None:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(ne):
-        atom.coulomb_host(Ph, out=Jh)
-        atom.exchange_host(Ph, out=Kh, symmetric=True, split=split)
+        atom.jk_host(Ph, J=Jh, K=Kh, symmetric=True, split=split)
     te = max(time.perf_counter() - t0, 1e-30)
     if dist is not None:
         t = torch.tensor([te], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         te = float(t.item())
-    e2e = {"value": ws * ne / te if ne else None, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nbf * nbf,
+    e2e = {"value": ws * ne / te if ne else None, "unit": UNIT, "h2d_bytes_per_step": 8 * nbf * nbf,
            "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
-           "path": "hfg_coulomb_host + hfg_exchange_host_ex (pinned host P, J, K; same K form as value)"}
+           "path": "hfg_jk_host (pinned host P, J, K; one staging of P, J copied back while K builds; "
+                   "same K form as value)"}
 
     if rank != 0:
         if dist is not None:

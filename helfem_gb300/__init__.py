@@ -71,6 +71,7 @@ _SIGS = {
     "hfg_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host_ex": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
+    "hfg_jk_host": ([_P, _D, _D, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_atom_work": ([_P, _P], ctypes.c_int),
     "hfg_dft_grid": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
@@ -375,6 +376,18 @@ class Atom:
         else:
             _check(_lib.hfg_exchange_host(self._h, _dptr(P), _dptr(K)))
         return K
+
+    def jk_host(self, PJ: np.ndarray, PK: np.ndarray = None, J: np.ndarray = None, K: np.ndarray = None,
+                symmetric: bool = False, split: bool = False):
+        """J(PJ) and K(PK) (PK defaults to PJ: one staging of the density)."""
+        PJ = np.asfortranarray(PJ, dtype=np.float64)
+        PK = PJ if PK is None else np.asfortranarray(PK, dtype=np.float64)
+        J = np.zeros_like(PJ, order="F") if J is None else J
+        K = np.zeros_like(PJ, order="F") if K is None else K
+        assert J.flags.f_contiguous and K.flags.f_contiguous and J.shape == K.shape == PJ.shape
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        _check(_lib.hfg_jk_host(self._h, _dptr(PJ), _dptr(PK), _dptr(J), _dptr(K), flags))
+        return J, K
 
 
 def _scf_desc(nela, nelb, method="hf", restricted=True, symmetry=1, fixed=None, nblocks=0, e_tol=0.0,

@@ -272,6 +272,61 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
   ck(cudaStreamSynchronize(st), "stream sync");
 }
 
+// J(PJ) and K(PK) with one staging of the density when PK == PJ, the
+// exchange build running while J is copied back on a second stream
+static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, double* K, int flags) {
+  need(a && PJ && PK && J && K, "null argument");
+  need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "unknown flags");
+  a->check_device();
+  a->staging();
+  const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
+  cudaStream_t st = a->own_stream;
+  if (!a->copy_stream) ck(cudaStreamCreateWithFlags(&a->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (!a->ev_j) ck(cudaEventCreateWithFlags(&a->ev_j, cudaEventDisableTiming), "cudaEventCreate");
+  const bool same = (PK == PJ);
+  if (!same) {
+    hfg_abi::AllocStream alloc_on(st);
+    if (a->h_in2.n != bytes) a->h_in2.alloc(bytes);
+  }
+  {
+    hfg_abi::AllocStream alloc_on(st);
+    if (a->h_out2.n != bytes) a->h_out2.alloc(bytes);
+  }
+  ck(cudaMemcpyAsync(a->h_in.p, PJ, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+  ck(hfg::launch_coulomb_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof),
+     "coulomb");
+  ck(cudaEventRecord(a->ev_j, st), "event");
+  ck(cudaStreamWaitEvent(a->copy_stream, a->ev_j, 0), "wait");
+  ck(cudaMemcpyAsync(J, a->h_out.p, bytes, cudaMemcpyDeviceToHost, a->copy_stream), "D2H copy");
+  const double* Pk = a->h_in.as<double>();
+  if (!same) {
+    ck(cudaMemcpyAsync(a->h_in2.p, PK, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+    Pk = a->h_in2.as<double>();
+  }
+  if (flags & HFG_EXCHANGE_SPLIT) {
+    const size_t b2 = sizeof(float2) * (size_t)a->host.nbf * a->host.nbf;
+    if (a->s_p2.n != b2) {
+      hfg_abi::AllocStream alloc_on(st);
+      a->s_p2.alloc(b2);
+      a->scr.p2 = a->s_p2.as<float2>();
+    }
+    ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, Pk, a->h_out2.as<double>(),
+                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof),
+       "exchange (split)");
+  } else {
+    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, Pk, a->h_out2.as<double>(),
+                                 (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof),
+       "exchange");
+  }
+  ck(cudaMemcpyAsync(K, a->h_out2.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
+  ck(cudaStreamSynchronize(st), "stream sync");
+  ck(cudaStreamSynchronize(a->copy_stream), "stream sync");
+}
+
+hfg_status hfg_jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, double* K, int flags) {
+  return guard([&] { jk_host(a, PJ, PK, J, K, flags); });
+}
+
 hfg_status hfg_coulomb_host(hfg_atom* a, const double* P, double* J) {
   return guard([&] { host_call(a, P, J, true, 0); });
 }

@@ -159,6 +159,10 @@ struct hfg_atom {
   hfg::KUnits units;
   // staging for the host-pointer entry points (allocated on first use)
   DBuf h_in, h_out, h_in2, h_out2, h_e;
+  // second stream and event of the combined J+K host entry point: J's copy
+  // back overlaps the exchange build
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_j = nullptr;
   // DFT grid (built on first use or by hfg_dft_grid)
   hfg::DevXC xc{};
   hfg::XcScratch xs{};
@@ -176,6 +180,11 @@ struct hfg_atom {
   }
 
   ~hfg_atom() {
+    if (ev_j) cudaEventDestroy(ev_j);
+    if (copy_stream) {
+      cudaStreamSynchronize(copy_stream);
+      cudaStreamDestroy(copy_stream);
+    }
     free_profiler();
     if (last_use) {
       if (own_stream) cudaStreamWaitEvent(own_stream, last_use, 0);

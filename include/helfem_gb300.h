@@ -183,6 +183,11 @@ hfg_status hfg_coulomb_host(hfg_atom* atom, const double* P, double* J);
 hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);
 /* hfg_exchange_host with the hfg_exchange_ex flags (symmetric / split). */
 hfg_status hfg_exchange_host_ex(hfg_atom* atom, const double* P, double* K, int flags);
+/* J(PJ) and K(PK) in one call (the Fock builder's pair of calls,
+ * src/atomic/main.cpp:424-443): the density is staged once when PK == PJ
+ * (same pointer), and J is copied back on a second stream while K is built.
+ * flags as hfg_exchange_ex. */
+hfg_status hfg_jk_host(hfg_atom* atom, const double* PJ, const double* PK, double* J, double* K, int flags);
 
 /* Algorithmic work of one J and one K build on this basis with every density
  * block active (the unit counts behind roofline figures). FLOPs count one

@@ -97,6 +97,15 @@ def test_host_entry_points_and_determinism():
     assert relerr(J1, F.coulomb(P)) < TOL and relerr(K1, F.exchange(P)) < TOL
     # fixed summation order: bitwise reproducible
     assert np.array_equal(J1, J2) and np.array_equal(K1, K2)
+    # the combined entry point: same results, one staging of the density
+    J3, K3 = A.jk_host(P)
+    assert np.array_equal(J3, J1) and np.array_equal(K3, K1)
+    Pk = 0.5 * P
+    J4, K4 = A.jk_host(P, Pk, symmetric=True)
+    assert np.array_equal(J4, J1)
+    assert relerr(K4, A.exchange_host(Pk)) < 1e-13
+    J5, K5 = A.jk_host(P, symmetric=True, split=True)
+    assert np.array_equal(J5, J1) and relerr(K5, K1) < 1e-12
 
 
 def test_zero_density():
