@@ -409,7 +409,8 @@ class Engine:
         self._h = h
 
     def submit(self, Z, bval, lval, mval, nela, nelb, method="hf", restricted=True, nnodes=15, symmetry=1,
-               fixed_occ=None, e_tol=0.0, diis_tol=0.0, frac_aufbau=False, split=False, l_occ=None) -> int:
+               fixed_occ=None, e_tol=0.0, diis_tol=0.0, frac_aufbau=False, split=False, l_occ=None,
+               maxiter=0) -> int:
         bval = np.ascontiguousarray(bval, dtype=np.float64)
         lval = np.ascontiguousarray(lval, dtype=np.int32)
         mval = np.ascontiguousarray(mval, dtype=np.int32)
@@ -421,7 +422,7 @@ class Engine:
             occ = np.array([v for m in ms for v in fixed_occ.get(m, (0, 0))], dtype=np.int32)
             nfix = len(ms)
         lo = None if l_occ is None else np.ascontiguousarray(np.asarray(l_occ, dtype=np.float64).ravel())
-        sd = _scf_desc(nela, nelb, method, restricted, symmetry, occ, nfix, e_tol, diis_tol,
+        sd = _scf_desc(nela, nelb, method, restricted, symmetry, occ, nfix, e_tol, diis_tol, maxiter=maxiter,
                        frac_aufbau=frac_aufbau, split=split, l_occ=lo)
         jid = ctypes.c_ulonglong()
         _check(_lib.hfg_engine_submit(self._h, ctypes.byref(ad), ctypes.byref(sd), ctypes.byref(jid)))

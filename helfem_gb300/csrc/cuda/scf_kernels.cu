@@ -57,6 +57,10 @@ __global__ void scale_cols(const double* __restrict__ X, int n, int m, const dou
     Y[idx] = X[idx] * s[idx / n];
 }
 
+__global__ void add_diag(double* __restrict__ A, int n, double v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) A[i + (size_t)i * n] += v;
+}
+
 inline int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
@@ -77,6 +81,10 @@ void k_add4(double* out, const double* a, const double* b, const double* c, cons
 }
 void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cudaStream_t st) {
   scale_cols<<<grid_for((size_t)n * m), 256, 0, st>>>(X, n, m, s, Y);
+}
+
+void k_add_diag(double* A, int n, double v, cudaStream_t st) {
+  add_diag<<<(n + 255) / 256, 256, 0, st>>>(A, n, v);
 }
 
 }  // namespace hfg

@@ -15,5 +15,7 @@ void k_antisym(const double* G, int n, double* E, cudaStream_t st);
 void k_add4(double* out, const double* a, const double* b, const double* c, const double* d, size_t n,
             cudaStream_t st);
 void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cudaStream_t st);
+// A[i,i] += v, A n x n column-major
+void k_add_diag(double* A, int n, double v, cudaStream_t st);
 
 }  // namespace hfg

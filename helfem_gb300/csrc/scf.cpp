@@ -440,6 +440,13 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     int it = 0, nh = 0;
     bool converged = false;
     int n_stable = 0;
+    // stabilisation: when the orbital gradient stalls above 1e-5 (DIIS
+    // oscillating between states, typical of diffuse anions and near-
+    // degenerate open shells) the virtual orbitals are level-shifted,
+    // F' += b (1 - Q Q^T) with Q the occupied orbitals of the previous
+    // iteration, and the DIIS history restarts
+    double shift = 0.0, emin = 1e300;
+    int it_improved = 0;
     double Ekin = 0, Enuc = 0, Ecoul = 0, Exx = 0, Exc = 0, Ngrid = 0, Etot = 0;
     PhaseTimer pt;
     for (it = 1; it <= maxiter; ++it) {
@@ -538,6 +545,18 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         break;
       }
       Eold = Etot;
+      if (emax < 0.5 * emin) {
+        emin = emax;
+        it_improved = it;
+      }
+      if (emax > 1e-5 && it >= 12 && it - it_improved >= 6 && shift < 2.0) {
+        shift = (shift == 0.0) ? 0.5 : 2.0;
+        it_improved = it;
+        emin = emax;
+        nh = 0;
+        std::fill(Bm.begin(), Bm.end(), 0.0);
+        if (verbose) std::fprintf(stderr, "hfg_scf it %3d level shift %.2f, DIIS restart\n", it, shift);
+      }
 
       // ---- DIIS extrapolation ----
       const int slot = (nh < nhist) ? nh : (it - 1) % nhist;
@@ -596,6 +615,22 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       ck(cudaMemsetAsync(dFo.p, 0, sizeof(double) * Ltot, st), "memset");
       for (int i = 0; i < nh; ++i)
         cb(cublasDaxpy(hd.bl, (int)Ltot, &c[i], dHF.as<double>() + Ltot * i, 1, dFo.as<double>(), 1), "axpy");
+      if (shift > 0.0)
+        for (int s = 0; s < nspin; ++s)
+          for (int k = 0; k < nblk; ++k) {
+            if (rep[k] != k) continue;
+            const Block& b = blocks[k];
+            int nocc = 0;
+            while (nocc < b.nk && occ[s][k][nocc] > 0) ++nocc;
+            double* Fo = dFo.as<double>() + Lblk * s + b.off;
+            hfg::k_add_diag(Fo, b.nk, shift, st);
+            if (nocc == 0) continue;
+            const double* Vk = dVec.as<double>() + Lblk * s + b.off;
+            const double mshift = -shift;
+            cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_T, b.nk, b.nk, nocc, &mshift, Vk, b.nk, Vk, b.nk, &one, Fo,
+                           b.nk),
+               "level shift");
+          }
       pt.lap(3);  // DIIS extrapolation
       for (int s = 0; s < nspin; ++s) diagonalise(dFo.as<double>(), s);
       occupy();
