@@ -72,6 +72,7 @@ _SIGS = {
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host_ex": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_jk_host": ([_P, _D, _D, _D, _D, ctypes.c_int], ctypes.c_int),
+    "hfg_fock_diag": ([_P, _P, ctypes.c_int, _P, _P, _P], ctypes.c_int),
     "hfg_atom_work": ([_P, _P], ctypes.c_int),
     "hfg_dft_grid": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
@@ -376,6 +377,11 @@ class Atom:
         else:
             _check(_lib.hfg_exchange_host(self._h, _dptr(P), _dptr(K)))
         return K
+
+    def fock_diag(self, F, C, eps, symmetry: int = 1, stream=None):
+        """Orbital energies eps (nbf) and AO coefficients C (nbf x nbf) of
+        the Fock matrix F per symmetry block (device buffers)."""
+        _check(_lib.hfg_fock_diag(self._h, _ptr(F), symmetry, _ptr(C), _ptr(eps), _stream(stream)))
 
     def jk_host(self, PJ: np.ndarray, PK: np.ndarray = None, J: np.ndarray = None, K: np.ndarray = None,
                 symmetric: bool = False, split: bool = False):

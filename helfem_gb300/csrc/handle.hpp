@@ -159,6 +159,7 @@ struct hfg_atom {
   hfg::KUnits units;
   // staging for the host-pointer entry points (allocated on first use)
   DBuf h_in, h_out, h_in2, h_out2, h_e;
+  DBuf d_xrad;  // radial orthonormaliser invh(S_rad), built by the first hfg_fock_diag
   // second stream and event of the combined J+K host entry point: J's copy
   // back overlaps the exchange build
   cudaStream_t copy_stream = nullptr;

@@ -178,6 +178,17 @@ hfg_status hfg_xc(hfg_atom* atom, int x_func, int c_func, const double* Pa, cons
 hfg_status hfg_xc_host(hfg_atom* atom, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
                        double* Hb, double* Exc, double* Nel, double thr);
 
+/* ---- Fock diagonalisation step ----
+ * Per symmetry block (symmetry 1: one block per m, unique m ascending;
+ * 2: one block per angular function) the orthonormal Fock block
+ * F'_k = X_k^T F X_k with the reference's symmetric orthonormaliser
+ * (scf_driver_common.h:176-187, 432-445; utils.cpp:120-159), its eigenpairs
+ * and the AO coefficients C_k = X_k V (scf_helpers.cpp:41-50 eig_gsym).
+ * F, C (nbf x nbf) and eps (nbf) are device pointers; eps holds the blocks'
+ * eigenvalues in block order, ascending within a block, and column j of C is
+ * the orbital of eps[j] (zero outside its block's rows). C^T S C = 1. */
+hfg_status hfg_fock_diag(hfg_atom* atom, const double* F, int symmetry, double* C, double* eps, void* stream);
+
 /* ---- host-pointer drop-ins (value semantics, synchronous) ---- */
 hfg_status hfg_coulomb_host(hfg_atom* atom, const double* P, double* J);
 hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);

@@ -9,6 +9,7 @@ import pytest
 
 import helfem_gb300 as hg
 from gpu_util import torch_cuda
+from oracle import tabulate as tab
 
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -66,3 +67,38 @@ def test_orbital_energies_match_oracle():
     e_gpu = np.sort(r["orbital_energies"])[:3]
     e_ora = np.sort(np.concatenate(o.eps[0]))[:3]
     assert np.abs(e_gpu - e_ora).max() < 1e-7, (e_gpu, e_ora)
+
+
+@pytest.mark.parametrize("symmetry", [1, 2])
+def test_fock_diag_matches_generalized_eigenproblem(symmetry):
+    """hfg_fock_diag: per-block generalized eigenpairs of F (here the core
+    Hamiltonian, block diagonal in (l,m)) in the S metric."""
+    import scipy.linalg
+    from gpu_util import to_dev, from_dev
+    torch = torch_cuda()
+    b = tab.get_grid(40.0, 5, 4, 2.0)
+    lv, mv = hg.angular_basis(1, 1)
+    A = hg.Atom(8, b, lv, mv)
+    S, H = A.overlap(), A.kinetic() + A.nuclear()
+    Fd = to_dev(torch, H)
+    Cd = torch.zeros_like(Fd)
+    ed = torch.zeros(A.nbf, dtype=torch.float64, device="cuda")
+    A.fock_diag(Fd, Cd, ed, symmetry=symmetry)
+    torch.cuda.synchronize()
+    C, eps = from_dev(Cd), ed.cpu().numpy()
+    n = A.nbf // len(lv)
+    if symmetry == 1:
+        groups = [[i for i in range(len(mv)) if mv[i] == m] for m in sorted(set(mv.tolist()))]
+    else:
+        groups = [[i] for i in range(len(lv))]
+    col = 0
+    for g in groups:
+        idx = np.concatenate([np.arange(i * n, (i + 1) * n) for i in g])
+        w = scipy.linalg.eigh(H[np.ix_(idx, idx)], S[np.ix_(idx, idx)], eigvals_only=True)
+        e = eps[col:col + len(idx)]
+        assert np.allclose(e, w, rtol=1e-10, atol=1e-10 * np.abs(w).max())
+        col += len(idx)
+    # S-orthonormal eigenvectors of H
+    assert np.abs(C.T @ S @ C - np.eye(A.nbf)).max() < 1e-9
+    R = H @ C - S @ C * eps[None, :]
+    assert np.abs(R).max() < 1e-8 * np.abs(H).max()
