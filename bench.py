@@ -550,10 +550,9 @@ def n2_setup(hg, host_only=False, nelem=30, lmax=12):
     return d, P, act
 
 
-def n2_cpu_sample(d, P, seconds):
-    """The oracle's exchange (the reference's loop structure, OpenMP) on a
-    bounded sample of output blocks, scaled to a full build by the work model;
-    plus the oracle's J on the full density."""
+def n2_oracle(d):
+    """The oracle's exchange (the reference's loop structure) fed with the
+    product's tables of the diatomic handle d: (DiatomicOracle, tables)."""
     import oracle
     from oracle import diatomic as dia
     nel, nn = d.dims["nel"], d.dims["nnodes"]
@@ -576,10 +575,17 @@ def n2_cpu_sample(d, P, seconds):
         cdB.append(fB); cds.append(fS)
     _, LM = dia.lm_maps(d.lval, d.mval)
     first = np.array([e * (nn - 1) for e in range(nel)])
-    bval = np.zeros(nel + 1)
-    D = dia.DiatomicTables(d.Z1, d.Z2, d.Rhalf, nn, bval, np.asarray(d.lval, int), np.asarray(d.mval, int),
-                           d.nrad, first, np.array(ni), lm, LM, P0, P2, Q0, Q2, cdB, cds)
-    F = oracle.DiatomicOracle(D)
+    D = dia.DiatomicTables(d.Z1, d.Z2, d.Rhalf, nn, np.zeros(nel + 1), np.asarray(d.lval, int),
+                           np.asarray(d.mval, int), d.nrad, first, np.array(ni), lm, LM, P0, P2, Q0, Q2, cdB, cds)
+    return oracle.DiatomicOracle(D), D
+
+
+def n2_cpu_sample(d, P, seconds):
+    """The oracle's exchange (the reference's loop structure, OpenMP) on a
+    bounded sample of output blocks, scaled to a full build by the work model;
+    J not included."""
+    import oracle
+    F, D = n2_oracle(d)
     Pd = np.asfortranarray(D.expand(0.5 * P))
     nang = d.nang
     mv = np.asarray(d.mval)

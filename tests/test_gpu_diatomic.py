@@ -179,3 +179,40 @@ def test_n2_full_size_properties():
     assert bool(torch.isfinite(Kp).all())
     assert float((Kp - Kg).abs().max()) <= SPLIT_TOL * float(Kg.abs().max())
     assert abs(float((Pd * (Kp - Kg)).sum())) <= SPLIT_E_TOL * abs(float((Pd * Kg).sum()))
+
+
+def test_n2_full_size_sampled_parity():
+    """The N2 benchmark basis and density (5 sigma, 1 pi+, 1 pi- seeded
+    orbitals): GPU K (FP64 and split) against the oracle's exchange on a
+    sample of output blocks at full size, using the product's tables (their
+    tabulation is checked against the oracle's at small sizes)."""
+    import bench
+    torch = torch_cuda()
+    d, P, _ = bench.n2_setup(hg)
+    Pa = 0.5 * P
+    Pd = torch.from_numpy(np.asfortranarray(Pa).ravel(order="F")).cuda()
+    K64 = torch.empty_like(Pd)
+    Ksp = torch.empty_like(Pd)
+    d.exchange(Pd, K64, symmetric=True)
+    d.exchange(Pd, Ksp, symmetric=True, split=True)
+    torch.cuda.synchronize()
+    nbf = d.nbf
+    K64 = K64.cpu().numpy().reshape(nbf, nbf).T  # column-major buffer -> (row, col)
+    Ksp = Ksp.cpu().numpy().reshape(nbf, nbf).T
+    F, D = bench.n2_oracle(d)
+    nang, nrad = d.nang, d.nrad
+    mv = np.asarray(d.mval)
+    rng = np.random.default_rng(3)
+    active = [j + k * nang for k in range(nang) for j in range(nang) if mv[j] == mv[k] and abs(mv[j]) <= 3]
+    sample = [int(x) for x in rng.choice(active, size=10, replace=False)]
+    Kd = F.exchange_dummy_blocks(np.asfortranarray(D.expand(Pa)), sample)
+    idx = d.pure_indices()
+    pos = {int(g): i for i, g in enumerate(idx)}
+    for jk in sample:
+        j, k = jk % nang, jk // nang
+        rows = [pos[j * nrad + r] for r in range(nrad) if (j * nrad + r) in pos]
+        cols = [pos[k * nrad + c] for c in range(nrad) if (k * nrad + c) in pos]
+        ref = Kd[np.ix_([idx[i] for i in rows], [idx[i] for i in cols])]
+        scale = max(np.abs(ref).max(), 1e-300)
+        assert np.abs(K64[np.ix_(rows, cols)] - ref).max() <= 1e-10 * scale, jk
+        assert np.abs(Ksp[np.ix_(rows, cols)] - ref).max() <= SPLIT_TOL * scale, jk
