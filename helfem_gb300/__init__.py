@@ -73,6 +73,7 @@ _SIGS = {
     "hfg_exchange_host_ex": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_jk_host": ([_P, _D, _D, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_fock_diag": ([_P, _P, ctypes.c_int, _P, _P, _P], ctypes.c_int),
+    "hfg_atom_autotune": ([_P, ctypes.c_int, _I, _D], ctypes.c_int),
     "hfg_atom_work": ([_P, _P], ctypes.c_int),
     "hfg_dft_grid": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
@@ -377,6 +378,14 @@ class Atom:
         else:
             _check(_lib.hfg_exchange_host(self._h, _dptr(P), _dptr(K)))
         return K
+
+    def autotune(self, symmetric: bool = True, split: bool = False) -> dict:
+        """Pick the exchange work partition by timing candidates (kept for
+        later calls on this handle)."""
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        ns, ms = ctypes.c_int(), ctypes.c_double()
+        _check(_lib.hfg_atom_autotune(self._h, flags, ctypes.byref(ns), ctypes.byref(ms)))
+        return {"nsplit": ns.value, "ms": ms.value}
 
     def fock_diag(self, F, C, eps, symmetry: int = 1, stream=None):
         """Orbital energies eps (nbf) and AO coefficients C (nbf x nbf) of

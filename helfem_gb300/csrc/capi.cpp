@@ -2,6 +2,7 @@
 // Every entry point converts exceptions and CUDA errors into status codes and
 // a thread-local message; nothing throws across the boundary.
 #include "handle.hpp"
+#include "cuda/scf_kernels.cuh"
 
 #include <mutex>
 
@@ -325,6 +326,64 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
 
 hfg_status hfg_jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, double* K, int flags) {
   return guard([&] { jk_host(a, PJ, PK, J, K, flags); });
+}
+
+// Autotuner: times the exchange tile kernel for candidate partitions of the
+// work units (output-block ranges per element pair) on a synthetic density
+// with every block active, keeps the fastest
+hfg_status hfg_atom_autotune(hfg_atom* a, int flags, int* best_nsplit, double* best_ms) {
+  return guard([&] {
+    need(a != nullptr, "hfg_atom_autotune: null argument");
+    need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "unknown flags");
+    a->check_device();
+    cudaStream_t st = a->own_stream;
+    hfg_abi::AllocStream alloc_on(st);
+    const size_t n = (size_t)a->host.nbf, bytes = sizeof(double) * n * n;
+    DBuf P, K;
+    P.alloc(bytes);
+    K.alloc(bytes);
+    hfg::fill_test_density(P.as<double>(), (int)n, st);
+    if ((flags & HFG_EXCHANGE_SPLIT) && a->s_p2.n != sizeof(float2) * n * n) {
+      a->s_p2.alloc(sizeof(float2) * n * n);
+      a->scr.p2 = a->s_p2.as<float2>();
+    }
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    auto run = [&]() {
+      const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
+      if (flags & HFG_EXCHANGE_SPLIT)
+        ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P.as<double>(), K.as<double>(), sym, st, nullptr),
+           "exchange");
+      else
+        ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P.as<double>(), K.as<double>(), sym, st, nullptr),
+           "exchange");
+    };
+    double best = 1e300;
+    int bestn = 0;
+    for (int ns : {0, 1, 2, 4, 8, 16}) {
+      a->nsplit_fixed = ns;
+      a->build_units();
+      run();
+      ck(cudaEventRecord(e0, st), "event");
+      for (int r = 0; r < 3; ++r) run();
+      ck(cudaEventRecord(e1, st), "event");
+      ck(cudaEventSynchronize(e1), "sync");
+      float ms = 0.f;
+      ck(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+      if (ms / 3.0 < best) {
+        best = ms / 3.0;
+        bestn = ns;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    a->nsplit_fixed = bestn;
+    a->build_units();
+    ck(cudaStreamSynchronize(st), "sync");
+    if (best_nsplit) *best_nsplit = bestn;
+    if (best_ms) *best_ms = best;
+  });
 }
 
 hfg_status hfg_coulomb_host(hfg_atom* a, const double* P, double* J) {

@@ -61,6 +61,19 @@ __global__ void add_diag(double* __restrict__ A, int n, double v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) A[i + (size_t)i * n] += v;
 }
 
+__global__ void test_density(double* __restrict__ P, int n) {
+  const size_t nn = (size_t)n * n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < nn; idx += (size_t)gridDim.x * blockDim.x) {
+    const unsigned r = (unsigned)(idx % n), c = (unsigned)(idx / n);
+    const unsigned lo = r < c ? r : c, hi = r < c ? c : r;
+    unsigned h = lo * 2654435761u ^ (hi * 40503u + 0x9e3779b9u);
+    h ^= h >> 15;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    P[idx] = 1e-3 * ((double)(h & 0xFFFFFF) / 16777216.0 - 0.5);
+  }
+}
+
 inline int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
@@ -81,6 +94,10 @@ void k_add4(double* out, const double* a, const double* b, const double* c, cons
 }
 void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cudaStream_t st) {
   scale_cols<<<grid_for((size_t)n * m), 256, 0, st>>>(X, n, m, s, Y);
+}
+
+void fill_test_density(double* P, int n, cudaStream_t st) {
+  test_density<<<grid_for((size_t)n * n), 256, 0, st>>>(P, n);
 }
 
 void k_add_diag(double* A, int n, double v, cudaStream_t st) {

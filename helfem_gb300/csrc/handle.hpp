@@ -312,6 +312,9 @@ struct hfg_atom {
   // angular blocks (enough units to keep every SM busy to the end), then
   // one unit per (diagonal element, output block); off-diagonal units first
   // so the short diagonal ones fill the tail.
+  // nsplit_fixed > 0: that many output-block ranges per off-diagonal element
+  // pair (set by the autotuner); 0: enough units to fill the GPU
+  int nsplit_fixed = 0;
   void build_units() {
     const hfg::AtomHost& H = host;
     const int nel = H.rad.nel, nang2 = H.nang * H.nang;
@@ -336,6 +339,7 @@ struct hfg_atom {
       std::vector<int4> u;
       const long npairs = sym ? (long)nel * (nel - 1) / 2 : (long)nel * (nel - 1);
       int nsplit = (int)std::min<long>(std::max<long>(1, (2432 + npairs - 1) / std::max<long>(npairs, 1)), 8);
+      if (nsplit_fixed > 0) nsplit = nsplit_fixed;
       nsplit = std::min(nsplit, nang2);
       const std::vector<int> cut = ranges(nsplit);
       for (int a = 0; a < nel; ++a)

@@ -146,6 +146,13 @@ hfg_status hfg_exchange(hfg_atom* atom, const double* P, double* K, void* stream
 #define HFG_EXCHANGE_SPLIT 2
 hfg_status hfg_exchange_ex(hfg_atom* atom, const double* P, double* K, int flags, void* stream);
 
+/* Autotuner of the exchange work partition: times the tile kernel (form
+ * given by flags) for candidate numbers of output-block ranges per element
+ * pair on a synthetic density with every block active, and keeps the
+ * fastest for the later calls of this handle. Synchronous; results and
+ * layouts of K do not change. */
+hfg_status hfg_atom_autotune(hfg_atom* atom, int flags, int* best_nsplit, double* best_ms);
+
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
  * fixed 4 MiB array in the library's static device memory rather than the
  * handle's buffers. No counterpart in the reference; it exists for callers

@@ -108,6 +108,19 @@ def test_host_entry_points_and_determinism():
     assert np.array_equal(J5, J1) and relerr(K5, K1) < 1e-12
 
 
+def test_autotune_keeps_results():
+    """The work-partition autotuner changes which CTA computes what, not the
+    arithmetic of an output tile: K is bitwise unchanged."""
+    torch = torch_cuda()
+    A, O = make_pair(36, 2, 2, 6)
+    P = random_density(O.nbf, 5, seed=11, S=O.S)
+    K1 = A.exchange_host(P, symmetric=True, split=True)
+    r = A.autotune(symmetric=True, split=True)
+    assert r["nsplit"] in (0, 1, 2, 4, 8, 16) and r["ms"] > 0
+    K2 = A.exchange_host(P, symmetric=True, split=True)
+    assert np.array_equal(K1, K2)
+
+
 def test_zero_density():
     torch = torch_cuda()
     A, O = make_pair(2, 0, 0, 3)
