@@ -102,6 +102,10 @@ _SIGS = {
     "hfg_diatomic_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_diatomic_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_diatomic_work": ([_P, _P, _P, _P], ctypes.c_int),
+    "hfg_diatomic_dft_grid": ([_P, ctypes.c_int], ctypes.c_int),
+    "hfg_diatomic_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
+    "hfg_diatomic_xc_host": ([_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, ctypes.c_double],
+                             ctypes.c_int),
 }
 KERNEL_CLASSES = ("j_contract", "j_scatter", "k_block_norms", "k_tiles", "k_fixup")
 XC_IDS = {"lda_x": 1, "lda_c_vwn": 7, "lda_c_pw": 12, "gga_x_pbe": 101, "gga_c_pbe": 130}
@@ -632,6 +636,32 @@ class Diatomic:
         flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
         _check(_lib.hfg_diatomic_exchange_host(self._h, _dptr(P), _dptr(K), flags))
         return K
+
+    # ---- XC on the pure-m grid ----
+    def dft_grid(self, lang: int = 0):
+        """(Re)build the pure-m grid: lang cos(nu) points (0 -> 4 lmax + 12)."""
+        _check(_lib.hfg_diatomic_dft_grid(self._h, lang))
+
+    def xc(self, x_func, c_func, Pa, Ha, Pb=None, Hb=None, energies=None, thr=1e-12, stream=None):
+        """Device pointers (torch tensors, column-major pure-basis matrices);
+        Pb None: restricted, Pa the total density."""
+        _check(_lib.hfg_diatomic_xc(self._h, x_func, c_func, _ptr(Pa), _ptr(Pb) if Pb is not None else None,
+                                    _ptr(Ha), _ptr(Hb) if Hb is not None else None,
+                                    _ptr(energies) if energies is not None else None, thr, _stream(stream)))
+
+    def xc_host(self, x_func, c_func, Pa, Pb=None, thr=1e-12):
+        """Returns (Ha, Hb or None, Exc, Nel)."""
+        Pa = np.asfortranarray(Pa, dtype=np.float64)
+        Ha = np.zeros_like(Pa, order="F")
+        Pb_ = Hb = None
+        if Pb is not None:
+            Pb_ = np.asfortranarray(Pb, dtype=np.float64)
+            Hb = np.zeros_like(Pa, order="F")
+        exc, nel = ctypes.c_double(), ctypes.c_double()
+        _check(_lib.hfg_diatomic_xc_host(self._h, x_func, c_func, _dptr(Pa), _dptr(Pb_) if Pb_ is not None else None,
+                                         _dptr(Ha), _dptr(Hb) if Hb is not None else None,
+                                         ctypes.byref(exc), ctypes.byref(nel), thr))
+        return Ha, Hb, exc.value, nel.value
 
     def work(self, act: np.ndarray = None, jk_mask: np.ndarray = None) -> dict:
         """Exchange work model (flops) for a density-block activity mask

@@ -79,6 +79,34 @@ struct DevDiatomicScratch {
 
 #define DNORM_SPLIT 8
 
+// pure-m DFT grid: nq mu points per element, na nu points, npair same-m
+// ordered angular pairs (s, t)
+struct DevDiatomicXC {
+  int nq = 0, na = 0, npair = 0;
+  const int* ps = nullptr;     // [npair]
+  const int* pt = nullptr;
+  const int* prev = nullptr;   // index of (t, s)
+  const double* W = nullptr;   // [k*na + a]
+  const double* Wt = nullptr;
+  const double* R = nullptr;   // [(e*nq + q)*nn + p]
+  const double* dR = nullptr;
+  const double* w = nullptr;   // [(e*nq + q)*na + a]
+  const double* hinv = nullptr;
+};
+struct DiatomicXcScratch {
+  double* D;      // [nsd][nel][nq][npair]
+  double* Dr;     // same
+  double* F;      // [nout][3][nel][nq][na]
+  double* U;      // [nout][3][nel][npair][nq]
+  double* epart;  // [nel*nq][2]
+};
+// Pb == nullptr: restricted (Pa is the total density, Ha the potential).
+// Densities and potentials are in the dummy basis (nd x nd); H is
+// overwritten. energies (device, may be null) receives {Exc, Nel}.
+cudaError_t launch_diatomic_xc(const DevDiatomic& D, const DevDiatomicXC& X, const DiatomicXcScratch& S, int xid,
+                               int cid, const double* Pa, const double* Pb, double* Ha, double* Hb, double* energies,
+                               double thr, cudaStream_t st);
+
 cudaError_t launch_diatomic_expand(const double* P, int nbf, const int* pure, double* Pd, int nd, cudaStream_t st);
 cudaError_t launch_diatomic_gather(const double* Fd, int nd, const int* pure, int nbf, double* F, cudaStream_t st);
 cudaError_t launch_diatomic_tx(const DevDiatomic& D, double* tx, cudaStream_t st);

@@ -91,29 +91,6 @@ __global__ void xc_rad(DevAtom A, DevXC X, XcScratch S, const double* __restrict
   }
 }
 
-template <int N>
-__device__ void eval_func(int xid, int cid, double ra, double rb, double saa, double sab, double sbb,
-                          double& e, double* v) {
-  using namespace xcf;
-  const Dual<N> a = var<N>(ra, 0), b = var<N>(rb, 1);
-  const Dual<N> xaa = var<N>(saa, 2), xab = var<N>(sab, 3), xbb = var<N>(sbb, 4);
-  Dual<N> tot = cst<N>(0.0);
-  const int ids[2] = {xid, cid};
-  for (int k = 0; k < 2; ++k) {
-    switch (ids[k]) {
-      case 1: tot = tot + slater_x(a, b); break;
-      case 7: tot = tot + vwn5_c(a, b); break;
-      case 12: tot = tot + pw92_c(a, b); break;
-      case 101: tot = tot + pbe_x(a, b, xaa, xbb); break;
-      case 130: tot = tot + pbe_c(a, b, xaa, xab, xbb); break;
-      default: break;
-    }
-  }
-  e = tot.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) v[i] = tot.d[i];
-}
-
 // grid (nel, nquad); threads over angular points
 __global__ void xc_point(DevAtom A, DevXC X, XcScratch S, int xid, int cid, int gga, int nsd, int polarized,
                          double thr) {

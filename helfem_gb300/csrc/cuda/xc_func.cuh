@@ -127,10 +127,13 @@ __device__ __forceinline__ Dual<N> pow(const Dual<N>& a, double p) {
 
 constexpr double PI = 3.14159265358979323846;
 
+// f(zeta) from opz = 1 + zeta = 2 rho_a / n and omz = 1 - zeta = 2 rho_b / n,
+// formed from the spin densities rather than by subtracting zeta from one
+// (which loses the relative precision of a minority spin density)
 template <class T>
-__device__ __forceinline__ T fzeta(const T& z) {
+__device__ __forceinline__ T fzeta(const T& opz, const T& omz) {
   const double den = 1.0 / (2.5198420997897464 - 2.0);  // 2^{4/3} - 2
-  return (pow(1.0 + z, 4.0 / 3.0) + pow(1.0 - z, 4.0 / 3.0) - 2.0) * den;
+  return (pow(opz, 4.0 / 3.0) + pow(omz, 4.0 / 3.0) - 2.0) * den;
 }
 
 // ---------------------------------------------------------------- Slater x
@@ -157,11 +160,12 @@ __device__ __forceinline__ T vwn5_c(const T& ra, const T& rb) {
   const T z = (ra - rb) / n;
   const T rs = pow((3.0 / (4.0 * PI)) / n, 1.0 / 3.0);
   const T x = sqrt(rs);
+  const T opz = 2.0 * ra / n, omz = 2.0 * rb / n;
   const T eP = vwn_eps(x, 0.0310907, 3.72744, 12.9352, -0.10498);
   const T eF = vwn_eps(x, 0.01554535, 7.06042, 18.0578, -0.32500);
   const T ac = vwn_eps(x, -1.0 / (6.0 * PI * PI), 1.13107, 13.0045, -0.0047584);
   const double fpp = 4.0 / (9.0 * (1.2599210498948732 - 1.0));
-  const T f = fzeta(z);
+  const T f = fzeta(opz, omz);
   const T z2 = z * z;
   const T z4 = z2 * z2;
   return n * (eP + ac * f * (1.0 / fpp) * (1.0 - z4) + (eF - eP) * f * z4);
@@ -178,7 +182,7 @@ __device__ __forceinline__ T pw_G(const T& rs, const PWPar& p) {
 }
 
 template <class T>
-__device__ __forceinline__ T pw_eps(const T& n, const T& z, bool mod) {
+__device__ __forceinline__ T pw_eps(const T& n, const T& z, const T& opz, const T& omz, bool mod) {
   const PWPar P = {mod ? 0.0310907 : 0.031091, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294};
   const PWPar F = {mod ? 0.01554535 : 0.015545, 0.20548, 14.1189, 6.1977, 3.3662, 0.62517};
   const PWPar Ap = {mod ? 0.0168869 : 0.016887, 0.11125, 10.357, 3.6231, 0.88026, 0.49671};
@@ -187,7 +191,7 @@ __device__ __forceinline__ T pw_eps(const T& n, const T& z, bool mod) {
   const T eP = pw_G(rs, P);
   const T eF = pw_G(rs, F);
   const T ac = -pw_G(rs, Ap);
-  const T f = fzeta(z);
+  const T f = fzeta(opz, omz);
   const T z2 = z * z;
   const T z4 = z2 * z2;
   return eP + ac * f * (1.0 / fpp) * (1.0 - z4) + (eF - eP) * f * z4;
@@ -196,7 +200,7 @@ __device__ __forceinline__ T pw_eps(const T& n, const T& z, bool mod) {
 template <class T>
 __device__ __forceinline__ T pw92_c(const T& ra, const T& rb) {
   const T n = ra + rb;
-  return n * pw_eps(n, (ra - rb) / n, false);
+  return n * pw_eps(n, (ra - rb) / n, 2.0 * ra / n, 2.0 * rb / n, false);
 }
 
 // -------------------------------------------------------------------- PBE
@@ -224,8 +228,9 @@ template <class T>
 __device__ __forceinline__ T pbe_c(const T& ra, const T& rb, const T& saa, const T& sab, const T& sbb) {
   const T n = ra + rb;
   const T z = (ra - rb) / n;
-  const T ec = pw_eps(n, z, true);
-  const T phi = 0.5 * (pow(1.0 + z, 2.0 / 3.0) + pow(1.0 - z, 2.0 / 3.0));
+  const T opz = 2.0 * ra / n, omz = 2.0 * rb / n;
+  const T ec = pw_eps(n, z, opz, omz, true);
+  const T phi = 0.5 * (pow(opz, 2.0 / 3.0) + pow(omz, 2.0 / 3.0));
   const T kf = pow(3.0 * PI * PI * n, 1.0 / 3.0);
   const T ks = sqrt((4.0 / PI) * kf);
   const T sig = saa + 2.0 * sab + sbb;
@@ -239,4 +244,30 @@ __device__ __forceinline__ T pbe_c(const T& ra, const T& rb, const T& saa, const
 }
 
 }  // namespace xcf
+
+// energy density and its partial derivatives (v_a, v_b, v_aa, v_ab, v_bb)
+// of the exchange + correlation pair at one point; ids as in hfg_xc
+template <int N>
+__device__ inline void eval_func(int xid, int cid, double ra, double rb, double saa, double sab, double sbb,
+                                 double& e, double* v) {
+  using namespace xcf;
+  const Dual<N> a = var<N>(ra, 0), b = var<N>(rb, 1);
+  const Dual<N> xaa = var<N>(saa, 2), xab = var<N>(sab, 3), xbb = var<N>(sbb, 4);
+  Dual<N> tot = cst<N>(0.0);
+  const int ids[2] = {xid, cid};
+  for (int k = 0; k < 2; ++k) {
+    switch (ids[k]) {
+      case 1: tot = tot + slater_x(a, b); break;
+      case 7: tot = tot + vwn5_c(a, b); break;
+      case 12: tot = tot + pw92_c(a, b); break;
+      case 101: tot = tot + pbe_x(a, b, xaa, xbb); break;
+      case 130: tot = tot + pbe_c(a, b, xaa, xab, xbb); break;
+      default: break;
+    }
+  }
+  e = tot.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = tot.d[i];
+}
+
 }  // namespace hfg

@@ -25,6 +25,12 @@ struct hfg_diatomic {
   DBuf h_in, h_out;
   cudaEvent_t last_use = nullptr;
   std::vector<double> lmfac_host;
+  // pure-m DFT grid (built on first use)
+  hfg::DevDiatomicXC xc{};
+  hfg::DiatomicXcScratch xs{};
+  bool xc_ready = false;
+  DBuf x_ps, x_pt, x_prev, x_W, x_Wt, x_R, x_dR, x_w, x_hinv, xs_D, xs_Dr, xs_F, xs_U, xs_ep, s_Pd2, s_Fd2, h_in2,
+      h_out2, h_e;
 
   ~hfg_diatomic() {
     if (last_use) {
@@ -206,6 +212,63 @@ struct hfg_diatomic {
     mark_use(st);
   }
 
+  void setup_xc(int lang) {
+    check_device();
+    hfg_abi::AllocStream alloc_on(own_stream);
+    host.build_xc_grid(lang);
+    const hfg::DiatomicHost& H = host;
+    need(H.xc_lang <= 1024, "hfg_diatomic_dft_grid: at most 1024 nu points");
+    xc.nq = H.xc_nq;
+    xc.na = H.xc_lang;
+    xc.npair = H.xc_npair;
+    xc.ps = x_ps.upload(H.xc_ps);
+    xc.pt = x_pt.upload(H.xc_pt);
+    xc.prev = x_prev.upload(H.xc_prev);
+    xc.W = x_W.upload(H.xc_W);
+    xc.Wt = x_Wt.upload(H.xc_Wt);
+    xc.R = x_R.upload(H.xc_R);
+    xc.dR = x_dR.upload(H.xc_dR);
+    xc.w = x_w.upload(H.xc_w);
+    xc.hinv = x_hinv.upload(H.xc_hinv);
+    const size_t nel = H.nel, nq = H.xc_nq, np = H.xc_npair, na = H.xc_lang;
+    xs_D.alloc(sizeof(double) * 2 * nel * nq * np);
+    xs_Dr.alloc(sizeof(double) * 2 * nel * nq * np);
+    xs_F.alloc(sizeof(double) * 6 * nel * nq * na);
+    xs_U.alloc(sizeof(double) * 6 * nel * np * nq);
+    xs_ep.alloc(sizeof(double) * 2 * nel * nq);
+    xs.D = xs_D.as<double>();
+    xs.Dr = xs_Dr.as<double>();
+    xs.F = xs_F.as<double>();
+    xs.U = xs_U.as<double>();
+    xs.epart = xs_ep.as<double>();
+    ck(cudaStreamSynchronize(own_stream), "sync after grid upload");
+    xc_ready = true;
+  }
+
+  // XC potential of pure-basis spin densities (device pointers); Pb == null:
+  // restricted, Pa the total density
+  void xc_build(int xid, int cid, const double* Pa, const double* Pb, double* Ha, double* Hb, double* energies,
+                double thr, cudaStream_t st) {
+    check_device();
+    if (!xc_ready) setup_xc(0);
+    const hfg::DiatomicHost& H = host;
+    if (Pb && s_Pd2.n == 0) {
+      hfg_abi::AllocStream alloc_on(own_stream);
+      s_Pd2.alloc(sizeof(double) * (size_t)H.ndummy * H.ndummy);
+      s_Fd2.alloc(sizeof(double) * (size_t)H.ndummy * H.ndummy);
+      ck(cudaStreamSynchronize(own_stream), "sync");
+    }
+    const int* pure = d_pure.as<int>();
+    ck(hfg::launch_diatomic_expand(Pa, H.nbf, pure, s_Pd.as<double>(), H.ndummy, st), "expand");
+    if (Pb) ck(hfg::launch_diatomic_expand(Pb, H.nbf, pure, s_Pd2.as<double>(), H.ndummy, st), "expand");
+    ck(hfg::launch_diatomic_xc(dev, xc, xs, xid, cid, s_Pd.as<double>(), Pb ? s_Pd2.as<double>() : nullptr,
+                               s_Fd.as<double>(), Pb ? s_Fd2.as<double>() : nullptr, energies, thr, st),
+       "xc kernels");
+    ck(hfg::launch_diatomic_gather(s_Fd.as<double>(), H.ndummy, pure, H.nbf, Ha, st), "gather");
+    if (Pb) ck(hfg::launch_diatomic_gather(s_Fd2.as<double>(), H.ndummy, pure, H.nbf, Hb, st), "gather");
+    mark_use(st);
+  }
+
   void build_host(const double* P, double* F, bool exchange, bool symmetric, bool split = false) {
     check_device();
     hfg_abi::AllocStream alloc_on(own_stream);
@@ -364,6 +427,60 @@ hfg_status hfg_diatomic_exchange_host(hfg_diatomic* d, const double* P, double* 
     need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0,
          "hfg_diatomic_exchange_host: unsupported flags");
     d->build_host(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0, (flags & HFG_EXCHANGE_SPLIT) != 0);
+  });
+}
+
+hfg_status hfg_diatomic_dft_grid(hfg_diatomic* d, int lang) {
+  return guard([&] {
+    need(d != nullptr && lang >= 0, "hfg_diatomic_dft_grid: bad arguments");
+    d->setup_xc(lang);
+  });
+}
+
+static void check_dxc_args(int x_func, int c_func) {
+  need(hfg::xc_func_supported(x_func) && hfg::xc_func_supported(c_func),
+       "hfg_diatomic_xc: unsupported functional id (supported: 1 lda_x, 7 lda_c_vwn, 12 lda_c_pw, 101 gga_x_pbe, "
+       "130 gga_c_pbe)");
+}
+
+hfg_status hfg_diatomic_xc(hfg_diatomic* d, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
+                           double* Hb, double* energies, double thr, void* stream) {
+  return guard([&] {
+    need(d && Pa && Ha, "hfg_diatomic_xc: null argument");
+    need(!Pb || Hb, "hfg_diatomic_xc: an unrestricted call needs Hb");
+    check_dxc_args(x_func, c_func);
+    d->xc_build(x_func, c_func, Pa, Pb, Ha, Hb, energies, thr, to_stream(stream));
+  });
+}
+
+hfg_status hfg_diatomic_xc_host(hfg_diatomic* d, int x_func, int c_func, const double* Pa, const double* Pb,
+                                double* Ha, double* Hb, double* Exc, double* Nel, double thr) {
+  return guard([&] {
+    need(d && Pa && Ha, "hfg_diatomic_xc_host: null argument");
+    need(!Pb || Hb, "hfg_diatomic_xc_host: an unrestricted call needs Hb");
+    check_dxc_args(x_func, c_func);
+    d->check_device();
+    const size_t bytes = sizeof(double) * (size_t)d->host.nbf * d->host.nbf;
+    {
+      hfg_abi::AllocStream alloc_on(d->own_stream);
+      if (d->h_in.n != bytes) d->h_in.alloc(bytes);
+      if (d->h_out.n != bytes) d->h_out.alloc(bytes);
+      if (Pb && d->h_in2.n != bytes) d->h_in2.alloc(bytes);
+      if (Pb && d->h_out2.n != bytes) d->h_out2.alloc(bytes);
+      if (d->h_e.n == 0) d->h_e.alloc(2 * sizeof(double));
+    }
+    cudaStream_t st = d->own_stream;
+    ck(cudaMemcpyAsync(d->h_in.p, Pa, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+    if (Pb) ck(cudaMemcpyAsync(d->h_in2.p, Pb, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+    d->xc_build(x_func, c_func, d->h_in.as<double>(), Pb ? d->h_in2.as<double>() : nullptr, d->h_out.as<double>(),
+                Pb ? d->h_out2.as<double>() : nullptr, d->h_e.as<double>(), thr, st);
+    double e[2];
+    ck(cudaMemcpyAsync(Ha, d->h_out.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
+    if (Pb) ck(cudaMemcpyAsync(Hb, d->h_out2.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
+    ck(cudaMemcpyAsync(e, d->h_e.p, sizeof(e), cudaMemcpyDeviceToHost, st), "D2H copy");
+    ck(cudaStreamSynchronize(st), "stream sync");
+    if (Exc) *Exc = e[0];
+    if (Nel) *Nel = e[1];
   });
 }
 

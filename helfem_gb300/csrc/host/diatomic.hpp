@@ -69,6 +69,18 @@ struct DiatomicHost {
   std::vector<int> kjk_ptr;    // [nang*nang+1]
   std::vector<int> kent_L, kent_Ma, kent_ilm;
 
+  // ---- pure-m DFT grid (src/diatomic/dftgrid_purem.cpp:34-199) -----------
+  // Per mu element: xc_nq Chebyshev points in mu; xc_lang Chebyshev points in
+  // cos(nu); the phi integral is analytic (2 pi). Only the same-m angular
+  // pairs (s, t) couple; pair k has xc_ps[k] = s, xc_pt[k] = t and
+  // xc_prev[k] = the index of (t, s).
+  int xc_lang = 0, xc_nq = 0, xc_npair = 0;
+  std::vector<int> xc_ps, xc_pt, xc_prev;
+  std::vector<double> xc_W, xc_Wt;     // [k*lang + a]: Y_s Y_t, (dY_s/dnu) Y_t at phi = 0
+  std::vector<double> xc_R, xc_dR;     // [(e*nq + q)*nn + p]: B_p, dB_p/dmu
+  std::vector<double> xc_w, xc_hinv;   // [(e*nq + q)*lang + a]: weight, 1/h
+  void build_xc_grid(int lang);
+
   void build(int Z1, int Z2, double Rhalf, int nnodes, const std::vector<double>& bval,
              const std::vector<int>& lval, const std::vector<int>& mval, double cd_thresh);
   // pure-basis one-electron matrices (nbf x nbf, column-major)

@@ -405,6 +405,24 @@ typedef struct {
 hfg_status hfg_diatomic_work(const hfg_diatomic* d, const unsigned char* act, const unsigned char* jk_mask,
                              hfg_diatomic_work_t* w);
 
+/* XC potential on the pure-m diatomic DFT grid: replaces
+ * helfem::diatomic::dftgrid_purem::PureMDFTGrid::eval_Fxc (both overloads,
+ * src/diatomic/dftgrid_purem.h:154-161, dftgrid_purem.cpp:668-742), the XC
+ * path the reference takes when the orbitals do not mix m (symmetry >= 1,
+ * src/diatomic/main.cpp:319-330): the phi integral is analytic and only the
+ * (m, m) blocks of the density and the potential enter. Functional ids, the
+ * restricted/unrestricted convention, `energies` and thr are as in hfg_xc;
+ * densities and potentials are in the pure basis (nbf x nbf, column-major)
+ * and Ha/Hb are overwritten. */
+/* (Re)build the grid: lang Chebyshev points in cos(nu) (0 -> 4*lmax+12,
+ * src/diatomic/main.cpp:316) and 5*nnodes Chebyshev points in mu per
+ * element (main.cpp:191). Called implicitly by the first XC call. */
+hfg_status hfg_diatomic_dft_grid(hfg_diatomic* d, int lang);
+hfg_status hfg_diatomic_xc(hfg_diatomic* d, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
+                           double* Hb, double* energies, double thr, void* stream);
+hfg_status hfg_diatomic_xc_host(hfg_diatomic* d, int x_func, int c_func, const double* Pa, const double* Pb,
+                                double* Ha, double* Hb, double* Exc, double* Nel, double thr);
+
 #ifdef __cplusplus
 }
 #endif

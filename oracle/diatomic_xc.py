@@ -1,0 +1,149 @@
+"""Oracle (test infrastructure only): numpy restatement of HelFEM's pure-m
+diatomic DFT grid, the XC potential of a diatomic whose orbitals do not mix
+m (symmetry >= 1).
+
+This module is the CHECKER for the GPU product. Only tests, the smoke check
+and the CPU-baseline leg of the benchmark may import it.
+
+Reference files restated here (paths inside the HelFEM project):
+
+* ``src/diatomic/dftgrid_purem.cpp:34-80``  nu rule: modified Gauss-Chebyshev
+  in cos(nu) of order lang (default 4 lmax + 12, ``src/diatomic/main.cpp:316``);
+  angular factors Y_l^m(nu, phi = 0) and
+  dY/dnu = m cot(nu) Y_l^m + sqrt((l-m)(l+m+1)) Y_l^{m+1}.
+* ``src/diatomic/dftgrid_purem.cpp:83-199``  per radial point: the element's
+  Chebyshev rule of 5 Nnodes points in mu (``main.cpp:191``, radial weight
+  wr = element half-length x wq, ``basis.cpp:496-503``), scale factor
+  h = Rhalf sqrt(sinh^2 mu + sin^2 nu) and weight
+  w = 2 pi wang wr Rhalf^3 sinh mu (sinh^2 mu + sin^2 nu); basis values per
+  m block over the dummy functions of the element (``basis.cpp:2379-2397``).
+* ``src/diatomic/dftgrid_purem.cpp:213-291,306-369``  density of each m block
+  from the (m, m) sub-block of the dummy-expanded density; gradient
+  components along mu and nu, divided by h.
+* ``src/diatomic/dftgrid_purem.cpp:480-530,575-650``  the Fock increments
+  w v_rho B B' (LDA) and X + X' with X = sum_c dB_c diag(w (2 v_ss g_c +
+  v_ab g'_c) / h) B' (GGA); only (m, m) blocks are non-zero.
+* ``src/diatomic/dftgrid_purem.cpp:668-712``  element/radial loop, energy and
+  electron count, and the removal of the boundary functions.
+
+The +m/-m mirroring of the reference is an optimisation that does not change
+the numbers; every m block is evaluated here.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import xc as xcmod
+from .diatomic import DiatomicTables
+from .tabulate import chebyshev, lip_eval, lobatto, theta_lm
+
+
+class PureMGrid:
+    """(mu, nu) product grid per radial element with the phi integral done
+    analytically (2 pi)."""
+
+    def __init__(self, tab: DiatomicTables, lang: int = 0, nquad: int = 0):
+        self.tab = tab
+        self.lang = lang or 4 * int(np.max(tab.lval)) + 12
+        self.nquad = nquad or 5 * tab.nnodes
+        self.cth, self.wang = chebyshev(self.lang)
+        self.xq, self.wq = chebyshev(self.nquad)
+        self.x0, _ = lobatto(tab.nnodes)
+        self.mlist = sorted(set(int(m) for m in tab.mval))
+        c = self.cth
+        sth = np.sqrt(np.maximum((1.0 - c) * (1.0 + c), 0.0))
+        cot = np.where(sth > 0, c / np.where(sth > 0, sth, 1.0), 0.0)
+        self.sth = sth
+        self.Y = {}
+        self.dY = {}
+        for m in self.mlist:
+            sh = [ia for ia in range(tab.nang) if int(tab.mval[ia]) == m]
+            Y, dY = [], []
+            for ia in sh:
+                l = int(tab.lval[ia])
+                y = theta_lm(l, m, c)
+                d = m * cot * y
+                if m < l:
+                    d = d + math.sqrt((l - m) * (l + m + 1.0)) * theta_lm(l, m + 1, c)
+                Y.append(y)
+                dY.append(d)
+            self.Y[m] = (sh, np.array(Y), np.array(dY))
+        self._cache = {}
+
+    def element(self, iel):
+        if iel in self._cache:
+            return self._cache[iel]
+        tab = self.tab
+        nn = tab.nnodes
+        b0, b1 = tab.bval[iel], tab.bval[iel + 1]
+        sf, mid = 0.5 * (b1 - b0), 0.5 * (b1 + b0)
+        mu = mid + sf * self.xq
+        wr = sf * self.wq
+        en = np.arange(nn) if iel < tab.nel - 1 else np.arange(nn - 1)
+        B = lip_eval(self.xq, self.x0, 0)[:, en]
+        dB = lip_eval(self.xq, self.x0, 1)[:, en] / sf
+        shmu = np.sinh(mu)
+        s2 = shmu[:, None] ** 2 + self.sth[None, :] ** 2          # (nq, na)
+        Rh = tab.Rhalf
+        h = Rh * np.sqrt(s2)
+        w = 2 * np.pi * self.wang[None, :] * wr[:, None] * Rh ** 3 * shmu[:, None] * s2
+        first = int(tab.first[iel])
+        blocks = []
+        for m in self.mlist:
+            sh, Y, dY = self.Y[m]
+            # functions (shell s, radial j) x points (q, a)
+            bf = np.einsum("sa,qj->sjqa", Y, B).reshape(len(sh) * len(en), -1)
+            dr = np.einsum("sa,qj->sjqa", Y, dB).reshape(len(sh) * len(en), -1)
+            dt = np.einsum("sa,qj->sjqa", dY, B).reshape(len(sh) * len(en), -1)
+            idx = np.concatenate([ia * tab.nrad + first + en for ia in sh])
+            blocks.append((idx, bf, dr, dt))
+        res = dict(w=w.ravel(), h=h.ravel(), blocks=blocks)
+        self._cache[iel] = res
+        return res
+
+    def eval_Fxc(self, names, Pa, Pb, thr=1e-12):
+        """Return (Ha, Hb, Exc, Nel) in the pure basis for spin densities
+        Pa, Pb given in the pure basis."""
+        tab = self.tab
+        gga = any(xcmod.FUNCTIONALS[f][0] == "gga" for f in names)
+        Pad, Pbd = tab.expand(Pa), tab.expand(Pb)
+        nd = tab.ndummy
+        Ha = np.zeros((nd, nd))
+        Hb = np.zeros((nd, nd))
+        Exc = Nel = 0.0
+        for iel in range(tab.nel):
+            E = self.element(iel)
+            w, h = E["w"], E["h"]
+            ra = np.zeros_like(w)
+            rb = np.zeros_like(w)
+            ga = [np.zeros_like(w), np.zeros_like(w)]
+            gb = [np.zeros_like(w), np.zeros_like(w)]
+            for idx, bf, dr, dt in E["blocks"]:
+                for P, rho, g in ((Pad, ra, ga), (Pbd, rb, gb)):
+                    Pv = P[np.ix_(idx, idx)] @ bf
+                    rho += np.sum(Pv * bf, axis=0)
+                    if gga:
+                        g[0] += 2 * np.sum(Pv * dr, axis=0) / h
+                        g[1] += 2 * np.sum(Pv * dt, axis=0) / h
+            Nel += float(np.sum(w * (ra + rb)))
+            if gga:
+                saa = ga[0] ** 2 + ga[1] ** 2
+                sab = ga[0] * gb[0] + ga[1] * gb[1]
+                sbb = gb[0] ** 2 + gb[1] ** 2
+            else:
+                saa = sab = sbb = None
+            e, va, vb, vaa, vab, vbb = xcmod.eval_functionals(names, ra, rb, saa, sab, sbb, thr)
+            Exc += float(np.sum(w * e))
+            for H, v, gown, goth, vss in ((Ha, va, ga, gb, vaa), (Hb, vb, gb, ga, vbb)):
+                for idx, bf, dr, dt in E["blocks"]:
+                    M = (bf * (w * v)) @ bf.T
+                    if gga:
+                        X = np.zeros_like(M)
+                        for c, dbf in enumerate((dr, dt)):
+                            coef = w * (2 * vss * gown[c] + vab * goth[c]) / h
+                            X += (dbf * coef) @ bf.T
+                        M += X + X.T
+                    H[np.ix_(idx, idx)] += M
+        return tab.remove(Ha), tab.remove(Hb), Exc, Nel

@@ -37,8 +37,10 @@ H_STEP = 1e-40
 # --------------------------------------------------------------------------
 
 
-def _fzeta(z):
-    return ((1 + z) ** (4.0 / 3.0) + (1 - z) ** (4.0 / 3.0) - 2.0) / (2.0 ** (4.0 / 3.0) - 2.0)
+def _fzeta(opz, omz):
+    # opz = 1 + zeta = 2 rho_a / n, omz = 1 - zeta = 2 rho_b / n, formed from the
+    # spin densities (1 - zeta by subtraction loses a minority spin's precision)
+    return (opz ** (4.0 / 3.0) + omz ** (4.0 / 3.0) - 2.0) / (2.0 ** (4.0 / 3.0) - 2.0)
 
 
 FPP0 = 4.0 / (9.0 * (2.0 ** (1.0 / 3.0) - 1.0))
@@ -74,7 +76,7 @@ def vwn5_c(ra, rb):
     eP = _vwn_eps(x, *VWN5_P)
     eF = _vwn_eps(x, *VWN5_F)
     ac = _vwn_eps(x, *VWN5_A)
-    f = _fzeta(z)
+    f = _fzeta(2 * ra / n, 2 * rb / n)
     z4 = z ** 4
     eps = eP + ac * f / FPP0 * (1 - z4) + (eF - eP) * f * z4
     return n * eps
@@ -99,19 +101,19 @@ PW92_MOD = dict(
 )
 
 
-def _pw_eps(n, z, par):
+def _pw_eps(n, z, opz, omz, par):
     rs = _rs(n)
     eP = _pw_G(rs, *par["P"])
     eF = _pw_G(rs, *par["F"])
     ac = -_pw_G(rs, *par["A"])
-    f = _fzeta(z)
+    f = _fzeta(opz, omz)
     z4 = z ** 4
     return eP + ac * f / par["fpp"] * (1 - z4) + (eF - eP) * f * z4
 
 
 def pw92_c(ra, rb):
     n = ra + rb
-    return n * _pw_eps(n, (ra - rb) / n, PW92)
+    return n * _pw_eps(n, (ra - rb) / n, 2 * ra / n, 2 * rb / n, PW92)
 
 
 PBE_KAPPA = 0.804
@@ -137,8 +139,9 @@ def pbe_x(ra, rb, saa, sab, sbb):
 def pbe_c(ra, rb, saa, sab, sbb):
     n = ra + rb
     z = (ra - rb) / n
-    ec = _pw_eps(n, z, PW92_MOD)
-    phi = 0.5 * ((1 + z) ** (2.0 / 3.0) + (1 - z) ** (2.0 / 3.0))
+    opz, omz = 2 * ra / n, 2 * rb / n
+    ec = _pw_eps(n, z, opz, omz, PW92_MOD)
+    phi = 0.5 * (opz ** (2.0 / 3.0) + omz ** (2.0 / 3.0))
     kf = (3 * np.pi ** 2 * n) ** (1.0 / 3.0)
     ks = np.sqrt(4 * kf / np.pi)
     sig = saa + 2 * sab + sbb

@@ -8,9 +8,9 @@ Writes diatomic.json with
              prolate spheroidal range), l <= 12 and l in {16,20,26,32,40},
              m <= 8, read from
              src/legendre/legendre_reference_data.h;
-  scf        converged diatomic HF energies recorded by the reference's own
-             test harness (tests/refs/ci.json) with the run arguments
-             (tests/cases.json).
+  scf        converged diatomic HF and DFT (pure-m XC grid) energies recorded
+             by the reference's own test harness (tests/refs/ci.json) with
+             the run arguments (tests/cases.json).
 Only numbers and run arguments are extracted; no reference source is copied.
 """
 from __future__ import annotations
@@ -21,7 +21,9 @@ import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-KEEP = {"diatomic-H2-hf-r", "diatomic-H2-hf-u", "diatomic-He-dummy-hf", "diatomic-Ne-dummy-hf"}
+KEEP = {"diatomic-H2-hf-r", "diatomic-H2-hf-u", "diatomic-He-dummy-hf", "diatomic-Ne-dummy-hf",
+        "diatomic-H2-purem-on", "diatomic-Ne-dummy-lda", "diatomic-Ne-dummy-gga", "diatomic-NH-lda-u",
+        "diatomic-NH-lda-absm"}
 
 
 def find(obj, key):
@@ -58,7 +60,7 @@ def main(root):
             k, v = a.lstrip("-").split("=", 1)
             args[k] = v
         scf.append({"name": c["name"], "args": args,
-                    "ref": {k: r[k] for k in ("total", "kinetic", "nuclear", "Coulomb", "Exx", "Enucr")}})
+                    "ref": {k: r[k] for k in ("total", "kinetic", "nuclear", "Coulomb", "Exx", "XC", "Enucr") if k in r}})
     out = {"legendre": leg, "scf": scf}
     with open(os.path.join(HERE, "diatomic.json"), "w") as f:
         json.dump(out, f, indent=0)
