@@ -712,6 +712,26 @@ def run_n2(args):
     j_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
     k_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
     value = ws * args.steps / (ms * 1e-3)
+    # DFT form of the same Fock build: J plus the PBE potential on the pure-m
+    # grid (the XC path of the reference's diatomic driver at symmetry >= 1)
+    xid, cid = hg.parse_xc("gga_x_pbe-gga_c_pbe")
+    Hx = torch.empty_like(Pd)
+    en = torch.zeros(2, dtype=torch.float64, device="cuda")
+    d.xc(xid, cid, Pd, Hx, energies=en, stream=stream)  # first call builds the grid
+    torch.cuda.synchronize()
+    x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nx = 5
+    x0.record(stream)
+    for _ in range(nx):
+        d.xc(xid, cid, Pd, Hx, energies=en, stream=stream)
+    x1.record(stream)
+    torch.cuda.synchronize()
+    xc_ms = x0.elapsed_time(x1) / nx
+    dft = {"functional": "gga_x_pbe-gga_c_pbe (restricted)", "xc_ms": xc_ms, "coulomb_ms": j_ms,
+           "fock_builds_per_s": 1e3 / (j_ms + xc_ms), "exc_eh": float(en[0]), "nel_on_grid": float(en[1]),
+           "grid": "5 nnodes Chebyshev mu points per element x (4 lmax + 12) Chebyshev cos(nu) points, "
+                   "phi analytic", "path": "hfg_diatomic_coulomb + hfg_diatomic_xc (device pointers)"}
+    del Hx
     Ecoul = 0.5 * float((Pd * Jd).sum())
     Exx = 0.5 * float((Pa * Kd).sum()) * 2.0
     # end to end through the host-pointer drop-ins (pinned host buffers)
@@ -751,6 +771,7 @@ def run_n2(args):
                 + ", symmetric exchange mode",
         "kernel_ms": {"coulomb": j_ms, "exchange": k_ms},
         "plain_fp64": plain,
+        "dft": dft,
         "energies_eh": {"coulomb": Ecoul, "exchange": Exx},
         "roofline": ({"bound": "fp32", "kernel": "dk_tiles_split (whole exchange call)",
                       "achieved": achieved * 12.0, "peak": fp32_peak_tflops(torch), "unit": "TFLOP/s",

@@ -80,29 +80,31 @@ struct DevDiatomicScratch {
 #define DNORM_SPLIT 8
 
 // pure-m DFT grid: nq mu points per element, na nu points, npair same-m
-// ordered angular pairs (s, t)
+// unordered angular pairs (s <= t)
 struct DevDiatomicXC {
-  int nq = 0, na = 0, npair = 0;
+  int nq = 0, na = 0, npair = 0, nbf = 0;
   const int* ps = nullptr;     // [npair]
   const int* pt = nullptr;
-  const int* prev = nullptr;   // index of (t, s)
-  const double* W = nullptr;   // [k*na + a]
-  const double* Wt = nullptr;
+  const double* mult = nullptr;  // 2 (s != t) or 1
+  const double* W = nullptr;   // [k*na + a]: Y_s Y_t
+  const double* Wt = nullptr;  //             Y_s' Y_t + Y_s Y_t'
   const double* R = nullptr;   // [(e*nq + q)*nn + p]
   const double* dR = nullptr;
   const double* w = nullptr;   // [(e*nq + q)*na + a]
   const double* hinv = nullptr;
+  const int* off = nullptr;    // [nang] pure index of (s, start[s])
+  const int* start = nullptr;  // [nang] first kept radial function of shell s
 };
 struct DiatomicXcScratch {
-  double* D;      // [nsd][nel][nq][npair]
-  double* Dr;     // same
+  double* D;      // [nsd][nel][nq][npair]  mult * B^T P_st B
+  double* Dr;     // same                   mult/2 * (dB^T P_st B + B^T P_st dB)
   double* F;      // [nout][3][nel][nq][na]
   double* U;      // [nout][3][nel][npair][nq]
   double* epart;  // [nel*nq][2]
 };
 // Pb == nullptr: restricted (Pa is the total density, Ha the potential).
-// Densities and potentials are in the dummy basis (nd x nd); H is
-// overwritten. energies (device, may be null) receives {Exc, Nel}.
+// Densities and potentials are in the pure basis (nbf x nbf, column-major);
+// H is overwritten. energies (device, may be null) receives {Exc, Nel}.
 cudaError_t launch_diatomic_xc(const DevDiatomic& D, const DevDiatomicXC& X, const DiatomicXcScratch& S, int xid,
                                int cid, const double* Pa, const double* Pb, double* Ha, double* Hb, double* energies,
                                double thr, cudaStream_t st);

@@ -5,19 +5,23 @@
 // and 306-369 density and gradient, 480-530 and 575-650 Fock increments,
 // 668-712 element loop) in separable form. On mu element e, at mu point q and
 // nu point a, the dummy function (s, p) has the value Y_s(a) B_p(q); only
-// same-m angular pairs k = (s, t) couple. With
-//   D_k(q)  = B(q)^T P_st B(q),   Dr_k(q) = dB(q)^T P_st B(q)
+// same-m angular pairs couple. Everything is symmetric under s <-> t, so the
+// sums run over unordered pairs k = (s <= t) with multiplicity c_k = 2 (s != t)
+// or 1. With
+//   D_k(q)  = c_k B(q)^T P_st B(q)
+//   Dr_k(q) = c_k/2 [dB(q)^T P_st B(q) + B(q)^T P_st dB(q)]
 // the density and its gradient components along mu and nu are
-//   rho(q,a) = sum_k D_k(q) W_k(a),        W_k  = Y_s Y_t
+//   rho(q,a) = sum_k D_k(q) W_k(a),          W_k  = Y_s Y_t
 //   g_mu     = 2/h sum_k Dr_k(q) W_k(a)
-//   g_nu     = 2/h sum_k D_k(q) Wt_k(a),   Wt_k = (dY_s/dnu) Y_t
-// and the Fock tile of pair k on element e is
-//   V_{(s,i),(t,j)} = sum_q B_i B_j U0_k(q) + X + X^T,
-//   X_{(s,i),(t,j)} = sum_q [dB_i B_j Umu_k(q) + B_i B_j Unu_k(q)],
-//   Uc_k(q) = sum_a f_c(q,a) Wc_k(a)
+//   g_nu     = 1/h sum_k D_k(q) Wt_k(a),     Wt_k = Y_s' Y_t + Y_s Y_t'
+// and the Fock tile of pair k on element e (the X + X^T of the reference
+// summed over both orders of the pair) is the symmetric nn x nn matrix
+//   V_ij = sum_q B_i B_j (U0_k + Unu_k) + (dB_i B_j + B_i dB_j) Umu_k,
+//   U0_k = sum_a f_0 W_k,  Umu_k = sum_a f_mu W_k,  Unu_k = sum_a f_nu Wt_k
 // with f_0 = w v_rho and f_c = w (2 v_ss g_c,s + v_ab g_c,s') / h
 // (dftgrid_purem.cpp:509-528, 594-615). The same quadrature sums as the
-// reference.
+// reference. Densities are read and potentials written in the pure basis
+// directly (the mu = 0 function of an m != 0 shell is absent).
 //
 // Kernels: dxc_rad (D, Dr), dxc_point (density, functional, point weights,
 // energy partials), dxc_ang (U), dxc_fock (tiles, shared-boundary corner),
@@ -50,21 +54,29 @@ __device__ double block_sum(double v, double* red) {
 
 __device__ __forceinline__ int dgfun(const DevDiatomic& D, int e, int p) { return e * (D.nn - 1) + p; }
 
+// pure index of radial function g of shell s, or -1 where the function is
+// not in the pure basis
+__device__ __forceinline__ int dpure(const DevDiatomic& D, const DevDiatomicXC& X, int s, int g) {
+  const int st = X.start[s];
+  return (g >= st && g < D.nrad) ? X.off[s] + g - st : -1;
+}
+
 // D[s][e][q][k], Dr likewise; grid (nel, npair, nsd)
 __global__ void dxc_rad(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, const double* __restrict__ P0,
                         const double* __restrict__ P1) {
   const int e = blockIdx.x, k = blockIdx.y, s = blockIdx.z;
   const int nn = D.nn, nq = X.nq;
   const int sa = X.ps[k], ta = X.pt[k];
+  const double c = X.mult[k];
   const double* P = s ? P1 : P0;
   extern __shared__ double sm[];
-  double* Pt = sm;            // nn*nn
+  double* Pt = sm;            // nn*nn, rows (sa, i), columns (ta, j)
   double* R = Pt + nn * nn;   // nq*nn
   double* dR = R + nq * nn;   // nq*nn
   for (int idx = threadIdx.x; idx < nn * nn; idx += blockDim.x) {
     const int i = idx % nn, j = idx / nn;
-    const int gi = dgfun(D, e, i), gj = dgfun(D, e, j);
-    Pt[idx] = (gi < D.nrad && gj < D.nrad) ? P[(size_t)(ta * D.nrad + gj) * D.nd + (size_t)sa * D.nrad + gi] : 0.0;
+    const int pi = dpure(D, X, sa, dgfun(D, e, i)), pj = dpure(D, X, ta, dgfun(D, e, j));
+    Pt[idx] = (pi >= 0 && pj >= 0) ? P[(size_t)pj * X.nbf + pi] : 0.0;
   }
   for (int idx = threadIdx.x; idx < nq * nn; idx += blockDim.x) {
     R[idx] = X.R[(size_t)e * nq * nn + idx];
@@ -76,18 +88,18 @@ __global__ void dxc_rad(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, con
     const double* dRq = dR + q * nn;
     double d = 0.0, dr = 0.0;
     for (int j = 0; j < nn; ++j) {
-      double t = 0.0, td = 0.0;
+      double t = 0.0, u = 0.0;  // (P R)_j-column partials: t = sum_i R_i P_ij, u = sum_i dR_i P_ij
       for (int i = 0; i < nn; ++i) {
         const double p = Pt[i + j * nn];
         t += Rq[i] * p;
-        td += dRq[i] * p;
+        u += dRq[i] * p;
       }
       d += t * Rq[j];
-      dr += td * Rq[j];
+      dr += u * Rq[j] + t * dRq[j];
     }
     const size_t o = (((size_t)s * D.nel + e) * nq + q) * X.npair + k;
-    S.D[o] = d;
-    S.Dr[o] = dr;
+    S.D[o] = c * d;
+    S.Dr[o] = 0.5 * c * dr;
   }
 }
 
@@ -137,7 +149,7 @@ __global__ void dxc_point(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, i
     double g[2][2];
     for (int s = 0; s < 2; ++s) {
       g[s][0] = 2.0 * gm[s] * hinv;
-      g[s][1] = 2.0 * gn[s] * hinv;
+      g[s][1] = gn[s] * hinv;
     }
     if (!polarized) {  // restricted: equal spin densities from the total P
       rho[0] *= 0.5;
@@ -203,43 +215,58 @@ __global__ void dxc_ang(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, int
   }
 }
 
-__device__ __forceinline__ double dfock_value(const DevDiatomic& D, const DevDiatomicXC& X,
-                                              const DiatomicXcScratch& S, int o, int e, int k, int i, int j,
-                                              int gga) {
-  const int nq = X.nq, nn = D.nn, np = X.npair;
-  const double* R = X.R + (size_t)e * nq * nn;
-  const double* dR = X.dR + (size_t)e * nq * nn;
-  auto U = [&](int c, int kk) { return S.U + ((((size_t)o * 3 + c) * D.nel + e) * np + kk) * nq; };
-  const double* U0 = U(0, k);
-  double v = 0.0;
-  for (int q = 0; q < nq; ++q) v += R[q * nn + i] * R[q * nn + j] * U0[q];
-  if (gga) {
-    const int kr = X.prev[k];
-    const double *Um = U(1, k), *Un = U(2, k), *Vm = U(1, kr), *Vn = U(2, kr);
-    for (int q = 0; q < nq; ++q) {
-      const double Ri = R[q * nn + i], Rj = R[q * nn + j];
-      v += dR[q * nn + i] * Rj * Um[q] + Ri * Rj * Un[q];  // X
-      v += dR[q * nn + j] * Ri * Vm[q] + Ri * Rj * Vn[q];  // X^T
-    }
-  }
-  return v;
-}
-
-// grid (npair, nel, nout); H written on the element-diagonal tiles of the
-// same-m blocks (the rest of H is zero)
+// grid (npair, nel, nout); writes the (s, t) tile and, for s != t, its
+// transpose into the (t, s) block of the pure H (the rest of H is zero)
 __global__ void dxc_fock(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, int gga, double* __restrict__ H0,
                          double* __restrict__ H1) {
   const int k = blockIdx.x, e = blockIdx.y, o = blockIdx.z;
-  const int nn = D.nn, sa = X.ps[k], ta = X.pt[k];
+  const int nn = D.nn, nq = X.nq, np = X.npair;
+  const int sa = X.ps[k], ta = X.pt[k];
   double* H = o ? H1 : H0;
+  extern __shared__ double sm[];
+  double* R = sm;             // nq*nn
+  double* dR = R + nq * nn;   // nq*nn
+  double* Us = dR + nq * nn;  // nq: U0 + Unu
+  double* Um = Us + nq;       // nq: Umu
+  __shared__ double corner;
+  auto U = [&](int c, int ee) { return S.U + ((((size_t)o * 3 + c) * D.nel + ee) * np + k) * nq; };
+  for (int idx = threadIdx.x; idx < nq * nn; idx += blockDim.x) {
+    R[idx] = X.R[(size_t)e * nq * nn + idx];
+    dR[idx] = X.dR[(size_t)e * nq * nn + idx];
+  }
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    Us[q] = U(0, e)[q] + (gga ? U(2, e)[q] : 0.0);
+    Um[q] = gga ? U(1, e)[q] : 0.0;
+  }
+  // the first function of element e is the last of element e-1: its diagonal
+  // value there, V_{nn-1,nn-1}(e-1)
+  if (threadIdx.x < 32) {
+    double c = 0.0;
+    if (e > 0) {
+      const double* Rp = X.R + (size_t)(e - 1) * nq * nn;
+      const double* dRp = X.dR + (size_t)(e - 1) * nq * nn;
+      for (int q = threadIdx.x; q < nq; q += 32) {
+        const double r = Rp[q * nn + nn - 1], dr = dRp[q * nn + nn - 1];
+        c += r * r * (U(0, e - 1)[q] + (gga ? U(2, e - 1)[q] : 0.0)) + (gga ? 2.0 * dr * r * U(1, e - 1)[q] : 0.0);
+      }
+    }
+    c = warp_sum(c);
+    if (threadIdx.x == 0) corner = c;
+  }
+  __syncthreads();
   for (int idx = threadIdx.x; idx < nn * nn; idx += blockDim.x) {
     const int i = idx % nn, j = idx / nn;
     if (i == nn - 1 && j == nn - 1) continue;  // owned by the next element (or dropped)
-    const int gi = dgfun(D, e, i), gj = dgfun(D, e, j);
-    if (gi >= D.nrad || gj >= D.nrad) continue;
-    double v = dfock_value(D, X, S, o, e, k, i, j, gga);
-    if (i == 0 && j == 0 && e > 0) v += dfock_value(D, X, S, o, e - 1, k, nn - 1, nn - 1, gga);
-    H[(size_t)(ta * D.nrad + gj) * D.nd + (size_t)sa * D.nrad + gi] = v;
+    const int pi = dpure(D, X, sa, dgfun(D, e, i)), pj = dpure(D, X, ta, dgfun(D, e, j));
+    if (pi < 0 || pj < 0) continue;
+    double v = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      const double Ri = R[q * nn + i], Rj = R[q * nn + j];
+      v += Ri * (Rj * Us[q] + dR[q * nn + j] * Um[q]) + dR[q * nn + i] * Rj * Um[q];
+    }
+    if (i == 0 && j == 0) v += corner;
+    H[(size_t)pj * X.nbf + pi] = v;
+    if (sa != ta) H[(size_t)pi * X.nbf + pj] = v;
   }
 }
 
@@ -268,16 +295,18 @@ cudaError_t launch_diatomic_xc(const DevDiatomic& D, const DevDiatomicXC& X, con
   const bool gga = xc_func_is_gga(xid) || xc_func_is_gga(cid);
   const int ncomp = gga ? 3 : 1;
   if (X.na > 1024 || X.npair <= 0) return cudaErrorInvalidValue;
-  const size_t bytes = sizeof(double) * (size_t)D.nd * D.nd;
+  const size_t bytes = sizeof(double) * (size_t)X.nbf * X.nbf;
   cudaError_t err = cudaMemsetAsync(Ha, 0, bytes, st);
   if (err == cudaSuccess && polarized) err = cudaMemsetAsync(Hb, 0, bytes, st);
   if (err != cudaSuccess) return err;
-  dxc_rad<<<dim3(D.nel, X.npair, nsd), 128, sizeof(double) * (D.nn * D.nn + 2 * X.nq * D.nn), st>>>(D, X, S, Pa,
-                                                                                                   Pb);
+  const int tq = ((X.nq + 31) / 32) * 32;
+  dxc_rad<<<dim3(D.nel, X.npair, nsd), tq, sizeof(double) * (D.nn * D.nn + 2 * X.nq * D.nn), st>>>(D, X, S, Pa,
+                                                                                                  Pb);
   const int tp = ((X.na + 31) / 32) * 32;
   dxc_point<<<dim3(D.nel, X.nq), tp, 0, st>>>(D, X, S, xid, cid, gga ? 1 : 0, nsd, polarized ? 1 : 0, thr);
   dxc_ang<<<dim3(D.nel, X.nq, nout), 256, sizeof(double) * ncomp * X.na, st>>>(D, X, S, ncomp);
-  dxc_fock<<<dim3(X.npair, D.nel, nout), ((D.nn * D.nn + 31) / 32) * 32, 0, st>>>(D, X, S, gga ? 1 : 0, Ha, Hb);
+  dxc_fock<<<dim3(X.npair, D.nel, nout), ((D.nn * D.nn + 31) / 32) * 32, sizeof(double) * (2 * X.nq * D.nn + 2 * X.nq),
+             st>>>(D, X, S, gga ? 1 : 0, Ha, Hb);
   if (energies) dxc_energy<<<1, 512, 0, st>>>(S.epart, D.nel * X.nq, energies);
   return cudaGetLastError();
 }

@@ -29,7 +29,7 @@ struct hfg_diatomic {
   hfg::DevDiatomicXC xc{};
   hfg::DiatomicXcScratch xs{};
   bool xc_ready = false;
-  DBuf x_ps, x_pt, x_prev, x_W, x_Wt, x_R, x_dR, x_w, x_hinv, xs_D, xs_Dr, xs_F, xs_U, xs_ep, s_Pd2, s_Fd2, h_in2,
+  DBuf x_ps, x_pt, x_mult, x_W, x_Wt, x_R, x_dR, x_w, x_hinv, x_off, x_start, xs_D, xs_Dr, xs_F, xs_U, xs_ep, h_in2,
       h_out2, h_e;
 
   ~hfg_diatomic() {
@@ -221,9 +221,12 @@ struct hfg_diatomic {
     xc.nq = H.xc_nq;
     xc.na = H.xc_lang;
     xc.npair = H.xc_npair;
+    xc.nbf = H.nbf;
     xc.ps = x_ps.upload(H.xc_ps);
     xc.pt = x_pt.upload(H.xc_pt);
-    xc.prev = x_prev.upload(H.xc_prev);
+    xc.mult = x_mult.upload(H.xc_mult);
+    xc.off = x_off.upload(H.xc_off);
+    xc.start = x_start.upload(H.xc_start);
     xc.W = x_W.upload(H.xc_W);
     xc.Wt = x_Wt.upload(H.xc_Wt);
     xc.R = x_R.upload(H.xc_R);
@@ -251,21 +254,7 @@ struct hfg_diatomic {
                 double thr, cudaStream_t st) {
     check_device();
     if (!xc_ready) setup_xc(0);
-    const hfg::DiatomicHost& H = host;
-    if (Pb && s_Pd2.n == 0) {
-      hfg_abi::AllocStream alloc_on(own_stream);
-      s_Pd2.alloc(sizeof(double) * (size_t)H.ndummy * H.ndummy);
-      s_Fd2.alloc(sizeof(double) * (size_t)H.ndummy * H.ndummy);
-      ck(cudaStreamSynchronize(own_stream), "sync");
-    }
-    const int* pure = d_pure.as<int>();
-    ck(hfg::launch_diatomic_expand(Pa, H.nbf, pure, s_Pd.as<double>(), H.ndummy, st), "expand");
-    if (Pb) ck(hfg::launch_diatomic_expand(Pb, H.nbf, pure, s_Pd2.as<double>(), H.ndummy, st), "expand");
-    ck(hfg::launch_diatomic_xc(dev, xc, xs, xid, cid, s_Pd.as<double>(), Pb ? s_Pd2.as<double>() : nullptr,
-                               s_Fd.as<double>(), Pb ? s_Fd2.as<double>() : nullptr, energies, thr, st),
-       "xc kernels");
-    ck(hfg::launch_diatomic_gather(s_Fd.as<double>(), H.ndummy, pure, H.nbf, Ha, st), "gather");
-    if (Pb) ck(hfg::launch_diatomic_gather(s_Fd2.as<double>(), H.ndummy, pure, H.nbf, Hb, st), "gather");
+    ck(hfg::launch_diatomic_xc(dev, xc, xs, xid, cid, Pa, Pb, Ha, Hb, energies, thr, st), "xc kernels");
     mark_use(st);
   }
 

@@ -71,14 +71,17 @@ struct DiatomicHost {
 
   // ---- pure-m DFT grid (src/diatomic/dftgrid_purem.cpp:34-199) -----------
   // Per mu element: xc_nq Chebyshev points in mu; xc_lang Chebyshev points in
-  // cos(nu); the phi integral is analytic (2 pi). Only the same-m angular
-  // pairs (s, t) couple; pair k has xc_ps[k] = s, xc_pt[k] = t and
-  // xc_prev[k] = the index of (t, s).
+  // cos(nu); the phi integral is analytic (2 pi). Only same-m angular pairs
+  // couple, and every quantity is symmetric under s <-> t, so the tables run
+  // over unordered pairs k = (s <= t): xc_ps[k] = s, xc_pt[k] = t,
+  // xc_mult[k] = 2 (s != t) or 1.
   int xc_lang = 0, xc_nq = 0, xc_npair = 0;
-  std::vector<int> xc_ps, xc_pt, xc_prev;
-  std::vector<double> xc_W, xc_Wt;     // [k*lang + a]: Y_s Y_t, (dY_s/dnu) Y_t at phi = 0
+  std::vector<int> xc_ps, xc_pt;
+  std::vector<double> xc_mult;
+  std::vector<double> xc_W, xc_Wt;     // [k*lang + a]: Y_s Y_t and Y_s' Y_t + Y_s Y_t' (phi = 0)
   std::vector<double> xc_R, xc_dR;     // [(e*nq + q)*nn + p]: B_p, dB_p/dmu
   std::vector<double> xc_w, xc_hinv;   // [(e*nq + q)*lang + a]: weight, 1/h
+  std::vector<int> xc_off, xc_start;   // [s]: pure index of (s, xc_start[s]); first kept radial function
   void build_xc_grid(int lang);
 
   void build(int Z1, int Z2, double Rhalf, int nnodes, const std::vector<double>& bval,

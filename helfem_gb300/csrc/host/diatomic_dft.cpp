@@ -13,7 +13,8 @@
 //
 // Everything the device needs factorises into per-(element, mu point) radial
 // rows, per-(element, point) weights and per-(pair, nu point) angular
-// products, as in the atomic grid.
+// products, as in the atomic grid. The pairs are unordered (s <= t): the
+// density, the potential and the Fock tiles are symmetric under s <-> t.
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
@@ -53,28 +54,35 @@ void DiatomicHost::build_xc_grid(int lang) {
       dY[(size_t)s * na + a] = d;
     }
   }
-  // same-m ordered pairs
+  // same-m unordered pairs s <= t
   xc_ps.clear();
   xc_pt.clear();
-  std::vector<int> index((size_t)nang * nang, -1);
+  xc_mult.clear();
   for (int t = 0; t < nang; ++t)
-    for (int s = 0; s < nang; ++s)
+    for (int s = 0; s <= t; ++s)
       if (mval[s] == mval[t]) {
-        index[s + (size_t)t * nang] = (int)xc_ps.size();
         xc_ps.push_back(s);
         xc_pt.push_back(t);
+        xc_mult.push_back(s == t ? 1.0 : 2.0);
       }
   xc_npair = (int)xc_ps.size();
-  xc_prev.resize(xc_npair);
   xc_W.assign((size_t)xc_npair * na, 0.0);
   xc_Wt.assign((size_t)xc_npair * na, 0.0);
   for (int k = 0; k < xc_npair; ++k) {
     const int s = xc_ps[k], t = xc_pt[k];
-    xc_prev[k] = index[t + (size_t)s * nang];
     for (int a = 0; a < na; ++a) {
-      xc_W[(size_t)k * na + a] = Y[(size_t)s * na + a] * Y[(size_t)t * na + a];
-      xc_Wt[(size_t)k * na + a] = dY[(size_t)s * na + a] * Y[(size_t)t * na + a];
+      const size_t ia = (size_t)s * na + a, ib = (size_t)t * na + a;
+      xc_W[(size_t)k * na + a] = Y[ia] * Y[ib];
+      xc_Wt[(size_t)k * na + a] = dY[ia] * Y[ib] + Y[ia] * dY[ib];
     }
+  }
+  // pure index of (s, g) = xc_off[s] + g - xc_start[s] (basis.cpp:712-736)
+  xc_off.assign(nang, 0);
+  xc_start.assign(nang, 0);
+  for (int s = 0, o = 0; s < nang; ++s) {
+    xc_start[s] = mval[s] == 0 ? 0 : 1;
+    xc_off[s] = o;
+    o += nrad - xc_start[s];
   }
   // radial rows and point weights
   std::vector<double> xq, wq;

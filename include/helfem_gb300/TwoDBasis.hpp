@@ -9,6 +9,8 @@
 //            kinetic / nuclear           (src/diatomic/basis.h:300-337)
 //   DFTGrid::eval_Fxc(x, c, P, H, Exc, Nel, thr) and the Pa/Pb overload
 //                                        (src/atomic/dftgrid.h:156-159)
+//   diatomic PureMDFTGrid::eval_Fxc, both overloads
+//                                        (src/diatomic/dftgrid_purem.h:154-161)
 //
 // Matrix is any column-major dense type with Matrix(rows, cols), rows(),
 // cols() and data() (Eigen::MatrixXd, helfem::Matrix). Status codes come back
@@ -221,6 +223,49 @@ class DiatomicTwoDBasis {
   std::vector<double> bval_;
   std::vector<int> lval_, mval_;
   std::unique_ptr<hfg_diatomic, Del> host_, gpu_;
+};
+
+// PureMDFTGrid over a diatomic basis: the XC potential when the orbitals do
+// not mix m. lang = 0 takes the reference default 4 lmax + 12. External
+// functional parameters are not supported (the x_pars/c_pars arguments of the
+// reference are absent); Ekin of meta-GGAs is not part of this path and
+// returns 0. `beta` is accepted for signature compatibility: Hb is always
+// assigned, zero when the beta density is zero (dftgrid_purem.cpp:731-742).
+template <class Matrix>
+class DiatomicPureMDFTGrid {
+ public:
+  DiatomicPureMDFTGrid(const DiatomicTwoDBasis<Matrix>* basis, int lang) : b_(basis), lang_(lang) {}
+  void eval_Fxc(int x_func, int c_func, const Matrix& P, Matrix& H, double& Exc, double& Nel, double& Ekin,
+                double thr) const {
+    prepare();
+    detail::require_square(P, b_->Nbf(), "eval_Fxc");
+    H = Matrix(P.rows(), P.cols());
+    check(hfg_diatomic_xc_host(b_->handle(), x_func, c_func, P.data(), nullptr, H.data(), nullptr, &Exc, &Nel, thr));
+    Ekin = 0.0;
+  }
+  void eval_Fxc(int x_func, int c_func, const Matrix& Pa, const Matrix& Pb, Matrix& Ha, Matrix& Hb, double& Exc,
+                double& Nel, double& Ekin, bool /*beta*/, double thr) const {
+    prepare();
+    detail::require_square(Pa, b_->Nbf(), "eval_Fxc");
+    detail::require_square(Pb, b_->Nbf(), "eval_Fxc");
+    Ha = Matrix(Pa.rows(), Pa.cols());
+    Hb = Matrix(Pb.rows(), Pb.cols());
+    check(hfg_diatomic_xc_host(b_->handle(), x_func, c_func, Pa.data(), Pb.data(), Ha.data(), Hb.data(), &Exc, &Nel,
+                               thr));
+    Ekin = 0.0;
+  }
+
+ private:
+  void prepare() const {
+    if (!b_->handle()) detail::no_tei();
+    if (!built_) {
+      check(hfg_diatomic_dft_grid(b_->handle(), lang_));
+      built_ = true;
+    }
+  }
+  const DiatomicTwoDBasis<Matrix>* b_;
+  int lang_;
+  mutable bool built_ = false;
 };
 
 }  // namespace helfem_gb300

@@ -36,8 +36,23 @@ import math
 import numpy as np
 
 from . import xc as xcmod
-from .diatomic import DiatomicTables
+from .diatomic import DiatomicTables, MuBasis, get_grid, lm_maps, lm_to_l_m
 from .tabulate import chebyshev, lip_eval, lobatto, theta_lm
+
+
+def grid_tables(Z1: int, Z2: int, Rbond: float, nnodes: int, nelem: int, lmmax, Rmax: float = 40.0,
+                igrid: int = 4, zexp: float = 1.0) -> DiatomicTables:
+    """The basis geometry alone (no integrals): enough for the XC grid, whose
+    inputs are the element boundaries, the angular functions and Rhalf."""
+    Rhalf = 0.5 * Rbond
+    bval = get_grid(math.acosh(Rmax / Rhalf), nelem, igrid, zexp)
+    rb = MuBasis(nnodes, bval)
+    lval, mval = lm_to_l_m(lmmax)
+    lm, LM = lm_maps(lval, mval)
+    first = np.array([rb.first(e) for e in range(rb.nel)])
+    ni = np.array([len(rb.enabled(e)) for e in range(rb.nel)])
+    return DiatomicTables(Z1, Z2, Rhalf, nnodes, np.asarray(bval, float), lval, mval, rb.nrad, first, ni, lm, LM,
+                          [], [], [], [], [], [])
 
 
 class PureMGrid:
@@ -98,20 +113,39 @@ class PureMGrid:
             dr = np.einsum("sa,qj->sjqa", Y, dB).reshape(len(sh) * len(en), -1)
             dt = np.einsum("sa,qj->sjqa", dY, B).reshape(len(sh) * len(en), -1)
             idx = np.concatenate([ia * tab.nrad + first + en for ia in sh])
-            blocks.append((idx, bf, dr, dt))
+            blocks.append((m, idx, bf, dr, dt))
         res = dict(w=w.ravel(), h=h.ravel(), blocks=blocks)
-        self._cache[iel] = res
+        # keep small grids; large ones are rebuilt element by element
+        if sum(b[2].nbytes for b in blocks) * 3 * tab.nel < 2e9:
+            self._cache[iel] = res
         return res
 
-    def eval_Fxc(self, names, Pa, Pb, thr=1e-12):
-        """Return (Ha, Hb, Exc, Nel) in the pure basis for spin densities
-        Pa, Pb given in the pure basis."""
+    def mblocks(self):
+        """{m: (pure positions, dummy indices)} of every symmetry block."""
+        tab = self.tab
+        pidx = tab.pure_indices()
+        mv = tab.mval[pidx // tab.nrad]
+        return {m: (np.where(mv == m)[0], pidx[mv == m]) for m in self.mlist}
+
+    def eval_Fxc_blocks(self, names, Pa, Pb, thr=1e-12):
+        """The (m, m) blocks only: Pa, Pb map m -> the block of the spin
+        density over the block's pure functions (ascending pure index).
+        Returns ({m: Ha_m}, {m: Hb_m}, Exc, Nel)."""
         tab = self.tab
         gga = any(xcmod.FUNCTIONALS[f][0] == "gga" for f in names)
-        Pad, Pbd = tab.expand(Pa), tab.expand(Pb)
-        nd = tab.ndummy
-        Ha = np.zeros((nd, nd))
-        Hb = np.zeros((nd, nd))
+        mb = self.mblocks()
+        loc, Pae, Pbe, Hae, Hbe = {}, {}, {}, {}, {}
+        for m, (_, dum) in mb.items():
+            n = len(dum)
+            lm = np.full(tab.ndummy, n)  # dropped boundary functions -> a zero row
+            lm[dum] = np.arange(n)
+            loc[m] = lm
+            for src, dst in ((Pa, Pae), (Pb, Pbe)):
+                X = np.zeros((n + 1, n + 1))
+                X[:n, :n] = src[m]
+                dst[m] = X
+            Hae[m] = np.zeros((n + 1, n + 1))
+            Hbe[m] = np.zeros((n + 1, n + 1))
         Exc = Nel = 0.0
         for iel in range(tab.nel):
             E = self.element(iel)
@@ -120,9 +154,10 @@ class PureMGrid:
             rb = np.zeros_like(w)
             ga = [np.zeros_like(w), np.zeros_like(w)]
             gb = [np.zeros_like(w), np.zeros_like(w)]
-            for idx, bf, dr, dt in E["blocks"]:
-                for P, rho, g in ((Pad, ra, ga), (Pbd, rb, gb)):
-                    Pv = P[np.ix_(idx, idx)] @ bf
+            for m, idx, bf, dr, dt in E["blocks"]:
+                li = loc[m][idx]
+                for P, rho, g in ((Pae[m], ra, ga), (Pbe[m], rb, gb)):
+                    Pv = P[np.ix_(li, li)] @ bf
                     rho += np.sum(Pv * bf, axis=0)
                     if gga:
                         g[0] += 2 * np.sum(Pv * dr, axis=0) / h
@@ -136,8 +171,8 @@ class PureMGrid:
                 saa = sab = sbb = None
             e, va, vb, vaa, vab, vbb = xcmod.eval_functionals(names, ra, rb, saa, sab, sbb, thr)
             Exc += float(np.sum(w * e))
-            for H, v, gown, goth, vss in ((Ha, va, ga, gb, vaa), (Hb, vb, gb, ga, vbb)):
-                for idx, bf, dr, dt in E["blocks"]:
+            for H, v, gown, goth, vss in ((Hae, va, ga, gb, vaa), (Hbe, vb, gb, ga, vbb)):
+                for m, idx, bf, dr, dt in E["blocks"]:
                     M = (bf * (w * v)) @ bf.T
                     if gga:
                         X = np.zeros_like(M)
@@ -145,5 +180,20 @@ class PureMGrid:
                             coef = w * (2 * vss * gown[c] + vab * goth[c]) / h
                             X += (dbf * coef) @ bf.T
                         M += X + X.T
-                    H[np.ix_(idx, idx)] += M
-        return tab.remove(Ha), tab.remove(Hb), Exc, Nel
+                    li = loc[m][idx]
+                    H[m][np.ix_(li, li)] += M
+        strip = lambda H: {m: X[:-1, :-1] for m, X in H.items()}
+        return strip(Hae), strip(Hbe), Exc, Nel
+
+    def eval_Fxc(self, names, Pa, Pb, thr=1e-12):
+        """Return (Ha, Hb, Exc, Nel) in the pure basis for spin densities
+        Pa, Pb given in the pure basis (only their (m, m) blocks enter)."""
+        mb = self.mblocks()
+        blk = lambda P: {m: P[np.ix_(pos, pos)] for m, (pos, _) in mb.items()}
+        Hab, Hbb, Exc, Nel = self.eval_Fxc_blocks(names, blk(Pa), blk(Pb), thr)
+        Ha = np.zeros_like(Pa)
+        Hb = np.zeros_like(Pb)
+        for m, (pos, _) in mb.items():
+            Ha[np.ix_(pos, pos)] = Hab[m]
+            Hb[np.ix_(pos, pos)] = Hbb[m]
+        return Ha, Hb, Exc, Nel

@@ -65,6 +65,17 @@ int main(int argc, char** argv) {
     for (long j = 0; j < Pd.cols(); ++j) Pd(i, j) = 1e-3 / (1.0 + i + j);
   Mat Jd = mol.coulomb(Pd), Kd = mol.exchange(Pd);
   std::printf("diatomic trPJ %.15e trPK %.15e\n", trace_prod(Pd, Jd), trace_prod(Pd, Kd));
+  // pure-m XC: LDA restricted and PBE unrestricted
+  helfem_gb300::DiatomicPureMDFTGrid<Mat> grid(&mol, 0);
+  Mat Hx, Ha, Hb;
+  double exc = 0.0, nel = 0.0, ekin = 0.0, exc2 = 0.0, nel2 = 0.0;
+  grid.eval_Fxc(1, 7, Pd, Hx, exc, nel, ekin, 1e-12);
+  Mat Pb(mol.Nbf(), mol.Nbf());
+  for (long i = 0; i < Pb.rows(); ++i)
+    for (long j = 0; j < Pb.cols(); ++j) Pb(i, j) = 0.5 * Pd(i, j);
+  grid.eval_Fxc(101, 130, Pd, Pb, Ha, Hb, exc2, nel2, ekin, true, 1e-12);
+  std::printf("diatomic-xc trPH %.15e Exc %.15e Nel %.15e trPHa %.15e trPbHb %.15e Exc2 %.15e\n",
+              trace_prod(Pd, Hx), exc, nel, trace_prod(Pd, Ha), trace_prod(Pb, Hb), exc2);
   try {
     mol.coulomb(Mat(3, 3));
   } catch (const std::runtime_error& e) {

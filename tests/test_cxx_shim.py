@@ -68,4 +68,12 @@ def test_shim_gpu(tmp_path):
     tjd = rd["trPJ"]
     assert abs(tjd - np.sum(Pd * d.coulomb_host(Pd))) < 1e-12 * abs(tjd)
     assert abs(rd["trPK"] - np.sum(Pd * d.exchange_host(Pd))) < 1e-12 * abs(rd["trPK"])
+    rx = numbers(out, "diatomic-xc")
+    H, _, exc, nel = d.xc_host(1, 7, Pd)
+    assert abs(rx["trPH"] - np.sum(Pd * H)) < 1e-12 * abs(rx["trPH"])
+    assert abs(rx["Exc"] - exc) < 1e-12 * abs(exc) and abs(rx["Nel"] - nel) < 1e-12 * abs(nel)
+    Ha, Hb, exc2, _ = d.xc_host(101, 130, Pd, 0.5 * Pd)
+    assert abs(rx["trPHa"] - np.sum(Pd * Ha)) < 1e-12 * abs(rx["trPHa"])
+    assert abs(rx["trPbHb"] - np.sum(0.5 * Pd * Hb)) < 1e-12 * abs(rx["trPbHb"])
+    assert abs(rx["Exc2"] - exc2) < 1e-12 * abs(exc2)
     assert "runtime_error" in out

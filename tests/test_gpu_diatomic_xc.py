@@ -119,3 +119,34 @@ def test_pure_m_dft_energy_through_gpu(name):
     r, ref = run_case(name, fock=lambda D: _GpuJ(d), grid=lambda D: _GpuXC(d))
     assert r.converged
     assert abs(r.Etot + ref["Enucr"] - ref["total"]) < BAR.get(name, 2e-9), (r.Etot + ref["Enucr"], ref["total"])
+
+
+def test_n2_full_size_xc_parity():
+    """The N2 benchmark basis and density (30 mu-elements, l <= 12 for
+    |m| <= 3, 33114 functions): every (m, m) block of the GPU PBE potential
+    against the oracle grid at full size, with Exc and the electron count."""
+    import bench
+    from oracle.diatomic_xc import grid_tables
+    torch = torch_cuda()
+    d, P, _ = bench.n2_setup(hg)
+    D = grid_tables(7, 7, 2.074, 15, 30, [12] * 4)
+    g = PureMGrid(D)
+    mb = g.mblocks()
+    blk = {m: 0.5 * P[np.ix_(pos, pos)] for m, (pos, _) in mb.items()}
+    Hr, _, Er, Nr = g.eval_Fxc_blocks(["gga_x_pbe", "gga_c_pbe"], blk, blk)
+    nbf = d.nbf
+    Pd = torch.zeros((nbf, nbf), dtype=torch.float64, device="cuda")
+    for m, (pos, _) in mb.items():
+        ix = torch.from_numpy(pos).cuda()
+        Pd[ix[:, None], ix[None, :]] = torch.from_numpy(2.0 * blk[m]).cuda()  # symmetric: layout-free
+    Hd = torch.empty_like(Pd)
+    en = torch.zeros(2, dtype=torch.float64, device="cuda")
+    x, c = hg.parse_xc("gga_x_pbe-gga_c_pbe")
+    d.xc(x, c, Pd, Hd, energies=en)
+    torch.cuda.synchronize()
+    del Pd
+    assert abs(float(en[0]) - Er) < 1e-11 * abs(Er) and abs(float(en[1]) - Nr) < 1e-11 * Nr, (en, Er, Nr)
+    for m, (pos, _) in mb.items():
+        ix = torch.from_numpy(pos).cuda()
+        got = Hd[ix[:, None], ix[None, :]].cpu().numpy().T
+        assert relerr(got, Hr[m]) < TOL, (m, relerr(got, Hr[m]))
