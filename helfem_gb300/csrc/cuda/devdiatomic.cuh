@@ -2,7 +2,9 @@
 //
 // Radial layout: element e owns an nn x nn primitive tile; primitive p is the
 // global function g(e,p) = e*(nn-1) + p, valid for g < nrad. Dummy AO index
-// = iang*nrad + irad (nd = nang*nrad); matrices are column-major FP64.
+// = iang*nrad + irad (nd = nang*nrad); the pure index of (s, g) is
+// poff[s] + g - pstart[s] for g >= pstart[s] (m != 0 shells drop g = 0).
+// Matrices are column-major FP64.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,7 +12,9 @@
 namespace hfg {
 
 struct DevDiatomic {
-  int nn, nel, nrad, nang, nd, nlm, rmax, Lmax, mmax, nM;
+  int nn, nel, nrad, nang, nd, nlm, rmax, Lmax, mmax, nM, nbf;
+  const int* poff;       // [nang] pure index of (s, pstart[s])
+  const int* pstart;     // [nang] first radial function of shell s in the pure basis
   // per (ilm, e) padded nn x nn tiles
   const double* p0;
   const double* p2;
@@ -65,7 +69,7 @@ struct DevDiatomic {
 };
 
 struct DevDiatomicScratch {
-  double* jin;            // [nchan*nel*2*nn^2]
+  double* jin;            // [nchan*nel*2*nn^2] in-element channel tiles, then the full channel tiles
   double* jscal;          // [nchan*nel*4]
   double* khalo;          // [nel*nel*nang^2*(2nn-1)]
   double* bnorm;          // [nang^2*DNORM_SPLIT]
@@ -82,7 +86,7 @@ struct DevDiatomicScratch {
 // pure-m DFT grid: nq mu points per element, na nu points, npair same-m
 // unordered angular pairs (s <= t)
 struct DevDiatomicXC {
-  int nq = 0, na = 0, npair = 0, nbf = 0;
+  int nq = 0, na = 0, npair = 0;
   const int* ps = nullptr;     // [npair]
   const int* pt = nullptr;
   const double* mult = nullptr;  // 2 (s != t) or 1
@@ -92,8 +96,12 @@ struct DevDiatomicXC {
   const double* dR = nullptr;
   const double* w = nullptr;   // [(e*nq + q)*na + a]
   const double* hinv = nullptr;
-  const int* off = nullptr;    // [nang] pure index of (s, start[s])
-  const int* start = nullptr;  // [nang] first kept radial function of shell s
+  // Fock-side pairs: tiles built for pairs fk[0..nfock), each also written to
+  // the mirror shells (fms, fmt) of opposite m when fms >= 0
+  int nfock = 0;
+  const int* fk = nullptr;
+  const int* fms = nullptr;
+  const int* fmt = nullptr;
 };
 struct DiatomicXcScratch {
   double* D;      // [nsd][nel][nq][npair]  mult * B^T P_st B
@@ -112,7 +120,8 @@ cudaError_t launch_diatomic_xc(const DevDiatomic& D, const DevDiatomicXC& X, con
 cudaError_t launch_diatomic_expand(const double* P, int nbf, const int* pure, double* Pd, int nd, cudaStream_t st);
 cudaError_t launch_diatomic_gather(const double* Fd, int nd, const int* pure, int nbf, double* F, cudaStream_t st);
 cudaError_t launch_diatomic_tx(const DevDiatomic& D, double* tx, cudaStream_t st);
-cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd, double* Jd,
+// J of a pure-basis density, written to the pure-basis J (overwritten)
+cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScratch& S, const double* P, double* J,
                                     cudaStream_t st);
 cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
                                      double* Kd, bool symmetric, cudaStream_t st);

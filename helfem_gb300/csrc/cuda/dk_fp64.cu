@@ -54,6 +54,13 @@ __device__ double dblock_sum(double v, double* red) {
 }
 
 __device__ __forceinline__ int dgf(const DevDiatomic& D, int e, int p) { return e * (D.nn - 1) + p; }
+
+// pure index of radial function g of shell s, or -1 where it is not in the
+// pure basis (g = 0 of an m != 0 shell, or g >= nrad)
+__device__ __forceinline__ int dpure_idx(const DevDiatomic& D, int s, int g) {
+  const int st = D.pstart[s];
+  return (g >= st && g < D.nrad) ? D.poff[s] + g - st : -1;
+}
 __device__ __forceinline__ int al_idx(const DevDiatomic& D, int a, int L, int M) {
   return (a * (D.Lmax + 1) + L) * D.nM + M + 2 * D.mmax;
 }
@@ -101,7 +108,7 @@ __global__ void d_build_tx(DevDiatomic D, double* __restrict__ tx) {
 }
 
 // ------------------------------------------------------------------ Coulomb
-__global__ void dj_contract(DevDiatomic D, DevDiatomicScratch S, const double* __restrict__ Pd) {
+__global__ void dj_contract(DevDiatomic D, DevDiatomicScratch S, const double* __restrict__ P) {
   const int ch = blockIdx.x, e = blockIdx.y;
   const int nn = D.nn, n2 = nn * nn, L = D.ch_L[ch], M = D.ch_M[ch], ilm = D.ch_ilm[ch];
   const double fac = D.ch_fac[ch];
@@ -115,10 +122,13 @@ __global__ void dj_contract(DevDiatomic D, DevDiatomicScratch S, const double* _
     double x0 = 0.0, x2 = 0.0;
     if (gp < D.nrad && gq < D.nrad)
       for (int k = 0; k < D.nang; ++k) {
+        const int pk = dpure_idx(D, k, gp);
+        if (pk < 0) continue;
         const int ix = al_idx(D, k, L, M);
         for (int u = D.al_ptr[ix]; u < D.al_ptr[ix + 1]; ++u) {
-          const int l = D.al_b[u];
-          const double v = Pd[(size_t)(l * D.nrad + gq) * D.nd + (size_t)k * D.nrad + gp];
+          const int pl = dpure_idx(D, D.al_b[u], gq);
+          if (pl < 0) continue;
+          const double v = P[(size_t)pl * D.nbf + pk];
           x0 += D.al_c0[u] * v;
           x2 += D.al_c2[u] * v;
         }
@@ -170,57 +180,63 @@ __global__ void dj_contract(DevDiatomic D, DevDiatomicScratch S, const double* _
   }
 }
 
-constexpr int DJMAXTERMS = 64;
+// The full potential tiles of channel ch on element e (both multipole
+// channels), in place over the in-element part:
+//   T0 = big_e P0 + small_e Q0 + jin0,  T2 = -big_e P2 - small_e Q2 + jin2,
+// big_e / small_e the traces of the outer / inner elements with the channel
+// signs. grid (nchan, nel)
+__global__ void dj_tiles(DevDiatomic D, DevDiatomicScratch S) {
+  const int ch = blockIdx.x, e = blockIdx.y;
+  const int n2 = D.nn * D.nn;
+  __shared__ double bs[2];
+  if (threadIdx.x == 0) {
+    const double* sc = S.jscal + (size_t)ch * D.nel * 4;
+    double big = 0.0, small = 0.0;
+    for (int e2 = e + 1; e2 < D.nel; ++e2) big += sc[4 * e2 + 1] - sc[4 * e2 + 3];
+    for (int e2 = 0; e2 < e; ++e2) small += sc[4 * e2 + 0] - sc[4 * e2 + 2];
+    bs[0] = big;
+    bs[1] = small;
+  }
+  __syncthreads();
+  const double big = bs[0], small = bs[1];
+  const size_t le = (size_t)D.ch_ilm[ch] * D.nel + e;
+  double* jt = S.jin + ((size_t)ch * D.nel + e) * 2 * n2;
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+    jt[t] += big * D.p0[le * n2 + t] + small * D.q0[le * n2 + t];
+    jt[n2 + t] += -big * D.p2[le * n2 + t] - small * D.q2[le * n2 + t];
+  }
+}
 
-__global__ void dj_scatter(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Jd) {
+// J tile of output block (i, j) on element e = the bra sum of the channel
+// tiles; the shared first function adds element e-1's corner. Written to the
+// pure-basis J. grid (nang^2, nel)
+__global__ void dj_scatter(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ J) {
   const int ij = blockIdx.x, e = blockIdx.y;
   const int i = ij % D.nang, j = ij / D.nang;
   const int b0 = D.jbra_ptr[ij], b1 = D.jbra_ptr[ij + 1];
   const int nt = b1 - b0;
   if (nt == 0) return;
   const int nn = D.nn, n2 = nn * nn;
-  __shared__ double Bg[DJMAXTERMS], Sm[DJMAXTERMS], Bg1[DJMAXTERMS], Sm1[DJMAXTERMS];
-  for (int u = threadIdx.x; u < nt; u += blockDim.x) {
-    const double* sc = S.jscal + (size_t)D.jbra_chan[b0 + u] * D.nel * 4;
-    double big = 0.0, small = 0.0;
-    for (int e2 = e + 1; e2 < D.nel; ++e2) big += sc[4 * e2 + 1] - sc[4 * e2 + 3];
-    for (int e2 = 0; e2 < e; ++e2) small += sc[4 * e2 + 0] - sc[4 * e2 + 2];
-    Bg[u] = big;
-    Sm[u] = small;
-    if (e > 0) {
-      Bg1[u] = big + (sc[4 * e + 1] - sc[4 * e + 3]);
-      Sm1[u] = small - (sc[4 * (e - 1) + 0] - sc[4 * (e - 1) + 2]);
-    }
-  }
-  __syncthreads();
   for (int t = threadIdx.x; t < n2; t += blockDim.x) {
     const int p = t % nn, q = t / nn;
     // the corner on the boundary function shared with the next element is
     // owned by that element's tile
     if (p == nn - 1 && q == nn - 1) continue;
-    const int gp = dgf(D, e, p), gq = dgf(D, e, q);
-    if (gp >= D.nrad || gq >= D.nrad) continue;
+    const int pp = dpure_idx(D, i, dgf(D, e, p)), pq = dpure_idx(D, j, dgf(D, e, q));
+    if (pp < 0 || pq < 0) continue;
     double v = 0.0;
-    for (int u = 0; u < nt; ++u) {
-      const int ch = D.jbra_chan[b0 + u];
-      const size_t le = (size_t)D.ch_ilm[ch] * D.nel + e;
-      const double* jin = S.jin + ((size_t)ch * D.nel + e) * 2 * n2;
-      const double j0 = Bg[u] * D.p0[le * n2 + t] + Sm[u] * D.q0[le * n2 + t] + jin[t];
-      const double j2 = -Bg[u] * D.p2[le * n2 + t] - Sm[u] * D.q2[le * n2 + t] + jin[n2 + t];
-      v += D.jbra_c0[b0 + u] * j0 + D.jbra_c2[b0 + u] * j2;
+    for (int u = b0; u < b1; ++u) {
+      const double* jt = S.jin + ((size_t)D.jbra_chan[u] * D.nel + e) * 2 * n2;
+      v += D.jbra_c0[u] * jt[t] + D.jbra_c2[u] * jt[n2 + t];
     }
     if (p == 0 && q == 0 && e > 0) {
       const int c = (nn - 1) + (nn - 1) * nn;
-      for (int u = 0; u < nt; ++u) {
-        const int ch = D.jbra_chan[b0 + u];
-        const size_t le = (size_t)D.ch_ilm[ch] * D.nel + (e - 1);
-        const double* jin = S.jin + ((size_t)ch * D.nel + (e - 1)) * 2 * n2;
-        const double j0 = Bg1[u] * D.p0[le * n2 + c] + Sm1[u] * D.q0[le * n2 + c] + jin[c];
-        const double j2 = -Bg1[u] * D.p2[le * n2 + c] - Sm1[u] * D.q2[le * n2 + c] + jin[n2 + c];
-        v += D.jbra_c0[b0 + u] * j0 + D.jbra_c2[b0 + u] * j2;
+      for (int u = b0; u < b1; ++u) {
+        const double* jt = S.jin + ((size_t)D.jbra_chan[u] * D.nel + (e - 1)) * 2 * n2;
+        v += D.jbra_c0[u] * jt[c] + D.jbra_c2[u] * jt[n2 + c];
       }
     }
-    Jd[(size_t)(j * D.nrad + gq) * D.nd + (size_t)i * D.nrad + gp] = v;
+    J[(size_t)pq * D.nbf + pp] = v;
   }
 }
 
@@ -660,14 +676,15 @@ cudaError_t launch_diatomic_tx(const DevDiatomic& D, double* tx, cudaStream_t st
   return cudaGetLastError();
 }
 
-cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd, double* Jd,
+cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScratch& S, const double* P, double* J,
                                     cudaStream_t st) {
   const int n2 = D.nn * D.nn, th = dthreads(n2);
-  cudaError_t e = cudaMemsetAsync(Jd, 0, sizeof(double) * (size_t)D.nd * D.nd, st);
+  cudaError_t e = cudaMemsetAsync(J, 0, sizeof(double) * (size_t)D.nbf * D.nbf, st);
   if (e != cudaSuccess) return e;
   const size_t sm1 = sizeof(double) * (2 * n2 + D.rmax + 32);
-  dj_contract<<<dim3(D.nchan, D.nel), th, sm1, st>>>(D, S, Pd);
-  dj_scatter<<<dim3(D.nang * D.nang, D.nel), th, 0, st>>>(D, S, Jd);
+  dj_contract<<<dim3(D.nchan, D.nel), th, sm1, st>>>(D, S, P);
+  dj_tiles<<<dim3(D.nchan, D.nel), th, 0, st>>>(D, S);
+  dj_scatter<<<dim3(D.nang * D.nang, D.nel), th, 0, st>>>(D, S, J);
   return cudaGetLastError();
 }
 

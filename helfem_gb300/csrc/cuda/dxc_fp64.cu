@@ -56,9 +56,9 @@ __device__ __forceinline__ int dgfun(const DevDiatomic& D, int e, int p) { retur
 
 // pure index of radial function g of shell s, or -1 where the function is
 // not in the pure basis
-__device__ __forceinline__ int dpure(const DevDiatomic& D, const DevDiatomicXC& X, int s, int g) {
-  const int st = X.start[s];
-  return (g >= st && g < D.nrad) ? X.off[s] + g - st : -1;
+__device__ __forceinline__ int dpure(const DevDiatomic& D, int s, int g) {
+  const int st = D.pstart[s];
+  return (g >= st && g < D.nrad) ? D.poff[s] + g - st : -1;
 }
 
 // D[s][e][q][k], Dr likewise; grid (nel, npair, nsd)
@@ -75,8 +75,8 @@ __global__ void dxc_rad(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, con
   double* dR = R + nq * nn;   // nq*nn
   for (int idx = threadIdx.x; idx < nn * nn; idx += blockDim.x) {
     const int i = idx % nn, j = idx / nn;
-    const int pi = dpure(D, X, sa, dgfun(D, e, i)), pj = dpure(D, X, ta, dgfun(D, e, j));
-    Pt[idx] = (pi >= 0 && pj >= 0) ? P[(size_t)pj * X.nbf + pi] : 0.0;
+    const int pi = dpure(D, sa, dgfun(D, e, i)), pj = dpure(D, ta, dgfun(D, e, j));
+    Pt[idx] = (pi >= 0 && pj >= 0) ? P[(size_t)pj * D.nbf + pi] : 0.0;
   }
   for (int idx = threadIdx.x; idx < nq * nn; idx += blockDim.x) {
     R[idx] = X.R[(size_t)e * nq * nn + idx];
@@ -193,10 +193,11 @@ __global__ void dxc_point(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, i
   }
 }
 
-// U[o][c][e][k][q] = sum_a F[o][c][e][q][a] Wc[k][a]; grid (nel, nq, nout)
+// U[o][c][e][k][q] = sum_a F[o][c][e][q][a] Wc[k][a] for the Fock-side pairs k;
+// grid (nel, nq, nout)
 __global__ void dxc_ang(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, int ncomp) {
   const int e = blockIdx.x, q = blockIdx.y, o = blockIdx.z;
-  const int nq = X.nq, na = X.na, np = X.npair;
+  const int nq = X.nq, na = X.na, np = X.npair, nf = X.nfock;
   extern __shared__ double Fq[];  // [ncomp][na]
   const size_t cstride = (size_t)D.nel * nq * na;
   for (int idx = threadIdx.x; idx < ncomp * na; idx += blockDim.x) {
@@ -205,8 +206,8 @@ __global__ void dxc_ang(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, int
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int row = w; row < ncomp * np; row += nw) {
-    const int c = row / np, k = row % np;
+  for (int row = w; row < ncomp * nf; row += nw) {
+    const int c = row / nf, k = X.fk[row % nf];
     const double* Wc = (c == 2) ? X.Wt : X.W;
     double acc = 0.0;
     for (int a = lane; a < na; a += 32) acc += Fq[c * na + a] * Wc[(size_t)k * na + a];
@@ -215,13 +216,24 @@ __global__ void dxc_ang(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, int
   }
 }
 
-// grid (npair, nel, nout); writes the (s, t) tile and, for s != t, its
-// transpose into the (t, s) block of the pure H (the rest of H is zero)
+// value v at row (a, gi), column (b, gj) of the pure H and at the transposed
+// position, where both functions are in the pure basis
+__device__ __forceinline__ void dxc_put(const DevDiatomic& D, double* H, int a, int gi, int b, int gj, double v) {
+  const int pi = dpure(D, a, gi), pj = dpure(D, b, gj);
+  if (pi < 0 || pj < 0) return;
+  H[(size_t)pj * D.nbf + pi] = v;
+  H[(size_t)pi * D.nbf + pj] = v;
+}
+
+// grid (nfock, nel, nout). The tile of a pair is symmetric in (i, j): each
+// thread builds one i <= j entry and writes it to the (s, t) and (t, s)
+// blocks at both (i, j) and (j, i), and to the mirror blocks of opposite m.
+// The rest of H is zero.
 __global__ void dxc_fock(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, int gga, double* __restrict__ H0,
                          double* __restrict__ H1) {
-  const int k = blockIdx.x, e = blockIdx.y, o = blockIdx.z;
+  const int kf = blockIdx.x, e = blockIdx.y, o = blockIdx.z;
   const int nn = D.nn, nq = X.nq, np = X.npair;
-  const int sa = X.ps[k], ta = X.pt[k];
+  const int k = X.fk[kf], sa = X.ps[k], ta = X.pt[k], ms = X.fms[kf], mt = X.fmt[kf];
   double* H = o ? H1 : H0;
   extern __shared__ double sm[];
   double* R = sm;             // nq*nn
@@ -254,19 +266,28 @@ __global__ void dxc_fock(DevDiatomic D, DevDiatomicXC X, DiatomicXcScratch S, in
     if (threadIdx.x == 0) corner = c;
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < nn * nn; idx += blockDim.x) {
-    const int i = idx % nn, j = idx / nn;
+  const int ntri = nn * (nn + 1) / 2;
+  for (int idx = threadIdx.x; idx < ntri; idx += blockDim.x) {
+    // idx -> (i <= j), j-major
+    int j = (int)((sqrtf(8.0f * idx + 1.0f) - 1.0f) * 0.5f);
+    while (j * (j + 1) / 2 > idx) --j;
+    while ((j + 1) * (j + 2) / 2 <= idx) ++j;
+    const int i = idx - j * (j + 1) / 2;
     if (i == nn - 1 && j == nn - 1) continue;  // owned by the next element (or dropped)
-    const int pi = dpure(D, X, sa, dgfun(D, e, i)), pj = dpure(D, X, ta, dgfun(D, e, j));
-    if (pi < 0 || pj < 0) continue;
+    const int gi = dgfun(D, e, i), gj = dgfun(D, e, j);
+    if (gi >= D.nrad || gj >= D.nrad) continue;
     double v = 0.0;
     for (int q = 0; q < nq; ++q) {
       const double Ri = R[q * nn + i], Rj = R[q * nn + j];
       v += Ri * (Rj * Us[q] + dR[q * nn + j] * Um[q]) + dR[q * nn + i] * Rj * Um[q];
     }
     if (i == 0 && j == 0) v += corner;
-    H[(size_t)pj * X.nbf + pi] = v;
-    if (sa != ta) H[(size_t)pi * X.nbf + pj] = v;
+    dxc_put(D, H, sa, gi, ta, gj, v);
+    dxc_put(D, H, sa, gj, ta, gi, v);
+    if (ms >= 0) {
+      dxc_put(D, H, ms, gi, mt, gj, v);
+      dxc_put(D, H, ms, gj, mt, gi, v);
+    }
   }
 }
 
@@ -294,8 +315,8 @@ cudaError_t launch_diatomic_xc(const DevDiatomic& D, const DevDiatomicXC& X, con
   const int nsd = polarized ? 2 : 1, nout = nsd;
   const bool gga = xc_func_is_gga(xid) || xc_func_is_gga(cid);
   const int ncomp = gga ? 3 : 1;
-  if (X.na > 1024 || X.npair <= 0) return cudaErrorInvalidValue;
-  const size_t bytes = sizeof(double) * (size_t)X.nbf * X.nbf;
+  if (X.na > 1024 || X.npair <= 0 || X.nfock <= 0) return cudaErrorInvalidValue;
+  const size_t bytes = sizeof(double) * (size_t)D.nbf * D.nbf;
   cudaError_t err = cudaMemsetAsync(Ha, 0, bytes, st);
   if (err == cudaSuccess && polarized) err = cudaMemsetAsync(Hb, 0, bytes, st);
   if (err != cudaSuccess) return err;
@@ -305,7 +326,8 @@ cudaError_t launch_diatomic_xc(const DevDiatomic& D, const DevDiatomicXC& X, con
   const int tp = ((X.na + 31) / 32) * 32;
   dxc_point<<<dim3(D.nel, X.nq), tp, 0, st>>>(D, X, S, xid, cid, gga ? 1 : 0, nsd, polarized ? 1 : 0, thr);
   dxc_ang<<<dim3(D.nel, X.nq, nout), 256, sizeof(double) * ncomp * X.na, st>>>(D, X, S, ncomp);
-  dxc_fock<<<dim3(X.npair, D.nel, nout), ((D.nn * D.nn + 31) / 32) * 32, sizeof(double) * (2 * X.nq * D.nn + 2 * X.nq),
+  const int ntri = D.nn * (D.nn + 1) / 2;
+  dxc_fock<<<dim3(X.nfock, D.nel, nout), ((ntri + 31) / 32) * 32, sizeof(double) * (2 * X.nq * D.nn + 2 * X.nq),
              st>>>(D, X, S, gga ? 1 : 0, Ha, Hb);
   if (energies) dxc_energy<<<1, 512, 0, st>>>(S.epart, D.nel * X.nq, energies);
   return cudaGetLastError();

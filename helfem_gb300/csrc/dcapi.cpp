@@ -19,7 +19,7 @@ struct hfg_diatomic {
   hfg::DevDiatomicScratch scr{};
   DBuf d_p0, d_p2, d_q0, d_q2, d_cdB, d_cds, d_cdrank, d_tx, d_lmfac, d_al_ptr, d_al_b, d_al_c0, d_al_c2, d_chL,
       d_chM, d_chilm, d_chfac, d_jbra_ptr, d_jbra_chan, d_jbra_c0, d_jbra_c2, d_kjk_ptr, d_kentL, d_kentMa,
-      d_kentilm, d_kentjk, d_pairs_all, d_pairs_sym, d_pure;
+      d_kentilm, d_kentjk, d_pairs_all, d_pairs_sym, d_pure, d_poff, d_pstart;
   DBuf s_jin, s_jscal, s_khalo, s_bnorm, s_act, s_entact, s_jkact, s_jklist, s_counts, s_Pd, s_Fd;
   DBuf d_p0s, d_p2s, d_q0s, d_q2s, d_txs, d_alc0s, d_alc2s, d_lmfacs, d_kexp, s_pd2;  // split-precision path
   DBuf h_in, h_out;
@@ -29,8 +29,8 @@ struct hfg_diatomic {
   hfg::DevDiatomicXC xc{};
   hfg::DiatomicXcScratch xs{};
   bool xc_ready = false;
-  DBuf x_ps, x_pt, x_mult, x_W, x_Wt, x_R, x_dR, x_w, x_hinv, x_off, x_start, xs_D, xs_Dr, xs_F, xs_U, xs_ep, h_in2,
-      h_out2, h_e;
+  DBuf x_ps, x_pt, x_mult, x_W, x_Wt, x_R, x_dR, x_w, x_hinv, x_fk, x_fms, x_fmt, xs_D, xs_Dr, xs_F, xs_U, xs_ep,
+      h_in2, h_out2, h_e;
 
   ~hfg_diatomic() {
     if (last_use) {
@@ -66,6 +66,17 @@ struct hfg_diatomic {
     D.Lmax = H.Lmax;
     D.mmax = H.mmax;
     D.nM = H.nM;
+    D.nbf = H.nbf;
+    {
+      std::vector<int> off(H.nang), st(H.nang);
+      for (int a = 0, o = 0; a < H.nang; ++a) {
+        st[a] = H.mval[a] == 0 ? 0 : 1;
+        off[a] = o;
+        o += H.nrad - st[a];
+      }
+      D.poff = d_poff.upload(off);
+      D.pstart = d_pstart.upload(st);
+    }
     D.p0 = d_p0.upload(H.p0);
     D.p2 = d_p2.upload(H.p2);
     D.q0 = d_q0.upload(H.q0);
@@ -95,8 +106,6 @@ struct hfg_diatomic {
     D.jbra_chan = d_jbra_chan.upload(H.jbra_chan);
     D.jbra_c0 = d_jbra_c0.upload(H.jbra_c0);
     D.jbra_c2 = d_jbra_c2.upload(H.jbra_c2);
-    for (int ij = 0; ij < H.nang * H.nang; ++ij)
-      if (H.jbra_ptr[ij + 1] - H.jbra_ptr[ij] > 64) throw std::invalid_argument("too many Coulomb bra terms");
     D.nent = (int)H.kent_L.size();
     D.kjk_ptr = d_kjk_ptr.upload(H.kjk_ptr);
     D.kent_L = d_kentL.upload(H.kent_L);
@@ -200,14 +209,17 @@ struct hfg_diatomic {
     check_device();
     const hfg::DiatomicHost& H = host;
     if (split) ensure_split();
+    if (!exchange) {  // J reads the pure density and writes the pure J directly
+      ck(hfg::launch_diatomic_coulomb(dev, scr, P, F, st), "coulomb");
+      mark_use(st);
+      return;
+    }
     ck(hfg::launch_diatomic_expand(P, H.nbf, d_pure.as<int>(), s_Pd.as<double>(), H.ndummy, st), "expand");
-    if (exchange && split)
+    if (split)
       ck(hfg::launch_diatomic_exchange_split(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st),
          "exchange (split)");
-    else if (exchange)
-      ck(hfg::launch_diatomic_exchange(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st), "exchange");
     else
-      ck(hfg::launch_diatomic_coulomb(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), st), "coulomb");
+      ck(hfg::launch_diatomic_exchange(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st), "exchange");
     ck(hfg::launch_diatomic_gather(s_Fd.as<double>(), H.ndummy, d_pure.as<int>(), H.nbf, F, st), "gather");
     mark_use(st);
   }
@@ -221,12 +233,13 @@ struct hfg_diatomic {
     xc.nq = H.xc_nq;
     xc.na = H.xc_lang;
     xc.npair = H.xc_npair;
-    xc.nbf = H.nbf;
     xc.ps = x_ps.upload(H.xc_ps);
     xc.pt = x_pt.upload(H.xc_pt);
     xc.mult = x_mult.upload(H.xc_mult);
-    xc.off = x_off.upload(H.xc_off);
-    xc.start = x_start.upload(H.xc_start);
+    xc.nfock = (int)H.xc_fk.size();
+    xc.fk = x_fk.upload(H.xc_fk);
+    xc.fms = x_fms.upload(H.xc_fms);
+    xc.fmt = x_fmt.upload(H.xc_fmt);
     xc.W = x_W.upload(H.xc_W);
     xc.Wt = x_Wt.upload(H.xc_Wt);
     xc.R = x_R.upload(H.xc_R);

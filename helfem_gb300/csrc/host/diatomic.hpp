@@ -81,7 +81,11 @@ struct DiatomicHost {
   std::vector<double> xc_W, xc_Wt;     // [k*lang + a]: Y_s Y_t and Y_s' Y_t + Y_s Y_t' (phi = 0)
   std::vector<double> xc_R, xc_dR;     // [(e*nq + q)*nn + p]: B_p, dB_p/dmu
   std::vector<double> xc_w, xc_hinv;   // [(e*nq + q)*lang + a]: weight, 1/h
-  std::vector<int> xc_off, xc_start;   // [s]: pure index of (s, xc_start[s]); first kept radial function
+  // Fock-side pair list: V_xc is one phi-independent field, so the tile of a
+  // -m pair equals that of its +m mirror (same l's). xc_fk lists the pairs
+  // whose tiles are built (m >= 0, or without a mirror); xc_fms / xc_fmt are
+  // the mirror shells the same tile is also written to (-1: none).
+  std::vector<int> xc_fk, xc_fms, xc_fmt;
   void build_xc_grid(int lang);
 
   void build(int Z1, int Z2, double Rhalf, int nnodes, const std::vector<double>& bval,

@@ -76,13 +76,21 @@ void DiatomicHost::build_xc_grid(int lang) {
       xc_Wt[(size_t)k * na + a] = dY[ia] * Y[ib] + Y[ia] * dY[ib];
     }
   }
-  // pure index of (s, g) = xc_off[s] + g - xc_start[s] (basis.cpp:712-736)
-  xc_off.assign(nang, 0);
-  xc_start.assign(nang, 0);
-  for (int s = 0, o = 0; s < nang; ++s) {
-    xc_start[s] = mval[s] == 0 ? 0 : 1;
-    xc_off[s] = o;
-    o += nrad - xc_start[s];
+  // mirror shells (same l, opposite m) and the Fock-side pair list
+  std::vector<int> mir(nang, -1);
+  for (int s = 0; s < nang; ++s)
+    for (int s2 = 0; s2 < nang; ++s2)
+      if (mval[s] != 0 && lval[s2] == lval[s] && mval[s2] == -mval[s]) mir[s] = s2;
+  xc_fk.clear();
+  xc_fms.clear();
+  xc_fmt.clear();
+  for (int k = 0; k < xc_npair; ++k) {
+    const int s = xc_ps[k], t = xc_pt[k], m = mval[s];
+    const bool mirrored = mir[s] >= 0 && mir[t] >= 0;
+    if (m < 0 && mirrored) continue;  // written by its +m mirror
+    xc_fk.push_back(k);
+    xc_fms.push_back(m > 0 && mirrored ? mir[s] : -1);
+    xc_fmt.push_back(m > 0 && mirrored ? mir[t] : -1);
   }
   // radial rows and point weights
   std::vector<double> xq, wq;
