@@ -74,6 +74,75 @@ __global__ void test_density(double* __restrict__ P, int n) {
   }
 }
 
+// Davidson residuals: R[:, j] = AX[:, j] - theta[j] X[:, j] and their norms;
+// one block per column
+__global__ void dav_residual(const double* __restrict__ AX, const double* __restrict__ X,
+                             const double* __restrict__ theta, int n, double* __restrict__ R,
+                             double* __restrict__ norms) {
+  const int j = blockIdx.x;
+  const double t = theta[j];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double r = AX[i + (size_t)j * n] - t * X[i + (size_t)j * n];
+    R[i + (size_t)j * n] = r;
+    s += r * r;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+    norms[j] = sqrt(v);
+  }
+}
+
+// Olsen-corrected, reference-preconditioned Davidson update in the reference
+// eigenbasis: with d_i = 1/(lam_i - theta_j),
+//   eps = (zx . d zr) / (zx . d zx),  zt = d (zr - eps zx),
+// which makes the correction orthogonal to the Ritz vector; one block per
+// column. |lam_i - theta_j| is kept above floor.
+__global__ void dav_olsen(const double* __restrict__ Zr, const double* __restrict__ Zx,
+                          const double* __restrict__ lam, const double* __restrict__ theta, int n, double floor_,
+                          double* __restrict__ Zt) {
+  const int j = blockIdx.x;
+  const double t = theta[j];
+  const double* zr = Zr + (size_t)j * n;
+  const double* zx = Zx + (size_t)j * n;
+  auto dinv = [&](int i) {
+    double g = lam[i] - t;
+    if (fabs(g) < floor_) g = (g < 0.0) ? -floor_ : floor_;
+    return 1.0 / g;
+  };
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double d = dinv(i);
+    a += zx[i] * d * zr[i];
+    b += zx[i] * d * zx[i];
+  }
+  __shared__ double ra[32], rb[32], e;
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    ra[threadIdx.x >> 5] = a;
+    rb[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sa = 0.0, sb = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      sa += ra[w];
+      sb += rb[w];
+    }
+    e = (sb != 0.0) ? sa / sb : 0.0;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) Zt[i + (size_t)j * n] = dinv(i) * (zr[i] - e * zx[i]);
+}
+
 inline int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
@@ -98,6 +167,16 @@ void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cud
 
 void fill_test_density(double* P, int n, cudaStream_t st) {
   test_density<<<grid_for((size_t)n * n), 256, 0, st>>>(P, n);
+}
+
+void k_dav_residual(const double* AX, const double* X, const double* theta, int n, int k, double* R, double* norms,
+                    cudaStream_t st) {
+  dav_residual<<<k, 256, 0, st>>>(AX, X, theta, n, R, norms);
+}
+
+void k_dav_olsen(const double* Zr, const double* Zx, const double* lam, const double* theta, int n, int k,
+                 double floor_, double* Zt, cudaStream_t st) {
+  dav_olsen<<<k, 256, 0, st>>>(Zr, Zx, lam, theta, n, floor_, Zt);
 }
 
 void k_add_diag(double* A, int n, double v, cudaStream_t st) {

@@ -19,5 +19,12 @@ void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cud
 void fill_test_density(double* P, int n, cudaStream_t st);
 // A[i,i] += v, A n x n column-major
 void k_add_diag(double* A, int n, double v, cudaStream_t st);
+// Davidson steps (n x k column blocks): residuals R = AX - X diag(theta) with
+// column norms; reference-preconditioned Olsen corrections in the reference
+// eigenbasis (Zr = Vr^T R, Zx = Vr^T X -> Zt)
+void k_dav_residual(const double* AX, const double* X, const double* theta, int n, int k, double* R, double* norms,
+                    cudaStream_t st);
+void k_dav_olsen(const double* Zr, const double* Zx, const double* lam, const double* theta, int n, int k,
+                 double floor_, double* Zt, cudaStream_t st);
 
 }  // namespace hfg

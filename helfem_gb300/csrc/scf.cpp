@@ -19,6 +19,7 @@
 #include <cfloat>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
@@ -29,6 +30,7 @@
 #include <numeric>
 
 #include "cuda/scf_kernels.cuh"
+#include "davidson.hpp"
 #include "handle.hpp"
 
 namespace {
@@ -246,17 +248,28 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       scr_split.p2 = dP2.as<float2>();
     }
 
-    // X^T M_k X for block k of AO matrix M into out (nk x nk)
-    auto to_ortho = [&](const double* M, const Block& b, double* out) {
-      hfg::k_gather_block(M, nbf, nrad, b.d_ang.as<int>(), b.nk, dFk.as<double>(), st);
+    // Blocks are kept in the non-orthonormal basis (F_k gathered from the AO
+    // matrix); the orthonormal F'_k = (I x X)^T F_k (I x X) is formed only for
+    // full eigensolves, and products with F'_k are taken as thin GEMMs.
+    auto gather = [&](const double* M, const Block& b, double* out) {
+      hfg::k_gather_block(M, nbf, nrad, b.d_ang.as<int>(), b.nk, out, st);
+    };
+    auto ortho_block = [&](const double* Fk, const Block& b, double* out) {
       const int p = (int)b.ang.size(), nk = b.nk;
-      cb(cublasDgemmStridedBatched(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, nk, nrad, nrad, &one, dFk.as<double>(), nk,
+      cb(cublasDgemmStridedBatched(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, nk, nrad, nrad, &one, Fk, nk,
                                    (long long)nrad * nk, dX.as<double>(), nrad, 0, &zero, dT1.as<double>(), nk,
                                    (long long)nrad * nk, p),
          "F X");
       cb(cublasDgemmStridedBatched(hd.bl, CUBLAS_OP_T, CUBLAS_OP_N, nrad, nk, nrad, &one, dX.as<double>(), nrad, 0,
                                    dT1.as<double>(), nk, nrad, &zero, out, nk, nrad, p),
          "X^T F X");
+    };
+    // out = (I x X) V or (I x X)^T V for an nk x cols block V
+    auto x_cols = [&](const Block& b, const double* Vin, int cols, double* out, bool trans) {
+      const int p = (int)b.ang.size(), nk = b.nk;
+      cb(cublasDgemmStridedBatched(hd.bl, trans ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, nrad, cols, nrad, &one,
+                                   dX.as<double>(), nrad, 0, Vin, nk, nrad, &zero, out, nk, nrad, p),
+         "X V");
     };
 
     // orbitals: eps (all blocks, per spin), occupations
@@ -290,10 +303,16 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     std::vector<char> hwork;
     size_t work_bytes = 0;
 
-    auto diagonalise = [&](const double* Fo_all, int s) {
+    // full eigensolves of the representative blocks selected by `full`
+    // (all when empty); results copied to every block they represent
+    auto diagonalise = [&](const double* Fo_all, int s, const std::vector<char>& full = {}) {
       double* Vs = dVec.as<double>() + Lblk * s;
       double* Ws = deps.as<double>() + (size_t)nbf * s;
-      for (auto& grp : by_size) {
+      for (auto& grp0 : by_size) {
+        std::pair<int, std::vector<int>> grp{grp0.first, {}};
+        for (int k : grp0.second)
+          if (full.empty() || full[k]) grp.second.push_back(k);
+        if (grp.second.empty()) continue;
         const int n = grp.first, nb = (int)grp.second.size();
         const size_t n2 = (size_t)n * n;
         if (dBatch.n < sizeof(double) * n2 * nb) dBatch.alloc(sizeof(double) * n2 * nb);
@@ -420,6 +439,159 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       }
     };
 
+    // Eigensolver policy: full batched solves for the first three
+    // diagonalisations (and whenever a block has no reference yet), then
+    // Davidson refinement of the previous orbitals of each representative
+    // block, preconditioned by that block's last full eigendecomposition, to
+    // residuals |F'x - theta x| <= dav_tol = 1e-2 x the current orbital
+    // gradient, clamped to [1e-8, 1e-4] Eh (the gradient target is 1e-7;
+    // early iterations need no more). A block whose refinement does not
+    // converge in 12 iterations is solved in full (and becomes the new
+    // reference); one that needed 6 or more is solved in full next time.
+    // HFG_SCF_EIGENSOLVER=full keeps full solves throughout; HFG_SCF_NFULL
+    // sets the number of full solves before the refinement starts.
+    const char* eenv = std::getenv("HFG_SCF_EIGENSOLVER");
+    const bool use_davidson = !(eenv && std::strcmp(eenv, "full") == 0);
+    const char* nenv = std::getenv("HFG_SCF_NFULL");  // full solves before refinement (default 3)
+    const int n_full_first = (nenv && std::atoi(nenv) > 0) ? std::atoi(nenv) : 3;
+    DBuf dVref, dLam, dFx;
+    dVref.alloc(sizeof(double) * Ltot);
+    dLam.alloc(sizeof(double) * (size_t)nbf * nspin);
+    if (orbital_energies) dFx.alloc(sizeof(double) * Ltot);
+    std::vector<char> have_ref((size_t)nspin * nblk, 0), want_full((size_t)nspin * nblk, 0);
+    hfg::DavidsonWork dav;
+    DBuf dFp, dOpA, dOpB, dOpC;  // orthonormal blocks of the full solves; operator temporaries
+    dFp.alloc(sizeof(double) * Ltot);
+    double shift = 0.0;  // level shift of the virtual space (set by the stabilisation below)
+    auto nocc_of = [&](int s, int k) {
+      int n = 0;
+      while (n < blocks[k].nk && occ[s][k][n] > 0) ++n;
+      return n;
+    };
+    // F'_k (+ the level shift b (1 - V_occ V_occ^T) with the previous
+    // occupied orbitals) into dFp, for a full eigensolve
+    auto form_ortho = [&](const double* Fo_all, int s, int k) {
+      const Block& b = blocks[k];
+      double* Fp = dFp.as<double>() + Lblk * s + b.off;
+      ortho_block(Fo_all + Lblk * s + b.off, b, Fp);
+      if (shift > 0.0) {
+        hfg::k_add_diag(Fp, b.nk, shift, st);
+        const int nocc = nocc_of(s, k);
+        if (nocc > 0) {
+          const double* Vk = dVec.as<double>() + Lblk * s + b.off;
+          const double mshift = -shift;
+          cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_T, b.nk, b.nk, nocc, &mshift, Vk, b.nk, Vk, b.nk, &one, Fp,
+                         b.nk),
+             "level shift");
+        }
+      }
+    };
+    int ndiag = 0;
+    double dav_tol = 1e-8;
+    bool last_partial = false;
+    long dav_iters = 0, dav_solves = 0, dav_fallbacks = 0;
+
+    auto solve_blocks = [&](const double* Fo_all, int s) {
+      std::vector<char> full(nblk, 0);
+      bool partial = false;
+      const bool aufbau = !d->l_occ && !d->fixed_occ;
+      for (int k = 0; k < nblk; ++k) {
+        if (rep[k] != k) continue;
+        const Block& b = blocks[k];
+        const size_t key = (size_t)s * nblk + k;
+        bool f = !use_davidson || ndiag < n_full_first || !have_ref[key] || want_full[key] || b.nk < 96;
+        if (!f) {
+          int nocc = 0;
+          while (nocc < b.nk && occ[s][k][nocc] > 0) ++nocc;
+          // fixed occupations need the occupied pairs only; the Aufbau order
+          // also the lowest virtuals
+          const int kconv = std::min(b.nk, std::max(1, nocc + (aufbau ? 3 : 0)));
+          const int kk = std::min(b.nk, kconv + 4);
+          double* V = dVec.as<double>() + Lblk * s + b.off;
+          const double* Fk = Fo_all + Lblk * s + b.off;
+          // F' Q = X^T F_k X Q (+ b (Q - V_occ V_occ^T Q)); V keeps the
+          // previous orbitals until the refinement succeeds
+          const hfg::BlockOperator apply = [&](const double* Q, int c, double* AQ) {
+            const size_t need = sizeof(double) * (size_t)b.nk * c;
+            if (dOpA.n < need) dOpA.alloc(need);
+            if (dOpB.n < need) dOpB.alloc(need);
+            x_cols(b, Q, c, dOpA.as<double>(), false);
+            cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, b.nk, c, b.nk, &one, Fk, b.nk, dOpA.as<double>(), b.nk,
+                           &zero, dOpB.as<double>(), b.nk),
+               "F (X Q)");
+            x_cols(b, dOpB.as<double>(), c, AQ, true);
+            if (shift > 0.0) {
+              cb(cublasDaxpy(hd.bl, b.nk * c, &shift, Q, 1, AQ, 1), "shift Q");
+              if (nocc > 0) {
+                if (dOpC.n < sizeof(double) * (size_t)nocc * c) dOpC.alloc(sizeof(double) * (size_t)nocc * c);
+                const double mshift = -shift;
+                cb(cublasDgemm(hd.bl, CUBLAS_OP_T, CUBLAS_OP_N, nocc, c, b.nk, &one, V, b.nk, Q, b.nk, &zero,
+                               dOpC.as<double>(), nocc),
+                   "V^T Q");
+                cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, b.nk, c, nocc, &mshift, V, b.nk, dOpC.as<double>(),
+                               nocc, &one, AQ, b.nk),
+                   "shift projector");
+              }
+            }
+          };
+          std::vector<double> th;
+          const int itd = hfg::davidson_lowest(hd.bl, st, apply, b.nk, kk, kconv, V,
+                                               dVref.as<double>() + Lblk * s + b.off,
+                                               dLam.as<double>() + (size_t)nbf * s + eoff[k], th, dav, 12, dav_tol);
+          if (itd < 0) {
+            f = true;
+            ++dav_fallbacks;
+          } else {
+            ++dav_solves;
+            dav_iters += itd;
+            want_full[key] = itd >= 6;
+            partial = true;
+            // the kk Ritz values; the rest out of reach of the Aufbau order
+            std::vector<double> ev(b.nk, 1e300);
+            std::copy(th.begin(), th.end(), ev.begin());
+            for (int q = 0; q < nblk; ++q) {
+              if (rep[q] != k) continue;
+              ck(cudaMemcpyAsync(deps.as<double>() + (size_t)nbf * s + eoff[q], ev.data(), sizeof(double) * b.nk,
+                                 cudaMemcpyHostToDevice, st),
+                 "eigenvalues");
+              if (q != k)
+                ck(cudaMemcpyAsync(dVec.as<double>() + Lblk * s + blocks[q].off, V, sizeof(double) * b.nk * kk,
+                                   cudaMemcpyDeviceToDevice, st),
+                   "copy vectors");
+            }
+            ck(cudaStreamSynchronize(st), "sync");
+          }
+        }
+        full[k] = f ? 1 : 0;
+      }
+      if (std::find(full.begin(), full.end(), 1) != full.end()) {
+        for (int k = 0; k < nblk; ++k)
+          if (full[k]) form_ortho(Fo_all, s, k);
+        diagonalise(dFp.as<double>(), s, full);
+        for (int k = 0; k < nblk; ++k) {
+          if (!full[k]) continue;
+          const Block& b = blocks[k];
+          ck(cudaMemcpyAsync(dVref.as<double>() + Lblk * s + b.off, dVec.as<double>() + Lblk * s + b.off,
+                             sizeof(double) * b.nk * b.nk, cudaMemcpyDeviceToDevice, st),
+             "reference vectors");
+          ck(cudaMemcpyAsync(dLam.as<double>() + (size_t)nbf * s + eoff[k], deps.as<double>() + (size_t)nbf * s + eoff[k],
+                             sizeof(double) * b.nk, cudaMemcpyDeviceToDevice, st),
+             "reference values");
+          have_ref[(size_t)s * nblk + k] = 1;
+          want_full[(size_t)s * nblk + k] = 0;
+        }
+      }
+      return partial;
+    };
+    auto solve_all = [&](const double* Fo_all) {
+      if (orbital_energies)
+        ck(cudaMemcpyAsync(dFx.p, Fo_all, sizeof(double) * Ltot, cudaMemcpyDeviceToDevice, st), "copy F'");
+      bool partial = false;
+      for (int s = 0; s < nspin; ++s) partial = solve_blocks(Fo_all, s) || partial;
+      last_partial = partial;
+      ++ndiag;
+    };
+
     auto dot = [&](const double* x, const double* y) {
       double r = 0.0;
       cb(cublasDdot(hd.bl, (int)nb2, x, 1, y, 1, &r), "ddot");
@@ -431,8 +603,8 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     ck(cudaMemsetAsync(dEo.p, 0, sizeof(double) * Ltot, st), "memset");
     for (int s = 0; s < nspin; ++s)
       for (int k = 0; k < nblk; ++k)
-        if (rep[k] == k) to_ortho(dH.as<double>(), blocks[k], dFo.as<double>() + Lblk * s + blocks[k].off);
-    for (int s = 0; s < nspin; ++s) diagonalise(dFo.as<double>(), s);
+        if (rep[k] == k) gather(dH.as<double>(), blocks[k], dFo.as<double>() + Lblk * s + blocks[k].off);
+    solve_all(dFo.as<double>());
     occupy();
     build_density();
 
@@ -445,7 +617,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     // degenerate open shells) the virtual orbitals are level-shifted,
     // F' += b (1 - Q Q^T) with Q the occupied orbitals of the previous
     // iteration, and the DIIS history restarts
-    double shift = 0.0, emin = 1e300;
+    double emin = 1e300;
     int it_improved = 0;
     double Ekin = 0, Enuc = 0, Ecoul = 0, Exx = 0, Exc = 0, Ngrid = 0, Etot = 0;
     PhaseTimer pt;
@@ -495,7 +667,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       Etot = Ekin + Enuc + Ecoul + Exx + Exc;
       pt.lap(1);  // energies
 
-      // ---- orthonormal Fock blocks and DIIS errors F'D' - D'F' ----
+      // ---- Fock blocks and DIIS errors F'D' - D'F' (orthonormal basis) ----
       double emax = 0.0;
       for (int s = 0; s < nspin; ++s)
         for (int k = 0; k < nblk; ++k) {
@@ -503,7 +675,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
           const Block& b = blocks[k];
           double* Fo = dFo.as<double>() + Lblk * s + b.off;
           double* Eo = dEo.as<double>() + Lblk * s + b.off;
-          to_ortho(dF[s].as<double>(), b, Fo);
+          gather(dF[s].as<double>(), b, Fo);
           int nocc = 0;
           while (nocc < b.nk && occ[s][k][nocc] > 0) ++nocc;
           if (nocc == 0) {
@@ -511,10 +683,12 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
             continue;
           }
           const double* Vk = dVec.as<double>() + Lblk * s + b.off;
-          // W = F' V_occ diag(occ);  G = W V_occ^T;  E = G - G^T
-          cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, b.nk, nocc, b.nk, &one, Fo, b.nk, Vk, b.nk, &zero,
-                         dW.as<double>(), b.nk),
-             "F' V");
+          // W = F' V_occ = X^T F_k (X V_occ);  G = W diag(occ) V_occ^T;  E = G - G^T
+          x_cols(b, Vk, nocc, dCo.as<double>(), false);
+          cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, b.nk, nocc, b.nk, &one, Fo, b.nk, dCo.as<double>(), b.nk,
+                         &zero, dT1.as<double>(), b.nk),
+             "F (X V)");
+          x_cols(b, dT1.as<double>(), nocc, dW.as<double>(), true);
           hfg::k_scale_cols(dW.as<double>(), b.nk, nocc, dOcc.as<double>() + (size_t)nbf * s + eoff[k],
                             dCo.as<double>(), st);
           cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_T, b.nk, b.nk, nocc, &one, dCo.as<double>(), b.nk, Vk, b.nk,
@@ -530,6 +704,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         emax = std::fabs(emax);
       }
       pt.lap(2);  // orthonormal blocks + DIIS errors
+      dav_tol = std::min(1e-4, std::max(1e-8, 1e-2 * emax));
       if (verbose) std::fprintf(stderr, "hfg_scf it %3d E %.12f dE % .3e diis %.3e\n", it, Etot, Etot - Eold, emax);
       // energy change within etol + 1e-12 |E| (heavy atoms: |E| ~ 1e4 Eh puts
       // the FP64 summation noise of the grid and matrix traces near 1e-9 Eh)
@@ -615,31 +790,30 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       ck(cudaMemsetAsync(dFo.p, 0, sizeof(double) * Ltot, st), "memset");
       for (int i = 0; i < nh; ++i)
         cb(cublasDaxpy(hd.bl, (int)Ltot, &c[i], dHF.as<double>() + Ltot * i, 1, dFo.as<double>(), 1), "axpy");
-      if (shift > 0.0)
-        for (int s = 0; s < nspin; ++s)
-          for (int k = 0; k < nblk; ++k) {
-            if (rep[k] != k) continue;
-            const Block& b = blocks[k];
-            int nocc = 0;
-            while (nocc < b.nk && occ[s][k][nocc] > 0) ++nocc;
-            double* Fo = dFo.as<double>() + Lblk * s + b.off;
-            hfg::k_add_diag(Fo, b.nk, shift, st);
-            if (nocc == 0) continue;
-            const double* Vk = dVec.as<double>() + Lblk * s + b.off;
-            const double mshift = -shift;
-            cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_T, b.nk, b.nk, nocc, &mshift, Vk, b.nk, Vk, b.nk, &one, Fo,
-                           b.nk),
-               "level shift");
-          }
+      // (the level shift, if any, is applied when the blocks are solved)
       pt.lap(3);  // DIIS extrapolation
-      for (int s = 0; s < nspin; ++s) diagonalise(dFo.as<double>(), s);
+      solve_all(dFo.as<double>());
       occupy();
       pt.lap(4);  // eigensolves + occupations
       build_density();
       ck(cudaStreamSynchronize(st), "sync");
       pt.lap(5);  // density
     }
+    if (orbital_energies && last_partial) {
+      // the full spectrum of the blocks diagonalised last (refinement gives
+      // only the lowest pairs)
+      for (int s = 0; s < nspin; ++s) {
+        for (int k = 0; k < nblk; ++k)
+          if (rep[k] == k) form_ortho(dFx.as<double>(), s, k);
+        diagonalise(dFp.as<double>(), s);
+      }
+      ck(cudaMemcpyAsync(eps.data(), deps.p, sizeof(double) * eps.size(), cudaMemcpyDeviceToHost, st), "D2H eps");
+    }
     ck(cudaStreamSynchronize(st), "sync");
+    if (verbose)
+      std::fprintf(stderr, "hfg_scf eigensolver: %d diagonalisations, %ld refined blocks (%.2f iterations each), "
+                           "%ld fell back to full\n",
+                   ndiag, dav_solves, dav_solves ? (double)dav_iters / dav_solves : 0.0, dav_fallbacks);
     a->mark_use(st);
     res->Etot = Etot;
     res->Ekin = Ekin;
