@@ -74,6 +74,7 @@ _SIGS = {
     "hfg_jk_host": ([_P, _D, _D, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_fock_diag": ([_P, _P, ctypes.c_int, _P, _P, _P], ctypes.c_int),
     "hfg_atom_autotune": ([_P, ctypes.c_int, _I, _D], ctypes.c_int),
+    "hfg_atom_set_partition": ([_P, ctypes.c_int], ctypes.c_int),
     "hfg_atom_work": ([_P, _P], ctypes.c_int),
     "hfg_dft_grid": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
@@ -390,6 +391,10 @@ class Atom:
         ns, ms = ctypes.c_int(), ctypes.c_double()
         _check(_lib.hfg_atom_autotune(self._h, flags, ctypes.byref(ns), ctypes.byref(ms)))
         return {"nsplit": ns.value, "ms": ms.value}
+
+    def set_partition(self, nsplit: int = 0):
+        """Exchange work partition as the autotuner would set it (0 = automatic)."""
+        _check(_lib.hfg_atom_set_partition(self._h, nsplit))
 
     def fock_diag(self, F, C, eps, symmetry: int = 1, stream=None):
         """Orbital energies eps (nbf) and AO coefficients C (nbf x nbf) of

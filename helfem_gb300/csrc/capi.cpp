@@ -386,6 +386,18 @@ hfg_status hfg_atom_autotune(hfg_atom* a, int flags, int* best_nsplit, double* b
   });
 }
 
+hfg_status hfg_atom_set_partition(hfg_atom* a, int nsplit) {
+  return guard([&] {
+    need(a != nullptr && nsplit >= 0, "hfg_atom_set_partition: bad arguments");
+    a->check_device();
+    hfg_abi::AllocStream alloc_on(a->own_stream);
+    ck(cudaStreamSynchronize(a->own_stream), "sync");
+    a->nsplit_fixed = nsplit;
+    a->build_units();
+    ck(cudaStreamSynchronize(a->own_stream), "sync");
+  });
+}
+
 hfg_status hfg_coulomb_host(hfg_atom* a, const double* P, double* J) {
   return guard([&] { host_call(a, P, J, true, 0); });
 }

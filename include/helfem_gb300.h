@@ -152,6 +152,9 @@ hfg_status hfg_exchange_ex(hfg_atom* atom, const double* P, double* K, int flags
  * fastest for the later calls of this handle. Synchronous; results and
  * layouts of K do not change. */
 hfg_status hfg_atom_autotune(hfg_atom* atom, int flags, int* best_nsplit, double* best_ms);
+/* Set the exchange work partition directly (the value hfg_atom_autotune
+ * picks): nsplit output-block ranges per element pair, 0 = automatic. */
+hfg_status hfg_atom_set_partition(hfg_atom* atom, int nsplit);
 
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
  * fixed 4 MiB array in the library's static device memory rather than the

@@ -119,6 +119,9 @@ def test_autotune_keeps_results():
     assert r["nsplit"] in (0, 1, 2, 4, 8, 16) and r["ms"] > 0
     K2 = A.exchange_host(P, symmetric=True, split=True)
     assert np.array_equal(K1, K2)
+    for ns in (1, 3, 0):
+        A.set_partition(ns)
+        assert np.array_equal(K1, A.exchange_host(P, symmetric=True, split=True))
 
 
 def test_zero_density():
