@@ -384,11 +384,21 @@ __global__ void __launch_bounds__(320) k_tiles_split(DevAtom A, DevScratch S, co
   for (int w = u.z; w < u.w; ++w) {
     const int jk = diag ? diag_jk[w] : w;
     ffv yacc = {0.f, 0.f};
-    for (int ent = A.kjk_ptr[jk]; ent < A.kjk_ptr[jk + 1]; ++ent) {
-      if (!S.ent_act[ent]) continue;  // uniform over the CTA
+    // the recoupled density tile of the next active entry is loaded while the
+    // current one is contracted (its global loads overlap the FP32 work)
+    const int ent_end = A.kjk_ptr[jk + 1];
+    int ent = A.kjk_ptr[jk];
+    while (ent < ent_end && !S.ent_act[ent]) ++ent;  // uniform over the CTA
+    float2 xcur = make_float2(0.f, 0.f);
+    if (ent < ent_end && vpq) xcur = ff2(k_recouple_ff(A, p2base, act, ent));
+    while (ent < ent_end) {
       const int L = A.kent_L[ent];
-      if (live) X[t] = vpq ? ff2(k_recouple_ff(A, p2base, act, ent)) : make_float2(0.f, 0.f);
+      if (live) X[t] = xcur;
       __syncthreads();
+      int ent_next = ent + 1;
+      while (ent_next < ent_end && !S.ent_act[ent_next]) ++ent_next;
+      float2 xnext = make_float2(0.f, 0.f);
+      if (ent_next < ent_end && vpq) xnext = ff2(k_recouple_ff(A, p2base, act, ent_next));
       ffv acc = {0.f, 0.f};
       if (diag) {
         if (live) {
@@ -430,6 +440,8 @@ __global__ void __launch_bounds__(320) k_tiles_split(DevAtom A, DevScratch S, co
       }
       yacc = ff_add(yacc, ff_norm(acc.hi, acc.lo));
       __syncthreads();
+      ent = ent_next;
+      xcur = xnext;
     }
     const double y = ff_to_d(yacc);  // FP64 recombination, once per output element
     if (live) k_store(A, S, K, a, b, jk, p, q, -y);
