@@ -476,7 +476,8 @@ __global__ void __launch_bounds__(320) dk_tiles(DevDiatomic D, DevDiatomicScratc
 // TwoProd/TwoSum products on the FP32 pipe, the per-multipole results summed
 // as float pairs and recombined in FP64 once per output element.
 template <int NN>
-__global__ void __launch_bounds__(320) dk_tiles_split(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd,
+// 15-node elements: 256 threads, at most 51 registers so that five CTAs share an SM
+__global__ void __launch_bounds__(NN == 15 ? 256 : 320, NN == 15 ? 5 : 1) dk_tiles_split(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd,
                                                       int symmetric) {
   const int nn = NN > 0 ? NN : D.nn, n2 = nn * nn, nang2 = D.nang * D.nang;
   const int n_act = S.counts[0], n_dact = symmetric ? S.counts[1] : S.counts[0];
@@ -568,7 +569,13 @@ __global__ void __launch_bounds__(320) dk_tiles_split(DevDiatomic D, DevDiatomic
             const float2* txb = tx + (size_t)ab * n2 * n2;
             const float2* Xb = X + ab * n2;
             for (int v0 = 0; v0 < n2; v0 += nn) {
-              for (int v = v0; v < v0 + nn; ++v) acc = ff_fma(acc, txb[t + (size_t)v * n2], Xb[v]);
+              if (NN > 0) {  // unrolled: the nn table loads are issued together
+#pragma unroll
+                for (int c = 0; c < (NN > 0 ? NN : 1); ++c)
+                  acc = ff_fma(acc, txb[t + (size_t)(v0 + c) * n2], Xb[v0 + c]);
+              } else {
+                for (int v = v0; v < v0 + nn; ++v) acc = ff_fma(acc, txb[t + (size_t)v * n2], Xb[v]);
+              }
               acc = ff_norm(acc.hi, acc.lo);
             }
           }
