@@ -75,6 +75,10 @@ _SIGS = {
     "hfg_fock_diag": ([_P, _P, ctypes.c_int, _P, _P, _P], ctypes.c_int),
     "hfg_atom_autotune": ([_P, ctypes.c_int, _I, _D], ctypes.c_int),
     "hfg_atom_set_partition": ([_P, ctypes.c_int], ctypes.c_int),
+    "hfg_atom_compute_yukawa": ([_P, ctypes.c_double], ctypes.c_int),
+    "hfg_atom_yukawa_tables": ([_P, ctypes.c_int, ctypes.c_int, _D, _D, _D], ctypes.c_int),
+    "hfg_rs_exchange": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
+    "hfg_rs_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_atom_work": ([_P, _P], ctypes.c_int),
     "hfg_dft_grid": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hfg_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
@@ -391,6 +395,31 @@ class Atom:
         ns, ms = ctypes.c_int(), ctypes.c_double()
         _check(_lib.hfg_atom_autotune(self._h, flags, ctypes.byref(ns), ctypes.byref(ms)))
         return {"nsplit": ns.value, "ms": ms.value}
+
+    # ---- range-separated (Yukawa-screened) exchange ----
+    def compute_yukawa(self, lam: float):
+        """Screened radial tables for the kernel exp(-lam r12)/r12."""
+        _check(_lib.hfg_atom_compute_yukawa(self._h, lam))
+
+    def yukawa_tables(self, L: int, iel: int):
+        """(r_small, r_big, tk) of the screened tables as stored (padded)."""
+        nn = self.nnodes
+        rs = np.zeros((nn, nn), order="F")
+        rb = np.zeros((nn, nn), order="F")
+        tk = np.zeros((nn * nn, nn * nn), order="F")
+        _check(_lib.hfg_atom_yukawa_tables(self._h, L, iel, _dptr(rs), _dptr(rb), _dptr(tk)))
+        return rs, rb, tk
+
+    def rs_exchange(self, P, K, stream=None, symmetric: bool = False, split: bool = False):
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        _check(_lib.hfg_rs_exchange(self._h, _ptr(P), _ptr(K), flags, _stream(stream)))
+
+    def rs_exchange_host(self, P: np.ndarray, symmetric: bool = False, split: bool = False) -> np.ndarray:
+        P = np.asfortranarray(P, dtype=np.float64)
+        K = np.zeros_like(P, order="F")
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        _check(_lib.hfg_rs_exchange_host(self._h, _dptr(P), _dptr(K), flags))
+        return K
 
     def set_partition(self, nsplit: int = 0):
         """Exchange work partition as the autotuner would set it (0 = automatic)."""

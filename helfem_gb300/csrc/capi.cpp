@@ -243,10 +243,13 @@ hfg_status hfg_exchange_ex(hfg_atom* a, const double* P, double* K, int flags, v
   });
 }
 
-static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, int flags) {
+static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, int flags, bool screened = false) {
   need(a && P && out, "null argument");
   need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "unknown flags");
   a->check_device();
+  if (screened && !a->rs_ready)
+    throw std::logic_error("Primitive teis have not been computed!\n");
+  const hfg::DevAtom& ctx = screened ? a->dev_rs : a->dev;
   a->staging();
   const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
   cudaStream_t st = a->own_stream;
@@ -261,11 +264,11 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
       a->s_p2.alloc(b2);
       a->scr.p2 = a->s_p2.as<float2>();
     }
-    ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
+    ck(hfg::launch_exchange_split(ctx, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
                                   (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof),
        "exchange (split)");
   } else {
-    ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
+    ck(hfg::launch_exchange_fp64(ctx, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof),
        "exchange");
   }
@@ -396,6 +399,57 @@ hfg_status hfg_atom_set_partition(hfg_atom* a, int nsplit) {
     a->build_units();
     ck(cudaStreamSynchronize(a->own_stream), "sync");
   });
+}
+
+hfg_status hfg_atom_compute_yukawa(hfg_atom* a, double lambda) {
+  return guard([&] {
+    need(a != nullptr && lambda > 0.0, "hfg_atom_compute_yukawa: bad arguments");
+    if (a->on_device)
+      a->setup_yukawa(lambda);
+    else
+      a->host.build_yukawa(lambda);  // host-only handle: tables for checking
+  });
+}
+
+hfg_status hfg_atom_yukawa_tables(const hfg_atom* a, int L, int iel, double* rsmall, double* rbig, double* tk) {
+  return guard([&] {
+    need(a != nullptr, "hfg_atom_yukawa_tables: null handle");
+    const hfg::AtomHost& H = a->host;
+    need(H.y_lambda > 0.0, "hfg_atom_yukawa_tables: hfg_atom_compute_yukawa has not been called");
+    need(L >= 0 && L < H.NL && iel >= 0 && iel < H.rad.nel, "hfg_atom_yukawa_tables: L or iel out of range");
+    const size_t n2 = (size_t)H.rad.nn * H.rad.nn, le = (size_t)L * H.rad.nel + iel;
+    if (rsmall) std::copy(H.y_rs.begin() + le * n2, H.y_rs.begin() + (le + 1) * n2, rsmall);
+    if (rbig) std::copy(H.y_rb.begin() + le * n2, H.y_rb.begin() + (le + 1) * n2, rbig);
+    if (tk) std::copy(H.y_tk.begin() + le * n2 * n2, H.y_tk.begin() + (le + 1) * n2 * n2, tk);
+  });
+}
+
+hfg_status hfg_rs_exchange(hfg_atom* a, const double* P, double* K, int flags, void* stream) {
+  return guard([&] {
+    need(a && P && K, "hfg_rs_exchange: null argument");
+    need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "hfg_rs_exchange: unknown flags");
+    a->check_device();
+    if (!a->rs_ready) throw std::logic_error("Primitive teis have not been computed!\n");
+    const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
+    if (flags & HFG_EXCHANGE_SPLIT) {
+      const size_t b2 = sizeof(float2) * (size_t)a->host.nbf * a->host.nbf;
+      if (a->s_p2.n != b2) {
+        hfg_abi::AllocStream alloc_on(a->own_stream);
+        a->s_p2.alloc(b2);
+        a->scr.p2 = a->s_p2.as<float2>();
+      }
+      ck(hfg::launch_exchange_split(a->dev_rs, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
+         "screened exchange (split)");
+    } else {
+      ck(hfg::launch_exchange_fp64(a->dev_rs, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
+         "screened exchange");
+    }
+    a->mark_use((cudaStream_t)stream);
+  });
+}
+
+hfg_status hfg_rs_exchange_host(hfg_atom* a, const double* P, double* K, int flags) {
+  return guard([&] { host_call(a, P, K, false, flags, true); });
 }
 
 hfg_status hfg_coulomb_host(hfg_atom* a, const double* P, double* J) {

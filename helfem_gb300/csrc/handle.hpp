@@ -164,6 +164,34 @@ struct hfg_atom {
   // back overlaps the exchange build
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_j = nullptr;
+  // Yukawa-screened exchange: the exchange context with the screened radial
+  // tables (built by hfg_atom_compute_yukawa)
+  hfg::DevAtom dev_rs{};
+  bool rs_ready = false;
+  DBuf y_rs, y_rb, y_tk, y_rs2, y_rb2, y_tk2;
+  void setup_yukawa(double lambda) {
+    check_device();
+    host.build_yukawa(lambda);
+    hfg_abi::AllocStream alloc_on(own_stream);
+    ck(cudaStreamSynchronize(own_stream), "sync");
+    auto split = [](const std::vector<double>& v) {
+      std::vector<float2> o(v.size());
+      for (size_t i = 0; i < v.size(); ++i) {
+        const float hi = (float)v[i];
+        o[i] = make_float2(hi, (float)(v[i] - (double)hi));
+      }
+      return o;
+    };
+    dev_rs = dev;
+    dev_rs.rs = y_rs.upload(host.y_rs);
+    dev_rs.rb = y_rb.upload(host.y_rb);
+    dev_rs.tk = y_tk.upload(host.y_tk);
+    dev_rs.rs2 = y_rs2.upload(split(host.y_rs));
+    dev_rs.rb2 = y_rb2.upload(split(host.y_rb));
+    dev_rs.tk2 = y_tk2.upload(split(host.y_tk));
+    ck(cudaStreamSynchronize(own_stream), "sync after upload");
+    rs_ready = true;
+  }
   // DFT grid (built on first use or by hfg_dft_grid)
   hfg::DevXC xc{};
   hfg::XcScratch xs{};

@@ -11,7 +11,6 @@
 #include "atom.hpp"
 
 namespace hfg {
-namespace {
 
 // Greedy pivoted Cholesky with an absolute tolerance on the residual
 // diagonal, the factorisation HelFEM uses for the in-element tensor
@@ -46,8 +45,6 @@ std::vector<double> pivoted_cholesky(const std::vector<double>& A, int n, double
   }
   return L;
 }
-
-}  // namespace
 
 void AtomHost::build(int Z_, int nnodes, const std::vector<double>& bval, const std::vector<int>& lv,
                      const std::vector<int>& mv, int nquad_, double tol) {

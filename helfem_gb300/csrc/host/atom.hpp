@@ -12,12 +12,20 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
 namespace hfg {
 
 double gaunt_coeff(int L, int M, int l, int m, int lp);
+
+// greedy pivoted Cholesky of the n x n column-major A with an absolute
+// tolerance on the residual diagonal: n x rank column-major factor
+std::vector<double> pivoted_cholesky(const std::vector<double>& A, int n, double tol, int& rank);
+// modified spherical Bessel functions i_L, k_L (normalisation in yukawa.cpp)
+double bessel_il(double x, int L);
+double bessel_kl(double x, int L);
 
 // 1-D rules and Lagrange interpolating polynomials
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);
@@ -48,9 +56,15 @@ struct RadialBasis {
   void dR(int e, const std::vector<double>& x, std::vector<double>& out) const;
   // int R_a R_b r^(k+2) dr, nn x nn padded
   std::vector<double> radial_integral(int k, int e) const;
+  // int B_a B_b f(r) dr = int R_a R_b f(r) r^2 dr, nn x nn padded
+  std::vector<double> weighted_integral(const std::function<double(double)>& f, int e) const;
   std::vector<double> kinetic(int e) const;  // 1/2 int B'_a B'_b dr
   // in-element (ab|cd)_L, (nn^2 x nn^2) padded, pair index a + b*nn
   std::vector<double> twoe(int L, int e) const;
+  // in-element tensor of a separable kernel g(r<, r>) = fin(r<) fout(r>):
+  // (ab|cd) = int int B_aB_b(r) B_cB_d(r') g(r<, r>), same layout as twoe
+  std::vector<double> twoe_separable(const std::function<double(double)>& fin,
+                                     const std::function<double(double)>& fout, int e) const;
 };
 
 struct AtomHost {
@@ -108,6 +122,19 @@ struct AtomHost {
   // R and dR/dr of the nn primitives: [(e*nquad + q)*nn + p]
   std::vector<double> xc_r, xc_wr, xc_R, xc_dR;
   void build_dft_grid(int ldft, int mdft);
+
+  // ---- Yukawa-screened (range-separated) exchange ----------------------
+  // (src/atomic/TwoDBasis.cpp:736-758, 1001-1131): e^{-lambda r12}/r12 =
+  // 4 pi lambda sum_LM i_L(lambda r<) k_L(lambda r>) Y Y*, with the modified
+  // spherical Bessel functions i_L = sqrt(pi/2x) I_{L+1/2}, k_L =
+  // sqrt(2/(pi x)) K_{L+1/2}. The tables below carry the factor (2L+1) lambda
+  // relative to the bare ones, so that the bare coupling coefficients (which
+  // include 4 pi/(2L+1)) give 4 pi lambda: per (L, e) padded nn x nn
+  // y_rs = (2L+1) lambda int B B i_L(lambda r), y_rb = int B B k_L(lambda r),
+  // and y_tk the exchange-ordered in-element tensor (scaled likewise).
+  double y_lambda = 0.0;
+  std::vector<double> y_rs, y_rb, y_tk;
+  void build_yukawa(double lambda);
 
   void build(int Z, int nnodes, const std::vector<double>& bval, const std::vector<int>& lval,
              const std::vector<int>& mval, int nquad, double chol_tol);

@@ -241,9 +241,33 @@ std::vector<double> RadialBasis::kinetic(int e) const {
   return M;
 }
 
+std::vector<double> RadialBasis::weighted_integral(const std::function<double(double)>& f, int e) const {
+  std::vector<double> x, w, Bv;
+  gauss_legendre(128, x, w);
+  B(e, x, 0, Bv);
+  const int np = (int)x.size();
+  std::vector<double> wt(np);
+  for (int i = 0; i < np; ++i) wt[i] = w[i] * sf(e) * f(mid(e) + sf(e) * x[i]);
+  std::vector<double> M((size_t)nn * nn, 0.0);
+  for (int b = 0; b < nn; ++b)
+    for (int a = 0; a <= b; ++a) {
+      double s = 0.0;
+      for (int i = 0; i < np; ++i) s += Bv[i + (size_t)a * np] * Bv[i + (size_t)b * np] * wt[i];
+      M[a + (size_t)b * nn] = M[b + (size_t)a * nn] = s;
+    }
+  return M;
+}
+
 std::vector<double> RadialBasis::twoe(int L, int e) const {
-  // (ij|kl) = int dr B_iB_j(r) r^{-L-1} G_kl(r) + (ij <-> kl),
-  // G_kl(r) = int_{rmin}^{r} B_k B_l r'^L dr'  (polynomial: exact Gauss rule)
+  return twoe_separable([L](double r) { return std::pow(r, L); }, [L](double r) { return std::pow(r, -L - 1.0); },
+                        e);
+}
+
+std::vector<double> RadialBasis::twoe_separable(const std::function<double(double)>& fin,
+                                                const std::function<double(double)>& fout, int e) const {
+  // (ij|kl) = int dr B_iB_j(r) fout(r) G_kl(r) + (ij <-> kl),
+  // G_kl(r) = int_{rmin}^{r} B_k B_l fin(r') dr'  (bare kernel: polynomial,
+  // exact Gauss rule)
   const int no = 128, ni = 48;
   std::vector<double> xo, wo, xi, wi;
   gauss_legendre(no, xo, wo);
@@ -258,7 +282,7 @@ std::vector<double> RadialBasis::twoe(int L, int e) const {
     for (int q = 0; q < ni; ++q) {
       const double r = rmin + half * (xi[q] + 1.0);
       xin[q + (size_t)p * ni] = (r - mid(e)) / sf(e);
-      win[q + (size_t)p * ni] = half * wi[q] * std::pow(r, L);
+      win[q + (size_t)p * ni] = half * wi[q] * fin(r);
     }
   }
   std::vector<double> Bin;
@@ -280,7 +304,7 @@ std::vector<double> RadialBasis::twoe(int L, int e) const {
   std::vector<double> wb((size_t)no * n2);
   for (int p = 0; p < no; ++p) {
     const double ro = mid(e) + sf(e) * xo[p];
-    const double wp = wo[p] * sf(e) * std::pow(ro, -L - 1.0);
+    const double wp = wo[p] * sf(e) * fout(ro);
     for (int j = 0; j < nn; ++j)
       for (int i = 0; i < nn; ++i) wb[(size_t)p * n2 + i + j * nn] = wp * Bo[p + (size_t)i * no] * Bo[p + (size_t)j * no];
   }

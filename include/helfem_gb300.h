@@ -156,6 +156,27 @@ hfg_status hfg_atom_autotune(hfg_atom* atom, int flags, int* best_nsplit, double
  * picks): nsplit output-block ranges per element pair, 0 = automatic. */
 hfg_status hfg_atom_set_partition(hfg_atom* atom, int nsplit);
 
+/* Range-separated exchange with the Yukawa kernel e^{-lambda r12}/r12.
+ * hfg_atom_compute_yukawa replaces TwoDBasisT::compute_yukawa
+ * (src/atomic/TwoDBasis.cpp:736-758): the screened disjoint factors
+ * int B B i_L(lambda r), int B B k_L(lambda r) (modified spherical Bessel
+ * functions, libhelfem/include/math.h:48-110) and the pivoted-Cholesky
+ * in-element tensors of the screened kernel, built on the host in FP64 and
+ * uploaded; calling it again replaces lambda. hfg_rs_exchange replaces
+ * TwoDBasisT::rs_exchange (src/atomic/TwoDBasis.cpp:1001-1131) for that
+ * kernel: the same sign, screening and flags as hfg_exchange_ex; before
+ * compute_yukawa it fails with HFG_ERR_STATE. (The erfc kernel of
+ * compute_erfc is not provided.) */
+hfg_status hfg_atom_compute_yukawa(hfg_atom* atom, double lambda);
+/* The screened tables of multipole L and element iel as stored (padded
+ * nnodes x nnodes; r_small carries (2L+1) lambda so that the bare coupling
+ * factor 4 pi/(2L+1) becomes 4 pi lambda; tk is the exchange-ordered
+ * in-element tensor nnodes^2 x nnodes^2, same factor). Any output may be
+ * NULL. Works on host-only handles (for checking). */
+hfg_status hfg_atom_yukawa_tables(const hfg_atom* atom, int L, int iel, double* rsmall, double* rbig, double* tk);
+hfg_status hfg_rs_exchange(hfg_atom* atom, const double* P, double* K, int flags, void* stream);
+hfg_status hfg_rs_exchange_host(hfg_atom* atom, const double* P, double* K, int flags);
+
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
  * fixed 4 MiB array in the library's static device memory rather than the
  * handle's buffers. No counterpart in the reference; it exists for callers

@@ -4,7 +4,8 @@
 // type it instantiates:
 //
 //   atomic   TwoDBasisT<double>::coulomb / exchange / compute_tei / overlap /
-//            kinetic / nuclear           (src/atomic/TwoDBasis.h:180-227)
+//            kinetic / nuclear, compute_yukawa / rs_exchange
+//                                        (src/atomic/TwoDBasis.h:180-227)
 //   diatomic TwoDBasis::coulomb / exchange / compute_tei / overlap /
 //            kinetic / nuclear           (src/diatomic/basis.h:300-337)
 //   DFTGrid::eval_Fxc(x, c, P, H, Exc, Nel, thr) and the Pa/Pb overload
@@ -90,6 +91,20 @@ class AtomicTwoDBasis {
     detail::require_square(P, Nbf(), "exchange");
     Matrix K(P.rows(), P.cols());
     check(hfg_exchange_host(gpu_.get(), P.data(), K.data()));
+    return K;
+  }
+
+  // range-separated exchange with the Yukawa kernel exp(-lambda r12)/r12
+  // (TwoDBasis.h compute_yukawa / rs_exchange); compute_tei first
+  void compute_yukawa(double lambda) {
+    if (!gpu_) detail::no_tei();
+    check(hfg_atom_compute_yukawa(gpu_.get(), lambda));
+  }
+  Matrix rs_exchange(const Matrix& P) const {
+    if (!gpu_) detail::no_tei();
+    detail::require_square(P, Nbf(), "rs_exchange");
+    Matrix K(P.rows(), P.cols());
+    check(hfg_rs_exchange_host(gpu_.get(), P.data(), K.data(), 0));
     return K;
   }
 
