@@ -79,6 +79,7 @@ void AtomHost::build(int Z_, int nnodes, const std::vector<double>& bval, const 
   chol_rank.assign((size_t)NL * nel, 0);
   std::vector<std::vector<double>> cholpad((size_t)NL * nel);
 
+  rad.prepare_twoe();
 #pragma omp parallel for collapse(2) schedule(dynamic)
   for (int L = 0; L < NL; ++L)
     for (int e = 0; e < nel; ++e) {
@@ -113,16 +114,21 @@ void AtomHost::build(int Z_, int nnodes, const std::vector<double>& bval, const 
       const size_t le = (size_t)L * nel + e;
       const int r = chol_rank[le];
       std::copy(cholpad[le].begin(), cholpad[le].begin() + (size_t)n2 * r, cholp.begin() + le * n2 * rmax);
-      // exchange ordering: K_ac = sum_bd (ab|cd) P_bd, rows (a + c nn), cols (b + d nn)
+      // exchange ordering: K_ac = sum_bd (ab|cd) P_bd, rows (a + c nn), cols (b + d nn);
+      // the factor rows are transposed first so that each dot product is contiguous
       double* out = &tk[le * n2 * n2];
       const std::vector<double>& Lc = cholpad[le];
+      std::vector<double> Lt((size_t)n2 * r);
+      for (int p = 0; p < r; ++p)
+        for (int ab = 0; ab < n2; ++ab) Lt[(size_t)ab * r + p] = Lc[ab + (size_t)p * n2];
       for (int d = 0; d < nn; ++d)
         for (int b = 0; b < nn; ++b)
           for (int c = 0; c < nn; ++c)
             for (int a = 0; a < nn; ++a) {
               double s = 0.0;
-              const size_t ab = a + (size_t)b * nn, cd = c + (size_t)d * nn;
-              for (int p = 0; p < r; ++p) s += Lc[ab + (size_t)p * n2] * Lc[cd + (size_t)p * n2];
+              const double* x = &Lt[(a + (size_t)b * nn) * r];
+              const double* y = &Lt[(c + (size_t)d * nn) * r];
+              for (int p = 0; p < r; ++p) s += x[p] * y[p];
               out[(a + (size_t)c * nn) + (size_t)(b + d * nn) * n2] = s;
             }
     }

@@ -65,6 +65,11 @@ struct RadialBasis {
   // (ab|cd) = int int B_aB_b(r) B_cB_d(r') g(r<, r>), same layout as twoe
   std::vector<double> twoe_separable(const std::function<double(double)>& fin,
                                      const std::function<double(double)>& fout, int e) const;
+  // LIP values at the in-element tensor's quadrature points, which in
+  // reference coordinates do not depend on the element (filled by
+  // prepare_twoe before parallel tabulation; computed per call otherwise)
+  std::vector<double> tw_Bo, tw_Bin;
+  void prepare_twoe();
 };
 
 struct AtomHost {

@@ -263,58 +263,92 @@ std::vector<double> RadialBasis::twoe(int L, int e) const {
                         e);
 }
 
+namespace {
+constexpr int TW_NO = 128, TW_NI = 48;  // outer / inner Gauss-Legendre orders of the in-element tensor
+
+// inner points of the outer point p in reference coordinates: the inner
+// rule on [rmin, r_p] maps to x = -1 + (x_p + 1)(x_q + 1)/2
+void tw_points(std::vector<double>& xo, std::vector<double>& wo, std::vector<double>& xi, std::vector<double>& wi,
+               std::vector<double>& xin) {
+  gauss_legendre(TW_NO, xo, wo);
+  gauss_legendre(TW_NI, xi, wi);
+  xin.resize((size_t)TW_NO * TW_NI);
+  for (int p = 0; p < TW_NO; ++p)
+    for (int q = 0; q < TW_NI; ++q) xin[q + (size_t)p * TW_NI] = -1.0 + 0.5 * (xo[p] + 1.0) * (xi[q] + 1.0);
+}
+}  // namespace
+
+void RadialBasis::prepare_twoe() {
+  std::vector<double> xo, wo, xi, wi, xin;
+  tw_points(xo, wo, xi, wi, xin);
+  lip_eval(xo, nodes, 0, tw_Bo);
+  lip_eval(xin, nodes, 0, tw_Bin);
+}
+
 std::vector<double> RadialBasis::twoe_separable(const std::function<double(double)>& fin,
                                                 const std::function<double(double)>& fout, int e) const {
   // (ij|kl) = int dr B_iB_j(r) fout(r) G_kl(r) + (ij <-> kl),
   // G_kl(r) = int_{rmin}^{r} B_k B_l fin(r') dr'  (bare kernel: polynomial,
   // exact Gauss rule)
-  const int no = 128, ni = 48;
-  std::vector<double> xo, wo, xi, wi;
-  gauss_legendre(no, xo, wo);
-  gauss_legendre(ni, xi, wi);
+  const int no = TW_NO, ni = TW_NI;
+  std::vector<double> xo, wo, xi, wi, xin;
+  tw_points(xo, wo, xi, wi, xin);
   const double rmin = bval[e];
-  std::vector<double> Bo;
-  B(e, xo, 0, Bo);
-  std::vector<double> xin((size_t)no * ni), win((size_t)no * ni);
+  std::vector<double> Bo_raw, Bin_raw;
+  const std::vector<double>* Bo = &tw_Bo;
+  const std::vector<double>* Bin = &tw_Bin;
+  if (tw_Bo.empty() || tw_Bin.empty()) {
+    lip_eval(xo, nodes, 0, Bo_raw);
+    lip_eval(xin, nodes, 0, Bin_raw);
+    Bo = &Bo_raw;
+    Bin = &Bin_raw;
+  }
+  const size_t npin = xin.size();
+  std::vector<double> win(npin);
   for (int p = 0; p < no; ++p) {
     const double ro = mid(e) + sf(e) * xo[p];
     const double half = 0.5 * (ro - rmin);
     for (int q = 0; q < ni; ++q) {
       const double r = rmin + half * (xi[q] + 1.0);
-      xin[q + (size_t)p * ni] = (r - mid(e)) / sf(e);
       win[q + (size_t)p * ni] = half * wi[q] * fin(r);
     }
   }
-  std::vector<double> Bin;
-  B(e, xin, 0, Bin);
-  const size_t npin = xin.size();
+  // invalid primitives (the dropped r = 0 and r = Rmax functions) are zero
+  std::vector<char> ok(nn);
+  for (int k = 0; k < nn; ++k) ok[k] = valid(e, k);
   const int n2 = nn * nn;
   std::vector<double> G((size_t)no * n2, 0.0);  // G[p*n2 + k + l*nn]
   for (int p = 0; p < no; ++p)
     for (int l = 0; l < nn; ++l)
       for (int k = 0; k <= l; ++k) {
+        if (!ok[k] || !ok[l]) continue;
         double s = 0.0;
         for (int q = 0; q < ni; ++q) {
           const size_t iq = q + (size_t)p * ni;
-          s += win[iq] * Bin[iq + (size_t)k * npin] * Bin[iq + (size_t)l * npin];
+          s += win[iq] * (*Bin)[iq + (size_t)k * npin] * (*Bin)[iq + (size_t)l * npin];
         }
         G[(size_t)p * n2 + k + l * nn] = G[(size_t)p * n2 + l + k * nn] = s;
       }
   std::vector<double> T((size_t)n2 * n2, 0.0);
-  std::vector<double> wb((size_t)no * n2);
+  std::vector<double> wb((size_t)no * n2, 0.0);
   for (int p = 0; p < no; ++p) {
     const double ro = mid(e) + sf(e) * xo[p];
     const double wp = wo[p] * sf(e) * fout(ro);
     for (int j = 0; j < nn; ++j)
-      for (int i = 0; i < nn; ++i) wb[(size_t)p * n2 + i + j * nn] = wp * Bo[p + (size_t)i * no] * Bo[p + (size_t)j * no];
+      for (int i = 0; i < nn; ++i)
+        if (ok[i] && ok[j]) wb[(size_t)p * n2 + i + j * nn] = wp * (*Bo)[p + (size_t)i * no] * (*Bo)[p + (size_t)j * no];
   }
-  // T1[ij, kl] = sum_p wb[p, ij] G[p, kl];  T = T1 + T1^T
-  for (int kl = 0; kl < n2; ++kl)
-    for (int ij = 0; ij < n2; ++ij) {
-      double s = 0.0;
-      for (int p = 0; p < no; ++p) s += wb[(size_t)p * n2 + ij] * G[(size_t)p * n2 + kl];
-      T[ij + (size_t)kl * n2] = s;
+  // T1[ij, kl] = sum_p wb[p, ij] G[p, kl], p ascending, as rank-1 updates
+  // with a contiguous inner loop;  T = T1 + T1^T
+  for (int p = 0; p < no; ++p) {
+    const double* wbp = &wb[(size_t)p * n2];
+    for (int kl = 0; kl < n2; ++kl) {
+      const double g = G[(size_t)p * n2 + kl];
+      if (g == 0.0) continue;
+      double* Tc = &T[(size_t)kl * n2];
+      for (int ij = 0; ij < n2; ++ij) Tc[ij] += wbp[ij] * g;
     }
+  }
   for (int kl = 0; kl < n2; ++kl)
     for (int ij = 0; ij < kl; ++ij) {
       const double s = T[ij + (size_t)kl * n2] + T[kl + (size_t)ij * n2];

@@ -47,6 +47,7 @@ void AtomHost::build_yukawa(double lambda) {
   y_rs.assign((size_t)NL * nel * n2, 0.0);
   y_rb.assign((size_t)NL * nel * n2, 0.0);
   y_tk.assign((size_t)NL * nel * n2 * n2, 0.0);
+  rad.prepare_twoe();
 #pragma omp parallel for collapse(2) schedule(dynamic)
   for (int L = 0; L < NL; ++L)
     for (int e = 0; e < nel; ++e) {
@@ -64,13 +65,17 @@ void AtomHost::build_yukawa(double lambda) {
       const std::vector<double> Lc = pivoted_cholesky(T, n2, chol_tol, r);
       // exchange ordering: K_ac = sum_bd (ab|cd) P_bd, rows (a + c nn), cols (b + d nn)
       double* out = &y_tk[le * n2 * n2];
+      std::vector<double> Lt((size_t)n2 * r);
+      for (int p = 0; p < r; ++p)
+        for (int ab = 0; ab < n2; ++ab) Lt[(size_t)ab * r + p] = Lc[ab + (size_t)p * n2];
       for (int d = 0; d < nn; ++d)
         for (int b = 0; b < nn; ++b)
           for (int c = 0; c < nn; ++c)
             for (int a2 = 0; a2 < nn; ++a2) {
               double s = 0.0;
-              const size_t ab = a2 + (size_t)b * nn, cd = c + (size_t)d * nn;
-              for (int p = 0; p < r; ++p) s += Lc[ab + (size_t)p * n2] * Lc[cd + (size_t)p * n2];
+              const double* x = &Lt[(a2 + (size_t)b * nn) * r];
+              const double* y = &Lt[(c + (size_t)d * nn) * r];
+              for (int p = 0; p < r; ++p) s += x[p] * y[p];
               out[(a2 + (size_t)c * nn) + (size_t)(b + d * nn) * n2] = scale * s;
             }
     }
