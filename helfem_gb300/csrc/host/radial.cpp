@@ -15,13 +15,32 @@
 // (their r = 0 pole lies outside the element), which gives the same values to
 // a few ulps at a fraction of the cost.
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <stdexcept>
+#include <utility>
 
 #include "atom.hpp"
 
 namespace hfg {
 
+namespace {
+// rules are computed once per order (the tabulation asks for the same few
+// orders thousands of times, from several threads)
+std::mutex gl_mutex;
+std::map<int, std::pair<std::vector<double>, std::vector<double>>> gl_cache;
+}  // namespace
+
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  {
+    std::lock_guard<std::mutex> g(gl_mutex);
+    auto it = gl_cache.find(n);
+    if (it != gl_cache.end()) {
+      x = it->second.first;
+      w = it->second.second;
+      return;
+    }
+  }
   x.assign(n, 0.0);
   w.assign(n, 0.0);
   for (int i = 0; i < (n + 1) / 2; ++i) {
@@ -53,6 +72,8 @@ void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
     x[n - 1 - i] = z;
     w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * pp * pp);
   }
+  std::lock_guard<std::mutex> g(gl_mutex);
+  gl_cache.emplace(n, std::make_pair(x, w));
 }
 
 void gauss_lobatto(int n, std::vector<double>& x, std::vector<double>& w) {
@@ -329,32 +350,54 @@ std::vector<double> RadialBasis::twoe_separable(const std::function<double(doubl
         }
         G[(size_t)p * n2 + k + l * nn] = G[(size_t)p * n2 + l + k * nn] = s;
       }
-  std::vector<double> T((size_t)n2 * n2, 0.0);
-  std::vector<double> wb((size_t)no * n2, 0.0);
+  // T1[ij, kl] = sum_p wb[p, ij] G[p, kl] (p ascending) is symmetric under
+  // i <-> j and k <-> l: it is accumulated over the valid pairs i <= j,
+  // k <= l only, as rank-1 updates with a contiguous inner loop
+  std::vector<int> pi, pj;
+  for (int j = 0; j < nn; ++j)
+    for (int i = 0; i <= j; ++i)
+      if (ok[i] && ok[j]) { pi.push_back(i); pj.push_back(j); }
+  const int np = (int)pi.size();
+  std::vector<double> wb((size_t)no * np), Gp((size_t)no * np);
   for (int p = 0; p < no; ++p) {
     const double ro = mid(e) + sf(e) * xo[p];
     const double wp = wo[p] * sf(e) * fout(ro);
-    for (int j = 0; j < nn; ++j)
-      for (int i = 0; i < nn; ++i)
-        if (ok[i] && ok[j]) wb[(size_t)p * n2 + i + j * nn] = wp * (*Bo)[p + (size_t)i * no] * (*Bo)[p + (size_t)j * no];
-  }
-  // T1[ij, kl] = sum_p wb[p, ij] G[p, kl], p ascending, as rank-1 updates
-  // with a contiguous inner loop;  T = T1 + T1^T
-  for (int p = 0; p < no; ++p) {
-    const double* wbp = &wb[(size_t)p * n2];
-    for (int kl = 0; kl < n2; ++kl) {
-      const double g = G[(size_t)p * n2 + kl];
-      if (g == 0.0) continue;
-      double* Tc = &T[(size_t)kl * n2];
-      for (int ij = 0; ij < n2; ++ij) Tc[ij] += wbp[ij] * g;
+    for (int a = 0; a < np; ++a) {
+      wb[(size_t)p * np + a] = wp * (*Bo)[p + (size_t)pi[a] * no] * (*Bo)[p + (size_t)pj[a] * no];
+      Gp[(size_t)p * np + a] = G[(size_t)p * n2 + pi[a] + pj[a] * nn];
     }
   }
-  for (int kl = 0; kl < n2; ++kl)
-    for (int ij = 0; ij < kl; ++ij) {
-      const double s = T[ij + (size_t)kl * n2] + T[kl + (size_t)ij * n2];
-      T[ij + (size_t)kl * n2] = T[kl + (size_t)ij * n2] = s;
+  std::vector<double> T1((size_t)np * np, 0.0);  // T1[a + b*np], a = ij pair, b = kl pair
+  // four consecutive p per sweep over T1 (each entry still sums p in order)
+  static_assert(TW_NO % 4 == 0, "outer rule length must be a multiple of 4");
+  for (int p = 0; p < no; p += 4) {
+    const double* w0 = &wb[(size_t)p * np];
+    const double* w1 = w0 + np;
+    const double* w2 = w1 + np;
+    const double* w3 = w2 + np;
+    for (int b = 0; b < np; ++b) {
+      const double g0 = Gp[(size_t)p * np + b], g1 = Gp[(size_t)(p + 1) * np + b];
+      const double g2 = Gp[(size_t)(p + 2) * np + b], g3 = Gp[(size_t)(p + 3) * np + b];
+      double* Tc = &T1[(size_t)b * np];
+      for (int a = 0; a < np; ++a) {
+        double t = Tc[a];
+        t += w0[a] * g0;
+        t += w1[a] * g1;
+        t += w2[a] * g2;
+        t += w3[a] * g3;
+        Tc[a] = t;
+      }
     }
-  for (int ij = 0; ij < n2; ++ij) T[ij + (size_t)ij * n2] *= 2.0;
+  }
+  // T = T1 + T1^T, expanded to all (i, j), (k, l)
+  std::vector<double> T((size_t)n2 * n2, 0.0);
+  for (int b = 0; b < np; ++b)
+    for (int a = 0; a < np; ++a) {
+      const double v = (a == b) ? 2.0 * T1[a + (size_t)a * np] : T1[a + (size_t)b * np] + T1[b + (size_t)a * np];
+      const int i = pi[a], j = pj[a], k = pi[b], l = pj[b];
+      const size_t ij = i + (size_t)j * nn, ji = j + (size_t)i * nn, kl = k + (size_t)l * nn, lk = l + (size_t)k * nn;
+      T[ij + kl * n2] = T[ji + kl * n2] = T[ij + lk * n2] = T[ji + lk * n2] = v;
+    }
   return T;
 }
 
