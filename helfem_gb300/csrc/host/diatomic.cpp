@@ -363,6 +363,17 @@ void DiatomicHost::tabulate_radial() {
       for (int b = 0; b < nn; ++b)
         for (int a = 0; a <= b; ++a) { pa.push_back(a); pb.push_back(b); }
       const int np = (int)pa.size();
+      // element-dependent, channel-independent factors: hyperbolic functions
+      // of the quadrature points and the basis pair products (pair-contiguous)
+      std::vector<double> sh1(NGL_OUT), ch1(NGL_OUT), sh2(n2i), ch2(n2i);
+      for (int q = 0; q < NGL_OUT; ++q) { sh1[q] = std::sinh(mu1[q]); ch1[q] = std::cosh(mu1[q]); }
+      for (size_t i = 0; i < n2i; ++i) { sh2[i] = std::sinh(mu2[i]); ch2[i] = std::cosh(mu2[i]); }
+      std::vector<double> BB1((size_t)NGL_OUT * np), BB2(n2i * np);
+      for (int q = 0; q < NGL_OUT; ++q)
+        for (int k = 0; k < np; ++k)
+          BB1[(size_t)q * np + k] = B1[q + (size_t)pa[k] * NGL_OUT] * B1[q + (size_t)pb[k] * NGL_OUT];
+      for (size_t i = 0; i < n2i; ++i)
+        for (int k = 0; k < np; ++k) BB2[i * np + k] = B2[i + (size_t)pa[k] * n2i] * B2[i + (size_t)pb[k] * n2i];
       std::vector<double> inner0((size_t)NGL_OUT * np), inner2((size_t)NGL_OUT * np);
       std::vector<double> outer0((size_t)NGL_OUT * np), outer2((size_t)NGL_OUT * np);
       std::vector<double> res((size_t)4 * np * np);
@@ -371,14 +382,15 @@ void DiatomicHost::tabulate_radial() {
         const int L = lm_L[ilm], M = lm_M[ilm];
         const size_t lmo = (size_t)M * NLs + L;
         for (int q = 0; q < NGL_OUT; ++q) {
-          const double sh = std::sinh(mu1[q]), ch = std::cosh(mu1[q]);
+          const double sh = sh1[q], ch = ch1[q];
           const double wq0 = w1[q] * sh * Q1[(size_t)q * NMs * NLs + lmo];
           double* o0 = outer0.data() + (size_t)q * np;
           double* o2 = outer2.data() + (size_t)q * np;
           double* i0 = inner0.data() + (size_t)q * np;
           double* i2 = inner2.data() + (size_t)q * np;
+          const double* bq = BB1.data() + (size_t)q * np;
           for (int k = 0; k < np; ++k) {
-            const double bb = B1[q + (size_t)pa[k] * NGL_OUT] * B1[q + (size_t)pb[k] * NGL_OUT];
+            const double bb = bq[k];
             o0[k] = wq0 * bb;
             o2[k] = wq0 * ch * ch * bb;
             i0[k] = 0.0;
@@ -386,27 +398,32 @@ void DiatomicHost::tabulate_radial() {
           }
           for (int r = 0; r < NGL_IN; ++r) {
             const size_t ii = (size_t)q * NGL_IN + r;
-            const double sh2 = std::sinh(mu2[ii]), ch2 = std::cosh(mu2[ii]);
-            const double wr0 = w2[ii] * sh2 * P2[ii * NMs * NLs + lmo], wr2 = wr0 * ch2 * ch2;
+            const double wr0 = w2[ii] * sh2[ii] * P2[ii * NMs * NLs + lmo], wr2 = wr0 * ch2[ii] * ch2[ii];
+            const double* bi = BB2.data() + ii * np;
             for (int k = 0; k < np; ++k) {
-              const double bb = B2[ii + (size_t)pa[k] * n2i] * B2[ii + (size_t)pb[k] * n2i];
+              const double bb = bi[k];
               i0[k] += wr0 * bb;
               i2[k] += wr2 * bb;
             }
           }
         }
-        // res_kl[c + d*np] = sum_q outer_k[q][c] inner_l[q][d]
+        // res_kl[c + d*np] = sum_q outer_k[q][c] inner_l[q][d] (q ascending,
+        // as rank-1 updates with a contiguous inner loop)
         const double* outs[2] = {outer0.data(), outer2.data()};
         const double* ins[2] = {inner0.data(), inner2.data()};
+        std::fill(res.begin(), res.end(), 0.0);
         for (int k = 0; k < 2; ++k)
           for (int l = 0; l < 2; ++l) {
             double* R = res.data() + (size_t)(2 * k + l) * np * np;
-            for (int d = 0; d < np; ++d)
-              for (int c = 0; c < np; ++c) {
-                double s = 0.0;
-                for (int q = 0; q < NGL_OUT; ++q) s += outs[k][(size_t)q * np + c] * ins[l][(size_t)q * np + d];
-                R[c + (size_t)d * np] = s;
+            for (int q = 0; q < NGL_OUT; ++q) {
+              const double* oq = outs[k] + (size_t)q * np;
+              const double* iq = ins[l] + (size_t)q * np;
+              for (int d = 0; d < np; ++d) {
+                const double v = iq[d];
+                double* Rd = R + (size_t)d * np;
+                for (int c = 0; c < np; ++c) Rd[c] += oq[c] * v;
               }
+            }
           }
         // T_kl(cd, ab) = res_kl(cd, ab) + res_lk(ab, cd); W = [[T00, -T02], [-T02', T22]]
         auto T = [&](int k, int l, int c, int d) {
