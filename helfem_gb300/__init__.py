@@ -225,17 +225,24 @@ def _stream(stream):
 
 
 class Atom:
-    """One atomic basis with its cached two-electron tables (host FP64) and
-    their device copies. Mirrors TwoDBasisT construction + compute_tei."""
+    """One atomic basis with its cached two-electron tables (FP64) and their
+    device copies. Mirrors TwoDBasisT construction + compute_tei.
+
+    tabulate="device" (default) forms the in-element two-electron factors and
+    the exchange tensor on the GPU; "host" tabulates everything on the host
+    and uploads it. host_only=True builds the host tables only (no GPU)."""
 
     def __init__(self, Z: int, bval, lval, mval, nnodes: int = 15, nquad: int = 0,
-                 chol_tol: float = 0.0, host_only: bool = False):
+                 chol_tol: float = 0.0, host_only: bool = False, tabulate: str = "device"):
+        if tabulate not in ("device", "host"):
+            raise ValueError("tabulate must be 'device' or 'host'")
         self.Z = int(Z)
         self.bval = np.ascontiguousarray(bval, dtype=np.float64)
         self.lval = np.ascontiguousarray(lval, dtype=np.int32)
         self.mval = np.ascontiguousarray(mval, dtype=np.int32)
+        mode = 1 if host_only else (2 if tabulate == "host" else 0)
         d = _Desc(self.Z, nnodes, nquad, len(self.bval) - 1, _dptr(self.bval), len(self.lval),
-                  self.lval.ctypes.data_as(_I), self.mval.ctypes.data_as(_I), chol_tol, int(host_only))
+                  self.lval.ctypes.data_as(_I), self.mval.ctypes.data_as(_I), chol_tol, mode)
         h = _P()
         _check(_lib.hfg_atom_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h
@@ -463,12 +470,14 @@ class Engine:
 
     def submit(self, Z, bval, lval, mval, nela, nelb, method="hf", restricted=True, nnodes=15, symmetry=1,
                fixed_occ=None, e_tol=0.0, diis_tol=0.0, frac_aufbau=False, split=False, l_occ=None,
-               maxiter=0) -> int:
+               maxiter=0, tabulate="device") -> int:
+        if tabulate not in ("device", "host"):
+            raise ValueError("tabulate must be 'device' or 'host'")
         bval = np.ascontiguousarray(bval, dtype=np.float64)
         lval = np.ascontiguousarray(lval, dtype=np.int32)
         mval = np.ascontiguousarray(mval, dtype=np.int32)
         ad = _Desc(int(Z), nnodes, 0, len(bval) - 1, _dptr(bval), len(lval), lval.ctypes.data_as(_I),
-                   mval.ctypes.data_as(_I), 0.0, 0)
+                   mval.ctypes.data_as(_I), 0.0, 2 if tabulate == "host" else 0)
         occ, nfix = None, 0
         if fixed_occ is not None:
             ms = sorted(set(int(m) for m in mval))

@@ -118,8 +118,11 @@ hfg_status hfg_atom_create(const hfg_atom_desc* d, hfg_atom** out) {
     std::vector<int> lv(d->lval, d->lval + d->nang), mv(d->mval, d->mval + d->nang);
     for (int l : lv) need(l <= 3, "hfg_atom_create: l <= 3 supported");
     std::unique_ptr<hfg_atom> a(new hfg_atom());
-    a->host.build(d->Z, d->nnodes, bval, lv, mv, d->nquad, d->chol_tol);
-    if (!d->host_only) a->upload();
+    need(d->host_only >= 0 && d->host_only <= 2, "hfg_atom_create: host_only must be 0, 1 or 2");
+    // 0: device handle, two-electron tables tabulated on the device;
+    // 1: host only; 2: device handle with the host tabulation uploaded
+    a->host.build(d->Z, d->nnodes, bval, lv, mv, d->nquad, d->chol_tol, d->host_only != 0);
+    if (d->host_only != 1) a->upload();
     *out = a.release();
   });
 }
@@ -159,6 +162,7 @@ hfg_status hfg_atom_radial_tables(const hfg_atom* a, int L, int iel, int* ni, do
     need(a != nullptr, "null handle");
     const hfg::AtomHost& H = a->host;
     need(L >= 0 && L < H.NL && iel >= 0 && iel < H.rad.nel, "L or iel out of range");
+    const_cast<hfg_atom*>(a)->ensure_host_factors();
     const int nn = H.rad.nn, p0 = H.rad.pfirst(iel), n = H.rad.nfun(iel);
     const size_t le = (size_t)L * H.rad.nel + iel;
     if (ni) *ni = n;

@@ -74,6 +74,10 @@ size_t hfg_job_footprint(const hfg_atom_desc& a, const hfg_scf_desc& s) {
   const int nspin = s.restricted ? 1 : 2;
   b += 8.0 * nbf * nbf * 13;                                        // T V H P Ps J K XC F
   b += 8.0 * nbf * nbf * 0.5 * nspin * 20;                          // blocks, eigenvectors, DIIS history
+  // device tabulation scratch (pair-packed tensor, full-width factor), freed
+  // before the SCF buffers are allocated
+  const double tab = 8.0 * NL * nel * (1.5 * n2 * n2);
+  b += std::max(0.0, tab - 8.0 * nbf * nbf * (13 + 10 * nspin));
   if (s.x_func || s.c_func) {
     const double nq = a.nquad > 0 ? a.nquad : 5 * nn, nap = (4.0 * lmax + 12) * (4.0 * mmx + 12);
     b += 8.0 * (4 * nel * nang * nang * nq + 8 * nel * nq * nap + 8 * nel * nang * nang * nq + 3 * nang * nang * nap);
@@ -138,7 +142,7 @@ struct hfg_engine {
         try {
           std::unique_ptr<hfg_atom> atom(new hfg_atom());
           atom->host.build(job->atom.Z, job->atom.nnodes, job->bval, job->lval, job->mval, job->atom.nquad,
-                           job->atom.chol_tol);
+                           job->atom.chol_tol, job->atom.host_only == 2);
           atom->own_stream = st;  // the worker's stream; the atom does not own it
           atom->upload();
           t_setup = Clock::now();

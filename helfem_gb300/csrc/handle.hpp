@@ -6,7 +6,9 @@
 
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -14,6 +16,7 @@
 
 #include "helfem_gb300.h"
 #include "cuda/devatom.cuh"
+#include "cuda/tab.cuh"
 #include "host/atom.hpp"
 
 namespace hfg_abi {
@@ -264,12 +267,16 @@ struct hfg_atom {
     A.nang = H.nang;
     A.nbf = H.nbf;
     A.NL = H.NL;
-    A.rmax = H.rmax;
     A.rs = d_rs.upload(H.rs);
     A.rb = d_rb.upload(H.rb);
-    A.cholp = d_cholp.upload(H.cholp);
-    A.rank = d_rank.upload(H.chol_rank);
-    A.tk = d_tk.upload(H.tk);
+    if (H.twoe_on_host) {
+      A.cholp = d_cholp.upload(H.cholp);
+      A.rank = d_rank.upload(H.chol_rank);
+      A.tk = d_tk.upload(H.tk);
+    } else {
+      tabulate_device();
+    }
+    A.rmax = H.rmax;
     std::vector<int> chanL;
     for (auto& c : H.chans) chanL.push_back(c.L);
     A.nchan = (int)H.chans.size();
@@ -329,11 +336,99 @@ struct hfg_atom {
     };
     A.rs2 = d_rs2.upload(split(H.rs));
     A.rb2 = d_rb2.upload(split(H.rb));
-    A.tk2 = d_tk2.upload(split(H.tk));
+    {
+      const size_t ntk = (size_t)A.NL * A.nel * n2 * n2;
+      d_tk2.alloc(sizeof(float2) * std::max<size_t>(1, ntk));
+      ck(hfg::launch_split_f2(A.tk, d_tk2.as<float2>(), ntk, own_stream), "split copy of the exchange tensor");
+      A.tk2 = d_tk2.as<float2>();
+    }
     A.kterm_coef2 = d_kcoef2.upload(split(H.kterm_coef));
     build_units();
     ck(cudaStreamSynchronize(own_stream), "sync after upload");
     on_device = true;
+  }
+
+  // In-element factors and exchange tensor tabulated on the device (FP64,
+  // the host tabulation's quadrature and pivoting rule); fills the host's
+  // ranks and rmax. Scratch (pair-packed tensor, full-width factor) is
+  // released on the handle's stream.
+  void tabulate_device() {
+    using namespace hfg;
+    AtomHost& H = host;
+    const int nn = H.rad.nn, nel = H.rad.nel, NL = H.NL;
+    const size_t n2 = (size_t)nn * nn, nblk = (size_t)NL * nel;
+    std::vector<double> xo, wo, xi, wi, xin;
+    twoe_points(xo, wo, xi, wi, xin);
+    if (H.rad.tw_Bo.empty() || H.rad.tw_Bin.empty()) H.rad.prepare_twoe();
+    std::vector<unsigned char> ok((size_t)nel * nn);
+    for (int e = 0; e < nel; ++e)
+      for (int k = 0; k < nn; ++k) ok[(size_t)e * nn + k] = H.rad.valid(e, k) ? 1 : 0;
+    DBuf b_bval, b_xo, b_wo, b_xi, b_wi, b_Bo, b_Bin, b_ok, b_T1, b_L;
+    TabInput in{};
+    in.nn = nn;
+    in.nel = nel;
+    in.NL = NL;
+    in.no = TWOE_NO;
+    in.ni = TWOE_NI;
+    in.bval = b_bval.upload(H.rad.bval);
+    in.xo = b_xo.upload(xo);
+    in.wo = b_wo.upload(wo);
+    in.xi = b_xi.upload(xi);
+    in.wi = b_wi.upload(wi);
+    in.Bo = b_Bo.upload(H.rad.tw_Bo);
+    in.Bin = b_Bin.upload(H.rad.tw_Bin);
+    in.ok = b_ok.upload(ok);
+    in.tol = H.chol_tol;
+    b_T1.alloc(sizeof(double) * tab_t1_doubles(nn, nel, NL));
+    b_L.alloc(sizeof(double) * tab_factor_doubles(nn, nel, NL));
+    d_rank.alloc(sizeof(int) * nblk);
+    ck(launch_tab_factor(in, b_T1.as<double>(), b_L.as<double>(), d_rank.as<int>(), own_stream),
+       "in-element tensor and factor");
+    H.chol_rank.assign(nblk, 0);
+    ck(cudaMemcpyAsync(H.chol_rank.data(), d_rank.p, sizeof(int) * nblk, cudaMemcpyDeviceToHost, own_stream),
+       "factor ranks");
+    ck(cudaStreamSynchronize(own_stream), "sync after the factorisation");
+    H.rmax = 1;
+    for (int r : H.chol_rank) H.rmax = std::max(H.rmax, r);
+    d_cholp.alloc(sizeof(double) * nblk * n2 * H.rmax);
+    d_tk.alloc(sizeof(double) * nblk * n2 * n2);
+    ck(launch_tab_finish(in, b_L.as<double>(), d_rank.as<int>(), H.rmax, d_cholp.as<double>(), d_tk.as<double>(),
+                         own_stream),
+       "padded factor and exchange tensor");
+    dev.cholp = d_cholp.as<double>();
+    dev.rank = d_rank.as<int>();
+    dev.tk = d_tk.as<double>();
+  }
+
+  // Host copies of the factors of a device-tabulated handle (compact
+  // reference layout and the padded one), fetched on first request.
+  std::mutex host_fill_mu;
+  void ensure_host_factors() {
+    std::lock_guard<std::mutex> g(host_fill_mu);
+    hfg::AtomHost& H = host;
+    if (H.twoe_on_host || !H.chol.empty()) return;
+    check_device();
+    const int nn = H.rad.nn, nel = H.rad.nel;
+    const size_t n2 = (size_t)nn * nn, nblk = (size_t)H.NL * nel;
+    std::vector<double> cp(nblk * n2 * H.rmax);
+    ck(cudaMemcpyAsync(cp.data(), dev.cholp, sizeof(double) * cp.size(), cudaMemcpyDeviceToHost, own_stream),
+       "factor download");
+    ck(cudaStreamSynchronize(own_stream), "sync after the factor download");
+    std::vector<std::vector<double>> ch(nblk);
+    for (int L = 0; L < H.NL; ++L)
+      for (int e = 0; e < nel; ++e) {
+        const size_t le = (size_t)L * nel + e;
+        const int r = H.chol_rank[le], p0 = H.rad.pfirst(e), ni = H.rad.nfun(e);
+        std::vector<double>& c = ch[le];
+        c.assign((size_t)ni * ni * r, 0.0);
+        for (int p = 0; p < r; ++p)
+          for (int b = 0; b < ni; ++b)
+            for (int a2 = 0; a2 < ni; ++a2)
+              c[(a2 + (size_t)b * ni) + (size_t)p * ni * ni] =
+                  cp[le * n2 * H.rmax + (a2 + p0) + (size_t)(b + p0) * nn + (size_t)p * n2];
+      }
+    H.cholp = std::move(cp);
+    H.chol = std::move(ch);
   }
 
   // Exchange work units: element pairs split into balanced ranges of output

@@ -47,7 +47,7 @@ std::vector<double> pivoted_cholesky(const std::vector<double>& A, int n, double
 }
 
 void AtomHost::build(int Z_, int nnodes, const std::vector<double>& bval, const std::vector<int>& lv,
-                     const std::vector<int>& mv, int nquad_, double tol) {
+                     const std::vector<int>& mv, int nquad_, double tol, bool twoe_host) {
   if (nnodes < 3) throw std::invalid_argument("need at least 3 nodes per element");
   if (bval.size() < 2) throw std::invalid_argument("need at least one element");
   for (size_t i = 1; i < bval.size(); ++i)
@@ -79,6 +79,7 @@ void AtomHost::build(int Z_, int nnodes, const std::vector<double>& bval, const 
   chol_rank.assign((size_t)NL * nel, 0);
   std::vector<std::vector<double>> cholpad((size_t)NL * nel);
 
+  twoe_on_host = twoe_host;
   rad.prepare_twoe();
 #pragma omp parallel for collapse(2) schedule(dynamic)
   for (int L = 0; L < NL; ++L)
@@ -90,6 +91,7 @@ void AtomHost::build(int Z_, int nnodes, const std::vector<double>& bval, const 
         auto b = rad.radial_integral(-L - 1, e);
         std::copy(b.begin(), b.end(), rb.begin() + le * n2);
       }
+      if (!twoe_host) continue;
       const std::vector<double> T = rad.twoe(L, e);
       int r = 0;
       cholpad[le] = pivoted_cholesky(T, n2, chol_tol, r);
@@ -106,11 +108,18 @@ void AtomHost::build(int Z_, int nnodes, const std::vector<double>& bval, const 
     }
   rmax = 0;
   for (int r : chol_rank) rmax = std::max(rmax, r);
-  cholp.assign((size_t)NL * nel * n2 * rmax, 0.0);
-  tk.assign((size_t)NL * nel * n2 * n2, 0.0);
-#pragma omp parallel for collapse(2) schedule(dynamic)
+  if (twoe_host) {
+    cholp.assign((size_t)NL * nel * n2 * rmax, 0.0);
+    tk.assign((size_t)NL * nel * n2 * n2, 0.0);
+  } else {
+    chol.clear();
+    cholp.clear();
+    tk.clear();
+  }
+#pragma omp parallel for collapse(2) schedule(dynamic) if (twoe_host)
   for (int L = 0; L < NL; ++L)
     for (int e = 0; e < nel; ++e) {
+      if (!twoe_host) continue;
       const size_t le = (size_t)L * nel + e;
       const int r = chol_rank[le];
       std::copy(cholpad[le].begin(), cholpad[le].begin() + (size_t)n2 * r, cholp.begin() + le * n2 * rmax);

@@ -34,6 +34,13 @@ void cheb_rule(int n, std::vector<double>& x, std::vector<double>& w);
 // d^n L_i(x)/dx^n for all nodes, out[ix + i*npts]
 void lip_eval(const std::vector<double>& x, const std::vector<double>& nodes, int nder,
               std::vector<double>& out);
+// quadrature of the in-element two-electron tensor: outer Gauss-Legendre rule
+// (TWOE_NO points) on the element and, for outer point p, the inner rule
+// (TWOE_NI points) on [r_min, r_p], whose reference coordinates are
+// xin[q + p*TWOE_NI] = -1 + (xo[p] + 1)(xi[q] + 1)/2
+constexpr int TWOE_NO = 128, TWOE_NI = 48;
+void twoe_points(std::vector<double>& xo, std::vector<double>& wo, std::vector<double>& xi, std::vector<double>& wi,
+                 std::vector<double>& xin);
 
 struct RadialBasis {
   int nn = 0;    // nodes (functions) per element
@@ -141,8 +148,11 @@ struct AtomHost {
   std::vector<double> y_rs, y_rb, y_tk;
   void build_yukawa(double lambda);
 
+  // twoe_host = false leaves the in-element factors (chol, cholp, tk,
+  // chol_rank, rmax) to the device tabulation
   void build(int Z, int nnodes, const std::vector<double>& bval, const std::vector<int>& lval,
-             const std::vector<int>& mval, int nquad, double chol_tol);
+             const std::vector<int>& mval, int nquad, double chol_tol, bool twoe_host = true);
+  bool twoe_on_host = true;
   void build_couplings();
 };
 

@@ -284,24 +284,18 @@ std::vector<double> RadialBasis::twoe(int L, int e) const {
                         e);
 }
 
-namespace {
-constexpr int TW_NO = 128, TW_NI = 48;  // outer / inner Gauss-Legendre orders of the in-element tensor
-
-// inner points of the outer point p in reference coordinates: the inner
-// rule on [rmin, r_p] maps to x = -1 + (x_p + 1)(x_q + 1)/2
-void tw_points(std::vector<double>& xo, std::vector<double>& wo, std::vector<double>& xi, std::vector<double>& wi,
-               std::vector<double>& xin) {
-  gauss_legendre(TW_NO, xo, wo);
-  gauss_legendre(TW_NI, xi, wi);
-  xin.resize((size_t)TW_NO * TW_NI);
-  for (int p = 0; p < TW_NO; ++p)
-    for (int q = 0; q < TW_NI; ++q) xin[q + (size_t)p * TW_NI] = -1.0 + 0.5 * (xo[p] + 1.0) * (xi[q] + 1.0);
+void twoe_points(std::vector<double>& xo, std::vector<double>& wo, std::vector<double>& xi, std::vector<double>& wi,
+                 std::vector<double>& xin) {
+  gauss_legendre(TWOE_NO, xo, wo);
+  gauss_legendre(TWOE_NI, xi, wi);
+  xin.resize((size_t)TWOE_NO * TWOE_NI);
+  for (int p = 0; p < TWOE_NO; ++p)
+    for (int q = 0; q < TWOE_NI; ++q) xin[q + (size_t)p * TWOE_NI] = -1.0 + 0.5 * (xo[p] + 1.0) * (xi[q] + 1.0);
 }
-}  // namespace
 
 void RadialBasis::prepare_twoe() {
   std::vector<double> xo, wo, xi, wi, xin;
-  tw_points(xo, wo, xi, wi, xin);
+  twoe_points(xo, wo, xi, wi, xin);
   lip_eval(xo, nodes, 0, tw_Bo);
   lip_eval(xin, nodes, 0, tw_Bin);
 }
@@ -311,9 +305,9 @@ std::vector<double> RadialBasis::twoe_separable(const std::function<double(doubl
   // (ij|kl) = int dr B_iB_j(r) fout(r) G_kl(r) + (ij <-> kl),
   // G_kl(r) = int_{rmin}^{r} B_k B_l fin(r') dr'  (bare kernel: polynomial,
   // exact Gauss rule)
-  const int no = TW_NO, ni = TW_NI;
+  const int no = TWOE_NO, ni = TWOE_NI;
   std::vector<double> xo, wo, xi, wi, xin;
-  tw_points(xo, wo, xi, wi, xin);
+  twoe_points(xo, wo, xi, wi, xin);
   const double rmin = bval[e];
   std::vector<double> Bo_raw, Bin_raw;
   const std::vector<double>* Bo = &tw_Bo;
@@ -369,7 +363,7 @@ std::vector<double> RadialBasis::twoe_separable(const std::function<double(doubl
   }
   std::vector<double> T1((size_t)np * np, 0.0);  // T1[a + b*np], a = ij pair, b = kl pair
   // four consecutive p per sweep over T1 (each entry still sums p in order)
-  static_assert(TW_NO % 4 == 0, "outer rule length must be a multiple of 4");
+  static_assert(TWOE_NO % 4 == 0, "outer rule length must be a multiple of 4");
   for (int p = 0; p < no; p += 4) {
     const double* w0 = &wb[(size_t)p * np];
     const double* w1 = w0 + np;

@@ -59,9 +59,15 @@ typedef struct {
   const int* lval;     /* [nang] l of each angular function                  */
   const int* mval;     /* [nang] m of each angular function                  */
   double chol_tol;     /* pivoted-Cholesky tolerance; 0 -> 1e-12 (reference) */
-  int host_only;       /* 1: tabulate on the host only and never touch a GPU;
-                          the device entry points then fail with
-                          HFG_ERR_STATE (for CPU-side checks)             */
+  int host_only;       /* 0: device handle; the in-element two-electron
+                             factors and exchange tensor are tabulated on
+                             the GPU (rs/rb, one-electron and coupling
+                             tables on the host);
+                          1: tabulate on the host only and never touch a GPU;
+                             the device entry points then fail with
+                             HFG_ERR_STATE (for CPU-side checks);
+                          2: device handle with every table tabulated on
+                             the host and uploaded                          */
 } hfg_atom_desc;
 
 typedef struct {
