@@ -465,6 +465,7 @@ def run_scf_batch(args):
                      "p99": _percentile([r["setup_ms"] for r in res], 0.99),
                      "sum": float(sum(r["setup_ms"] for r in res)),
                      "form": "host tables + device tabulation and upload, per solve"},
+        "scf_phase_ms_sum": {k: float(sum(r["phase_ms"][k] for r in res)) for k in res[0]["phase_ms"]},
         "plain_path": {"value": len(jobs) / wall_p, "unit": "solves/s", "form": "one solve at a time, FP64 exchange",
                        "latency_ms_p99": _percentile([r["total_ms"] for r in res_p], 0.99)},
         "speedup_vs_plain": wall_p / wall,

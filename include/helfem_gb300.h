@@ -305,7 +305,7 @@ hfg_status hfg_scf_run(hfg_atom* atom, const hfg_scf_desc* desc, hfg_scf_result*
 
 /* ---- batched / serving runtime ----
  * Many atomic SCF solves on one GPU: worker threads, one CUDA stream each,
- * run whole solves (host tabulation, upload, device SCF) concurrently.
+ * run whole solves (tabulation, upload, device SCF) concurrently.
  * A queued job starts when its estimated device footprint fits in the HBM
  * budget still free (first fitting job in arrival order). The reference has
  * no counterpart (one atom per process); this serves the batched and
