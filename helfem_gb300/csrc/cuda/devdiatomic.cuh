@@ -125,9 +125,11 @@ cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScrat
                                     cudaStream_t st);
 cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
                                      double* Kd, bool symmetric, cudaStream_t st);
-// split-precision exchange (float-float on the FP32 pipe, FP64 recombination)
+// split-precision exchange (float-float on the FP32 pipe, FP64 recombination);
+// inline_diag: diagonal element tiles item by item inside the tile kernel
+// instead of the grouped kernel (bitwise the same K)
 cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
-                                           double* Kd, bool symmetric, cudaStream_t st);
+                                           double* Kd, bool symmetric, cudaStream_t st, bool inline_diag = false);
 // txs[i] = split(tx[i])
 cudaError_t launch_diatomic_split_tx(const double* tx, float2* txs, size_t n, cudaStream_t st);
 

@@ -478,13 +478,13 @@ __global__ void __launch_bounds__(320) dk_tiles(DevDiatomic D, DevDiatomicScratc
 template <int NN>
 // 15-node elements: 256 threads, at most 51 registers so that five CTAs share an SM
 __global__ void __launch_bounds__(NN == 15 ? 256 : 320, NN == 15 ? 5 : 1) dk_tiles_split(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd,
-                                                      int symmetric) {
+                                                      int symmetric, int with_diag) {
   const int nn = NN > 0 ? NN : D.nn, n2 = nn * nn, nang2 = D.nang * D.nang;
   const int n_act = S.counts[0], n_dact = symmetric ? S.counts[1] : S.counts[0];
   const int* dlist = symmetric ? S.jk_list + nang2 : S.jk_list;
   const int2* pairs = symmetric ? D.pairs_sym : D.pairs_all;
   const long npairs = symmetric ? D.npairs_sym : D.npairs_all;
-  const long n_off = npairs * n_act, total = n_off + (long)D.nel * n_dact;
+  const long n_off = npairs * n_act, total = n_off + (with_diag ? (long)D.nel * n_dact : 0L);
   extern __shared__ float2 sm2[];
   float2* X = sm2;           // [4*n2]
   float2* T = X + 4 * n2;    // [2*n2]
@@ -624,6 +624,171 @@ __global__ void __launch_bounds__(NN == 15 ? 256 : 320, NN == 15 ? 5 : 1) dk_til
   }
 }
 
+// Diagonal element tiles of the split exchange, G output blocks per item.
+// Item w: element e = w / ngroups, the active output blocks
+// dlist[G*(w % ngroups) ...]. The members' entry lists (ascending multipole
+// index ilm) are merged: per multipole present in any member, the members
+// holding it recouple their density tiles into shared memory, then one pass
+// over the exchange-ordered kernel table of (ilm, e) feeds all of them, so
+// each table element is loaded once per item instead of once per member.
+// Per member the operations and their order are those of the item-by-item
+// schedule in dk_tiles_split, so K is bitwise the same.
+constexpr int DIAG_GROUP = 8;
+
+template <int NN, int G>
+__global__ void __launch_bounds__(NN == 15 ? 256 : 320, NN == 15 ? 3 : 1) dk_diag_split(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd,
+                                                         int symmetric) {
+  const int nn = NN > 0 ? NN : D.nn, n2 = nn * nn, nang2 = D.nang * D.nang;
+  const int n_dact = symmetric ? S.counts[1] : S.counts[0];
+  const int* dlist = symmetric ? S.jk_list + nang2 : S.jk_list;
+  const int ngrp = (n_dact + G - 1) / G;
+  const long total = (long)D.nel * ngrp;
+  extern __shared__ float2 sm2[];
+  float2* X = sm2;  // [G][4*n2]
+  double* Y = reinterpret_cast<double*>(X + (size_t)G * 4 * n2);
+  unsigned char* act = reinterpret_cast<unsigned char*>(Y + n2);
+  __shared__ int s_ptr[G], s_end[G], s_jk[G], s_has[G];
+  __shared__ int s_ilm;
+  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.act[idx];
+  __syncthreads();
+  const int t = threadIdx.x;
+  const bool live = t < n2;
+  const int p = live ? t % nn : 0, q = live ? t / nn : 0;
+  for (long w = blockIdx.x; w < total; w += gridDim.x) {
+    const int e = (int)(w / ngrp), g0 = (int)(w % ngrp) * G;
+    const int ng = min(G, n_dact - g0);
+    if (t < G) {
+      if (t < ng) {
+        const int jk = dlist[g0 + t];
+        s_jk[t] = jk;
+        s_ptr[t] = D.kjk_ptr[jk];
+        s_end[t] = D.kjk_ptr[jk + 1];
+      } else {
+        s_jk[t] = -1;
+        s_ptr[t] = s_end[t] = 0;
+      }
+    }
+    __syncthreads();
+    const int gp = dgf(D, e, p), gq = dgf(D, e, q);
+    const bool vpq = live && gp < D.nrad && gq < D.nrad;
+    const float2* pbase = S.pd2 + (size_t)gq * D.nd + gp;
+    ffv yacc[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) yacc[g] = {0.f, 0.f};
+    for (;;) {
+      if (t < 32) {  // warp 0: skip inactive entries, smallest pending multipole
+        int pt = 0, me = 0x7fffffff;
+        if (t < G) {
+          pt = s_ptr[t];
+          while (pt < s_end[t] && !S.ent_act[pt]) ++pt;
+          s_ptr[t] = pt;
+          if (pt < s_end[t]) me = D.kent_ilm[pt];
+        }
+        int m = me;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (t < G) s_has[t] = (me == m && m != 0x7fffffff) ? 1 : 0;
+        if (t == 0) s_ilm = m;
+      }
+      __syncthreads();
+      const int ilm = s_ilm;
+      if (ilm == 0x7fffffff) break;
+#pragma unroll 1
+      for (int g = 0; g < G; ++g) {
+        float2* Xg = X + (size_t)g * 4 * n2;
+        if (!s_has[g]) {  // uniform over the CTA
+          if (live) Xg[t] = Xg[n2 + t] = Xg[2 * n2 + t] = Xg[3 * n2 + t] = make_float2(0.f, 0.f);
+          continue;
+        }
+        const int ent = s_ptr[g], jk = s_jk[g];
+        const int j = jk % D.nang, k = jk / D.nang;
+        const int L = D.kent_L[ent], Ma = D.kent_Ma[ent];
+        ffv x00 = {0.f, 0.f}, x02 = {0.f, 0.f}, x20 = {0.f, 0.f}, x22 = {0.f, 0.f};
+        if (vpq) {
+          for (int sgn = 0; sgn < (Ma ? 2 : 1); ++sgn) {
+            const int M = sgn ? -Ma : Ma;
+            const int xj = al_idx(D, j, L, M), xk = al_idx(D, k, L, M);
+            const int k0 = D.al_ptr[xk], k1 = D.al_ptr[xk + 1];
+            for (int uj = D.al_ptr[xj]; uj < D.al_ptr[xj + 1]; ++uj) {
+              const int i = D.al_b[uj];
+              ffv u0 = {0.f, 0.f}, u2 = {0.f, 0.f};
+              for (int uk = k0; uk < k1; ++uk) {
+                const int l = D.al_b[uk];
+                if (!act[i + l * D.nang]) continue;
+                const float2 v = pbase[(size_t)(l * D.nrad) * D.nd + (size_t)i * D.nrad];
+                u0 = ff_fma(u0, D.al_c0s[uk], v);
+                u2 = ff_fma(u2, D.al_c2s[uk], v);
+              }
+              const float2 U0 = ff2(u0), U2 = ff2(u2), c0 = D.al_c0s[uj], c2 = D.al_c2s[uj];
+              x00 = ff_fma(x00, c0, U0);
+              x02 = ff_fma(x02, c0, U2);
+              x20 = ff_fma(x20, c2, U0);
+              x22 = ff_fma(x22, c2, U2);
+            }
+          }
+        }
+        if (live) {
+          float2 fac = D.lmfacs[ilm];
+          if (Ma & 1) fac = make_float2(-fac.x, -fac.y);
+          const ffv z = {0.f, 0.f};
+          const float2 f00 = ff2(ff_fma(z, fac, ff2(x00))), f02 = ff2(ff_fma(z, fac, ff2(x02)));
+          const float2 f20 = ff2(ff_fma(z, fac, ff2(x20))), f22 = ff2(ff_fma(z, fac, ff2(x22)));
+          Xg[t] = f00;
+          Xg[n2 + t] = make_float2(-f02.x, -f02.y);
+          Xg[2 * n2 + t] = make_float2(-f20.x, -f20.y);
+          Xg[3 * n2 + t] = f22;
+        }
+      }
+      __syncthreads();
+      if (live) {
+        ffv acc[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) acc[g] = {0.f, 0.f};
+        const float2* tx = D.txs + ((size_t)ilm * D.nel + e) * 4 * n2 * n2;
+        for (int ab = 0; ab < 4; ++ab) {
+          const float2* txb = tx + (size_t)ab * n2 * n2;
+          for (int v0 = 0; v0 < n2; v0 += nn) {
+            if (NN > 0) {
+#pragma unroll
+              for (int c = 0; c < (NN > 0 ? NN : 1); ++c) {
+                const float2 tv = txb[t + (size_t)(v0 + c) * n2];
+#pragma unroll
+                for (int g = 0; g < G; ++g) acc[g] = ff_fma(acc[g], tv, X[(size_t)g * 4 * n2 + ab * n2 + v0 + c]);
+              }
+            } else {
+              for (int v = v0; v < v0 + nn; ++v) {
+                const float2 tv = txb[t + (size_t)v * n2];
+#pragma unroll
+                for (int g = 0; g < G; ++g) acc[g] = ff_fma(acc[g], tv, X[(size_t)g * 4 * n2 + ab * n2 + v]);
+              }
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) acc[g] = ff_norm(acc[g].hi, acc[g].lo);
+          }
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+          if (s_has[g]) yacc[g] = ff_add(yacc[g], ff_norm(acc[g].hi, acc[g].lo));
+      }
+      __syncthreads();
+      if (t < G && s_has[t]) ++s_ptr[t];
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (g >= ng) break;  // uniform over the CTA
+      const int jk = s_jk[g], j = jk % D.nang, k = jk / D.nang;
+      const double y = ff_to_d(yacc[g]);
+      if (live) dk_store(D, S, Kd, e, e, jk, p, q, -y);
+      if (symmetric && j != k) {
+        if (live) Y[t] = -y;
+        __syncthreads();
+        if (live) dk_store(D, S, Kd, e, e, k + j * D.nang, p, q, Y[q + p * nn]);
+      }
+      __syncthreads();
+    }
+  }
+}
+
 __global__ void d_split(const double* __restrict__ x, float2* __restrict__ y, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     y[i] = split_bits(x[i]);
@@ -726,7 +891,7 @@ cudaError_t launch_diatomic_split_tx(const double* tx, float2* txs, size_t n, cu
 }
 
 cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
-                                           double* Kd, bool symmetric, cudaStream_t st) {
+                                           double* Kd, bool symmetric, cudaStream_t st, bool inline_diag) {
   const int n2 = D.nn * D.nn, th = dthreads(n2), nang2 = D.nang * D.nang;
   cudaError_t e = cudaMemsetAsync(Kd, 0, sizeof(double) * (size_t)D.nd * D.nd, st);
   if (e != cudaSuccess) return e;
@@ -745,7 +910,20 @@ cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatom
   }
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, th, smem);
   if (e != cudaSuccess) return e;
-  kern<<<nsm * std::max(per, 1), th, smem, st>>>(D, S, Kd, symmetric ? 1 : 0);
+  kern<<<nsm * std::max(per, 1), th, smem, st>>>(D, S, Kd, symmetric ? 1 : 0, inline_diag ? 1 : 0);
+  if (!inline_diag) {
+    constexpr int G = DIAG_GROUP;
+    const size_t smd = sizeof(float2) * (size_t)G * 4 * n2 + sizeof(double) * n2 + nang2;
+    auto dkern = (D.nn == 15) ? dk_diag_split<15, G> : dk_diag_split<0, G>;
+    if (smd > 48 * 1024) {
+      e = cudaFuncSetAttribute(dkern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smd);
+      if (e != cudaSuccess) return e;
+    }
+    int dper = 1;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dper, dkern, th, smd);
+    if (e != cudaSuccess) return e;
+    dkern<<<nsm * std::max(dper, 1), th, smd, st>>>(D, S, Kd, symmetric ? 1 : 0);
+  }
   dk_fixup<<<D.nel * D.nel, 256, 0, st>>>(D, S, Kd);
   return cudaGetLastError();
 }

@@ -205,7 +205,8 @@ struct hfg_diatomic {
   }
 
   // J or K of a pure-basis density (device pointers) on stream st
-  void build(const double* P, double* F, bool exchange, bool symmetric, cudaStream_t st, bool split = false) {
+  void build(const double* P, double* F, bool exchange, bool symmetric, cudaStream_t st, bool split = false,
+             bool inline_diag = false) {
     check_device();
     const hfg::DiatomicHost& H = host;
     if (split) ensure_split();
@@ -216,7 +217,8 @@ struct hfg_diatomic {
     }
     ck(hfg::launch_diatomic_expand(P, H.nbf, d_pure.as<int>(), s_Pd.as<double>(), H.ndummy, st), "expand");
     if (split)
-      ck(hfg::launch_diatomic_exchange_split(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st),
+      ck(hfg::launch_diatomic_exchange_split(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st,
+                                             inline_diag),
          "exchange (split)");
     else
       ck(hfg::launch_diatomic_exchange(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st), "exchange");
@@ -411,8 +413,10 @@ hfg_status hfg_diatomic_coulomb(hfg_diatomic* d, const double* P, double* J, voi
 hfg_status hfg_diatomic_exchange(hfg_diatomic* d, const double* P, double* K, int flags, void* stream) {
   return guard([&] {
     need(d && P && K, "hfg_diatomic_exchange: null argument");
-    need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "hfg_diatomic_exchange: unsupported flags");
-    d->build(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0, to_stream(stream), (flags & HFG_EXCHANGE_SPLIT) != 0);
+    need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT | HFG_EXCHANGE_INLINE_DIAGONAL)) == 0,
+         "hfg_diatomic_exchange: unsupported flags");
+    d->build(P, K, true, (flags & HFG_EXCHANGE_SYMMETRIC) != 0, to_stream(stream), (flags & HFG_EXCHANGE_SPLIT) != 0,
+             (flags & HFG_EXCHANGE_INLINE_DIAGONAL) != 0);
   });
 }
 
