@@ -123,7 +123,7 @@ def parse_xc(method: str):
     return (ids + [0, 0])[:2]
 EXCHANGE_SYMMETRIC = 1
 EXCHANGE_SPLIT = 2
-EXCHANGE_INLINE_DIAGONAL = 4  # diatomic split form: the item-by-item diagonal schedule
+EXCHANGE_ITEMWISE = 4  # diatomic split form: one output block per work item (comparison schedule)
 
 
 
@@ -663,9 +663,9 @@ class Diatomic:
         _check(_lib.hfg_diatomic_coulomb(self._h, _ptr(P), _ptr(J), _stream(stream)))
 
     def exchange(self, P, K, symmetric: bool = False, stream=None, split: bool = False,
-                 inline_diagonal: bool = False):
+                 itemwise: bool = False):
         flags = ((EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
-                 | (EXCHANGE_INLINE_DIAGONAL if inline_diagonal else 0))
+                 | (EXCHANGE_ITEMWISE if itemwise else 0))
         _check(_lib.hfg_diatomic_exchange(self._h, _ptr(P), _ptr(K), flags, _stream(stream)))
 
     # ---- hot path: host arrays (drop-in value semantics) ----

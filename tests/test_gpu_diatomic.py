@@ -83,11 +83,11 @@ def test_diatomic_jk_match_oracle(case):
         d.exchange(Pd, Ks, symmetric=True)
         d.exchange(Pd, Kp, symmetric=True, split=True)
         d.exchange(Pd, Kq, split=True)
-        # the item-by-item diagonal schedule gives the same K bit for bit
+        # the item-by-item schedule gives the same K bit for bit
         Kpi = torch.full_like(Pd, np.nan)
         Kqi = torch.full_like(Pd, np.nan)
-        d.exchange(Pd, Kpi, symmetric=True, split=True, inline_diagonal=True)
-        d.exchange(Pd, Kqi, split=True, inline_diagonal=True)
+        d.exchange(Pd, Kpi, symmetric=True, split=True, itemwise=True)
+        d.exchange(Pd, Kqi, split=True, itemwise=True)
         torch.cuda.synchronize()
         assert torch.equal(Kp, Kpi) and torch.equal(Kq, Kqi)
         J, K, KS = from_dev(Jd), from_dev(Kd), from_dev(Ks)
@@ -202,9 +202,9 @@ def test_n2_full_size_sampled_parity():
     d.exchange(Pd, K64, symmetric=True)
     d.exchange(Pd, Ksp, symmetric=True, split=True)
     Ksi = torch.empty_like(Pd)
-    d.exchange(Pd, Ksi, symmetric=True, split=True, inline_diagonal=True)
+    d.exchange(Pd, Ksi, symmetric=True, split=True, itemwise=True)
     torch.cuda.synchronize()
-    assert torch.equal(Ksp, Ksi)  # grouped and item-by-item diagonal schedules
+    assert torch.equal(Ksp, Ksi)  # grouped and item-by-item schedules
     del Ksi
     nbf = d.nbf
     K64 = K64.cpu().numpy().reshape(nbf, nbf).T  # column-major buffer -> (row, col)
