@@ -123,7 +123,7 @@ def parse_xc(method: str):
     return (ids + [0, 0])[:2]
 EXCHANGE_SYMMETRIC = 1
 EXCHANGE_SPLIT = 2
-EXCHANGE_ITEMWISE = 4  # diatomic split form: one output block per work item (comparison schedule)
+EXCHANGE_ITEMWISE = 4  # diatomic split form: diagonal tiles one output block per item (comparison schedule)
 
 
 

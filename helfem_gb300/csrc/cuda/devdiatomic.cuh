@@ -76,9 +76,8 @@ struct DevDiatomicScratch {
   unsigned char* act;     // [nang^2] density block above the screen
   unsigned char* ent_act; // [nent]
   unsigned char* jk_act;  // [nang^2]
-  int* jk_list;           // [3*nang^2+1]: active output blocks, those with j <= k, then the
-                          // starts of the groups of consecutive active blocks with one k
-  int* counts;            // [3]: active blocks, those with j <= k, groups
+  int* jk_list;           // [2*nang^2]: active output blocks, then those with j <= k
+  int* counts;            // [2]
   float2* pd2;            // [nd*nd] split copy of the density (split path)
 };
 
@@ -127,11 +126,10 @@ cudaError_t launch_diatomic_coulomb(const DevDiatomic& D, const DevDiatomicScrat
 cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
                                      double* Kd, bool symmetric, cudaStream_t st);
 // split-precision exchange (float-float on the FP32 pipe, FP64 recombination);
-// itemwise: one output block per work item (the earlier schedule) instead of
-// groups of output blocks sharing recoupling sums and kernel-table passes
-// (bitwise the same K)
+// inline_diag: diagonal element tiles item by item inside the tile kernel
+// instead of the grouped kernel (bitwise the same K)
 cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
-                                           double* Kd, bool symmetric, cudaStream_t st, bool itemwise = false);
+                                           double* Kd, bool symmetric, cudaStream_t st, bool inline_diag = false);
 // txs[i] = split(tx[i])
 cudaError_t launch_diatomic_split_tx(const double* tx, float2* txs, size_t n, cudaStream_t st);
 

@@ -35,10 +35,6 @@
 namespace hfg {
 namespace {
 
-// output blocks per work item of the grouped split-exchange schedules
-constexpr int DIATOMIC_GROUP = 4;  // off-diagonal element pairs
-constexpr int DIAG_GROUP = 8;      // diagonal elements
-
 __device__ __forceinline__ double dwarp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -331,20 +327,6 @@ __global__ void dk_compact(DevDiatomic D, DevDiatomicScratch S) {
       S.jk_list[oa++] = jk;
       if (jk % D.nang <= jk / D.nang) S.jk_list[n + os++] = jk;
     }
-  __syncthreads();
-  // groups of at most DIATOMIC_GROUP consecutive active blocks with one k
-  if (threadIdx.x == 0) {
-    const int na_tot = S.counts[0];
-    int* grp = S.jk_list + 2 * n;
-    int ng = 0, start = 0;
-    for (int x = 0; x < na_tot; ++x)
-      if (x == 0 || S.jk_list[x] / D.nang != S.jk_list[x - 1] / D.nang || x - start == DIATOMIC_GROUP) {
-        grp[ng++] = x;
-        start = x;
-      }
-    grp[ng] = na_tot;
-    S.counts[2] = ng;
-  }
 }
 
 __device__ __forceinline__ size_t dhalo_idx(const DevDiatomic& D, int a, int b, int jk, int h) {
@@ -651,6 +633,8 @@ __global__ void __launch_bounds__(NN == 15 ? 256 : 320, NN == 15 ? 5 : 1) dk_til
 // each table element is loaded once per item instead of once per member.
 // Per member the operations and their order are those of the item-by-item
 // schedule in dk_tiles_split, so K is bitwise the same.
+constexpr int DIAG_GROUP = 8;
+
 template <int NN, int G>
 __global__ void __launch_bounds__(NN == 15 ? 256 : 320, NN == 15 ? 3 : 1) dk_diag_split(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd,
                                                          int symmetric) {
@@ -805,226 +789,6 @@ __global__ void __launch_bounds__(NN == 15 ? 256 : 320, NN == 15 ? 3 : 1) dk_dia
   }
 }
 
-// Off-diagonal element pairs of the split exchange, up to G output blocks
-// (j_g, k) with one k per item: pair pairs[w / ngroups], the group
-// w % ngroups of consecutive active blocks. The members' entry lists are
-// merged by multipole index as in dk_diag_split; per multipole and sign of M
-// the inner recoupling sums U_i = sum_l c(k; L, M; l) P_il over the union of
-// the members' i (ascending, the order of each member's own list) are formed
-// once and added to every member that couples i, and the element tables
-// (I, J channels) are loaded once for all members. Each member's operations
-// and their order are those of the item-by-item schedule in dk_tiles_split,
-// so K is bitwise the same.
-template <int NN, int G>
-__global__ void __launch_bounds__(NN == 15 ? 256 : 320, NN == 15 ? 3 : 1) dk_off_split(DevDiatomic D, DevDiatomicScratch S, double* __restrict__ Kd,
-                                                        int symmetric) {
-  const int nn = NN > 0 ? NN : D.nn, n2 = nn * nn, nang2 = D.nang * D.nang;
-  const int ngrp = S.counts[2];
-  const int* grp = S.jk_list + 2 * nang2;
-  const int2* pairs = symmetric ? D.pairs_sym : D.pairs_all;
-  const long npairs = symmetric ? D.npairs_sym : D.npairs_all;
-  const long total = npairs * ngrp;
-  extern __shared__ float2 sm2[];
-  float2* X = sm2;                              // [G][4*n2]
-  float2* T = X + (size_t)G * 4 * n2;           // [G][2*n2]
-  float2* Im = T + (size_t)G * 2 * n2;          // [2*n2]
-  float2* Jm = Im + 2 * n2;                     // [2*n2]
-  double* Y = reinterpret_cast<double*>(Jm + 2 * n2);
-  unsigned char* act = reinterpret_cast<unsigned char*>(Y + n2);
-  __shared__ int s_ptr[G], s_end[G], s_j[G], s_has[G];
-  __shared__ int s_ilm, s_k, s_ng, s_jk0;
-  for (int idx = threadIdx.x; idx < nang2; idx += blockDim.x) act[idx] = S.act[idx];
-  __syncthreads();
-  const int t = threadIdx.x;
-  const bool live = t < n2;
-  const int p = live ? t % nn : 0, q = live ? t / nn : 0;
-  for (long w = blockIdx.x; w < total; w += gridDim.x) {
-    const int2 pr = pairs[w / ngrp];
-    const int a = pr.x, b = pr.y, gi = (int)(w % ngrp);
-    if (t < G) {
-      const int x0 = grp[gi], x1 = grp[gi + 1];
-      const int ng = x1 - x0;
-      if (t < ng) {
-        const int jk = S.jk_list[x0 + t];
-        s_j[t] = jk % D.nang;
-        s_ptr[t] = D.kjk_ptr[jk];
-        s_end[t] = D.kjk_ptr[jk + 1];
-        if (t == 0) {
-          s_k = jk / D.nang;
-          s_ng = ng;
-          s_jk0 = x0;
-        }
-      } else {
-        s_j[t] = -1;
-        s_ptr[t] = s_end[t] = 0;
-      }
-    }
-    __syncthreads();
-    const int k = s_k, ng = s_ng;
-    const int gp = dgf(D, a, p), gq = dgf(D, b, q);
-    const bool vpq = live && gp < D.nrad && gq < D.nrad;
-    const float2* pbase = S.pd2 + (size_t)gq * D.nd + gp;
-    ffv yacc[G];
-#pragma unroll
-    for (int g = 0; g < G; ++g) yacc[g] = {0.f, 0.f};
-    for (;;) {
-      if (t < 32) {  // warp 0: skip inactive entries, smallest pending multipole
-        int pt = 0, me = 0x7fffffff;
-        if (t < G) {
-          pt = s_ptr[t];
-          while (pt < s_end[t] && !S.ent_act[pt]) ++pt;
-          s_ptr[t] = pt;
-          if (pt < s_end[t]) me = D.kent_ilm[pt];
-        }
-        int m = me;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (t < G) s_has[t] = (me == m && m != 0x7fffffff) ? 1 : 0;
-        if (t == 0) s_ilm = m;
-      }
-      __syncthreads();
-      const int ilm = s_ilm;
-      if (ilm == 0x7fffffff) break;
-      int L = 0, Ma = 0;
-#pragma unroll
-      for (int g = G - 1; g >= 0; --g)
-        if (s_has[g]) {
-          L = D.kent_L[s_ptr[g]];
-          Ma = D.kent_Ma[s_ptr[g]];
-        }
-      bool has[G];
-#pragma unroll
-      for (int g = 0; g < G; ++g) has[g] = s_has[g] != 0;
-      ffv x[G][4];
-#pragma unroll
-      for (int g = 0; g < G; ++g)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) x[g][c] = {0.f, 0.f};
-      if (vpq) {
-        for (int sgn = 0; sgn < (Ma ? 2 : 1); ++sgn) {
-          const int M = sgn ? -Ma : Ma;
-          const int xk = al_idx(D, k, L, M);
-          const int k0 = D.al_ptr[xk], k1 = D.al_ptr[xk + 1];
-          int pj[G], ej[G];
-#pragma unroll
-          for (int g = 0; g < G; ++g) {
-            if (has[g]) {
-              const int xj = al_idx(D, s_j[g], L, M);
-              pj[g] = D.al_ptr[xj];
-              ej[g] = D.al_ptr[xj + 1];
-            } else {
-              pj[g] = ej[g] = 0;
-            }
-          }
-          for (;;) {
-            int i = 0x7fffffff;
-#pragma unroll
-            for (int g = 0; g < G; ++g)
-              if (pj[g] < ej[g]) i = min(i, D.al_b[pj[g]]);
-            if (i == 0x7fffffff) break;
-            ffv u0 = {0.f, 0.f}, u2 = {0.f, 0.f};
-            for (int uk = k0; uk < k1; ++uk) {
-              const int l = D.al_b[uk];
-              if (!act[i + l * D.nang]) continue;
-              const float2 v = pbase[(size_t)(l * D.nrad) * D.nd + (size_t)i * D.nrad];
-              u0 = ff_fma(u0, D.al_c0s[uk], v);
-              u2 = ff_fma(u2, D.al_c2s[uk], v);
-            }
-            const float2 U0 = ff2(u0), U2 = ff2(u2);
-#pragma unroll
-            for (int g = 0; g < G; ++g)
-              if (pj[g] < ej[g] && D.al_b[pj[g]] == i) {
-                const float2 c0 = D.al_c0s[pj[g]], c2 = D.al_c2s[pj[g]];
-                x[g][0] = ff_fma(x[g][0], c0, U0);
-                x[g][1] = ff_fma(x[g][1], c0, U2);
-                x[g][2] = ff_fma(x[g][2], c2, U0);
-                x[g][3] = ff_fma(x[g][3], c2, U2);
-                ++pj[g];
-              }
-          }
-        }
-      }
-      if (live) {
-        float2 fac = D.lmfacs[ilm];
-        if (Ma & 1) fac = make_float2(-fac.x, -fac.y);
-        const ffv z = {0.f, 0.f};
-#pragma unroll
-        for (int g = 0; g < G; ++g) {
-          if (!has[g]) continue;
-          float2* Xg = X + (size_t)g * 4 * n2;
-          const float2 f00 = ff2(ff_fma(z, fac, ff2(x[g][0]))), f02 = ff2(ff_fma(z, fac, ff2(x[g][1])));
-          const float2 f20 = ff2(ff_fma(z, fac, ff2(x[g][2]))), f22 = ff2(ff_fma(z, fac, ff2(x[g][3])));
-          Xg[t] = f00;
-          Xg[n2 + t] = make_float2(-f02.x, -f02.y);
-          Xg[2 * n2 + t] = make_float2(-f20.x, -f20.y);
-          Xg[3 * n2 + t] = f22;
-        }
-        const size_t la = ((size_t)ilm * D.nel + a) * n2 + t, lb = ((size_t)ilm * D.nel + b) * n2 + t;
-        Im[t] = (a < b) ? D.p0s[la] : D.q0s[la];
-        Im[n2 + t] = (a < b) ? D.p2s[la] : D.q2s[la];
-        Jm[t] = (a < b) ? D.q0s[lb] : D.p0s[lb];
-        Jm[n2 + t] = (a < b) ? D.q2s[lb] : D.p2s[lb];
-      }
-      __syncthreads();
-      if (live) {
-#pragma unroll
-        for (int g = 0; g < G; ++g) {
-          if (!has[g]) continue;
-          const float2* Xg = X + (size_t)g * 4 * n2;
-          ffv s0 = {0.f, 0.f}, s2 = {0.f, 0.f};
-#pragma unroll
-          for (int c = 0; c < (NN > 0 ? NN : 17); ++c) {
-            if (NN == 0 && c >= nn) break;
-            const float2 j0 = Jm[q + c * nn], j2 = Jm[n2 + q + c * nn];
-            s0 = ff_fma(s0, Xg[p + c * nn], j0);
-            s0 = ff_fma(s0, Xg[n2 + p + c * nn], j2);
-            s2 = ff_fma(s2, Xg[2 * n2 + p + c * nn], j0);
-            s2 = ff_fma(s2, Xg[3 * n2 + p + c * nn], j2);
-          }
-          T[(size_t)g * 2 * n2 + t] = ff2(s0);
-          T[(size_t)g * 2 * n2 + n2 + t] = ff2(s2);
-        }
-      }
-      __syncthreads();
-      if (live) {
-        // undo the tables' power-of-two scaling: 2^(k_inner - k_outer) <= 1
-        const int ka = D.kexp[(size_t)ilm * D.nel + a], kb = D.kexp[(size_t)ilm * D.nel + b];
-        const int dk = (a < b) ? ka - kb : kb - ka;
-#pragma unroll
-        for (int g = 0; g < G; ++g) {
-          if (!has[g]) continue;
-          const float2* Tg = T + (size_t)g * 2 * n2;
-          ffv acc = {0.f, 0.f};
-#pragma unroll
-          for (int c = 0; c < (NN > 0 ? NN : 17); ++c) {
-            if (NN == 0 && c >= nn) break;
-            acc = ff_fma(acc, Im[p + c * nn], Tg[c + q * nn]);
-            acc = ff_fma(acc, Im[n2 + p + c * nn], Tg[n2 + c + q * nn]);
-          }
-          acc.hi = ldexpf(acc.hi, dk);
-          acc.lo = ldexpf(acc.lo, dk);
-          yacc[g] = ff_add(yacc[g], ff_norm(acc.hi, acc.lo));
-        }
-      }
-      __syncthreads();
-      if (t < G && s_has[t]) ++s_ptr[t];
-    }
-#pragma unroll
-    for (int g = 0; g < G; ++g) {
-      if (g >= ng) break;  // uniform over the CTA
-      const int jk = S.jk_list[s_jk0 + g], j = jk % D.nang;
-      const double y = ff_to_d(yacc[g]);
-      if (live) dk_store(D, S, Kd, a, b, jk, p, q, -y);
-      if (symmetric) {
-        if (live) Y[t] = -y;
-        __syncthreads();
-        if (live) dk_store(D, S, Kd, b, a, k + j * D.nang, p, q, Y[q + p * nn]);
-      }
-      __syncthreads();
-    }
-  }
-}
-
 __global__ void d_split(const double* __restrict__ x, float2* __restrict__ y, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     y[i] = split_bits(x[i]);
@@ -1127,7 +891,7 @@ cudaError_t launch_diatomic_split_tx(const double* tx, float2* txs, size_t n, cu
 }
 
 cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatomicScratch& S, const double* Pd,
-                                           double* Kd, bool symmetric, cudaStream_t st, bool itemwise) {
+                                           double* Kd, bool symmetric, cudaStream_t st, bool inline_diag) {
   const int n2 = D.nn * D.nn, th = dthreads(n2), nang2 = D.nang * D.nang;
   cudaError_t e = cudaMemsetAsync(Kd, 0, sizeof(double) * (size_t)D.nd * D.nd, st);
   if (e != cudaSuccess) return e;
@@ -1138,30 +902,16 @@ cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatom
   int dev = 0, nsm = 152, per = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (itemwise) {
-    const size_t smem = sizeof(float2) * 10 * n2 + sizeof(double) * n2 + nang2;
-    auto kern = (D.nn == 15) ? dk_tiles_split<15> : dk_tiles_split<0>;
-    if (smem > 48 * 1024) {
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-    }
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, th, smem);
+  const size_t smem = sizeof(float2) * 10 * n2 + sizeof(double) * n2 + nang2;
+  auto kern = (D.nn == 15) ? dk_tiles_split<15> : dk_tiles_split<0>;
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<nsm * std::max(per, 1), th, smem, st>>>(D, S, Kd, symmetric ? 1 : 0, 1);
-  } else {
-    {
-      constexpr int G = DIATOMIC_GROUP;
-      const size_t smo = sizeof(float2) * ((size_t)G * 6 * n2 + 4 * n2) + sizeof(double) * n2 + nang2;
-      auto okern = (D.nn == 15) ? dk_off_split<15, G> : dk_off_split<0, G>;
-      if (smo > 48 * 1024) {
-        e = cudaFuncSetAttribute(okern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smo);
-        if (e != cudaSuccess) return e;
-      }
-      int oper = 1;
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oper, okern, th, smo);
-      if (e != cudaSuccess) return e;
-      okern<<<nsm * std::max(oper, 1), th, smo, st>>>(D, S, Kd, symmetric ? 1 : 0);
-    }
+  }
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, th, smem);
+  if (e != cudaSuccess) return e;
+  kern<<<nsm * std::max(per, 1), th, smem, st>>>(D, S, Kd, symmetric ? 1 : 0, inline_diag ? 1 : 0);
+  if (!inline_diag) {
     constexpr int G = DIAG_GROUP;
     const size_t smd = sizeof(float2) * (size_t)G * 4 * n2 + sizeof(double) * n2 + nang2;
     auto dkern = (D.nn == 15) ? dk_diag_split<15, G> : dk_diag_split<0, G>;

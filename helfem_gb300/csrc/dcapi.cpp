@@ -139,8 +139,8 @@ struct hfg_diatomic {
     s_act.alloc(nang2);
     s_entact.alloc(std::max<size_t>(1, D.nent));
     s_jkact.alloc(nang2);
-    s_jklist.alloc(sizeof(int) * (3 * nang2 + 1));
-    s_counts.alloc(sizeof(int) * 3);
+    s_jklist.alloc(sizeof(int) * 2 * nang2);
+    s_counts.alloc(sizeof(int) * 2);
     s_Pd.alloc(sizeof(double) * nd * nd);
     s_Fd.alloc(sizeof(double) * nd * nd);
     scr.jin = s_jin.as<double>();
@@ -206,7 +206,7 @@ struct hfg_diatomic {
 
   // J or K of a pure-basis density (device pointers) on stream st
   void build(const double* P, double* F, bool exchange, bool symmetric, cudaStream_t st, bool split = false,
-             bool itemwise = false) {
+             bool inline_diag = false) {
     check_device();
     const hfg::DiatomicHost& H = host;
     if (split) ensure_split();
@@ -218,7 +218,7 @@ struct hfg_diatomic {
     ck(hfg::launch_diatomic_expand(P, H.nbf, d_pure.as<int>(), s_Pd.as<double>(), H.ndummy, st), "expand");
     if (split)
       ck(hfg::launch_diatomic_exchange_split(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st,
-                                             itemwise),
+                                             inline_diag),
          "exchange (split)");
     else
       ck(hfg::launch_diatomic_exchange(dev, scr, s_Pd.as<double>(), s_Fd.as<double>(), symmetric, st), "exchange");

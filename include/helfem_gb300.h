@@ -417,9 +417,9 @@ hfg_status hfg_diatomic_coulomb(hfg_diatomic* d, const double* P, double* J, voi
  * density-block screening. flags: HFG_EXCHANGE_SYMMETRIC (P = P^T),
  * HFG_EXCHANGE_SPLIT (split precision as for atoms; the first split call
  * allocates float-pair copies of the tables and an ndummy^2 density copy),
- * HFG_EXCHANGE_ITEMWISE (split form only: one output block per work item
- * instead of groups of output blocks that share the inner recoupling sums,
- * the element tables and the in-element kernel-table passes; the same K bit
+ * HFG_EXCHANGE_ITEMWISE (split form only: the diagonal element tiles one
+ * output block per work item inside the tile kernel, instead of in groups of
+ * output blocks sharing each in-element kernel-table pass; the same K bit
  * for bit, slower; kept for comparison). */
 #define HFG_EXCHANGE_ITEMWISE 4
 hfg_status hfg_diatomic_exchange(hfg_diatomic* d, const double* P, double* K, int flags, void* stream);
