@@ -92,6 +92,23 @@ def test_errors_are_status_codes():
     assert e.value.status == hg.HFG_ERR_STATE
 
 
+def test_creation_modes_are_validated():
+    """host_only selects the tabulation: 0 device, 1 host-only handle, 2 host
+    tables uploaded; anything else is an argument error before any work."""
+    b = tab.get_grid(40.0, 3, 4, 2.0)
+    lv = np.array([0], dtype=np.int32)
+    d = hg._Desc(2, 15, 0, len(b) - 1, hg._dptr(b), 1, lv.ctypes.data_as(hg._I), lv.ctypes.data_as(hg._I),
+                 0.0, 3)
+    h = hg._P()
+    assert hg._lib.hfg_atom_create(ctypes.byref(d), ctypes.byref(h)) == hg.HFG_ERR_ARG
+    assert "host_only" in hg._lib.hfg_last_error().decode()
+    with pytest.raises(ValueError):
+        hg.Atom(2, b, [0], [0], tabulate="gpu")
+    A = hg.Atom(2, b, [0], [0], host_only=True, tabulate="host")  # host-only wins
+    rs, rb, ch = A.radial_tables(0, 1)
+    assert ch.shape[1] >= 1 and np.isfinite(ch).all()
+
+
 def test_madelung_l_occupations():
     from helfem_gb300 import workloads as wl
     occ = wl.l_occupations(13, 13, 2)  # Fe: [Ar] 4s2 3d6 restricted-averaged -> 13 per spin
