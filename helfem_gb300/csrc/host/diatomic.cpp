@@ -374,84 +374,124 @@ void DiatomicHost::tabulate_radial() {
           BB1[(size_t)q * np + k] = B1[q + (size_t)pa[k] * NGL_OUT] * B1[q + (size_t)pb[k] * NGL_OUT];
       for (size_t i = 0; i < n2i; ++i)
         for (int k = 0; k < np; ++k) BB2[i * np + k] = B2[i + (size_t)pa[k] * n2i] * B2[i + (size_t)pb[k] * n2i];
-      std::vector<double> inner0((size_t)NGL_OUT * np), inner2((size_t)NGL_OUT * np);
-      std::vector<double> outer0((size_t)NGL_OUT * np), outer2((size_t)NGL_OUT * np);
-      std::vector<double> res((size_t)4 * np * np);
+      // Channels in chunks of CH: the inner and outer integrals of a chunk
+      // are formed with q outermost, so that each q's slice of the pair
+      // products (NGL_IN x np) is read once per chunk instead of once per
+      // channel. Per channel, q and pair the operations are unchanged.
+      constexpr int CH = 8;
+      const size_t qs = (size_t)NGL_OUT * np;  // one channel's [q][pair] block
+      std::vector<double> inner0(CH * qs), inner2(CH * qs), outer0(CH * qs), outer2(CH * qs);
+      std::vector<double> res((size_t)4 * np * np), Tt((size_t)3 * np * np);
       std::vector<double> W((size_t)4 * n2 * n2);
-      for (int ilm = 0; ilm < nlm; ++ilm) {
-        const int L = lm_L[ilm], M = lm_M[ilm];
-        const size_t lmo = (size_t)M * NLs + L;
+      std::vector<int> pidx(n2);
+      for (int b = 0; b < nn; ++b)
+        for (int a = 0; a < nn; ++a) {
+          const int lo = std::min(a, b), hi = std::max(a, b);
+          pidx[a + b * nn] = lo + hi * (hi + 1) / 2;
+        }
+      for (int ilm0 = 0; ilm0 < nlm; ilm0 += CH) {
+        const int nch = std::min(CH, nlm - ilm0);
         for (int q = 0; q < NGL_OUT; ++q) {
           const double sh = sh1[q], ch = ch1[q];
-          const double wq0 = w1[q] * sh * Q1[(size_t)q * NMs * NLs + lmo];
-          double* o0 = outer0.data() + (size_t)q * np;
-          double* o2 = outer2.data() + (size_t)q * np;
-          double* i0 = inner0.data() + (size_t)q * np;
-          double* i2 = inner2.data() + (size_t)q * np;
           const double* bq = BB1.data() + (size_t)q * np;
-          for (int k = 0; k < np; ++k) {
-            const double bb = bq[k];
-            o0[k] = wq0 * bb;
-            o2[k] = wq0 * ch * ch * bb;
-            i0[k] = 0.0;
-            i2[k] = 0.0;
-          }
-          for (int r = 0; r < NGL_IN; ++r) {
-            const size_t ii = (size_t)q * NGL_IN + r;
-            const double wr0 = w2[ii] * sh2[ii] * P2[ii * NMs * NLs + lmo], wr2 = wr0 * ch2[ii] * ch2[ii];
-            const double* bi = BB2.data() + ii * np;
+          for (int c = 0; c < nch; ++c) {
+            const int ilm = ilm0 + c;
+            const size_t lmo = (size_t)lm_M[ilm] * NLs + lm_L[ilm];
+            const double wq0 = w1[q] * sh * Q1[(size_t)q * NMs * NLs + lmo];
+            double* o0 = outer0.data() + c * qs + (size_t)q * np;
+            double* o2 = outer2.data() + c * qs + (size_t)q * np;
+            double* i0 = inner0.data() + c * qs + (size_t)q * np;
+            double* i2 = inner2.data() + c * qs + (size_t)q * np;
             for (int k = 0; k < np; ++k) {
-              const double bb = bi[k];
-              i0[k] += wr0 * bb;
-              i2[k] += wr2 * bb;
+              const double bb = bq[k];
+              o0[k] = wq0 * bb;
+              o2[k] = wq0 * ch * ch * bb;
+              i0[k] = 0.0;
+              i2[k] = 0.0;
             }
-          }
-        }
-        // res_kl[c + d*np] = sum_q outer_k[q][c] inner_l[q][d] (q ascending,
-        // as rank-1 updates with a contiguous inner loop)
-        const double* outs[2] = {outer0.data(), outer2.data()};
-        const double* ins[2] = {inner0.data(), inner2.data()};
-        std::fill(res.begin(), res.end(), 0.0);
-        for (int k = 0; k < 2; ++k)
-          for (int l = 0; l < 2; ++l) {
-            double* R = res.data() + (size_t)(2 * k + l) * np * np;
-            for (int q = 0; q < NGL_OUT; ++q) {
-              const double* oq = outs[k] + (size_t)q * np;
-              const double* iq = ins[l] + (size_t)q * np;
-              for (int d = 0; d < np; ++d) {
-                const double v = iq[d];
-                double* Rd = R + (size_t)d * np;
-                for (int c = 0; c < np; ++c) Rd[c] += oq[c] * v;
+            for (int r = 0; r < NGL_IN; ++r) {
+              const size_t ii = (size_t)q * NGL_IN + r;
+              const double wr0 = w2[ii] * sh2[ii] * P2[ii * NMs * NLs + lmo], wr2 = wr0 * ch2[ii] * ch2[ii];
+              const double* bi = BB2.data() + ii * np;
+              for (int k = 0; k < np; ++k) {
+                const double bb = bi[k];
+                i0[k] += wr0 * bb;
+                i2[k] += wr2 * bb;
               }
             }
           }
-        // T_kl(cd, ab) = res_kl(cd, ab) + res_lk(ab, cd); W = [[T00, -T02], [-T02', T22]]
-        auto T = [&](int k, int l, int c, int d) {
-          return res[(size_t)(2 * k + l) * np * np + c + (size_t)d * np] +
-                 res[(size_t)(2 * l + k) * np * np + d + (size_t)c * np];
-        };
-        std::vector<int> pidx(n2);
-        for (int b = 0; b < nn; ++b)
-          for (int a = 0; a < nn; ++a) {
-            const int lo = std::min(a, b), hi = std::max(a, b);
-            pidx[a + b * nn] = lo + hi * (hi + 1) / 2;
+        }
+        for (int c = 0; c < nch; ++c) {
+          const int ilm = ilm0 + c;
+          // res_kl[c + d*np] = sum_q outer_k[q][c] inner_l[q][d], q ascending,
+          // in 4 x 8 register blocks
+          const double* outs[2] = {outer0.data() + c * qs, outer2.data() + c * qs};
+          const double* ins[2] = {inner0.data() + c * qs, inner2.data() + c * qs};
+          for (int k = 0; k < 2; ++k)
+            for (int l = 0; l < 2; ++l) {
+              double* R = res.data() + (size_t)(2 * k + l) * np * np;
+              const double* Ok = outs[k];
+              const double* Il = ins[l];
+              for (int d0 = 0; d0 < np; d0 += 4)
+                for (int c0 = 0; c0 < np; c0 += 8) {
+                  if (d0 + 4 <= np && c0 + 8 <= np) {
+                    double acc[4][8] = {};
+                    for (int q = 0; q < NGL_OUT; ++q) {
+                      const double* oq = Ok + (size_t)q * np + c0;
+                      const double* iq = Il + (size_t)q * np + d0;
+                      for (int dd = 0; dd < 4; ++dd) {
+                        const double v = iq[dd];
+                        for (int cc = 0; cc < 8; ++cc) acc[dd][cc] += oq[cc] * v;
+                      }
+                    }
+                    for (int dd = 0; dd < 4; ++dd)
+                      for (int cc = 0; cc < 8; ++cc) R[(c0 + cc) + (size_t)(d0 + dd) * np] = acc[dd][cc];
+                  } else {
+                    for (int d = d0; d < std::min(np, d0 + 4); ++d)
+                      for (int cx = c0; cx < std::min(np, c0 + 8); ++cx) {
+                        double acc = 0.0;
+                        for (int q = 0; q < NGL_OUT; ++q) acc += Ok[(size_t)q * np + cx] * Il[(size_t)q * np + d];
+                        R[cx + (size_t)d * np] = acc;
+                      }
+                  }
+                }
+            }
+          // T_kl(c, d) = res_kl(c, d) + res_lk(d, c): T00, T02 (= T20 transposed) and T22
+          const double* r00 = res.data();
+          const double* r02 = res.data() + (size_t)np * np;
+          const double* r20 = res.data() + (size_t)2 * np * np;
+          const double* r22 = res.data() + (size_t)3 * np * np;
+          double* t00 = Tt.data();
+          double* t02 = Tt.data() + (size_t)np * np;
+          double* t22 = Tt.data() + (size_t)2 * np * np;
+          for (int d0 = 0; d0 < np; d0 += 16)
+            for (int c0 = 0; c0 < np; c0 += 16)
+              for (int d = d0; d < std::min(np, d0 + 16); ++d)
+                for (int cx = c0; cx < std::min(np, c0 + 16); ++cx) {
+                  const size_t cd = cx + (size_t)d * np, dc = d + (size_t)cx * np;
+                  t00[cd] = r00[cd] + r00[dc];
+                  t02[cd] = r02[cd] + r20[dc];
+                  t22[cd] = r22[cd] + r22[dc];
+                }
+          // W = [[T00, -T02], [-T02^T, T22]] over the pair index of (a, b).
+          // It is symmetric as assembled: T_kl(c, d) and T_lk(d, c) are the
+          // same two terms summed in the other order, so the reference's
+          // 0.5 (W + W^T) leaves every entry unchanged.
+          const int N = 2 * n2;
+          for (int col = 0; col < n2; ++col) {
+            const size_t dcol = (size_t)pidx[col] * np;
+            double* w0 = W.data() + (size_t)col * N;
+            double* w1c = W.data() + (size_t)(n2 + col) * N;
+            for (int row = 0; row < n2; ++row) {
+              const size_t cd = pidx[row] + dcol;
+              w0[row] = t00[cd];
+              w1c[row] = -t02[cd];
+              w0[n2 + row] = -t02[pidx[col] + (size_t)pidx[row] * np];
+              w1c[n2 + row] = t22[cd];
+            }
           }
-        const int N = 2 * n2;
-        for (int col = 0; col < n2; ++col)
-          for (int row = 0; row < n2; ++row) {
-            const int c = pidx[row], d = pidx[col];
-            const double t00 = T(0, 0, c, d), t02 = T(0, 1, c, d), t20 = T(1, 0, c, d), t22 = T(1, 1, c, d);
-            W[row + (size_t)col * N] = t00;
-            W[row + (size_t)(n2 + col) * N] = -t02;
-            W[(n2 + row) + (size_t)col * N] = -t20;
-            W[(n2 + row) + (size_t)(n2 + col) * N] = t22;
-          }
-        for (int col = 0; col < N; ++col)
-          for (int row = 0; row < col; ++row) {
-            const double v = 0.5 * (W[row + (size_t)col * N] + W[col + (size_t)row * N]);
-            W[row + (size_t)col * N] = W[col + (size_t)row * N] = v;
-          }
-        sign_cholesky(W, N, cd_thresh, fB[(size_t)ilm * nel + e], fS[(size_t)ilm * nel + e]);
+          sign_cholesky(W, N, cd_thresh, fB[(size_t)ilm * nel + e], fS[(size_t)ilm * nel + e]);
+        }
       }
     }
   }
