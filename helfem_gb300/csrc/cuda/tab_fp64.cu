@@ -6,8 +6,8 @@
 // (src/atomic/TwoDBasis.cpp:708-735 -> RadialBasis::twoe_integral /
 // twoe_integral_cholesky, libhelfem/src/RadialBasis.cpp:643-716;
 // quadrature::twoe_integral, libhelfem/src/quadrature.cpp:36-161), with the
-// quadrature of the host tabulation (Gauss-Legendre outer rule of TW_NO
-// points, inner rule of TW_NI points on [r_min, r]):
+// quadrature of the host tabulation (Gauss-Legendre outer rule of TWOE_NO
+// points, inner rule of TWOE_NI points on [r_min, r]):
 //   G_kl(r_p)  = sum_q win(p, q) B_k B_l (r_pq)                   (inner)
 //   T1[ij, kl] = sum_p wout(p) B_i B_j (r_p) G_kl(r_p)            (outer)
 //   T = T1 + T1^T,  T = L L^T (greedy pivoted Cholesky, absolute tolerance)

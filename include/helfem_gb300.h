@@ -112,7 +112,8 @@ hfg_status hfg_nuclear(const hfg_atom* atom, double* V);
  * compact layout (Ni x Ni; Cholesky factor Ni^2 x rank, pair index a + b*Ni,
  * CoulombExchangeFE.h:471-477). Any output may be NULL; rbig is zero for
  * iel = 0 (never used there). For checking against an independent
- * tabulation. */
+ * tabulation. On a device-tabulated handle the factors are copied from the
+ * device on the first call. */
 hfg_status hfg_atom_radial_tables(const hfg_atom* atom, int L, int iel, int* ni, double* rsmall,
                                   double* rbig, int* rank, double* chol);
 
