@@ -107,6 +107,14 @@ hfg_status hfg_atom_get_dims(const hfg_atom* atom, hfg_atom_dims_t* dims);
 hfg_status hfg_overlap(const hfg_atom* atom, double* S);
 hfg_status hfg_kinetic(const hfg_atom* atom, double* T);
 hfg_status hfg_nuclear(const hfg_atom* atom, double* V);
+/* Matrix of a screened-nucleus model potential, host output nbf x nbf:
+ * replaces TwoDBasisT::model_potential (src/atomic/TwoDBasis.cpp:444-455;
+ * the per-element integral of libhelfem/src/RadialBasis.cpp:605-619). model
+ * uses the reference's iguess numbering; 3 = Thomas-Fermi screened nucleus
+ * (TFAtom, src/general/model_potential.cpp:53-55: V = -Z_TF(r)/r with the
+ * screening function of arXiv physics/0511017). GSZ (1) and SAP (2) need
+ * tabulated parameters that are not part of this library: HFG_ERR_ARG. */
+hfg_status hfg_model_potential(const hfg_atom* atom, int model, double* V);
 
 /* Cached radial tables of multipole L and element iel, in the reference's
  * compact layout (Ni x Ni; Cholesky factor Ni^2 x rank, pair index a + b*Ni,

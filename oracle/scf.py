@@ -80,8 +80,11 @@ def _occupy(eps_blocks, nel, maxocc, fixed=None):
 def run_scf(atom: tab.AtomTables, nela: int, nelb: int, method: str = "hf",
             restricted: bool = True, fixed_occ=None, fock: FockOracle = None,
             grid: xcmod.AtomGrid = None, maxiter: int = 200, conv: float = 1e-10,
-            thr: float = 1e-12, verbose: bool = False) -> SCFResult:
-    """fixed_occ: dict m -> (nocc_alpha, nocc_beta) (restricted: total/2 each)."""
+            thr: float = 1e-12, verbose: bool = False, guess_H: np.ndarray = None) -> SCFResult:
+    """fixed_occ: dict m -> (nocc_alpha, nocc_beta) (restricted: total/2 each).
+    guess_H: one-electron Hamiltonian whose orbitals start the SCF (default
+    the core Hamiltonian T + V; T + a screened-nucleus model potential is
+    the reference's iguess 1-3, src/atomic/main.cpp:474-511)."""
     fock = fock or FockOracle(atom)
     names = xcmod.parse_method(method)
     have_xc = bool(names)
@@ -118,7 +121,7 @@ def run_scf(atom: tab.AtomTables, nela: int, nelb: int, method: str = "hf",
             P[np.ix_(idx, idx)] += (Ck * ok) @ Ck.T
         return P
 
-    eps0, C0 = diag(H)
+    eps0, C0 = diag(H if guess_H is None else guess_H)
     state = [(eps0, C0)] * nspin
     diis_F, diis_e = [], []
     Eold = 0.0
