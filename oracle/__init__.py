@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY. The product (``helfem_gb300``) never imports,
 links or executes anything in this package; only ``tests/``, the smoke check
 in ``__graft_entry__.py`` and the ``cpu_baseline`` / ``--impl reference`` legs
-of ``bench.py`` use it, and there only as the checker or as the timed CPU
+of ``bench.py`` use it, and there only as the oracle or as the timed CPU
 baseline.
 
 Parity pins: ``tests/test_oracle_golden.py`` checks this oracle against the

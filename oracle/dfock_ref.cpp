@@ -1,6 +1,6 @@
 // Oracle (test infrastructure only): C++17/OpenMP restatement of HelFEM's
-// diatomic exchange build. This is the CHECKER for the GPU product and the
-// timed CPU baseline of the diatomic path; nothing in the product links it.
+// diatomic exchange build. The GPU product is compared against it, and it is
+// the timed CPU baseline of the diatomic path; nothing in the product links it.
 //
 // Restated from (paths inside the HelFEM project):
 //   src/diatomic/basis.cpp:1817-2061   TwoDBasis::exchange: density blocks

@@ -2,8 +2,8 @@
 two-dimensional basis in prolate spheroidal coordinates (mu, nu, phi) and of
 the tables its Coulomb and exchange builds consume.
 
-This module is the CHECKER for the GPU product. Only tests, the smoke check
-and the CPU-baseline leg of the benchmark may import it. It is written
+The GPU product is compared against it. Only tests, the smoke check and
+the CPU-baseline leg of the benchmark may import it. It is written
 independently of the product's C++ tabulation: the associated Legendre
 functions are evaluated from mu (not from cosh mu), the angular couplings of
 the cos(nu) powers come from the three-term recurrence of Y_l^m rather than

@@ -2,8 +2,8 @@
 diatomic DFT grid, the XC potential of a diatomic whose orbitals do not mix
 m (symmetry >= 1).
 
-This module is the CHECKER for the GPU product. Only tests, the smoke check
-and the CPU-baseline leg of the benchmark may import it.
+The GPU product is compared against it. Only tests, the smoke check and
+the CPU-baseline leg of the benchmark may import it.
 
 Reference files restated here (paths inside the HelFEM project):
 

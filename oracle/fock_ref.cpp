@@ -1,6 +1,6 @@
 // Oracle (test infrastructure only): C++17/OpenMP restatement of HelFEM's
-// atomic Coulomb and exchange builds. This is the CHECKER for the GPU product
-// and the timed CPU baseline; nothing in the product links it.
+// atomic Coulomb and exchange builds. The GPU product is compared
+// against it, and it is the timed CPU baseline; nothing in the product links it.
 //
 // Restated from (paths inside the HelFEM project):
 //   src/atomic/TwoDBasis.cpp:773-877   TwoDBasisT::coulomb  (ket contraction

@@ -1,8 +1,8 @@
 """Oracle (test infrastructure only): screened-nucleus model potentials for
 the SCF guess, restated in numpy.
 
-This module is the CHECKER for the product. Only tests, the smoke check and
-the CPU-baseline leg of the benchmark may import it.
+The product is compared against it. Only tests, the smoke check and the
+CPU-baseline leg of the benchmark may import it.
 
 Restated (paths inside the HelFEM project):
 

@@ -2,8 +2,8 @@
 finite-element radial basis and of the tabulated quantities the Fock build
 consumes.
 
-This module is the CHECKER for the GPU product. Only tests, the smoke check
-and the CPU-baseline leg of the benchmark may import it. It is written
+The GPU product is compared against it. Only tests, the smoke check and
+the CPU-baseline leg of the benchmark may import it. It is written
 independently of the product's C++ tabulation (different quadrature rules,
 vectorised numpy) so that agreement between the two is evidence, not an echo.
 

@@ -1,8 +1,8 @@
 """Oracle (test infrastructure only): the Yukawa-screened exchange tables of
 HelFEM's range-separated exchange, restated in numpy.
 
-This module is the CHECKER for the GPU product. Only tests, the smoke check
-and the CPU-baseline leg of the benchmark may import it.
+The GPU product is compared against it. Only tests, the smoke check and
+the CPU-baseline leg of the benchmark may import it.
 
 Restated (paths inside the HelFEM project):
 
