@@ -77,4 +77,16 @@ struct BandedLU {
   }
 };
 
+// Factor M = band_w(F) - theta band_w(S) for dense column-major n x n F and
+// S (leading dimensions ldf, lds; entries with |i - j| > w are dropped) into
+// lu. Returns false when M is singular.
+inline bool factor_shifted_band(const double* F, int ldf, const double* S, int lds, int n, int w, double theta,
+                                BandedLU& lu) {
+  lu.reset(n, w, w);
+  for (int j = 0; j < n; ++j)
+    for (int i = std::max(0, j - w); i <= std::min(n - 1, j + w); ++i)
+      lu.at(i, j) = F[i + (size_t)j * ldf] - theta * S[i + (size_t)j * lds];
+  return lu.factor();
+}
+
 }  // namespace hfg
