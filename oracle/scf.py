@@ -80,11 +80,17 @@ def _occupy(eps_blocks, nel, maxocc, fixed=None):
 def run_scf(atom: tab.AtomTables, nela: int, nelb: int, method: str = "hf",
             restricted: bool = True, fixed_occ=None, fock: FockOracle = None,
             grid: xcmod.AtomGrid = None, maxiter: int = 200, conv: float = 1e-10,
-            thr: float = 1e-12, verbose: bool = False, guess_H: np.ndarray = None) -> SCFResult:
+            thr: float = 1e-12, verbose: bool = False, guess_H: np.ndarray = None,
+            l_occ=None) -> SCFResult:
     """fixed_occ: dict m -> (nocc_alpha, nocc_beta) (restricted: total/2 each).
     guess_H: one-electron Hamiltonian whose orbitals start the SCF (default
     the core Hamiltonian T + V; T + a screened-nucleus model potential is
-    the reference's iguess 1-3, src/atomic/main.cpp:474-511)."""
+    the reference's iguess 1-3, src/atomic/main.cpp:474-511).
+    l_occ: [(n_alpha, n_beta) per l] switches to one block per angular
+    function with fixed occupations: the electrons of each l shared equally
+    over its 2l+1 m blocks and filled lowest-first within a block (the
+    spherically averaged occupations of the engine's batch and serving
+    solves; symmetry 2 of the reference's atomic driver)."""
     fock = fock or FockOracle(atom)
     names = xcmod.parse_method(method)
     have_xc = bool(names)
@@ -93,13 +99,21 @@ def run_scf(atom: tab.AtomTables, nela: int, nelb: int, method: str = "hf",
         grid = xcmod.AtomGrid(atom)
     H = atom.T + atom.V
     S = atom.S
-    blocks = sym_blocks(atom)
+    if l_occ is not None:
+        n = atom.nrad
+        blocks = [(ia, ia * n + np.arange(n)) for ia in range(atom.nang)]
+    else:
+        blocks = sym_blocks(atom)
     X = [tab.invh(S[np.ix_(idx, idx)]) for _, idx in blocks]
     nspin = 1 if restricted else 2
     maxocc = 2.0 if restricted else 1.0
     nel_spin = [nela + nelb] if restricted else [nela, nelb]
     fixed = None
-    if fixed_occ is not None:
+    if l_occ is not None:
+        per = [[l_occ[atom.lval[ia]][sp] / (2 * atom.lval[ia] + 1) if atom.lval[ia] < len(l_occ) else 0.0
+                for ia in range(atom.nang)] for sp in range(2)]
+        fixed = [[a + b for a, b in zip(per[0], per[1])]] if restricted else per
+    elif fixed_occ is not None:
         if restricted:
             fixed = [[fixed_occ.get(m, (0, 0))[0] + fixed_occ.get(m, (0, 0))[1] for m, _ in blocks]]
         else:
