@@ -35,9 +35,28 @@ UNIT = "builds/s"
 WORKLOAD = ("Kr (Z=36) J+K Fock build: 40 elements r_i=61^(i/40)-1, 15-node LIP, l<=2, m<=2, "
             "Nbf=5031, L<=4, P=CC^T (18 cols, N(0,1), seed 12345, Loewdin in S)")
 KERNELS_PER_STEP = 5  # j_contract, j_scatter, k_block_norms, k_tiles, k_fixup
+# what the timed K form computes in (the dtype key names the arithmetic, the
+# form key the scheme)
+FORMS = {
+    "plain": {"dtype": "f64", "form": "plain FP64"},
+    "split": {"dtype": "f32-pair (FP64 recombination)",
+              "form": "split precision: float-pair (hi + lo FP32) contraction with error-free products "
+                      "and sums, recombined in FP64 once per output element"},
+}
 
 
 def kr_basis():
+    """The benchmark basis through the product's own grid and angular-basis
+    entry points (hfg_grid, hfg_angular_basis)."""
+    import helfem_gb300 as hg
+    bval = hg.get_grid(60.0, 40, 4, 1.0)
+    lval, mval = hg.angular_basis(2, 2)
+    return 36, bval, lval, mval
+
+
+def kr_basis_oracle():
+    """The same basis for the CPU legs, from the oracle alone (the reference
+    arm loads nothing of the product)."""
     from oracle import tabulate as tab
     bval = tab.get_grid(60.0, 40, 4, 1.0)
     lval, mval = tab.angular_basis(2, 2)
@@ -67,13 +86,14 @@ def host_cores() -> int:
 _CPU = {}
 
 
-def cpu_reference_builds(min_seconds: float, max_builds: int, min_builds: int = 1):
-    """Time full-size oracle J+K builds on the host cores; returns
-    (builds/s, builds, seconds, threads)."""
+def cpu_reference_builds(min_seconds: float, max_builds: int, min_builds: int = 1, threads: int = 0):
+    """Time full-size oracle J+K builds on the host cores (threads = 0: all
+    of them); returns (builds/s, builds, seconds, threads)."""
     import oracle
     from oracle import tabulate as tab
+    oracle.lib().ora_set_threads(threads)
     if not _CPU:
-        Z, bval, lval, mval = kr_basis()
+        Z, bval, lval, mval = kr_basis_oracle()
         A = tab.build_atom(Z, 15, bval, 2, 2)
         _CPU["P"] = kr_density(A.S)
         _CPU["F"] = oracle.FockOracle(A)
@@ -189,18 +209,6 @@ def fp32_peak_tflops(torch) -> float:
         return best
     finally:
         torch.backends.cuda.matmul.allow_tf32 = prev
-
-
-def profiled_traffic(kernel="k_tiles"):
-    """Per-launch DRAM bytes of the exchange tile kernel from its committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", kernel + "_kr.txt")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1])
-    except (OSError, ValueError):
-        pass
-    return None
 
 
 def measured_peaks():
@@ -359,7 +367,6 @@ def run_ours(args):
     achieved = kflops / (off_ms * 1e-3) / 1e12  # FP64-equivalent algorithmic FLOPs
     peak = fp64_peak_tflops(torch)
     fp32 = fp32_peak_tflops(torch)
-    traffic = profiled_traffic("k_tiles_split" if split else "k_tiles")
     hbm_peak = measured_peaks().get("hbm_gbs")
     kernel_ms = {k: (v[1] / max(v[0], 1)) for k, v in prof.items()}
     if split:
@@ -380,27 +387,36 @@ def run_ours(args):
                     "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (no FP64 figure in MEASURED_PEAKS.json)"}
     roofline.update({
         "flops_per_launch": kflops, "ms_per_launch": off_ms,
-        "traffic": traffic,
+        "traffic": None,
+        "traffic_note": "DRAM bytes are not measurable inside this run; the ncu captures of the tile kernel "
+                        "(profiles/) give them per launch",
         "hbm": {"achieved_gbs": (work["k_bytes"] / 2) / (off_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
                 "note": "the tile kernel reads P once; HBM is not its bound"},
         "kernel_ms_per_launch": kernel_ms,
     })
+    cpu1 = None
     if args.cpu_seconds > 0:
         cpu_rate, cpu_n, cpu_dt, cpu_threads = cpu_reference_builds(args.cpu_seconds, 1000)
+        # one thread, the reference's own test setting (OMP_NUM_THREADS=1)
+        r1, n1, dt1, _ = cpu_reference_builds(0.0, 1, 1, threads=1)
+        cpu_reference_builds(0.0, 0, 0, threads=0)  # restore every core
+        cpu1 = {"value": r1, "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": f"{n1} full-size Kr J+K build in {dt1:.1f} s (oracle, one OpenMP thread)"}
     else:
         cpu_rate, cpu_n, cpu_dt, cpu_threads = None, 0, 0.0, host_cores()
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": FORMS["split" if split else "plain"]["dtype"], "data": "synthetic",
         "config": {"workload": WORKLOAD, "nbf": nbf, "parallelism": f"replicas x{ws}",
                    "autotune": tuned,
                    "inputs_vs_l2": "P is 202 MB > 129 MB L2: no flush needed"},
         "roofline": roofline,
-        "form": "split precision (FP32-pair contraction, FP64 recombination)" if split else "plain FP64",
+        "form": FORMS["split" if split else "plain"]["form"],
         "plain_fp64": plain,
         "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_n} full-size Kr J+K builds in {cpu_dt:.1f} s (oracle, OpenMP)"},
+        "cpu_baseline_1thread": cpu1,
         "e2e": e2e,
         "clocks": clocks,
         "gpu_launches": KERNELS_PER_STEP * args.steps,

@@ -61,7 +61,6 @@ _SIGS = {
     "hfg_overlap": ([_P, _D], ctypes.c_int),
     "hfg_kinetic": ([_P, _D], ctypes.c_int),
     "hfg_nuclear": ([_P, _D], ctypes.c_int),
-    "hfg_model_potential": ([_P, ctypes.c_int, _D], ctypes.c_int),
     "hfg_atom_radial_tables": ([_P, ctypes.c_int, ctypes.c_int, _I, _D, _D, _I, _D], ctypes.c_int),
     "hfg_gaunt": ([ctypes.c_int] * 5 + [_D], ctypes.c_int),
     "hfg_coulomb": ([_P, _P, _P, _P], ctypes.c_int),
@@ -284,12 +283,6 @@ class Atom:
 
     def nuclear(self):
         return self._full(_lib.hfg_nuclear)
-
-    def model_potential(self, model: int = 3):
-        """Screened-nucleus model potential matrix (3 = Thomas-Fermi)."""
-        M = np.zeros((self.nbf, self.nbf), order="F")
-        _check(_lib.hfg_model_potential(self._h, int(model), _dptr(M)))
-        return M
 
     def radial_tables(self, L: int, iel: int):
         ni, rank = ctypes.c_int(), ctypes.c_int()

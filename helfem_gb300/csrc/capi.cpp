@@ -156,14 +156,6 @@ hfg_status hfg_nuclear(const hfg_atom* a, double* V) {
   return guard([&] { need(a && V, "null argument"); write_full(a, a->host.Vrad, -(double)a->host.Z, nullptr, V); });
 }
 
-hfg_status hfg_model_potential(const hfg_atom* a, int model, double* V) {
-  return guard([&] {
-    need(a && V, "null argument");
-    need(model == 3, "hfg_model_potential: only the Thomas-Fermi model (3) is available");
-    write_full(a, a->host.thomas_fermi_radial(), 1.0, nullptr, V);
-  });
-}
-
 hfg_status hfg_atom_radial_tables(const hfg_atom* a, int L, int iel, int* ni, double* rsmall, double* rbig,
                                   int* rank, double* chol) {
   return guard([&] {

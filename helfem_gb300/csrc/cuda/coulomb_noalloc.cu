@@ -2,9 +2,8 @@
 // instead of the per-handle buffers that hfg_atom_create allocates.
 //
 // Who needs this: callers whose per-call path may not allocate device memory
-// at all - code that runs while a CUDA stream is being captured into a graph
-// (cudaMalloc is not capturable), hosts that hand the engine a fixed device
-// budget and own every allocation themselves, and latency-critical loops
+// at all - hosts that hand the engine a fixed device budget and own every
+// allocation themselves (a framework's caching allocator), and latency-critical loops
 // that must not risk the implicit synchronisation or failure of an
 // allocation. They create the atom once at set-up, then call the
 // allocation-free Coulomb build as often as they like.

@@ -96,6 +96,7 @@ struct hfg_engine {
   std::map<unsigned long long, std::unique_ptr<Job>> jobs;
   std::vector<std::thread> workers;
   bool stop = false;
+  int waiters = 0;  // threads inside hfg_engine_wait (destroy waits for them to leave)
   int omp_threads = 1;
 
   Job* pick_locked() {
@@ -233,12 +234,27 @@ hfg_status hfg_engine_wait(hfg_engine* e, unsigned long long job_id, double time
   return guard([&] {
     need(e && out, "hfg_engine_wait: null argument");
     std::unique_lock<std::mutex> lk(e->mu);
-    auto it = e->jobs.find(job_id);
-    need(it != e->jobs.end(), "hfg_engine_wait: unknown job id");
-    Job* j = it->second.get();
-    auto done = [&] { return j->status >= 2; };
+    need(e->jobs.find(job_id) != e->jobs.end(), "hfg_engine_wait: unknown job id");
+    // counted while inside, so that destroy does not free the engine under a
+    // waiter; the job is looked up again after every wake-up because another
+    // waiter on the same id may have taken (and erased) the result
+    struct Count {
+      hfg_engine* e;
+      explicit Count(hfg_engine* e_) : e(e_) { ++e->waiters; }
+      ~Count() {
+        --e->waiters;
+        e->cv_done.notify_all();
+      }
+    } count(e);
+    auto done = [&] {
+      auto f = e->jobs.find(job_id);
+      return f == e->jobs.end() || f->second->status >= 2;
+    };
     if (timeout_s < 0) e->cv_done.wait(lk, done);
     else e->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done);
+    auto it = e->jobs.find(job_id);
+    need(it != e->jobs.end(), "hfg_engine_wait: the result of this job was taken by another waiter");
+    Job* j = it->second.get();
     std::memset(out, 0, sizeof(*out));
     out->status = j->status;
     out->footprint_bytes = (double)j->footprint;
@@ -278,7 +294,13 @@ hfg_status hfg_engine_destroy(hfg_engine* e) {
     }
     e->cv_work.notify_all();
     for (auto& t : e->workers) t.join();
-    e->cv_done.notify_all();
+    {
+      // every job is now done or cancelled: waiters wake, copy their result
+      // and leave before the engine is freed
+      std::unique_lock<std::mutex> lk(e->mu);
+      e->cv_done.notify_all();
+      e->cv_done.wait(lk, [&] { return e->waiters == 0; });
+    }
     delete e;
   });
 }

@@ -246,57 +246,3 @@ void AtomHost::build_couplings() {
 }
 
 }  // namespace hfg
-
-namespace hfg {
-
-// Thomas-Fermi screening of a nucleus of charge Z (the reference's TFAtom,
-// src/general/gsz.cpp:51-58): the fit of the Thomas-Fermi function by
-// Oulne, arXiv physics/0511017,
-//   Z_TF(r) = Z (1 + a sqrt(x) + b x e^{-g sqrt(x)})^2 e^{-2 a sqrt(x)},
-//   x = r (128 Z / (9 pi^2))^{1/3}.
-double thomas_fermi_charge(double r, int Z) {
-  const double a = 0.7280642371, b = -0.5430794693, g = 0.3612163121;
-  const double x = r * std::cbrt(128.0 * Z / (9.0 * M_PI * M_PI));
-  const double sx = std::sqrt(x);
-  const double f = 1.0 + a * sx + b * x * std::exp(-g * sx);
-  return Z * f * f * std::exp(-2.0 * a * sx);
-}
-
-std::vector<double> AtomHost::thomas_fermi_radial() const {
-  const int nn = rad.nn, nr = rad.nrad, z = Z;
-  std::vector<double> V((size_t)nr * nr, 0.0);
-  // Z_TF has a sqrt(r) term: on the element at the nucleus the rule is laid
-  // out in u with r = r_1 u^2, which makes the integrand analytic in u
-  std::vector<double> m0((size_t)nn * nn, 0.0);
-  {
-    std::vector<double> xg, wg, xr, Bv;
-    gauss_legendre(128, xg, wg);
-    const int np = (int)xg.size();
-    const double r1 = rad.bval[1];
-    std::vector<double> wt(np);
-    xr.resize(np);
-    for (int i = 0; i < np; ++i) {
-      const double u = 0.5 * (xg[i] + 1.0), r = r1 * u * u;
-      xr[i] = (r - rad.mid(0)) / rad.sf(0);
-      wt[i] = 0.5 * wg[i] * 2.0 * r1 * u * (-thomas_fermi_charge(r, z) / r);
-    }
-    rad.B(0, xr, 0, Bv);
-    for (int b = 0; b < nn; ++b)
-      for (int a = 0; a <= b; ++a) {
-        double s = 0.0;
-        for (int i = 0; i < np; ++i) s += Bv[i + (size_t)a * np] * Bv[i + (size_t)b * np] * wt[i];
-        m0[a + (size_t)b * nn] = m0[b + (size_t)a * nn] = s;
-      }
-  }
-  for (int e = 0; e < rad.nel; ++e) {
-    const auto m = e == 0 ? m0 : rad.weighted_integral([z](double r) { return -thomas_fermi_charge(r, z) / r; }, e);
-    for (int q = 0; q < nn; ++q)
-      for (int p = 0; p < nn; ++p) {
-        if (!rad.valid(e, p) || !rad.valid(e, q)) continue;
-        V[rad.g(e, p) + (size_t)rad.g(e, q) * nr] += m[p + (size_t)q * nn];
-      }
-  }
-  return V;
-}
-
-}  // namespace hfg

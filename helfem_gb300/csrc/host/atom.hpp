@@ -26,8 +26,6 @@ std::vector<double> pivoted_cholesky(const std::vector<double>& A, int n, double
 // modified spherical Bessel functions i_L, k_L (normalisation in yukawa.cpp)
 double bessel_il(double x, int L);
 double bessel_kl(double x, int L);
-// effective charge of the Thomas-Fermi screened nucleus, Z_TF(r)
-double thomas_fermi_charge(double r, int Z);
 
 // 1-D rules and Lagrange interpolating polynomials
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);
@@ -156,9 +154,6 @@ struct AtomHost {
              const std::vector<int>& mval, int nquad, double chol_tol, bool twoe_host = true);
   bool twoe_on_host = true;
   void build_couplings();
-  // assembled radial matrix (nrad x nrad) of the Thomas-Fermi screened
-  // nucleus, int B_a B_b (-Z_TF(r)/r) dr
-  std::vector<double> thomas_fermi_radial() const;
 };
 
 // normalised Y_l^m(theta, phi) with the Condon-Shortley phase (value of the

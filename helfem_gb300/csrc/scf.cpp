@@ -610,6 +610,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
 
     double Eold = 0.0;
     int it = 0, nh = 0;
+    int wcur = 0;  // DIIS ring write cursor: the next (oldest once full) slot
     bool converged = false;
     int n_stable = 0;
     // stabilisation: when the orbital gradient stalls above 1e-5 (DIIS
@@ -729,12 +730,14 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         it_improved = it;
         emin = emax;
         nh = 0;
+        wcur = 0;
         std::fill(Bm.begin(), Bm.end(), 0.0);
         if (verbose) std::fprintf(stderr, "hfg_scf it %3d level shift %.2f, DIIS restart\n", it, shift);
       }
 
       // ---- DIIS extrapolation ----
-      const int slot = (nh < nhist) ? nh : (it - 1) % nhist;
+      const int slot = wcur;
+      wcur = (wcur + 1) % nhist;
       ck(cudaMemcpyAsync(dHF.as<double>() + Ltot * slot, dFo.p, sizeof(double) * Ltot, cudaMemcpyDeviceToDevice, st),
          "copy");
       ck(cudaMemcpyAsync(dHE.as<double>() + Ltot * slot, dEo.p, sizeof(double) * Ltot, cudaMemcpyDeviceToDevice, st),

@@ -107,15 +107,6 @@ hfg_status hfg_atom_get_dims(const hfg_atom* atom, hfg_atom_dims_t* dims);
 hfg_status hfg_overlap(const hfg_atom* atom, double* S);
 hfg_status hfg_kinetic(const hfg_atom* atom, double* T);
 hfg_status hfg_nuclear(const hfg_atom* atom, double* V);
-/* Matrix of a screened-nucleus model potential, host output nbf x nbf:
- * replaces TwoDBasisT::model_potential (src/atomic/TwoDBasis.cpp:444-455;
- * the per-element integral of libhelfem/src/RadialBasis.cpp:605-619). model
- * uses the reference's iguess numbering; 3 = Thomas-Fermi screened nucleus
- * (TFAtom, src/general/model_potential.cpp:53-55: V = -Z_TF(r)/r with the
- * screening function of arXiv physics/0511017). GSZ (1) and SAP (2) need
- * tabulated parameters that are not part of this library: HFG_ERR_ARG. */
-hfg_status hfg_model_potential(const hfg_atom* atom, int model, double* V);
-
 /* Cached radial tables of multipole L and element iel, in the reference's
  * compact layout (Ni x Ni; Cholesky factor Ni^2 x rank, pair index a + b*Ni,
  * CoulombExchangeFE.h:471-477). Any output may be NULL; rbig is zero for
@@ -195,9 +186,10 @@ hfg_status hfg_rs_exchange_host(hfg_atom* atom, const double* P, double* K, int 
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
  * fixed 4 MiB array in the library's static device memory rather than the
  * handle's buffers. No counterpart in the reference; it exists for callers
- * whose per-call path cannot allocate device memory (inside CUDA stream
- * capture, under a host framework that owns every device allocation, or in
- * loops that must not risk an allocation's synchronisation or failure).
+ * whose per-call path cannot allocate device memory (a host framework that
+ * owns every device allocation and hands the library a fixed budget, or a
+ * loop that must not risk an allocation's implicit synchronisation or its
+ * failure).
  * Atoms needing more than 4 MiB of Coulomb scratch
  * (channels * elements * (nnodes^2 + 2) doubles) are rejected with
  * HFG_ERR_ARG. All calls share the one array: calls that overlap on the GPU
@@ -335,10 +327,13 @@ hfg_status hfg_engine_create(int n_workers, double hbm_budget_gb, hfg_engine** o
 hfg_status hfg_engine_submit(hfg_engine* e, const hfg_atom_desc* atom, const hfg_scf_desc* scf,
                              unsigned long long* job_id);
 /* waits up to timeout_s (< 0: no limit); a finished job's result is returned
- * once and then forgotten; status < 2 means it is still pending */
+ * once and then forgotten; status < 2 means it is still pending. Several
+ * threads may wait on the same id: one receives the result, the others an
+ * error. */
 hfg_status hfg_engine_wait(hfg_engine* e, unsigned long long job_id, double timeout_s, hfg_job_result* out);
 hfg_status hfg_engine_stats(hfg_engine* e, int* queued, int* running, double* in_use_gb);
-/* cancels queued jobs, waits for running ones */
+/* cancels queued jobs, waits for running ones and for every thread inside
+ * hfg_engine_wait to return, then frees the engine */
 hfg_status hfg_engine_destroy(hfg_engine* e);
 
 /* ---- per-kernel timing (counterpart of the reference's scf_driver::FockTimer,

@@ -78,14 +78,6 @@ class AtomicTwoDBasis {
   Matrix overlap() const { return one(hfg_overlap); }
   Matrix kinetic() const { return one(hfg_kinetic); }
   Matrix nuclear() const { return one(hfg_nuclear); }
-  // model_potential(new modelpotential::TFAtom(Z)) of the reference
-  // (TwoDBasis.cpp:444-455): the Thomas-Fermi screened nucleus of the guess
-  Matrix thomas_fermi_potential() const {
-    const size_t n = Nbf();
-    Matrix M(n, n);
-    check(hfg_model_potential(host_.get(), 3, M.data()));
-    return M;
-  }
 
   Matrix coulomb(const Matrix& P) const {
     if (!gpu_) detail::no_tei();

@@ -69,6 +69,7 @@ def lib():
                 getattr(_lib, fn).argtypes = [ctypes.POINTER(_OraAtom), ctypes.c_void_p, ctypes.c_void_p]
                 getattr(_lib, fn).restype = None
             _lib.ora_num_threads.restype = ctypes.c_int
+            _lib.ora_set_threads.argtypes = [ctypes.c_int]
     return _lib
 
 

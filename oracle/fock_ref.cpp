@@ -59,6 +59,16 @@ int ora_num_threads() {
 #endif
 }
 
+// thread count of the following oracle calls (the reference's tests run
+// with OMP_NUM_THREADS=1); n <= 0 restores every host core
+void ora_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
+#else
+  (void)n;
+#endif
+}
+
 }  // extern "C"
 
 namespace {

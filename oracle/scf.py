@@ -81,7 +81,7 @@ def run_scf(atom: tab.AtomTables, nela: int, nelb: int, method: str = "hf",
             restricted: bool = True, fixed_occ=None, fock: FockOracle = None,
             grid: xcmod.AtomGrid = None, maxiter: int = 200, conv: float = 1e-10,
             thr: float = 1e-12, verbose: bool = False, guess_H: np.ndarray = None,
-            l_occ=None) -> SCFResult:
+            l_occ=None, gtol: float = 1e-7) -> SCFResult:
     """fixed_occ: dict m -> (nocc_alpha, nocc_beta) (restricted: total/2 each).
     guess_H: one-electron Hamiltonian whose orbitals start the SCF (default
     the core Hamiltonian T + V; T + a screened-nucleus model potential is
@@ -90,7 +90,9 @@ def run_scf(atom: tab.AtomTables, nela: int, nelb: int, method: str = "hf",
     function with fixed occupations: the electrons of each l shared equally
     over its 2l+1 m blocks and filled lowest-first within a block (the
     spherically averaged occupations of the engine's batch and serving
-    solves; symmetry 2 of the reference's atomic driver)."""
+    solves; symmetry 2 of the reference's atomic driver).
+    Converged when the energy change is below conv and the largest element
+    of the orthonormal-basis commutator F P S - S P F is below gtol."""
     fock = fock or FockOracle(atom)
     names = xcmod.parse_method(method)
     have_xc = bool(names)
@@ -184,7 +186,7 @@ def run_scf(atom: tab.AtomTables, nela: int, nelb: int, method: str = "hf",
         emax = float(np.max(np.abs(err)))
         if verbose:
             print(f"it {it:3d} E {E:.12f} dE {E - Eold: .3e} err {emax:.3e}")
-        if it > 1 and abs(E - Eold) < conv and emax < 1e-7:
+        if it > 1 and abs(E - Eold) < conv and emax < gtol:
             converged = True
             res.converged = True
             break

@@ -37,10 +37,6 @@ int main(int argc, char** argv) {
   double tr = 0.0;
   for (long i = 0; i < S.rows(); ++i) tr += S(i, i);
   std::printf("atomic nbf %zu trS %.15e\n", atom.Nbf(), tr);
-  Mat Vtf = atom.thomas_fermi_potential();
-  double trv = 0.0;
-  for (long i = 0; i < Vtf.rows(); ++i) trv += Vtf(i, i);
-  std::printf("atomic-tf trV %.15e\n", trv);
   std::vector<double> bd = {0.0, 0.8, 2.0, 4.7};
   helfem_gb300::DiatomicTwoDBasis<Mat> mol(1, 1, 0.7, 9, bd, {0, 1, 1, 1}, {0, 0, 1, -1});
   Mat Sd = mol.overlap();

@@ -36,8 +36,6 @@ def test_shim_host_side(tmp_path):
     out = subprocess.run([exe, "host"], capture_output=True, text=True, check=True).stdout
     a = hg.Atom(4, [0.0, 0.5, 2.0, 8.0, 40.0], [0, 1], [0, 0], nnodes=9, host_only=True)
     assert abs(parse(out, "atomic")["trS"] - np.trace(a.overlap())) < 1e-12 * abs(np.trace(a.overlap()))
-    trv = np.trace(a.model_potential(3))
-    assert abs(parse(out, "atomic-tf")["trV"] - trv) < 1e-12 * abs(trv)
     d = hg.Diatomic(1, 1, 0.7, [0.0, 0.8, 2.0, 4.7], [0, 1, 1, 1], [0, 0, 1, -1], nnodes=9, host_only=True)
     assert abs(parse(out, "diatomic")["trS"] - np.trace(d.overlap())) < 1e-12 * abs(np.trace(d.overlap()))
     assert "logic_error: Primitive teis have not been computed!" in out

@@ -57,16 +57,65 @@ def test_symmetry_blocks_agree():
     assert abs(a["Etot"] - b["Etot"]) < 1e-9
 
 
-def test_orbital_energies_match_oracle():
+def _tight_pair(Z, nelem, lmax, mmax, zexp, nel, monkeypatch):
+    """One GPU SCF and one oracle SCF of the same atom, both converged to an
+    orbital gradient (largest orthonormal-basis commutator element) below
+    1e-10 from the core-Hamiltonian guess, with full eigensolves on the GPU
+    so that the gradient can fall below the refinement's residual floor."""
+    from oracle import scf as oscf
+    monkeypatch.setenv("HFG_SCF_EIGENSOLVER", "full")
+    atom = hg.Atom.from_grid(Z, nelem, 40.0, lmax, mmax, igrid=4, zexp=zexp)
+    r = atom.scf(nel, nel, "hf", restricted=True, symmetry=1, e_tol=1e-12, diis_tol=1e-10, maxiter=300)
+    A = tab.build_atom(Z, 15, tab.get_grid(40.0, nelem, 4, zexp), lmax, mmax)
+    o = oscf.run_scf(A, nel, nel, "hf", True, conv=1e-12, gtol=1e-10, maxiter=300)
+    return r, o
+
+
+def _check_spectrum(r, o, nocc):
+    e_gpu = np.sort(r["orbital_energies"])[:nocc + 1]
+    e_ora = np.sort(np.concatenate([np.ravel(x) for x in o.eps]))[:nocc + 1]
+    scale = np.abs(e_ora[:nocc]).max()
+    # occupied orbitals at 1e-10 relative each; the first virtual (near zero
+    # in a finite box) at 1e-10 of the occupied spectrum's scale
+    tol = np.concatenate([1e-10 * np.abs(e_ora[:nocc]), [1e-10 * scale]])
+    d = np.abs(e_gpu - e_ora)
+    print("orbital energies", e_gpu, "max |d|", d.max(), "max |d|/tol", (d / tol).max())
+    assert (d <= tol).all(), (e_gpu, e_ora, d)
+
+
+def test_orbital_energies_match_oracle(monkeypatch):
+    """He (the reference's CI geometry): total energy at 1e-10 relative, the
+    occupied and first virtual orbital energies at 1e-10 relative."""
+    torch_cuda()
+    r, o = _tight_pair(2, 5, 0, 0, 2.0, 1, monkeypatch)
+    assert r["converged"] and o.converged
+    assert abs(r["Etot"] - o.Etot) < 1e-10 * abs(o.Etot), (r["Etot"], o.Etot)
+    _check_spectrum(r, o, 1)
+
+
+def test_ne_config1_matches_oracle(monkeypatch):
+    """Ne as the first benchmark configuration states it: Z = 10 restricted
+    HF, 10 elements with r_i = 41^(i/10) - 1 (zexp = 1, Rmax = 40), 15-node
+    LIP, l = 0..1 with m = 0 only (Nbf = 278), L = 0..2, core-Hamiltonian
+    guess. The default SCF path to the configuration's own criterion gives
+    the oracle's total energy at 1e-10 relative; converged tightly, the five
+    occupied and the first virtual orbital energies agree at 1e-10 relative
+    as well."""
     torch_cuda()
     from oracle import scf as oscf
-    from oracle import tabulate as tab
-    r = run_case("atomic-He-hf-r")
-    A = tab.build_atom(2, 15, tab.get_grid(40.0, 5, 4, 2.0), 0, 0)
-    o = oscf.run_scf(A, 1, 1, "hf", True)
-    e_gpu = np.sort(r["orbital_energies"])[:3]
-    e_ora = np.sort(np.concatenate(o.eps[0]))[:3]
-    assert np.abs(e_gpu - e_ora).max() < 1e-7, (e_gpu, e_ora)
+    atom = hg.Atom.from_grid(10, 10, 40.0, 1, 0, igrid=4, zexp=1.0)
+    assert atom.nbf == 278
+    r0 = atom.scf(5, 5, "hf", restricted=True, symmetry=1)
+    A = tab.build_atom(10, 15, tab.get_grid(40.0, 10, 4, 1.0), 1, 0)
+    o0 = oscf.run_scf(A, 5, 5, "hf", True)
+    assert r0["converged"] and o0.converged
+    assert abs(r0["Etot"] - o0.Etot) < 1e-10 * abs(o0.Etot), (r0["Etot"], o0.Etot)
+    r, o = _tight_pair(10, 10, 1, 0, 1.0, 5, monkeypatch)
+    assert r["converged"] and o.converged
+    assert abs(r["Etot"] - o.Etot) < 1e-10 * abs(o.Etot), (r["Etot"], o.Etot)
+    for k in ("Ekin", "Enuc", "Ecoul", "Exx"):
+        assert abs(r[k] - getattr(o, k)) < 1e-9 * abs(o.Etot), (k, r[k], getattr(o, k))
+    _check_spectrum(r, o, 5)
 
 
 @pytest.mark.parametrize("symmetry", [1, 2])

@@ -1,8 +1,8 @@
 """The allocation-free Coulomb entry point (hfg_coulomb_noalloc).
 
-Callers that cannot allocate device memory on their per-call path (code
-inside CUDA stream capture, hosts that own every device allocation) use this
-variant; its scratch is a fixed 4 MiB array in the library's static device
+Callers that cannot allocate device memory on their per-call path (hosts
+that own every device allocation and give the library a fixed budget, loops
+that must not risk an allocation's synchronisation) use this variant; its scratch is a fixed 4 MiB array in the library's static device
 memory. It must give the same J as hfg_coulomb, call after call (the shared
 array keeps the previous call's contents), and must refuse atoms whose
 scratch does not fit. This file is named to be collected last.
