@@ -57,6 +57,10 @@ _SIGS = {
     "hfg_angular_basis": ([ctypes.c_int, ctypes.c_int, _I, _I, _I], ctypes.c_int),
     "hfg_atom_create": ([ctypes.POINTER(_Desc), ctypes.POINTER(_P)], ctypes.c_int),
     "hfg_atom_destroy": ([_P], ctypes.c_int),
+    "hfg_tc_selftest": ([ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                         ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                         ctypes.c_int], ctypes.c_int),
+    "hfg_tc_peak": ([ctypes.c_int, ctypes.c_int, _D, _D], ctypes.c_int),
     "hfg_atom_get_dims": ([_P, ctypes.POINTER(_Dims)], ctypes.c_int),
     "hfg_overlap": ([_P, _D], ctypes.c_int),
     "hfg_kinetic": ([_P, _D], ctypes.c_int),
@@ -194,6 +198,27 @@ def angular_basis(lmax: int, mmax: int):
     mv = np.zeros(n.value, dtype=np.int32)
     _check(_lib.hfg_angular_basis(lmax, mmax, ctypes.byref(n), lv.ctypes.data_as(_I), mv.ctypes.data_as(_I)))
     return lv, mv
+
+
+def tc_selftest(A: np.ndarray, B: np.ndarray, a_mn_major: bool = False, b_mn_major: bool = False,
+                swap_offsets: bool = False) -> np.ndarray:
+    """D = A B^T through the library's tcgen05 operand layouts (A: 128 x K,
+    B: N x K, K a multiple of 16; operands rounded to bf16, FP32 sums)."""
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    assert A.shape[0] == 128 and A.shape[1] == B.shape[1] and A.shape[1] % 16 == 0
+    D = np.zeros((128, B.shape[0]), dtype=np.float32)
+    f = ctypes.POINTER(ctypes.c_float)
+    _check(_lib.hfg_tc_selftest(A.ctypes.data_as(f), B.ctypes.data_as(f), D.ctypes.data_as(f), B.shape[0],
+                                A.shape[1] // 16, int(a_mn_major), int(b_mn_major), int(swap_offsets)))
+    return D
+
+
+def tc_peak(ctas_per_sm: int = 2, iters: int = 4096) -> dict:
+    """Dense bf16 tcgen05 MMA rate of this GPU (M = 128, N = 256, K = 16)."""
+    tf, ms = ctypes.c_double(), ctypes.c_double()
+    _check(_lib.hfg_tc_peak(ctas_per_sm, iters, ctypes.byref(tf), ctypes.byref(ms)))
+    return {"tflops": tf.value, "ms": ms.value, "ctas_per_sm": ctas_per_sm, "iters": iters}
 
 
 def gaunt(L: int, M: int, l: int, m: int, lp: int) -> float:

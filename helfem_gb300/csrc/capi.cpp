@@ -219,6 +219,28 @@ hfg_status hfg_coulomb_noalloc(hfg_atom* a, const double* P, double* J, void* st
   });
 }
 
+hfg_status hfg_tc_selftest(const float* A, const float* B, float* D, int N, int ksteps, int a_mn_major,
+                           int b_mn_major, int swap_offsets) {
+  return guard([&] {
+    need(A && B && D, "hfg_tc_selftest: null argument");
+    need(N >= 16 && N <= 256 && N % 16 == 0 && ksteps >= 1 && ksteps <= 8, "hfg_tc_selftest: bad shape");
+    int timed_out = 0;
+    ck(hfg::tc_selftest(A, B, D, N, ksteps, a_mn_major ? 1 : 0, b_mn_major ? 1 : 0, swap_offsets ? 1 : 0,
+                        &timed_out),
+       "tensor-core self-test");
+    need(!timed_out, "hfg_tc_selftest: the MMA completion wait ran out");
+  });
+}
+
+hfg_status hfg_tc_peak(int ctas_per_sm, int iters, double* tflops, double* ms) {
+  return guard([&] {
+    need(tflops && ms && ctas_per_sm >= 1 && ctas_per_sm <= 2 && iters >= 1, "hfg_tc_peak: bad arguments");
+    int timed_out = 0;
+    ck(hfg::tc_peak(ctas_per_sm, iters, tflops, ms, &timed_out), "tensor-core peak probe");
+    need(!timed_out, "hfg_tc_peak: the MMA completion wait ran out");
+  });
+}
+
 hfg_status hfg_exchange(hfg_atom* a, const double* P, double* K, void* stream) {
   return hfg_exchange_ex(a, P, K, 0, stream);
 }

@@ -118,6 +118,10 @@ cudaError_t launch_xc_fp64(const DevAtom& A, const DevXC& X, const XcScratch& S,
 // device (coulomb_noalloc.cu). cudaErrorInvalidValue if doubles_needed
 // exceeds the capacity.
 cudaError_t noalloc_coulomb_scratch(size_t doubles_needed, double** out);
+// tensor-core probe (tc_probe.cu)
+cudaError_t tc_selftest(const float* A, const float* B, float* D, int N, int ksteps, int a_mn, int b_mn, int swap,
+                        int* timed_out);
+cudaError_t tc_peak(int ctas_per_sm, int iters, double* tflops, double* ms, int* timed_out);
 
 // launchers (jk_fp64.cu)
 cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* J,

@@ -1,0 +1,137 @@
+// Thin inline-PTX wrappers for the Blackwell tensor-core path (sm_103a):
+// tcgen05 tensor-memory allocation, MMA issue and completion, tensor-memory
+// loads, mbarriers, and the shared-memory operand descriptors.
+//
+// Operand tiles in shared memory use the no-swizzle canonical layout: the
+// tile is a grid of 8 x 16-byte "core matrices" (128 contiguous bytes each),
+// core (row block r, k block c) at byte offset r * SBO + c * LBO, with
+// LBO = 128 and SBO = 256 for a 16-wide K step (the two K blocks of a row
+// block are adjacent). Inside a core matrix a K-major operand stores its 8
+// rows of 8 K-consecutive bf16 values (16 bytes per row); an MN-major one
+// stores 8 K-rows of 8 MN-consecutive values.
+#pragma once
+
+#include <cstdint>
+
+namespace hfg {
+namespace tc {
+
+constexpr uint32_t kLBO = 128;  // bytes between the two K core matrices of a row block
+constexpr uint32_t kSBO = 256;  // bytes between consecutive 8-row blocks
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// byte offset of element (mn, k) of a 16-wide K step tile (bf16)
+__device__ __forceinline__ uint32_t off_kmajor(int mn, int k) {
+  return (uint32_t)((mn >> 3) * kSBO + (k >> 3) * kLBO + (mn & 7) * 16 + (k & 7) * 2);
+}
+__device__ __forceinline__ uint32_t off_mnmajor(int mn, int k) {
+  return (uint32_t)((mn >> 3) * kSBO + (k >> 3) * kLBO + (k & 7) * 16 + (mn & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start address, leading (K) and stride
+// (MN) byte offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo = kLBO, uint32_t sbo = kSBO) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+  d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor of kind::f16 with bf16 A and B and FP32 accumulation
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, int a_mn_major, int b_mn_major) {
+  return (1u << 4)                      // D: FP32
+         | (1u << 7)                    // A: BF16
+         | (1u << 10)                   // B: BF16
+         | ((uint32_t)a_mn_major << 15) // A major (0: K)
+         | ((uint32_t)b_mn_major << 16) // B major (0: K)
+         | ((uint32_t)(N >> 3) << 17)   // N / 8
+         | ((uint32_t)(M >> 4) << 24);  // M / 16
+}
+
+// ---- tensor memory (one warp, whole-warp instructions) ----
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// ---- MMA (issued by one thread) ----
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// the mbarrier receives one arrival when every MMA issued so far by this
+// thread has completed
+__device__ __forceinline__ void mma_commit(uint64_t* mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(mbar))
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// generic-proxy shared-memory writes become visible to the tensor core
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---- mbarrier ----
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(mbar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait on the phase with the given parity: false when the limit ran
+// out (the caller records an error and leaves)
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t limit = (1u << 24)) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try_wait(mbar, parity)) return true;
+  return false;
+}
+
+// ---- tensor memory -> registers: 32 lanes x 16 consecutive 32-bit columns
+// (warp w of a 128-thread group reads lanes 32w..32w+31). The load and its
+// wait sit in one asm statement so that no use of the registers can be
+// scheduled before the data has arrived. ----
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace tc
+}  // namespace hfg

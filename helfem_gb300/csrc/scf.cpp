@@ -716,7 +716,10 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       // changing; the energy error is quadratic in it, far below etol)
       const bool estable = it > 1 && std::fabs(Etot - Eold) < etol + 1e-12 * std::fabs(Etot);
       n_stable = estable ? n_stable + 1 : 0;
-      if ((estable && emax < dtol) || (n_stable >= 3 && emax < 1e-5)) {
+      // (the stable-energy fallback applies only under the default gradient
+      // target; a caller-set diis_tol is a hard requirement)
+      const bool floor_ok = d->diis_tol <= 0 && n_stable >= 3 && emax < 1e-5;
+      if ((estable && emax < dtol) || floor_ok) {
         converged = true;
         break;
       }

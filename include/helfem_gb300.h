@@ -197,6 +197,21 @@ hfg_status hfg_rs_exchange_host(hfg_atom* atom, const double* P, double* K, int 
  * resolves the array's device address; make it before any stream capture. */
 hfg_status hfg_coulomb_noalloc(hfg_atom* atom, const double* P, double* J, void* stream);
 
+/* ---- tensor-core probe (no counterpart in the reference) ----
+ * hfg_tc_selftest: D (128 x N, row-major, host) = A B^T with A 128 x K and
+ * B N x K (row-major host floats, K = 16 ksteps, 1 <= ksteps <= 8,
+ * N in 16..256 step 16), the operands rounded to bf16 and staged in shared
+ * memory in this library's tcgen05 operand layouts (a_mn_major /
+ * b_mn_major: MN-major instead of K-major), accumulated in FP32 in tensor
+ * memory. swap_offsets exchanges the two core-matrix strides of the
+ * descriptors (a diagnostic: the product is then wrong). For integer
+ * operands with exactly representable sums the result is exact.
+ * hfg_tc_peak: dense bf16 MMA rate (M = 128, N = 256, K = 16 back to back
+ * on resident operands, ctas_per_sm in 1..2), TFLOP/s and milliseconds. */
+hfg_status hfg_tc_selftest(const float* A, const float* B, float* D, int N, int ksteps, int a_mn_major,
+                           int b_mn_major, int swap_offsets);
+hfg_status hfg_tc_peak(int ctas_per_sm, int iters, double* tflops, double* ms);
+
 /* ---- XC potential on the atomic DFT grid ----
  * Replaces DFTGrid::eval_Fxc (src/atomic/dftgrid.h:156-159,
  * src/atomic/dftgrid.cpp:591-712) with functionals restated from the papers
@@ -273,7 +288,9 @@ typedef struct {
   double kfrac;            /* exact-exchange fraction; < 0 -> 1 for HF, 0 for DFT */
   int maxiter;             /* 0 -> 200                                        */
   double e_tol;            /* |dE| convergence; 0 -> 1e-10                    */
-  double diis_tol;         /* max |F'D' - D'F'|; 0 -> 1e-7                    */
+  double diis_tol;         /* max |F'D' - D'F'|; 0 -> 1e-7, or below 1e-5 with
+                              the energy stable for three iterations; > 0:
+                              required as given                            */
   const int* fixed_occ;    /* NULL: Aufbau; else [n_fixed_blocks][2] (alpha, beta)
                               electrons per block, blocks in ascending m (the
                               reference's --readocc)                           */
