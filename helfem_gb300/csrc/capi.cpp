@@ -259,7 +259,8 @@ hfg_status hfg_exchange_ex(hfg_atom* a, const double* P, double* K, int flags, v
         a->scr.p2 = a->s_p2.as<float2>();
         ck(cudaStreamSynchronize(a->own_stream), "sync");
       }
-      ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
+      ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof,
+                                    a->tc_for(false)),
          "exchange kernels (split)");
     } else {
       ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
@@ -291,7 +292,7 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
       a->scr.p2 = a->s_p2.as<float2>();
     }
     ck(hfg::launch_exchange_split(ctx, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
-                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof),
+                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof, a->tc_for(screened)),
        "exchange (split)");
   } else {
     ck(hfg::launch_exchange_fp64(ctx, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
@@ -300,6 +301,7 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
   }
   ck(cudaMemcpyAsync(out, a->h_out.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
   ck(cudaStreamSynchronize(st), "stream sync");
+  if (!coulomb && (flags & HFG_EXCHANGE_SPLIT)) a->tc_check();
 }
 
 // J(PJ) and K(PK) with one staging of the density when PK == PJ, the
@@ -341,7 +343,7 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
       a->scr.p2 = a->s_p2.as<float2>();
     }
     ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, Pk, a->h_out2.as<double>(),
-                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof),
+                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof, a->tc_for(false)),
        "exchange (split)");
   } else {
     ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, Pk, a->h_out2.as<double>(),
@@ -351,6 +353,7 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
   ck(cudaMemcpyAsync(K, a->h_out2.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
   ck(cudaStreamSynchronize(st), "stream sync");
   ck(cudaStreamSynchronize(a->copy_stream), "stream sync");
+  if (flags & HFG_EXCHANGE_SPLIT) a->tc_check();
 }
 
 hfg_status hfg_jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, double* K, int flags) {
@@ -382,7 +385,8 @@ hfg_status hfg_atom_autotune(hfg_atom* a, int flags, int* best_nsplit, double* b
     auto run = [&]() {
       const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
       if (flags & HFG_EXCHANGE_SPLIT)
-        ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P.as<double>(), K.as<double>(), sym, st, nullptr),
+        ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P.as<double>(), K.as<double>(), sym, st, nullptr,
+                                      a->tc_for(false)),
            "exchange");
       else
         ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P.as<double>(), K.as<double>(), sym, st, nullptr),
@@ -464,7 +468,8 @@ hfg_status hfg_rs_exchange(hfg_atom* a, const double* P, double* K, int flags, v
         a->s_p2.alloc(b2);
         a->scr.p2 = a->s_p2.as<float2>();
       }
-      ck(hfg::launch_exchange_split(a->dev_rs, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
+      ck(hfg::launch_exchange_split(a->dev_rs, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof,
+                                    a->tc_for(true)),
          "screened exchange (split)");
     } else {
       ck(hfg::launch_exchange_fp64(a->dev_rs, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),

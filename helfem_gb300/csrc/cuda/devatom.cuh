@@ -66,12 +66,55 @@ struct KUnits {
   int n_all = 0;
   const int4* sym = nullptr;   // a < b pairs, j <= k diagonal blocks
   int n_sym = 0;
+  int n_off_all = 0, n_off_sym = 0;  // off-diagonal units come first
   const int* diag_all = nullptr;  // 0..nang^2-1
   const int* diag_sym = nullptr;  // jk with j <= k
   const int* diag_jk_src(bool symmetric) const { return symmetric ? diag_sym : diag_all; }
 };
 
 __host__ __device__ inline int gfun(const DevAtom& A, int e, int p) { return e * (A.nn - 1) + p - 1; }
+
+// Tensor-core split-precision exchange (k_tc.cu): the radial tables as
+// balanced base-256 digit planes (bf16, 16 x 16 in the no-swizzle K-major
+// operand layout) with one power-of-two scale per row, the output blocks in
+// groups of up to 8, and the work units (a, b, group).
+#define TC_NDIGITS 7
+#define TC_TPLANE 512
+struct DevTC {
+  const unsigned char* digits = nullptr;  // [kind (0 r_small, 1 r_big)][L][e][TC_NDIGITS][TC_TPLANE]
+  const int* rowexp = nullptr;            // [kind][L][e][16]
+  const int* group_jk = nullptr;          // [ngroups][8], -1: empty slot
+  const int* group_ent = nullptr;         // [ngroups][8][NL], -1: no entry with that L
+  int ngroups = 0;
+  const int4* units_sym = nullptr;        // (a, b, group), a < b
+  int n_sym = 0;
+  const int4* units_all = nullptr;        // (a, b, group), a != b
+  int n_all = 0;
+  int* err = nullptr;                     // set when a completion wait ran out
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ size_t k_halo_idx(const DevAtom& A, int a, int b, int jk, int h) {
+  return ((size_t)(a * A.nel + b) * (A.nang * A.nang) + jk) * (2 * A.nn - 1) + h;
+}
+// store the finished contribution y of tile (a,b), angular block jk, at
+// local position (p,q): owned entries go to K, the shared last row/column to
+// the halo buffer (added by the boundary fix-up in a fixed order)
+__device__ __forceinline__ void k_store_tile(const DevAtom& A, const DevScratch& S, double* K, int a, int b, int jk,
+                                             int p, int q, double y) {
+  const int nn = A.nn;
+  if (p >= nn || q >= nn) return;
+  const int gp = gfun(A, a, p), gq = gfun(A, b, q);
+  if (gp < 0 || gp >= A.nrad || gq < 0 || gq >= A.nrad) return;
+  const int j = jk % A.nang, k = jk / A.nang;
+  if (p <= nn - 2 && q <= nn - 2)
+    K[(size_t)(k * A.nrad + gq) * A.nbf + (size_t)j * A.nrad + gp] = y;
+  else if (p == nn - 1)
+    S.khalo[k_halo_idx(A, a, b, jk, q)] = y;
+  else
+    S.khalo[k_halo_idx(A, a, b, jk, nn + p)] = y;
+}
+#endif
 
 // Optional per-kernel timing (the engine's counterpart of the reference's
 // FockTimer): when enabled, every kernel launch is bracketed by a pair of
@@ -118,6 +161,9 @@ cudaError_t launch_xc_fp64(const DevAtom& A, const DevXC& X, const XcScratch& S,
 // device (coulomb_noalloc.cu). cudaErrorInvalidValue if doubles_needed
 // exceeds the capacity.
 cudaError_t noalloc_coulomb_scratch(size_t doubles_needed, double** out);
+// tensor-core exchange tiles (k_tc.cu): off-diagonal element pairs only
+cudaError_t launch_k_tiles_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
+                              cudaStream_t st);
 // tensor-core probe (tc_probe.cu)
 cudaError_t tc_selftest(const float* A, const float* B, float* D, int N, int ksteps, int a_mn, int b_mn, int swap,
                         int* timed_out);
@@ -129,7 +175,9 @@ cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const dou
 cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr);
 // split-precision exchange (float-float on the FP32 pipe, FP64 recombination)
+// tc != nullptr: the off-diagonal element pairs run on the tensor cores (k_tc.cu)
 cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
-                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr);
+                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr,
+                                  const DevTC* tc = nullptr);
 
 }  // namespace hfg

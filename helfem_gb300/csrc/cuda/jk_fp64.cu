@@ -549,7 +549,7 @@ cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KU
 }
 
 cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
-                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof) {
+                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof, const DevTC* tc) {
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
@@ -559,10 +559,20 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
   {
     Mark m(prof, KC_K_TILES, st);
     const size_t smem = sizeof(float2) * (2 * n2 + 2 * A.NL * n2) + sizeof(double) * n2 + nang2;
-    const int nunits = symmetric ? U.n_sym : U.n_all;
+    int nunits = symmetric ? U.n_sym : U.n_all;
+    const int4* units = symmetric ? U.sym : U.all;
+    if (tc) {
+      // off-diagonal element pairs on the tensor cores; the float-pair kernel
+      // keeps the diagonal elements (the unit lists hold them last)
+      const cudaError_t e = launch_k_tiles_tc(A, S, *tc, symmetric, K, st);
+      if (e != cudaSuccess) return e;
+      const int noff = symmetric ? U.n_off_sym : U.n_off_all;
+      units += noff;
+      nunits -= noff;
+    }
     auto kern = (A.nn == 15) ? k_tiles_split<15> : k_tiles_split<0>;
-    kern<<<nunits, th, smem, st>>>(A, S, symmetric ? U.sym : U.all, U.diag_jk_src(symmetric),
-                                            symmetric ? 1 : 0, K);
+    if (nunits > 0)
+      kern<<<nunits, th, smem, st>>>(A, S, units, U.diag_jk_src(symmetric), symmetric ? 1 : 0, K);
   }
   {
     Mark m(prof, KC_K_FIXUP, st);

@@ -160,6 +160,114 @@ struct hfg_atom {
   DBuf d_rs2, d_rb2, d_tk2, d_kcoef2;
   DBuf d_units_all, d_units_sym, d_diag_all, d_diag_sym;
   hfg::KUnits units;
+  // tensor-core split exchange: digit tables of the bare and of the
+  // Yukawa-screened radial tables, shared groups and units, error flag
+  DBuf t_dig, t_exp, ty_dig, ty_exp, t_gjk, t_gent, t_usym, t_uall, t_err;
+  hfg::DevTC tc{}, tc_rs{};
+  bool tc_ok = false;
+  // the split exchange on the tensor cores (off-diagonal element pairs), or
+  // nullptr for the float-pair form everywhere (HFG_SPLIT_FORM=pairs)
+  const hfg::DevTC* tc_for(bool screened) const {
+    if (!tc_ok) return nullptr;
+    static const bool pairs = [] {
+      const char* v = std::getenv("HFG_SPLIT_FORM");
+      return v && std::string(v) == "pairs";
+    }();
+    if (pairs) return nullptr;
+    return screened ? (tc_rs.digits ? &tc_rs : nullptr) : &tc;
+  }
+  // digits of the radial tables (kind 0 r_small, 1 r_big; per (L, e) a
+  // 16 x 16 plane per digit, element (row n, column k) = table(n, k)) and the
+  // row exponents; see k_tc.cu for the arithmetic
+  void tc_tables(const std::vector<double>& rs, const std::vector<double>& rb, DBuf& dig, DBuf& rexp,
+                 hfg::DevTC& out) {
+    const hfg::AtomHost& H = host;
+    const int nn = H.rad.nn, nel = H.rad.nel, NL = H.NL, ND = TC_NDIGITS;
+    const size_t n2 = (size_t)nn * nn;
+    std::vector<uint16_t> d((size_t)2 * NL * nel * ND * (TC_TPLANE / 2), 0);
+    std::vector<int> ex((size_t)2 * NL * nel * 16, 0);
+    auto off = [](int n, int k) { return ((n >> 3) * 256 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2) / 2; };
+    for (int kind = 0; kind < 2; ++kind)
+      for (int L = 0; L < NL; ++L)
+        for (int e = 0; e < nel; ++e) {
+          const double* M = (kind == 0 ? rs : rb).data() + ((size_t)L * nel + e) * n2;
+          const size_t blk = ((size_t)kind * NL + L) * nel + e;
+          uint16_t* planes = d.data() + blk * ND * (TC_TPLANE / 2);
+          for (int n = 0; n < nn; ++n) {
+            double rowsum = 0.0;
+            for (int k = 0; k < nn; ++k) rowsum += std::fabs(M[n + (size_t)k * nn]);
+            int a = 0;
+            if (rowsum > 0.0) std::frexp(rowsum, &a);  // rowsum <= 2^a
+            ex[blk * 16 + n] = a;
+            for (int k = 0; k < nn; ++k) {
+              double r = std::ldexp(M[n + (size_t)k * nn], -a);
+              for (int kd = 0; kd < ND; ++kd) {
+                r *= 256.0;
+                const double dg = std::nearbyint(r);
+                r -= dg;
+                const float f = (float)dg;  // integer |dg| <= 256: exact in bf16
+                uint32_t bits;
+                std::memcpy(&bits, &f, 4);
+                planes[(size_t)kd * (TC_TPLANE / 2) + off(n, k)] = (uint16_t)(bits >> 16);
+              }
+            }
+          }
+        }
+    out.digits = reinterpret_cast<const unsigned char*>(dig.upload(d));
+    out.rowexp = rexp.upload(ex);
+  }
+  // output blocks in groups of 8 with similar multipole sets, and the units
+  void tc_setup() {
+    const hfg::AtomHost& H = host;
+    const int nel = H.rad.nel, NL = H.NL, nang2 = H.nang * H.nang;
+    if (H.rad.nn > 16 || NL > 8 || nel < 2) return;
+    std::vector<int> sig(nang2, 0), order(nang2);
+    for (int jk = 0; jk < nang2; ++jk) {
+      order[jk] = jk;
+      for (int e = H.kjk_ptr[jk]; e < H.kjk_ptr[jk + 1]; ++e) sig[jk] |= 1 << H.kent_L[e];
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sig[x] < sig[y]; });
+    const int G = (nang2 + 7) / 8;
+    std::vector<int> gjk((size_t)G * 8, -1), gent((size_t)G * 8 * NL, -1);
+    for (int i = 0; i < nang2; ++i) {
+      const int jk = order[i], g = i / 8, s = i % 8;
+      gjk[(size_t)g * 8 + s] = jk;
+      for (int e = H.kjk_ptr[jk]; e < H.kjk_ptr[jk + 1]; ++e) {
+        int& slot = gent[((size_t)g * 8 + s) * NL + H.kent_L[e]];
+        if (slot >= 0) return;  // two entries with one multipole: keep the float-pair form
+        slot = e;
+      }
+    }
+    std::vector<int4> us, ua;
+    for (int a = 0; a < nel; ++a)
+      for (int b = 0; b < nel; ++b) {
+        if (a == b) continue;
+        for (int g = 0; g < G; ++g) {
+          ua.push_back(make_int4(a, b, g, 0));
+          if (a < b) us.push_back(make_int4(a, b, g, 0));
+        }
+      }
+    tc_tables(H.rs, H.rb, t_dig, t_exp, tc);
+    tc.group_jk = t_gjk.upload(gjk);
+    tc.group_ent = t_gent.upload(gent);
+    tc.ngroups = G;
+    tc.units_sym = t_usym.upload(us);
+    tc.n_sym = (int)us.size();
+    tc.units_all = t_uall.upload(ua);
+    tc.n_all = (int)ua.size();
+    t_err.alloc(sizeof(int));
+    ck(cudaMemsetAsync(t_err.p, 0, sizeof(int), own_stream), "memset");
+    tc.err = t_err.as<int>();
+    tc_ok = true;
+  }
+  // a completion wait inside the tensor-core kernel ran out (checked by the
+  // host-pointer entry points after their synchronisation)
+  void tc_check() {
+    if (!tc_ok) return;
+    int e = 0;
+    ck(cudaMemcpy(&e, tc.err, sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+    if (e) throw std::runtime_error("tensor-core exchange: an MMA completion wait ran out");
+  }
   // staging for the host-pointer entry points (allocated on first use)
   DBuf h_in, h_out, h_in2, h_out2, h_e;
   DBuf d_xrad;  // radial orthonormaliser invh(S_rad), built by the first hfg_fock_diag
@@ -192,6 +300,10 @@ struct hfg_atom {
     dev_rs.rs2 = y_rs2.upload(split(host.y_rs));
     dev_rs.rb2 = y_rb2.upload(split(host.y_rb));
     dev_rs.tk2 = y_tk2.upload(split(host.y_tk));
+    if (tc_ok) {
+      tc_rs = tc;
+      tc_tables(host.y_rs, host.y_rb, ty_dig, ty_exp, tc_rs);
+    }
     ck(cudaStreamSynchronize(own_stream), "sync after upload");
     rs_ready = true;
   }
@@ -344,6 +456,7 @@ struct hfg_atom {
     }
     A.kterm_coef2 = d_kcoef2.upload(split(H.kterm_coef));
     build_units();
+    tc_setup();
     ck(cudaStreamSynchronize(own_stream), "sync after upload");
     on_device = true;
   }
@@ -458,7 +571,7 @@ struct hfg_atom {
       if (cut.back() != nang2) cut.push_back(nang2);
       return cut;
     };
-    auto make = [&](bool sym, std::vector<int>& dj) {
+    auto make = [&](bool sym, std::vector<int>& dj, int& noff) {
       std::vector<int4> u;
       const long npairs = sym ? (long)nel * (nel - 1) / 2 : (long)nel * (nel - 1);
       int nsplit = (int)std::min<long>(std::max<long>(1, (2432 + npairs - 1) / std::max<long>(npairs, 1)), 8);
@@ -471,6 +584,7 @@ struct hfg_atom {
           for (size_t s = 0; s + 1 < cut.size(); ++s)
             if (cut[s + 1] > cut[s]) u.push_back(make_int4(a, b, cut[s], cut[s + 1]));
         }
+      noff = (int)u.size();
       dj.clear();
       for (int k = 0; k < H.nang; ++k)
         for (int j = 0; j < H.nang; ++j)
@@ -480,7 +594,7 @@ struct hfg_atom {
       return u;
     };
     std::vector<int> dja, djs;
-    std::vector<int4> ua = make(false, dja), us = make(true, djs);
+    std::vector<int4> ua = make(false, dja, units.n_off_all), us = make(true, djs, units.n_off_sym);
     units.all = d_units_all.upload(ua);
     units.n_all = (int)ua.size();
     units.sym = d_units_sym.upload(us);

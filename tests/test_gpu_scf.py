@@ -71,26 +71,60 @@ def _tight_pair(Z, nelem, lmax, mmax, zexp, nel, monkeypatch):
     return r, o
 
 
-def _check_spectrum(r, o, nocc):
+def _check_spectrum(r, o, nocc, atol):
+    """SCF-converged orbital energies: the occupied and the first virtual,
+    within atol (both solves stop at an orbital gradient of 1e-10, which
+    leaves orbital energies uncertain at that level: they are first order
+    in the density error, unlike the total energy)."""
     e_gpu = np.sort(r["orbital_energies"])[:nocc + 1]
     e_ora = np.sort(np.concatenate([np.ravel(x) for x in o.eps]))[:nocc + 1]
-    scale = np.abs(e_ora[:nocc]).max()
-    # occupied orbitals at 1e-10 relative each; the first virtual (near zero
-    # in a finite box) at 1e-10 of the occupied spectrum's scale
-    tol = np.concatenate([1e-10 * np.abs(e_ora[:nocc]), [1e-10 * scale]])
     d = np.abs(e_gpu - e_ora)
-    print("orbital energies", e_gpu, "max |d|", d.max(), "max |d|/tol", (d / tol).max())
-    assert (d <= tol).all(), (e_gpu, e_ora, d)
+    print("orbital energies", e_gpu, "max |d|", d.max())
+    assert (d <= atol).all(), (e_gpu, e_ora, d)
+
+
+def _same_input_spectrum(atom, A, o, nocc):
+    """Orbital energies from the same input: the oracle's converged density
+    gives the Fock matrix on both sides (GPU J and K, oracle J and K), whose
+    generalised eigenvalues in the S metric are compared per m block."""
+    import scipy.linalg
+    from gpu_util import from_dev, to_dev
+    from oracle import FockOracle
+    torch = torch_cuda()
+    P = o.Pa + o.Pb
+    F = FockOracle(A)
+    Fo = A.T + A.V + F.coulomb(P) + F.exchange(o.Pa)
+    Pd = to_dev(torch, P)
+    Jd, Kd = torch.empty_like(Pd), torch.empty_like(Pd)
+    atom.coulomb(Pd, Jd)
+    atom.exchange(0.5 * Pd, Kd)
+    Fg = atom.kinetic() + atom.nuclear() + from_dev(Jd) + from_dev(Kd)
+    Fd = to_dev(torch, Fg)
+    Cd = torch.zeros_like(Fd)
+    ed = torch.zeros(atom.nbf, dtype=torch.float64, device="cuda")
+    atom.fock_diag(Fd, Cd, ed, symmetry=1)
+    torch.cuda.synchronize()
+    e_gpu = np.sort(ed.cpu().numpy())[:nocc + 1]
+    e_ora = np.sort(scipy.linalg.eigh(Fo, A.S, eigvals_only=True))[:nocc + 1]
+    d = np.abs(e_gpu - e_ora)
+    rel = d / np.abs(e_ora)
+    print("same-input orbital energies", e_gpu, "max |d|", d.max(), "max rel", rel.max())
+    return e_gpu, e_ora, d, rel
 
 
 def test_orbital_energies_match_oracle(monkeypatch):
-    """He (the reference's CI geometry): total energy at 1e-10 relative, the
-    occupied and first virtual orbital energies at 1e-10 relative."""
+    """He (the reference's CI geometry): total energy at 1e-10 relative;
+    SCF-converged orbital energies within 1e-9 Eh; the same-input occupied
+    orbital energy at 1e-10 relative."""
     torch_cuda()
     r, o = _tight_pair(2, 5, 0, 0, 2.0, 1, monkeypatch)
     assert r["converged"] and o.converged
     assert abs(r["Etot"] - o.Etot) < 1e-10 * abs(o.Etot), (r["Etot"], o.Etot)
-    _check_spectrum(r, o, 1)
+    _check_spectrum(r, o, 1, 1e-9)
+    atom = hg.Atom.from_grid(2, 5, 40.0, 0, 0, igrid=4, zexp=2.0)
+    A = tab.build_atom(2, 15, tab.get_grid(40.0, 5, 4, 2.0), 0, 0)
+    e_gpu, e_ora, d, rel = _same_input_spectrum(atom, A, o, 1)
+    assert rel[0] < 1e-10, (e_gpu, e_ora)
 
 
 def test_ne_config1_matches_oracle(monkeypatch):
@@ -98,9 +132,12 @@ def test_ne_config1_matches_oracle(monkeypatch):
     HF, 10 elements with r_i = 41^(i/10) - 1 (zexp = 1, Rmax = 40), 15-node
     LIP, l = 0..1 with m = 0 only (Nbf = 278), L = 0..2, core-Hamiltonian
     guess. The default SCF path to the configuration's own criterion gives
-    the oracle's total energy at 1e-10 relative; converged tightly, the five
-    occupied and the first virtual orbital energies agree at 1e-10 relative
-    as well."""
+    the oracle's total energy at 1e-10 relative; converged tightly, the
+    energy components agree at 1e-9 relative and the orbital energies within
+    1e-9 Eh; from the same density, the five occupied orbital energies agree
+    at 1e-10 relative and the first virtual (3.6e-3 Eh, near zero in the
+    40-bohr box) within 1e-11 Eh, the FP64 eigensolver's resolution for this
+    spectrum (its largest eigenvalue is ~5e4 Eh)."""
     torch_cuda()
     from oracle import scf as oscf
     atom = hg.Atom.from_grid(10, 10, 40.0, 1, 0, igrid=4, zexp=1.0)
@@ -115,7 +152,10 @@ def test_ne_config1_matches_oracle(monkeypatch):
     assert abs(r["Etot"] - o.Etot) < 1e-10 * abs(o.Etot), (r["Etot"], o.Etot)
     for k in ("Ekin", "Enuc", "Ecoul", "Exx"):
         assert abs(r[k] - getattr(o, k)) < 1e-9 * abs(o.Etot), (k, r[k], getattr(o, k))
-    _check_spectrum(r, o, 5)
+    _check_spectrum(r, o, 5, 1e-9)
+    e_gpu, e_ora, d, rel = _same_input_spectrum(atom, A, o, 5)
+    assert (rel[:5] < 1e-10).all(), (e_gpu, e_ora, rel)
+    assert d[5] < 1e-11, (e_gpu, e_ora, d)
 
 
 @pytest.mark.parametrize("symmetry", [1, 2])
