@@ -77,7 +77,7 @@ __host__ __device__ inline int gfun(const DevAtom& A, int e, int p) { return e *
 // Tensor-core split-precision exchange (k_tc.cu): the radial tables as
 // balanced base-256 digit planes (bf16, 16 x 16 in the no-swizzle K-major
 // operand layout) with one power-of-two scale per row, the output blocks in
-// groups of up to 8, and the work units (a, b, group).
+// groups of up to 8, and the work units (a, b, range of groups).
 #define TC_NDIGITS 7
 #define TC_TPLANE 512
 struct DevTC {
@@ -86,11 +86,25 @@ struct DevTC {
   const int* group_jk = nullptr;          // [ngroups][8], -1: empty slot
   const int* group_ent = nullptr;         // [ngroups][8][NL], -1: no entry with that L
   int ngroups = 0;
-  const int4* units_sym = nullptr;        // (a, b, group), a < b
+  const int4* units_sym = nullptr;        // (a, b, first group, end group), a < b
   int n_sym = 0;
-  const int4* units_all = nullptr;        // (a, b, group), a != b
+  const int4* units_all = nullptr;        // (a, b, first group, end group), a != b
   int n_all = 0;
   int* err = nullptr;                     // set when a completion wait ran out
+  // diagonal element tiles: the exchange-ordered tensor as digit planes
+  // [L][e][row tile][K step][digit][128 x 16], per-row exponents, groups of
+  // up to 16 output blocks (j <= k in symmetric mode), units (a, group, row tile)
+  const unsigned char* tk_digits = nullptr;
+  const int* tk_rowexp = nullptr;         // [L][e][row tile][128]
+  int dmtiles = 0, dksteps = 0;
+  const int* dgroup_jk_sym = nullptr;     // [groups][16]
+  const int* dgroup_ent_sym = nullptr;    // [groups][16][NL]
+  const int* dgroup_jk_all = nullptr;
+  const int* dgroup_ent_all = nullptr;
+  const int4* dunits_sym = nullptr;
+  int n_dsym = 0;
+  const int4* dunits_all = nullptr;
+  int n_dall = 0;
 };
 
 #ifdef __CUDACC__
@@ -164,6 +178,10 @@ cudaError_t noalloc_coulomb_scratch(size_t doubles_needed, double** out);
 // tensor-core exchange tiles (k_tc.cu): off-diagonal element pairs only
 cudaError_t launch_k_tiles_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
                               cudaStream_t st);
+cudaError_t launch_k_diag_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
+                             cudaStream_t st);
+cudaError_t launch_tk_digits(const DevAtom& A, int mtiles, int ksteps, unsigned char* out, int* rowexp,
+                             cudaStream_t st);
 // tensor-core probe (tc_probe.cu)
 cudaError_t tc_selftest(const float* A, const float* B, float* D, int N, int ksteps, int a_mn, int b_mn, int swap,
                         int* timed_out);

@@ -562,13 +562,12 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
     int nunits = symmetric ? U.n_sym : U.n_all;
     const int4* units = symmetric ? U.sym : U.all;
     if (tc) {
-      // off-diagonal element pairs on the tensor cores; the float-pair kernel
-      // keeps the diagonal elements (the unit lists hold them last)
-      const cudaError_t e = launch_k_tiles_tc(A, S, *tc, symmetric, K, st);
+      // every element pair on the tensor cores: the off-diagonal tiles, then
+      // the diagonal ones through the exchange-ordered tensor
+      cudaError_t e = launch_k_tiles_tc(A, S, *tc, symmetric, K, st);
+      if (e == cudaSuccess) e = launch_k_diag_tc(A, S, *tc, symmetric, K, st);
       if (e != cudaSuccess) return e;
-      const int noff = symmetric ? U.n_off_sym : U.n_off_all;
-      units += noff;
-      nunits -= noff;
+      nunits = 0;
     }
     auto kern = (A.nn == 15) ? k_tiles_split<15> : k_tiles_split<0>;
     if (nunits > 0)

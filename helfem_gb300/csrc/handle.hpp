@@ -163,6 +163,7 @@ struct hfg_atom {
   // tensor-core split exchange: digit tables of the bare and of the
   // Yukawa-screened radial tables, shared groups and units, error flag
   DBuf t_dig, t_exp, ty_dig, ty_exp, t_gjk, t_gent, t_usym, t_uall, t_err;
+  DBuf t_tkd, t_tke, ty_tkd, ty_tke, t_dgjk_s, t_dgent_s, t_dgjk_a, t_dgent_a, t_dus, t_dua;
   hfg::DevTC tc{}, tc_rs{};
   bool tc_ok = false;
   // the split exchange on the tensor cores (off-diagonal element pairs), or
@@ -216,6 +217,54 @@ struct hfg_atom {
     out.digits = reinterpret_cast<const unsigned char*>(dig.upload(d));
     out.rowexp = rexp.upload(ex);
   }
+  // digit planes of an exchange-ordered tensor (built on the device)
+  void tc_tk_tables(const double* tk_dev, DBuf& dig, DBuf& rexp, hfg::DevTC& out) {
+    const hfg::AtomHost& H = host;
+    const int n2 = H.rad.nn * H.rad.nn;
+    out.dmtiles = (n2 + 127) / 128;
+    out.dksteps = (n2 + 15) / 16;
+    const size_t nslice = (size_t)H.NL * H.rad.nel * out.dmtiles;
+    dig.alloc(nslice * out.dksteps * TC_NDIGITS * 4096);
+    rexp.alloc(sizeof(int) * nslice * 128);
+    hfg::DevAtom A = dev;
+    A.tk = tk_dev;
+    ck(hfg::launch_tk_digits(A, out.dmtiles, out.dksteps, dig.as<unsigned char>(), rexp.as<int>(), own_stream),
+       "exchange tensor digits");
+    out.tk_digits = dig.as<unsigned char>();
+    out.tk_rowexp = rexp.as<int>();
+  }
+  // groups of up to 16 diagonal output blocks (sorted by multipole set) and
+  // the diagonal units (element, group, row tile)
+  void tc_diag_groups(bool sym, DBuf& djk, DBuf& dent, DBuf& du, const int*& gjk_out, const int*& gent_out,
+                      const int4*& u_out, int& n_out, int mtiles) {
+    const hfg::AtomHost& H = host;
+    const int NL = H.NL, nel = H.rad.nel;
+    std::vector<int> blocks;
+    for (int k = 0; k < H.nang; ++k)
+      for (int j = 0; j < H.nang; ++j)
+        if (!sym || j <= k) blocks.push_back(j + k * H.nang);
+    std::vector<int> sig(blocks.size(), 0);
+    for (size_t i = 0; i < blocks.size(); ++i)
+      for (int e = H.kjk_ptr[blocks[i]]; e < H.kjk_ptr[blocks[i] + 1]; ++e) sig[i] |= 1 << H.kent_L[e];
+    std::vector<int> order(blocks.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sig[x] < sig[y]; });
+    const int G = ((int)blocks.size() + 15) / 16;
+    std::vector<int> gjk((size_t)G * 16, -1), gent((size_t)G * 16 * NL, -1);
+    for (size_t i = 0; i < order.size(); ++i) {
+      const int jk = blocks[order[i]], g = (int)i / 16, s2 = (int)i % 16;
+      gjk[(size_t)g * 16 + s2] = jk;
+      for (int e = H.kjk_ptr[jk]; e < H.kjk_ptr[jk + 1]; ++e) gent[((size_t)g * 16 + s2) * NL + H.kent_L[e]] = e;
+    }
+    std::vector<int4> u;
+    for (int a = 0; a < nel; ++a)
+      for (int mt = 0; mt < mtiles; ++mt)
+        for (int g = 0; g < G; ++g) u.push_back(make_int4(a, g, mt, 0));
+    gjk_out = djk.upload(gjk);
+    gent_out = dent.upload(gent);
+    u_out = du.upload(u);
+    n_out = (int)u.size();
+  }
   // output blocks in groups of 8 with similar multipole sets, and the units
   void tc_setup() {
     const hfg::AtomHost& H = host;
@@ -238,15 +287,22 @@ struct hfg_atom {
         slot = e;
       }
     }
-    std::vector<int4> us, ua;
-    for (int a = 0; a < nel; ++a)
-      for (int b = 0; b < nel; ++b) {
-        if (a == b) continue;
-        for (int g = 0; g < G; ++g) {
-          ua.push_back(make_int4(a, b, g, 0));
-          if (a < b) us.push_back(make_int4(a, b, g, 0));
+    // a unit is a range of groups of one element pair: the pair's tables and
+    // the tensor memory are set up once per unit; ranges are sized so that
+    // the launch has about eight waves of two CTAs per SM
+    auto units_of = [&](bool sym) {
+      const long npairs = sym ? (long)nel * (nel - 1) / 2 : (long)nel * (nel - 1);
+      const long want = 8L * 2 * 152;
+      const int per = (int)std::max<long>(1, std::min<long>(G, (npairs * G + want - 1) / want));
+      std::vector<int4> u;
+      for (int a = 0; a < nel; ++a)
+        for (int b = 0; b < nel; ++b) {
+          if (a == b || (sym && b < a)) continue;
+          for (int g = 0; g < G; g += per) u.push_back(make_int4(a, b, g, std::min(G, g + per)));
         }
-      }
+      return u;
+    };
+    std::vector<int4> us = units_of(true), ua = units_of(false);
     tc_tables(H.rs, H.rb, t_dig, t_exp, tc);
     tc.group_jk = t_gjk.upload(gjk);
     tc.group_ent = t_gent.upload(gent);
@@ -258,6 +314,11 @@ struct hfg_atom {
     t_err.alloc(sizeof(int));
     ck(cudaMemsetAsync(t_err.p, 0, sizeof(int), own_stream), "memset");
     tc.err = t_err.as<int>();
+    tc_tk_tables(dev.tk, t_tkd, t_tke, tc);
+    tc_diag_groups(true, t_dgjk_s, t_dgent_s, t_dus, tc.dgroup_jk_sym, tc.dgroup_ent_sym, tc.dunits_sym, tc.n_dsym,
+                   tc.dmtiles);
+    tc_diag_groups(false, t_dgjk_a, t_dgent_a, t_dua, tc.dgroup_jk_all, tc.dgroup_ent_all, tc.dunits_all, tc.n_dall,
+                   tc.dmtiles);
     tc_ok = true;
   }
   // a completion wait inside the tensor-core kernel ran out (checked by the
@@ -303,6 +364,7 @@ struct hfg_atom {
     if (tc_ok) {
       tc_rs = tc;
       tc_tables(host.y_rs, host.y_rb, ty_dig, ty_exp, tc_rs);
+      tc_tk_tables(dev_rs.tk, ty_tkd, ty_tke, tc_rs);
     }
     ck(cudaStreamSynchronize(own_stream), "sync after upload");
     rs_ready = true;
