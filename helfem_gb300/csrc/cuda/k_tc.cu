@@ -232,6 +232,30 @@ __device__ __forceinline__ int digitise(ffv (&x)[8], unsigned char* A1, int row,
   return E;
 }
 
+// the 8 values y[j] of tile (a,b), block jk, at row p and columns q0 + j:
+// one pass over the columns with the block's base address computed once;
+// owned entries go to K, the shared last row / column to the halo buffer
+__device__ __forceinline__ void store_rows(const DevAtom& A, const DevScratch& S, double* K, int a, int b, int jk,
+                                           int p, int q0, const double (&y)[8]) {
+  const int nn = A.nn;
+  const int gp = gfun(A, a, p);
+  if (p >= nn || gp < 0 || gp >= A.nrad) return;
+  const int j = jk % A.nang, k = jk / A.nang;
+  double* base = K + (size_t)k * A.nrad * A.nbf + (size_t)j * A.nrad + gp;
+  double* halo = S.khalo + ((size_t)(a * A.nel + b) * (A.nang * A.nang) + jk) * (2 * nn - 1);
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    const int q = q0 + jj, gq = gfun(A, b, q);
+    if (q >= nn || gq < 0 || gq >= A.nrad) continue;
+    if (p <= nn - 2 && q <= nn - 2)
+      base[(size_t)gq * A.nbf] = y[jj];
+    else if (p == nn - 1)
+      halo[q] = y[jj];
+    else
+      halo[nn + p] = y[jj];
+  }
+}
+
 struct Smem {
   unsigned char* A1;  // NDX planes: rows (slot, q), K = p (K-major)
   unsigned char* A2;  // ND planes: rows (slot, i), K = q (MN-major)
@@ -431,8 +455,9 @@ __global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, De
       tc::fence_after_sync();
       if (sm.fail[0]) break;
 
-      // ---- second product: D2[(slot,i), 16 level + r] ----
-      if (t == 0) {
+      // ---- second product: D2[(slot,i), 16 level + r], issued from another
+      // warp than the first product so that the issue cost is shared ----
+      if (t == 128) {
 #pragma unroll 1
         for (int ky = 0; ky < ND; ++ky)
           tc::mma_bf16(tD2 + 16 * ky, dA2 + (uint64_t)(ky * APLANE >> 4), dT2 + (uint64_t)(L * ND * TPLANE >> 4),
@@ -476,22 +501,17 @@ __global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, De
     double y[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) y[j] = failed ? __longlong_as_double(0x7ff8000000000000ll) : -pair_to_d(acc[j]);
-    if (jk >= 0) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) k_store_tile(A, S, K, a, b, jk, oi, 8 * half + j, y[j]);
-    }
+    if (jk >= 0) store_rows(A, S, K, a, b, jk, oi, 8 * half, y);
     if (symmetric) {
       double* stage = reinterpret_cast<double*>(sm.A1);  // 8 x 16 x 16 doubles; every MMA has completed
 #pragma unroll
       for (int j = 0; j < 8; ++j) stage[(oslot * 16 + oi) * 16 + 8 * half + j] = y[j];
       __syncthreads();
       if (jk >= 0) {
-        const int j0 = jk % A.nang, k0 = jk / A.nang;
+        // partner row p' = oi, columns q' = 8 half + j
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int qq = 8 * half + j;  // partner row p' = oi, column q' = qq
-          k_store_tile(A, S, K, b, a, k0 + j0 * A.nang, oi, qq, stage[(oslot * 16 + qq) * 16 + oi]);
-        }
+        for (int j = 0; j < 8; ++j) y[j] = stage[(oslot * 16 + 8 * half + j) * 16 + oi];
+        store_rows(A, S, K, b, a, (jk / A.nang) + (jk % A.nang) * A.nang, oi, 8 * half, y);
       }
     }
     __syncthreads();  // the stage (first operand) and the group tables are reused
