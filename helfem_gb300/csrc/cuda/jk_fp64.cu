@@ -171,19 +171,22 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   const int c1 = (int)((long)A.nrad * (blockIdx.y + 1) / NORM_SPLIT);
   double s = 0.0;
   float sf = 0.f;
-  const size_t n = (size_t)A.nrad * (c1 - c0);
-  for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
-    const size_t r = idx % A.nrad, c = c0 + idx / A.nrad;
-    const size_t o = (size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r;
-    const double v = P[o];
-    if (p2) {
-      // split path: integer-only split (no FP64-pipe instructions) and an
-      // FP32 norm of the high words for the screen
-      const float2 h = split_bits(v);
-      p2[o] = h;
-      sf = fmaf(h.x, h.x, sf);
-    } else {
-      s += v * v;
+  // the band's elements in column order (32-bit index arithmetic)
+  const int n = A.nrad * (c1 - c0);
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    const int r = idx % A.nrad, c = c0 + idx / A.nrad;
+    {
+      const size_t o = (size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r;
+      const double v = P[o];
+      if (p2) {
+        // split path: integer-only split (no FP64-pipe instructions) and an
+        // FP32 norm of the high words for the screen
+        const float2 h = split_bits(v);
+        p2[o] = h;
+        sf = fmaf(h.x, h.x, sf);
+      } else {
+        s += v * v;
+      }
     }
   }
   if (p2) s = (double)sf;

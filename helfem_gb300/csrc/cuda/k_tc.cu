@@ -101,32 +101,6 @@ __device__ __forceinline__ void tmem_ld_levels(uint32_t taddr, float (&v)[ND][8]
     for (int j = 0; j < 8; ++j) v[d][j] = __uint_as_float(r[8 * d + j]);
 }
 
-// all 7 levels of 4 consecutive columns, one wait
-__device__ __forceinline__ void tmem_ld_levels4(uint32_t taddr, float (&v)[ND][4]) {
-  static_assert(ND == 7, "level count of the load below");
-  uint32_t r[28];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%28];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4,%5,%6,%7}, [%29];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%8,%9,%10,%11}, [%30];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%12,%13,%14,%15}, [%31];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%32];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%20,%21,%22,%23}, [%33];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%24,%25,%26,%27}, [%34];\n"
-      "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27])
-      : "r"(taddr), "r"(taddr + 16), "r"(taddr + 32), "r"(taddr + 48), "r"(taddr + 64), "r"(taddr + 80),
-        "r"(taddr + 96)
-      : "memory");
-#pragma unroll
-  for (int d = 0; d < ND; ++d)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) v[d][j] = __uint_as_float(r[4 * d + j]);
-}
-
 // carry the level sums (weights 256^-(d+2)) into balanced digits
 // y_0..y_{ND-1} (weights 256^-(k+1)); the remainder of the last level is
 // rounded into its neighbour and dropped
@@ -285,8 +259,8 @@ __device__ __forceinline__ void store_rows(const DevAtom& A, const DevScratch& S
 struct Smem {
   unsigned char* A1;  // NDX planes: rows (slot, q), K = p (K-major)
   unsigned char* A2;  // ND planes: rows (slot, i), K = q (MN-major)
-  unsigned char* T1;  // 2 buffers x ND planes: left table of element a, one multipole
-  unsigned char* T2;  // 2 buffers x ND planes: right table of element b
+  unsigned char* T1;  // NL * ND planes of the left tables of element a
+  unsigned char* T2;  // NL * ND planes of the right tables of element b
   int* alpha;         // [NL][16] row exponents of the left tables
   int* beta;          // [NL][16] row exponents of the right tables
   int* ex;            // [2][8] tile exponents, by batch parity
@@ -295,14 +269,13 @@ struct Smem {
   int* gjk;           // [8] output block of the slot or -1
   unsigned char* act; // [nang^2] density block above the screen
   uint64_t* mbar;
-  uint64_t* mtab;     // [2] arrival of the table buffers
   uint32_t* tslot;
   int* fail;
 };
 
 }  // namespace
 
-__global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, DevTC T, const int4* __restrict__ units,
+__global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, DevTC T, const int4* __restrict__ units,
                                                      int symmetric, double* __restrict__ K) {
   const int4 u = units[blockIdx.x];
   const int a = u.x, b = u.y;
@@ -316,9 +289,9 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
     sm.A2 = p;
     p += ND * APLANE;
     sm.T1 = p;
-    p += 2 * ND * TPLANE;
+    p += NL * ND * TPLANE;
     sm.T2 = p;
-    p += 2 * ND * TPLANE;
+    p += NL * ND * TPLANE;
     int* ip = reinterpret_cast<int*>(p);
     sm.alpha = ip;
     ip += NL * 16;
@@ -335,25 +308,23 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
     sm.fail = ip;
     ip += 2;
     sm.mbar = reinterpret_cast<uint64_t*>(ip);
-    sm.mtab = sm.mbar + 1;
-    sm.tslot = reinterpret_cast<uint32_t*>(sm.mbar + 3);
+    sm.tslot = reinterpret_cast<uint32_t*>(sm.mbar + 1);
     sm.act = reinterpret_cast<unsigned char*>(sm.tslot + 2);
   }
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int qw = warp & 3, half = warp >> 2;
-  const int kl = (a < b) ? 0 : 1, kr = (a < b) ? 1 : 0;  // left: r_small(a) if a < b
-  // the digit planes of one multipole's left and right tables (3.5 KB each,
-  // contiguous) stream into table buffer bf; thread 0 only
-  auto load_tables = [&](int L, int bf) {
-    constexpr uint32_t bytes = ND * TPLANE;
-    tc::mbar_expect_tx(&sm.mtab[bf], 2 * bytes);
-    tc::bulk_g2s(sm.T1 + bf * bytes, T.digits + (((size_t)kl * NL + L) * A.nel + a) * bytes, bytes, &sm.mtab[bf]);
-    tc::bulk_g2s(sm.T2 + bf * bytes, T.digits + (((size_t)kr * NL + L) * A.nel + b) * bytes, bytes, &sm.mtab[bf]);
-  };
-  uint32_t ntab[2] = {0, 0};  // completed phases of the table barriers (thread 0)
 
-  // ---- set-up once per unit: row exponents of this element pair, block flags ----
+  // ---- set-up once per unit: tables of this element pair, block flags ----
   {
+    const int kl = (a < b) ? 0 : 1, kr = (a < b) ? 1 : 0;  // left: r_small(a) if a < b
+    const uint4* s1 = reinterpret_cast<const uint4*>(T.digits) + (size_t)(kl * NL * A.nel) * (ND * TPLANE / 16);
+    const uint4* s2 = reinterpret_cast<const uint4*>(T.digits) + (size_t)(kr * NL * A.nel) * (ND * TPLANE / 16);
+    const int per = ND * TPLANE / 16;  // uint4 per (L, e)
+    for (int idx = t; idx < NL * per; idx += blockDim.x) {
+      const int L = idx / per, o = idx % per;
+      reinterpret_cast<uint4*>(sm.T1)[idx] = s1[((size_t)L * A.nel + a) * per + o];
+      reinterpret_cast<uint4*>(sm.T2)[idx] = s2[((size_t)L * A.nel + b) * per + o];
+    }
     for (int idx = t; idx < NL * 16; idx += blockDim.x) {
       const int L = idx / 16, r = idx % 16;
       sm.alpha[idx] = T.rowexp[((size_t)(kl * NL + L) * A.nel + a) * 16 + r];
@@ -364,22 +335,16 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
   }
   // operand rows of an idle slot are never cleared: a tensor-core row only
   // feeds the same row of the result, and idle rows are never read back
-  // the second product's levels reuse the first product's tensor-memory
-  // columns: they are written only after every thread has read the first
   if (warp == 0) {
-    tc::tmem_alloc(sm.tslot, 128);
+    tc::tmem_alloc(sm.tslot, 256);
     tc::tmem_relinquish();
   }
-  if (t == 0) {
-    tc::mbar_init(sm.mbar, 1);
-    tc::mbar_init(&sm.mtab[0], 1);
-    tc::mbar_init(&sm.mtab[1], 1);
-  }
+  if (t == 0) tc::mbar_init(sm.mbar, 1);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *sm.tslot;
-  const uint32_t tD1 = tbase, tD2 = tbase;
+  const uint32_t tD1 = tbase, tD2 = tbase + 128;
   const uint32_t lane_off = (uint32_t)(32 * qw) << 16;
   uint32_t phase = 0;
   const uint64_t dA1 = tc::smem_desc(tc::smem_u32(sm.A1)), dA2 = tc::smem_desc(tc::smem_u32(sm.A2));
@@ -413,7 +378,6 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
     return -1;
   };
 
-  int bc = 0;  // batches so far: table buffer bc & 1
   for (int g = u.z; g < u.w; ++g) {
     // ---- the group's entries and their activity ----
     for (int idx = t; idx < 8 * NL; idx += blockDim.x) {
@@ -428,10 +392,9 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[j] = {0.f, 0.f};
 
-    // prologue: the first active batch's tables and density tiles
+    // prologue: the first active batch's density tiles
     int L = next_active(0);
     int par = 0;
-    if (L >= 0 && t == 0) load_tables(L, bc & 1);
     if (L >= 0 && sm.sact[L * 8 + warp]) {
       ffv x[8];
       recouple(A, sm.act, sm.gent[warp * NL + L], pbase, vp, x);
@@ -446,19 +409,13 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
       __syncthreads();
       tc::fence_after_sync();
       if (sm.fail[0]) break;  // read after the barrier: uniform over the CTA
-      const int bf = bc & 1;
-      // ---- first product: D1[(slot,q), 16 level + i]; the next batch's
-      // tables stream into the other buffer (its MMAs have completed) ----
+      // ---- first product: D1[(slot,q), 16 level + i] ----
       if (t == 0) {
-        if (!tc::mbar_wait(&sm.mtab[bf], ntab[bf] & 1u)) atomicExch(sm.fail, 1);
-        ++ntab[bf];
-        tc::fence_after_sync();
 #pragma unroll 1
         for (int kx = 0; kx < NDX; ++kx)
-          tc::mma_bf16(tD1 + 16 * kx, dA1 + (uint64_t)(kx * APLANE >> 4), dT1 + (uint64_t)(bf * ND * TPLANE >> 4),
+          tc::mma_bf16(tD1 + 16 * kx, dA1 + (uint64_t)(kx * APLANE >> 4), dT1 + (uint64_t)(L * ND * TPLANE >> 4),
                        tc::idesc_bf16(128, 16 * (ND - kx), 0, 0), kx > 0 ? 1u : 0u);
         tc::mma_commit(sm.mbar);
-        if (Ln >= 0) load_tables(Ln, bf ^ 1);
       }
       // the next batch's recoupling (global loads) overlaps the tensor core
       ffv xn[8];
@@ -471,25 +428,26 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
       // ---- levels -> balanced digits of Y = A X, the second product's
       // MN-major operand: rows (slot, i), K = q (lane = (slot, q)) ----
       if (sm.sact[L * 8 + oslot] | sm.sact[L * 8 + pslot]) {
-#pragma unroll 1
-        for (int ps = 0; ps < 2; ++ps) {  // columns i = 8 half + 4 ps + j
-          float v[ND][4];
-          tmem_ld_levels4(tD1 + lane_off + 8 * half + 4 * ps, v);
+        float v[ND][8];
+        tmem_ld_levels(tD1 + lane_off + 8 * half, v);
+        uint32_t pk[ND][4];
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            float lv[ND], y[ND];
+        for (int j = 0; j < 8; ++j) {
+          float lv[ND], y[ND];
 #pragma unroll
-            for (int d = 0; d < ND; ++d) lv[d] = v[d][j];
-            carry(lv, y);
+          for (int d = 0; d < ND; ++d) lv[d] = v[d][j];
+          carry(lv, y);
 #pragma unroll
-            for (int k = 0; k < ND; ++k) v[k][j] = y[k];
-          }
-          const uint32_t off = tc::off_mnmajor(oslot * 16 + 8 * half + 4 * ps, oi);
-#pragma unroll
-          for (int k = 0; k < ND; ++k)
-            *reinterpret_cast<uint2*>(sm.A2 + k * APLANE + off) =
-                make_uint2(pack_bf16(v[k][0], v[k][1]), pack_bf16(v[k][2], v[k][3]));
+          for (int k = 0; k < ND; ++k) v[k][j] = y[k];
         }
+#pragma unroll
+        for (int k = 0; k < ND; ++k)
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) pk[k][jj] = pack_bf16(v[k][2 * jj], v[k][2 * jj + 1]);
+        const uint32_t off = tc::off_mnmajor(oslot * 16 + 8 * half, oi);
+#pragma unroll
+        for (int k = 0; k < ND; ++k)
+          *reinterpret_cast<uint4*>(sm.A2 + k * APLANE + off) = make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
       }
       tc::fence_async_smem();
       tc::fence_before_sync();
@@ -502,7 +460,7 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
       if (t == 128) {
 #pragma unroll 1
         for (int ky = 0; ky < ND; ++ky)
-          tc::mma_bf16(tD2 + 16 * ky, dA2 + (uint64_t)(ky * APLANE >> 4), dT2 + (uint64_t)(bf * ND * TPLANE >> 4),
+          tc::mma_bf16(tD2 + 16 * ky, dA2 + (uint64_t)(ky * APLANE >> 4), dT2 + (uint64_t)(L * ND * TPLANE >> 4),
                        tc::idesc_bf16(128, 16 * (ND - ky), 1, 0), ky > 0 ? 1u : 0u);
         tc::mma_commit(sm.mbar);
       }
@@ -517,28 +475,22 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
 
       // ---- levels -> float pairs, scaled, accumulated over the multipoles ----
       if (sm.sact[L * 8 + oslot] | sm.sact[L * 8 + pslot]) {
-        const int ea = sm.alpha[L * 16 + oi] + sm.ex[par * 8 + oslot];
-        const bool mine = sm.sact[L * 8 + oslot] != 0;
+        float v[ND][8];
+        tmem_ld_levels(tD2 + lane_off + 8 * half, v);
+        if (sm.sact[L * 8 + oslot]) {
+          const int ea = sm.alpha[L * 16 + oi] + sm.ex[par * 8 + oslot];
 #pragma unroll
-        for (int ps = 0; ps < 2; ++ps) {  // columns r = 8 half + 4 ps + j
-          float v[ND][4];
-          tmem_ld_levels4(tD2 + lane_off + 8 * half + 4 * ps, v);
-          if (mine) {
+          for (int j = 0; j < 8; ++j) {
+            float lv[ND];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              float lv[ND];
-#pragma unroll
-              for (int d = 0; d < ND; ++d) lv[d] = v[d][j];
-              acc[4 * ps + j] =
-                  ff_add(acc[4 * ps + j], levels_to_pair(lv, exp2i(ea + sm.beta[L * 16 + 8 * half + 4 * ps + j])));
-            }
+            for (int d = 0; d < ND; ++d) lv[d] = v[d][j];
+            acc[j] = ff_add(acc[j], levels_to_pair(lv, exp2i(ea + sm.beta[L * 16 + 8 * half + j])));
           }
         }
       }
       tc::fence_before_sync();
       L = Ln;
       par ^= 1;
-      ++bc;
     }
     __syncthreads();
 
@@ -574,7 +526,7 @@ __global__ void __launch_bounds__(256, 3) k_tiles_tc(DevAtom A, DevScratch S, De
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, 128);
+  if (warp == 0) tc::tmem_dealloc(tbase, 256);
 }
 
 // ------------------------------------------------------------------------
@@ -829,8 +781,8 @@ __global__ void __launch_bounds__(256, 2) k_diag_tc(DevAtom A, DevScratch S, Dev
 }
 
 size_t tc_smem_bytes(int NL, int nang) {
-  return (size_t)(NDX + ND) * APLANE + (size_t)4 * ND * TPLANE +
-         sizeof(int) * (2 * NL * 16 + 16 + 8 * NL + 8 * NL + 8 + 2) + 3 * 8 + 8 + (size_t)nang * nang + 64;
+  return (size_t)(NDX + ND) * APLANE + (size_t)2 * NL * ND * TPLANE +
+         sizeof(int) * (2 * NL * 16 + 16 + 8 * NL + 8 * NL + 8 + 2) + 16 + (size_t)nang * nang + 64;
 }
 
 size_t tc_diag_smem_bytes(int NL, int ksteps, int nang) {
