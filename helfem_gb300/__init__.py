@@ -61,6 +61,7 @@ _SIGS = {
                          ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                          ctypes.c_int], ctypes.c_int),
     "hfg_tc_peak": ([ctypes.c_int, ctypes.c_int, _D, _D], ctypes.c_int),
+    "hfg_atom_tc_work": ([_P, ctypes.c_int, _D], ctypes.c_int),
     "hfg_atom_get_dims": ([_P, ctypes.POINTER(_Dims)], ctypes.c_int),
     "hfg_overlap": ([_P, _D], ctypes.c_int),
     "hfg_kinetic": ([_P, _D], ctypes.c_int),
@@ -335,6 +336,12 @@ class Atom:
             _check(_lib.hfg_exchange_ex(self._h, _ptr(P), _ptr(K), flags, _stream(stream)))
         else:
             _check(_lib.hfg_exchange(self._h, _ptr(P), _ptr(K), _stream(stream)))
+
+    def tc_work(self, symmetric: bool = True) -> float:
+        """bf16 MMA FLOPs of one split-precision exchange (all entries active)."""
+        f = ctypes.c_double()
+        _check(_lib.hfg_atom_tc_work(self._h, int(symmetric), ctypes.byref(f)))
+        return f.value
 
     def work(self) -> dict:
         w = _Work()

@@ -495,6 +495,14 @@ hfg_status hfg_exchange_host_ex(hfg_atom* a, const double* P, double* K, int fla
   return guard([&] { host_call(a, P, K, false, flags); });
 }
 
+hfg_status hfg_atom_tc_work(const hfg_atom* a, int symmetric, double* mma_flops) {
+  return guard([&] {
+    need(a != nullptr && mma_flops != nullptr, "hfg_atom_tc_work: null argument");
+    a->check_device();
+    *mma_flops = a->tc_ok ? a->tc_mma_flops[symmetric ? 0 : 1] : 0.0;
+  });
+}
+
 hfg_status hfg_atom_work(const hfg_atom* a, hfg_work_t* w) {
   return guard([&] {
     need(a != nullptr && w != nullptr, "hfg_atom_work: null argument");

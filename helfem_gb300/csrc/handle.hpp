@@ -166,6 +166,9 @@ struct hfg_atom {
   DBuf t_tkd, t_tke, ty_tkd, ty_tke, t_dgjk_s, t_dgent_s, t_dgjk_a, t_dgent_a, t_dus, t_dua;
   hfg::DevTC tc{}, tc_rs{};
   bool tc_ok = false;
+  // bf16 MMA FLOPs one tensor-core exchange issues with every entry active
+  // (index 0: symmetric mode, 1: general)
+  double tc_mma_flops[2] = {0.0, 0.0};
   // the split exchange on the tensor cores (off-diagonal element pairs), or
   // nullptr for the float-pair form everywhere (HFG_SPLIT_FORM=pairs)
   const hfg::DevTC* tc_for(bool screened) const {
@@ -260,6 +263,18 @@ struct hfg_atom {
     for (int a = 0; a < nel; ++a)
       for (int mt = 0; mt < mtiles; ++mt)
         for (int g = 0; g < G; ++g) u.push_back(make_int4(a, g, mt, 0));
+    {
+      long nb = 0;  // (group, L) batches with at least one entry
+      for (int g = 0; g < G; ++g)
+        for (int L = 0; L < NL; ++L) {
+          bool any = false;
+          for (int s2 = 0; s2 < 16; ++s2) any |= gent[((size_t)g * 16 + s2) * NL + L] >= 0;
+          nb += any ? 1 : 0;
+        }
+      // per batch and row tile: K steps x (N = 112 + 96 + ... + 16) x 128 x 16
+      const int ksteps = (H.rad.nn * H.rad.nn + 15) / 16;
+      tc_mma_flops[sym ? 0 : 1] += 2.0 * 128 * 16 * 448 * ksteps * (double)nb * nel * mtiles;
+    }
     gjk_out = djk.upload(gjk);
     gent_out = dent.upload(gent);
     u_out = du.upload(u);
@@ -303,6 +318,19 @@ struct hfg_atom {
       return u;
     };
     std::vector<int4> us = units_of(true), ua = units_of(false);
+    {
+      long nb = 0;  // (group, L) batches with at least one entry
+      for (int g = 0; g < G; ++g)
+        for (int L = 0; L < NL; ++L) {
+          bool any = false;
+          for (int s2 = 0; s2 < 8; ++s2) any |= gent[((size_t)g * 8 + s2) * NL + L] >= 0;
+          nb += any ? 1 : 0;
+        }
+      // per batch: 27 + 28 digit-plane products of 128 x 16 x 16
+      const double per = 2.0 * 128 * 16 * 16 * 55;
+      tc_mma_flops[0] += per * nb * ((double)nel * (nel - 1) / 2);
+      tc_mma_flops[1] += per * nb * ((double)nel * (nel - 1));
+    }
     tc_tables(H.rs, H.rb, t_dig, t_exp, tc);
     tc.group_jk = t_gjk.upload(gjk);
     tc.group_ent = t_gent.upload(gent);

@@ -271,6 +271,11 @@ typedef struct {
   int n_k_terms;           /* recoupling terms over all entries               */
 } hfg_work_t;
 hfg_status hfg_atom_work(const hfg_atom* atom, hfg_work_t* work);
+/* bf16 tensor-core FLOPs (digit-plane MMAs) one split-precision exchange
+ * issues with every exchange entry active: the executed tensor work that the
+ * roofline of the split form is measured against (0 when the handle runs the
+ * float-pair form). No counterpart in the reference. */
+hfg_status hfg_atom_tc_work(const hfg_atom* atom, int symmetric, double* mma_flops);
 
 /* ---- atomic SCF on the device ----
  * The Fock-builder loop of the reference's atomic driver
