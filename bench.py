@@ -524,7 +524,8 @@ def run_scf_batch(args):
         wall, res = run_engine_batch(jobs, args.workers, 180.0, True)
     wall_p, res_p = run_engine_batch(jobs, 1, 180.0, False)
     ok = [r for r in res if r["status"] == 2 and r["converged"]]
-    dE = max(abs(a["Etot"] - b["Etot"]) for a, b in zip(res, res_p))
+    both = [(a, b) for a, b in zip(res, res_p) if a["status"] == 2 and b["status"] == 2]
+    dE = max((abs(a["Etot"] - b["Etot"]) for a, b in both), default=None)
     lat = [r["total_ms"] for r in res]
     svc = [r["setup_ms"] + r["scf_ms"] for r in res]
     out = {
@@ -535,7 +536,9 @@ def run_scf_batch(args):
                                "{10,13,15,17}, Rmax 40-80, lmax by occupied shells, HF / LDA(Slater+PW92) 50/50, "
                                "restricted, Madelung occupations per l (spherically averaged), per-(l,m) blocks, to 1e-10 Eh",
                    "workers": args.workers, "hbm_budget_gb": 180.0},
-        "converged": len(ok), "iterations_mean": float(np.mean([r["iterations"] for r in res])),
+        "converged": len(ok), "failed": len(res) - len(ok),
+        "failures": sorted(set(f"Z={j['Z']}: {r['error']}" for j, r in zip(jobs, res) if r["status"] != 2)),
+        "iterations_mean": float(np.mean([r["iterations"] for r in res])),
         "latency_ms": {"p50": _percentile(lat, 0.5), "p99": _percentile(lat, 0.99)},
         "service_ms": {"p50": _percentile(svc, 0.5), "p99": _percentile(svc, 0.99)},
         "setup_ms": {"p50": _percentile([r["setup_ms"] for r in res], 0.5),
@@ -602,7 +605,9 @@ def run_serve(args):
                        "form": "same request stream, one solve at a time, FP64 exchange",
                        "latency_ms": {"p50": _percentile(lat_p, 0.5), "p99": _percentile(lat_p, 0.99)}},
         "speedup_vs_plain": wall_p / wall,
-        "max_abs_dE_vs_plain_eh": max(abs(a["Etot"] - b["Etot"]) for a, b in zip(res, res_p)),
+        "max_abs_dE_vs_plain_eh": max((abs(a["Etot"] - b["Etot"]) for a, b in zip(res, res_p)
+                                       if a["status"] == 2 and b["status"] == 2), default=None),
+        "failures": sorted(set(r["error"] for r in res if r["status"] != 2)),
         "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)

@@ -150,6 +150,9 @@ struct hfg_engine {
           hfg_scf_impl(atom.get(), &job->scf, &res, nullptr, st, bl, so);
           atom.reset();
           if (cudaStreamSynchronize(st) != cudaSuccess) err = "stream error after the solve";
+          // an unconverged solve is a failed request, not an energy
+          else if (!res.converged)
+            err = "SCF did not converge in " + std::to_string(res.iterations) + " iterations";
         } catch (const std::exception& e) {
           err = e.what();
           cudaStreamSynchronize(st);

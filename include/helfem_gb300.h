@@ -335,7 +335,9 @@ hfg_status hfg_scf_run(hfg_atom* atom, const hfg_scf_desc* desc, hfg_scf_result*
  * streaming configurations. */
 typedef struct hfg_engine hfg_engine;
 typedef struct {
-  int status;               /* 0 queued, 1 running, 2 done, 3 failed          */
+  int status;               /* 0 queued, 1 running, 2 done (converged),
+                               3 failed: an error, or an SCF that did not
+                               converge (scf then holds its last iterate)  */
   hfg_scf_result scf;
   double queue_ms;          /* submit -> start                                 */
   double setup_ms;          /* host tabulation + upload                        */
