@@ -394,9 +394,20 @@ hfg_status hfg_atom_autotune(hfg_atom* a, int flags, int* best_nsplit, double* b
     };
     double best = 1e300;
     int bestn = 0;
-    for (int ns : {0, 1, 2, 4, 8, 16}) {
-      a->nsplit_fixed = ns;
-      a->build_units();
+    // the tensor-core split form: groups of 8 output blocks per element-pair
+    // unit; otherwise output-block ranges per element pair
+    const bool tcform = (flags & HFG_EXCHANGE_SPLIT) && a->tc_for(false) != nullptr;
+    const std::vector<int> cand = tcform ? std::vector<int>{0, 1, 2, 3, 4, 6, a->tc.ngroups}
+                                         : std::vector<int>{0, 1, 2, 4, 8, 16};
+    for (int ns : cand) {
+      if (tcform) {
+        ck(cudaStreamSynchronize(st), "sync");
+        a->tc_per_fixed = ns;
+        a->tc_units();
+      } else {
+        a->nsplit_fixed = ns;
+        a->build_units();
+      }
       run();
       ck(cudaEventRecord(e0, st), "event");
       for (int r = 0; r < 3; ++r) run();
@@ -411,8 +422,14 @@ hfg_status hfg_atom_autotune(hfg_atom* a, int flags, int* best_nsplit, double* b
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    a->nsplit_fixed = bestn;
-    a->build_units();
+    ck(cudaStreamSynchronize(st), "sync");
+    if (tcform) {
+      a->tc_per_fixed = bestn;
+      a->tc_units();
+    } else {
+      a->nsplit_fixed = bestn;
+      a->build_units();
+    }
     ck(cudaStreamSynchronize(st), "sync");
     if (best_nsplit) *best_nsplit = bestn;
     if (best_ms) *best_ms = best;
@@ -427,6 +444,10 @@ hfg_status hfg_atom_set_partition(hfg_atom* a, int nsplit) {
     ck(cudaStreamSynchronize(a->own_stream), "sync");
     a->nsplit_fixed = nsplit;
     a->build_units();
+    if (a->tc_ok) {
+      a->tc_per_fixed = nsplit;
+      a->tc_units();
+    }
     ck(cudaStreamSynchronize(a->own_stream), "sync");
   });
 }

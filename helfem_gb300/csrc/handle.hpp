@@ -280,6 +280,38 @@ struct hfg_atom {
     u_out = du.upload(u);
     n_out = (int)u.size();
   }
+  // off-diagonal tensor-core units: a unit is a range of groups of one
+  // element pair (the pair's tables and the tensor memory are set up once per
+  // unit); tc_per_fixed groups per unit, or 0: about eight waves of two CTAs
+  // per SM. Any partition gives the same K bit for bit.
+  int tc_per_fixed = 0;
+  void tc_units() {
+    const int nel = host.rad.nel, G = tc.ngroups;
+    auto units_of = [&](bool sym) {
+      const long npairs = sym ? (long)nel * (nel - 1) / 2 : (long)nel * (nel - 1);
+      const long want = 8L * 2 * 152;
+      int per = (int)std::max<long>(1, std::min<long>(G, (npairs * G + want - 1) / want));
+      if (tc_per_fixed > 0) per = std::min(tc_per_fixed, G);
+      std::vector<int4> u;
+      for (int a = 0; a < nel; ++a)
+        for (int b = 0; b < nel; ++b) {
+          if (a == b || (sym && b < a)) continue;
+          for (int g = 0; g < G; g += per) u.push_back(make_int4(a, b, g, std::min(G, g + per)));
+        }
+      return u;
+    };
+    const std::vector<int4> us = units_of(true), ua = units_of(false);
+    tc.units_sym = t_usym.upload(us);
+    tc.n_sym = (int)us.size();
+    tc.units_all = t_uall.upload(ua);
+    tc.n_all = (int)ua.size();
+    if (tc_rs.digits) {
+      tc_rs.units_sym = tc.units_sym;
+      tc_rs.n_sym = tc.n_sym;
+      tc_rs.units_all = tc.units_all;
+      tc_rs.n_all = tc.n_all;
+    }
+  }
   // output blocks in groups of 8 with similar multipole sets, and the units
   void tc_setup() {
     const hfg::AtomHost& H = host;
@@ -302,22 +334,7 @@ struct hfg_atom {
         slot = e;
       }
     }
-    // a unit is a range of groups of one element pair: the pair's tables and
-    // the tensor memory are set up once per unit; ranges are sized so that
-    // the launch has about eight waves of two CTAs per SM
-    auto units_of = [&](bool sym) {
-      const long npairs = sym ? (long)nel * (nel - 1) / 2 : (long)nel * (nel - 1);
-      const long want = 8L * 2 * 152;
-      const int per = (int)std::max<long>(1, std::min<long>(G, (npairs * G + want - 1) / want));
-      std::vector<int4> u;
-      for (int a = 0; a < nel; ++a)
-        for (int b = 0; b < nel; ++b) {
-          if (a == b || (sym && b < a)) continue;
-          for (int g = 0; g < G; g += per) u.push_back(make_int4(a, b, g, std::min(G, g + per)));
-        }
-      return u;
-    };
-    std::vector<int4> us = units_of(true), ua = units_of(false);
+    tc.ngroups = G;
     {
       long nb = 0;  // (group, L) batches with at least one entry
       for (int g = 0; g < G; ++g)
@@ -334,11 +351,7 @@ struct hfg_atom {
     tc_tables(H.rs, H.rb, t_dig, t_exp, tc);
     tc.group_jk = t_gjk.upload(gjk);
     tc.group_ent = t_gent.upload(gent);
-    tc.ngroups = G;
-    tc.units_sym = t_usym.upload(us);
-    tc.n_sym = (int)us.size();
-    tc.units_all = t_uall.upload(ua);
-    tc.n_all = (int)ua.size();
+    tc_units();
     t_err.alloc(sizeof(int));
     ck(cudaMemsetAsync(t_err.p, 0, sizeof(int), own_stream), "memset");
     tc.err = t_err.as<int>();

@@ -152,14 +152,15 @@ hfg_status hfg_exchange(hfg_atom* atom, const double* P, double* K, void* stream
 #define HFG_EXCHANGE_SPLIT 2
 hfg_status hfg_exchange_ex(hfg_atom* atom, const double* P, double* K, int flags, void* stream);
 
-/* Autotuner of the exchange work partition: times the tile kernel (form
- * given by flags) for candidate numbers of output-block ranges per element
- * pair on a synthetic density with every block active, and keeps the
- * fastest for the later calls of this handle. Synchronous; results and
- * layouts of K do not change. */
+/* Autotuner of the exchange work partition: times the tile kernels (form
+ * given by flags) on a synthetic density with every block active for
+ * candidate partitions and keeps the fastest for the later calls of this
+ * handle: output-block ranges per element pair (plain and float-pair
+ * forms), or groups of 8 output blocks per element-pair unit (the
+ * tensor-core split form). Synchronous; K does not change, bit for bit. */
 hfg_status hfg_atom_autotune(hfg_atom* atom, int flags, int* best_nsplit, double* best_ms);
 /* Set the exchange work partition directly (the value hfg_atom_autotune
- * picks): nsplit output-block ranges per element pair, 0 = automatic. */
+ * picks; it sets both partitions): 0 = automatic. */
 hfg_status hfg_atom_set_partition(hfg_atom* atom, int nsplit);
 
 /* Range-separated exchange with the Yukawa kernel e^{-lambda r12}/r12.

@@ -109,14 +109,15 @@ def test_host_entry_points_and_determinism():
 
 
 def test_autotune_keeps_results():
-    """The work-partition autotuner changes which CTA computes what, not the
-    arithmetic of an output tile: K is bitwise unchanged."""
+    """The work-partition autotuner (output-block ranges, or block groups per
+    element-pair unit of the tensor-core form) changes which CTA computes
+    what, not the arithmetic of an output tile: K is bitwise unchanged."""
     torch = torch_cuda()
     A, O = make_pair(36, 2, 2, 6)
     P = random_density(O.nbf, 5, seed=11, S=O.S)
     K1 = A.exchange_host(P, symmetric=True, split=True)
     r = A.autotune(symmetric=True, split=True)
-    assert r["nsplit"] in (0, 1, 2, 4, 8, 16) and r["ms"] > 0
+    assert r["nsplit"] >= 0 and r["ms"] > 0
     K2 = A.exchange_host(P, symmetric=True, split=True)
     assert np.array_equal(K1, K2)
     for ns in (1, 3, 0):
