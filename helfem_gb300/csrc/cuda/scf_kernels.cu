@@ -157,6 +157,26 @@ void k_scatter_add_block(double* M, int nbf, int nrad, const int* ang, int nk, c
 void k_antisym(const double* G, int n, double* E, cudaStream_t st) {
   antisym<<<grid_for((size_t)n * n), 256, 0, st>>>(G, n, E);
 }
+namespace {
+__global__ void diffsum(double* __restrict__ out, const double* a1, const double* b1, const double* a2,
+                        const double* b2, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (a1[i] - b1[i]) + (a2 ? a2[i] - b2[i] : 0.0);
+}
+__global__ void lerp(double* out, const double* a, double lam, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = a[i] + lam * (out[i] - a[i]);
+}
+}  // namespace
+
+void k_diffsum(double* out, const double* a1, const double* b1, const double* a2, const double* b2, size_t n,
+               cudaStream_t st) {
+  diffsum<<<grid_for(n), 256, 0, st>>>(out, a1, b1, a2, b2, n);
+}
+void k_lerp(double* out, const double* a, double lam, size_t n, cudaStream_t st) {
+  lerp<<<grid_for(n), 256, 0, st>>>(out, a, lam, n);
+}
+
 void k_add4(double* out, const double* a, const double* b, const double* c, const double* d, size_t n,
             cudaStream_t st) {
   add4<<<grid_for(n), 256, 0, st>>>(out, a, b, c, d, n);

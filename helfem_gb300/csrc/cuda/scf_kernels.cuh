@@ -15,6 +15,11 @@ void k_antisym(const double* G, int n, double* E, cudaStream_t st);
 void k_add4(double* out, const double* a, const double* b, const double* c, const double* d, size_t n,
             cudaStream_t st);
 void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cudaStream_t st);
+// out = (a1 - b1) + (a2 - b2) (a2, b2 may be null)
+void k_diffsum(double* out, const double* a1, const double* b1, const double* a2, const double* b2, size_t n,
+               cudaStream_t st);
+// out = a + lam (out - a)
+void k_lerp(double* out, const double* a, double lam, size_t n, cudaStream_t st);
 // symmetric n x n test density with every entry nonzero (deterministic)
 void fill_test_density(double* P, int n, cudaStream_t st);
 // A[i,i] += v, A n x n column-major

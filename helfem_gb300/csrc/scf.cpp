@@ -620,6 +620,39 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     // iteration, and the DIIS history restarts
     double emin = 1e300;
     int it_improved = 0;
+    // optimal damping (ODA; E. Cances and C. Le Bris, Int. J. Quantum Chem.
+    // 79, 82 (2000)) for Hartree-Fock runs that still stall under the full
+    // level shift: the next density is the minimum of the energy on the
+    // segment between the damped density P~ and the Aufbau density P of
+    // F(P~). For HF the energy is quadratic on that segment,
+    //   E(lam) = E(P~) + lam s + lam^2 c / 2,
+    //   s = sum_s tr(F~_s dP_s),  c = sum_s tr((dJ + dK_s) dP_s),
+    // and J, K are linear in P, so the damped J and K are mixed like P with no
+    // second build. The level shift is off while ODA runs; the run goes back to
+    // DIIS (fresh history, shift restored) once the gradient has fallen by 100x
+    // or the full step is optimal twice in a row.
+    // HFG_SCF_ODA=0 turns it off; =first starts it at the first iteration
+    const char* oenv = std::getenv("HFG_SCF_ODA");
+    const int oda_mode = !oenv ? 0 : std::strcmp(oenv, "0") == 0 ? -1 : std::strcmp(oenv, "first") == 0 ? 1 : 0;
+    bool oda = false, oda_have = false;
+    double oda_shift = 0.0, oda_e0 = 0.0, oda_lam = 1.0;
+    int oda_full = 0;
+    DBuf dPt, dPst[2], dJt, dKt[2], dFt[2], dD1, dD2;
+    auto oda_alloc = [&]() {
+      if (dPt.p) return;
+      dPt.alloc(sizeof(double) * nb2);
+      dJt.alloc(sizeof(double) * nb2);
+      dD1.alloc(sizeof(double) * nb2);
+      dD2.alloc(sizeof(double) * nb2);
+      for (int s = 0; s < nspin; ++s) {
+        dPst[s].alloc(sizeof(double) * nb2);
+        dFt[s].alloc(sizeof(double) * nb2);
+        if (kfrac != 0.0) dKt[s].alloc(sizeof(double) * nb2);
+      }
+    };
+    auto copy_d = [&](DBuf& to, const DBuf& from) {
+      ck(cudaMemcpyAsync(to.p, from.p, sizeof(double) * nb2, cudaMemcpyDeviceToDevice, st), "copy");
+    };
     double Ekin = 0, Enuc = 0, Ecoul = 0, Exx = 0, Exc = 0, Ngrid = 0, Etot = 0;
     PhaseTimer pt;
     for (it = 1; it <= maxiter; ++it) {
@@ -642,12 +675,53 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
                                restricted ? nullptr : dPs[1].as<double>(), dXC[0].as<double>(),
                                restricted ? nullptr : dXC[1].as<double>(), dE.as<double>(), thr, st),
            "XC");
-      for (int s = 0; s < nspin; ++s) {
+      for (int s = 0; s < nspin; ++s)
         if (kfrac != 0.0 && kfrac != 1.0) {
           cb(cublasDscal(hd.bl, (int)nb2, &kfrac, dK[s].as<double>(), 1), "scal K");
         }
+      if (oda && oda_have) {
+        // line search between P~ (kept with its J, K, F) and the new density
+        double s1 = 0.0, c2 = 0.0;
+        for (int s = 0; s < nspin; ++s) {
+          // restricted: the total density pairs with F, J + K(P/2)
+          if (restricted)
+            hfg::k_diffsum(dD1.as<double>(), dP.as<double>(), dPt.as<double>(), nullptr, nullptr, nb2, st);
+          else
+            hfg::k_diffsum(dD1.as<double>(), dPs[s].as<double>(), dPst[s].as<double>(), nullptr, nullptr, nb2, st);
+          hfg::k_diffsum(dD2.as<double>(), dJ.as<double>(), dJt.as<double>(),
+                         kfrac != 0.0 ? dK[s].as<double>() : nullptr, kfrac != 0.0 ? dKt[s].as<double>() : nullptr,
+                         nb2, st);
+          s1 += dot(dFt[s].as<double>(), dD1.as<double>());
+          c2 += dot(dD2.as<double>(), dD1.as<double>());
+        }
+        double lam = 1.0;
+        if (c2 > 0.0) lam = std::min(1.0, std::max(0.0, -s1 / c2));
+        else if (s1 > 0.0) lam = 0.0;  // uphill and concave: cannot happen for an Aufbau step; keep P~
+        oda_lam = lam;
+        oda_full = lam >= 0.999 ? oda_full + 1 : 0;
+        if (verbose) std::fprintf(stderr, "hfg_scf it %3d ODA s %.3e c %.3e lambda %.4f\n", it, s1, c2, lam);
+        if (lam < 1.0) {
+          hfg::k_lerp(dP.as<double>(), dPt.as<double>(), lam, nb2, st);
+          hfg::k_lerp(dJ.as<double>(), dJt.as<double>(), lam, nb2, st);
+          for (int s = 0; s < nspin; ++s) {
+            hfg::k_lerp(dPs[s].as<double>(), dPst[s].as<double>(), lam, nb2, st);
+            if (kfrac != 0.0) hfg::k_lerp(dK[s].as<double>(), dKt[s].as<double>(), lam, nb2, st);
+          }
+        }
+      }
+      for (int s = 0; s < nspin; ++s)
         hfg::k_add4(dF[s].as<double>(), dH.as<double>(), dJ.as<double>(),
                     kfrac != 0.0 ? dK[s].as<double>() : nullptr, have_xc ? dXC[s].as<double>() : nullptr, nb2, st);
+      if (oda) {
+        // the (damped) state becomes P~ for the next line search
+        copy_d(dPt, dP);
+        copy_d(dJt, dJ);
+        for (int s = 0; s < nspin; ++s) {
+          copy_d(dPst[s], dPs[s]);
+          copy_d(dFt[s], dF[s]);
+          if (kfrac != 0.0) copy_d(dKt[s], dK[s]);
+        }
+        oda_have = true;
       }
       Ekin = dot(dP.as<double>(), T);
       pt.lap(0);  // Fock build (J, K, XC, assembly) + first blocking dot
@@ -719,7 +793,8 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       // (the stable-energy fallback applies only under the default gradient
       // target; a caller-set diis_tol is a hard requirement)
       const bool floor_ok = d->diis_tol <= 0 && n_stable >= 3 && emax < 1e-5;
-      if ((estable && emax < dtol) || floor_ok) {
+      // (a damped step is a fixed point only when it is the full step)
+      if (((estable && emax < dtol) || floor_ok) && (!oda || oda_lam >= 0.999)) {
         converged = true;
         break;
       }
@@ -728,7 +803,18 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         emin = emax;
         it_improved = it;
       }
-      if (emax > 1e-5 && it >= 12 && it - it_improved >= 6 && shift < 2.0) {
+      if (oda) {
+        if (emax < 1e-2 * oda_e0 || oda_full >= 2) {
+          oda = oda_have = false;
+          shift = oda_shift;
+          it_improved = it;
+          emin = emax;
+          nh = 0;
+          wcur = 0;
+          std::fill(Bm.begin(), Bm.end(), 0.0);
+          if (verbose) std::fprintf(stderr, "hfg_scf it %3d ODA done, DIIS restart\n", it);
+        }
+      } else if (emax > 1e-5 && it >= 12 && it - it_improved >= 6 && shift < 2.0) {
         shift = (shift == 0.0) ? 0.5 : 2.0;
         it_improved = it;
         emin = emax;
@@ -736,6 +822,41 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         wcur = 0;
         std::fill(Bm.begin(), Bm.end(), 0.0);
         if (verbose) std::fprintf(stderr, "hfg_scf it %3d level shift %.2f, DIIS restart\n", it, shift);
+      } else if (!have_xc && oda_mode >= 0 && emax > 1e-5 &&
+                 ((shift >= 2.0 && it - it_improved >= 10) || (oda_mode == 1 && it == 1))) {
+        // still stalled under the full shift: optimal damping from the
+        // current (Aufbau) density
+        oda_alloc();
+        oda = true;
+        oda_have = false;
+        oda_full = 0;
+        oda_lam = 1.0;
+        oda_e0 = emax;
+        oda_shift = shift;
+        shift = 0.0;
+        it_improved = it;
+        emin = emax;
+        copy_d(dPt, dP);
+        copy_d(dJt, dJ);
+        for (int s = 0; s < nspin; ++s) {
+          copy_d(dPst[s], dPs[s]);
+          copy_d(dFt[s], dF[s]);
+          if (kfrac != 0.0) copy_d(dKt[s], dK[s]);
+        }
+        oda_have = true;
+        if (verbose) std::fprintf(stderr, "hfg_scf it %3d optimal damping (ODA)\n", it);
+      }
+
+      if (oda) {
+        // Roothaan step from F(P~): the blocks gathered above
+        pt.lap(3);
+        solve_all(dFo.as<double>());
+        occupy();
+        pt.lap(4);
+        build_density();
+        ck(cudaStreamSynchronize(st), "sync");
+        pt.lap(5);
+        continue;
       }
 
       // ---- DIIS extrapolation ----
