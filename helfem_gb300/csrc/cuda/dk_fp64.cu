@@ -31,6 +31,7 @@
 
 #include "devdiatomic.cuh"
 #include "ff.cuh"
+#include "smem_limit.hpp"
 
 namespace hfg {
 namespace {
@@ -873,10 +874,8 @@ cudaError_t launch_diatomic_exchange(const DevDiatomic& D, const DevDiatomicScra
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const size_t smem = sizeof(double) * 10 * n2 + nang2;
-  if (smem > 48 * 1024) {
-    e = cudaFuncSetAttribute(dk_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  e = smem_limit(dk_tiles, smem);
+  if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dk_tiles, th, smem);
   if (e != cudaSuccess) return e;
   const int grid = nsm * std::max(per, 1);
@@ -904,10 +903,8 @@ cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatom
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const size_t smem = sizeof(float2) * 10 * n2 + sizeof(double) * n2 + nang2;
   auto kern = (D.nn == 15) ? dk_tiles_split<15> : dk_tiles_split<0>;
-  if (smem > 48 * 1024) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  e = smem_limit(kern, smem);
+  if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, th, smem);
   if (e != cudaSuccess) return e;
   kern<<<nsm * std::max(per, 1), th, smem, st>>>(D, S, Kd, symmetric ? 1 : 0, inline_diag ? 1 : 0);
@@ -915,10 +912,8 @@ cudaError_t launch_diatomic_exchange_split(const DevDiatomic& D, const DevDiatom
     constexpr int G = DIAG_GROUP;
     const size_t smd = sizeof(float2) * (size_t)G * 4 * n2 + sizeof(double) * n2 + nang2;
     auto dkern = (D.nn == 15) ? dk_diag_split<15, G> : dk_diag_split<0, G>;
-    if (smd > 48 * 1024) {
-      e = cudaFuncSetAttribute(dkern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smd);
-      if (e != cudaSuccess) return e;
-    }
+    e = smem_limit(dkern, smd);
+    if (e != cudaSuccess) return e;
     int dper = 1;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dper, dkern, th, smd);
     if (e != cudaSuccess) return e;

@@ -28,6 +28,7 @@
 
 #include "devatom.cuh"
 #include "ff.cuh"
+#include "smem_limit.hpp"
 
 namespace hfg {
 namespace {
@@ -591,6 +592,8 @@ cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KU
     Mark m(prof, KC_K_TILES, st);
     const size_t smem = sizeof(double) * (2 * n2 + 2 * A.NL * n2) + nang2;
     const int nunits = symmetric ? U.n_sym : U.n_all;
+    const cudaError_t e = smem_limit(k_tiles, smem);
+    if (e != cudaSuccess) return e;
     k_tiles<<<nunits, th, smem, st>>>(A, S, symmetric ? U.sym : U.all, U.diag_jk_src(symmetric), symmetric ? 1 : 0,
                                       P, K);
   }
@@ -630,6 +633,10 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
       nunits = 0;
     }
     auto kern = (A.nn == 15) ? k_tiles_split<15> : k_tiles_split<0>;
+    if (nunits > 0) {
+      const cudaError_t e = smem_limit(kern, smem);
+      if (e != cudaSuccess) return e;
+    }
     if (nunits > 0)
       kern<<<nunits, th, smem, st>>>(A, S, units, U.diag_jk_src(symmetric), symmetric ? 1 : 0, K);
   }

@@ -47,6 +47,7 @@
 #include <cstdint>
 
 #include "devatom.cuh"
+#include "smem_limit.hpp"
 #include "ff.cuh"
 #include "tc.cuh"
 
@@ -827,12 +828,8 @@ cudaError_t launch_k_tiles_tc(const DevAtom& A, const DevScratch& S, const DevTC
   const int n = symmetric ? T.n_sym : T.n_all;
   if (n == 0) return cudaSuccess;
   const size_t smem = tc_smem_bytes(A.NL, A.nang);
-  static thread_local size_t configured = 0;  // per-thread: the attribute is per device function
-  if (smem > configured) {
-    const cudaError_t e = cudaFuncSetAttribute(k_tiles_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = smem;
-  }
+  const cudaError_t e = smem_limit(k_tiles_tc, smem);
+  if (e != cudaSuccess) return e;
   k_tiles_tc<<<n, 256, smem, st>>>(A, S, T, symmetric ? T.units_sym : T.units_all, symmetric ? 1 : 0, K);
   return cudaGetLastError();
 }
@@ -851,12 +848,8 @@ cudaError_t launch_k_diag_tc(const DevAtom& A, const DevScratch& S, const DevTC&
   const int n = symmetric ? T.n_dsym : T.n_dall;
   if (n == 0) return cudaSuccess;
   const size_t smem = tc_diag_smem_bytes(A.NL, T.dksteps, A.nang);
-  static thread_local size_t configured = 0;
-  if (smem > configured) {
-    const cudaError_t e = cudaFuncSetAttribute(k_diag_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = smem;
-  }
+  const cudaError_t e = smem_limit(k_diag_tc, smem);
+  if (e != cudaSuccess) return e;
   k_diag_tc<<<n, 256, smem, st>>>(A, S, T, symmetric ? 1 : 0, K);
   return cudaGetLastError();
 }

@@ -30,6 +30,7 @@
 
 #include <algorithm>
 
+#include "smem_limit.hpp"
 #include "tab.cuh"
 
 namespace hfg {
@@ -280,8 +281,8 @@ cudaError_t launch_tab_finish(const TabInput& in, const double* Lsc, const int* 
   const int grid = (int)std::min<size_t>((total + 255) / 256, 152 * 16);
   tab_pack<<<grid, 256, 0, st>>>(in.nn, nblk, rmax, Lsc, rank, cholp);
   const size_t smem = sizeof(double) * 2 * in.nn * rmax;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(tab_tk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  {
+    const cudaError_t e = smem_limit(tab_tk, smem);
     if (e != cudaSuccess) return e;
   }
   tab_tk<<<dim3(n2, in.nel, in.NL), n2 <= 128 ? 128 : 320, smem, st>>>(in, rmax, Lsc, rank, tk);

@@ -13,6 +13,7 @@
 
 #include <cstdint>
 
+#include "smem_limit.hpp"
 #include "tc.cuh"
 
 namespace hfg {
@@ -133,9 +134,7 @@ cudaError_t tc_selftest(const float* A, const float* B, float* D, int N, int kst
   cudaMemcpy(dB, B, sizeof(float) * N * K, cudaMemcpyHostToDevice);
   cudaMemset(dD, 0, sizeof(float) * kM * N);
   cudaMemset(dErr, 0, sizeof(int));
-  if ((e = cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-      cudaSuccess)
-    return fail(e);
+  if ((e = smem_limit(tc_selftest_kernel, smem)) != cudaSuccess) return fail(e);
   tc_selftest_kernel<<<1, 128, smem>>>(dA, dB, dD, N, ksteps, a_mn, b_mn, swap, dErr);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
   if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);

@@ -53,6 +53,36 @@ def test_engine_mix_equals_alone_and_reference():
             assert abs(res[(name, rep)]["Etot"] - alone["Etot"]) < 1e-10
 
 
+def test_engine_mixed_shapes_split_exchange():
+    """Concurrent split-exchange solves of atoms whose tensor-core kernels
+    need different amounts of shared memory (1 to 7 multipoles, 10 and 15
+    nodes): every solve succeeds and matches the same solve run alone.
+    The kernels' shared-memory limits are shared by the worker threads; a
+    limit lowered by one thread under another's larger launch made that
+    launch fail with an invalid-argument error."""
+    torch_cuda()
+    shapes = [(2, 0), (10, 1), (10, 2), (10, 3)]
+    jobs = [dict(Z=Z, lmax=lm, nn=nn) for Z, lm in shapes for nn in (10, 15)]
+    eng = hg.Engine(n_workers=8, hbm_budget_gb=40.0)
+    ids = []
+    for rep in range(2):
+        for j in jobs:
+            lv, mv = wl.angular(j["lmax"], j["lmax"])
+            ids.append((j, eng.submit(j["Z"], wl.grid(40.0, 6), lv, mv, j["Z"] // 2, j["Z"] // 2, "hf", True,
+                                      nnodes=j["nn"], split=True)))
+    res = [(j, eng.wait(i)) for j, i in ids]
+    eng.close()
+    bad = [(j, r["error"]) for j, r in res if r["status"] != 2]
+    assert not bad, bad
+    for j in jobs[::3]:
+        lv, mv = wl.angular(j["lmax"], j["lmax"])
+        a = hg.Atom(j["Z"], wl.grid(40.0, 6), lv, mv, nnodes=j["nn"])
+        alone = a.scf(j["Z"] // 2, j["Z"] // 2, "hf", restricted=True, split=True)
+        for jj, r in res:
+            if jj is j:
+                assert abs(r["Etot"] - alone["Etot"]) < 1e-10, (j, r["Etot"], alone["Etot"])
+
+
 def test_engine_admission_and_failure():
     torch_cuda()
     # budget fits about one small job at a time: jobs queue, all complete
