@@ -91,7 +91,6 @@ struct DevTC {
   const int4* units_all = nullptr;        // (a, b, first group, end group), a != b
   int n_all = 0;
   int* err = nullptr;                     // set when a completion wait ran out
-  unsigned* tmax = nullptr;               // [nang^2][nel][nel] largest |P| per element tile (float bits)
   // diagonal element tiles: the exchange-ordered tensor as digit planes
   // [L][e][row tile][K step][digit][128 x 16], per-row exponents, groups of
   // up to 16 output blocks (j <= k in symmetric mode), units (a, group, row tile)

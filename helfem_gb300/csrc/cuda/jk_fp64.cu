@@ -195,56 +195,6 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   if (threadIdx.x == 0) part[blk * NORM_SPLIT + blockIdx.y] = s;
 }
 
-// The split pass of the tensor-core form: as k_block_norms (float-pair copy,
-// FP32 norm partials of the high words) plus the largest |P| of every element
-// tile (a, b) of every angular block, tmax[(blk * nel + a) * nel + b] as float
-// bits (zero-initialised by the caller). One thread per row (up to two rows),
-// columns of the band in order: a row's running maximum is flushed whenever
-// the column's element changes; a shared boundary row or column counts for
-// both of its elements.
-__global__ void k_norms_tmax(DevAtom A, const double* __restrict__ P, double* __restrict__ part,
-                             float2* __restrict__ p2, unsigned* __restrict__ tmax) {
-  __shared__ double red[32];
-  const int blk = blockIdx.x, i = blk % A.nang, l = blk / A.nang;
-  const int c0 = (int)((long)A.nrad * blockIdx.y / NORM_SPLIT);
-  const int c1 = (int)((long)A.nrad * (blockIdx.y + 1) / NORM_SPLIT);
-  const int w = A.nn - 1;
-  float sf = 0.f;
-  for (int r = threadIdx.x; r < A.nrad; r += blockDim.x) {
-    const int ea = min((r + 1) / w, A.nel - 1);
-    const bool rshared = (r + 1) % w == 0 && ea > 0;  // also the last row of element ea - 1
-    unsigned* trow = tmax + ((size_t)blk * A.nel + ea) * A.nel;
-    unsigned* trow2 = rshared ? tmax + ((size_t)blk * A.nel + ea - 1) * A.nel : nullptr;
-    auto flush = [&](int eb, float m) {
-      if (eb < 0 || m == 0.f) return;
-      atomicMax(trow + eb, __float_as_uint(m));
-      if (trow2) atomicMax(trow2 + eb, __float_as_uint(m));
-    };
-    int ceb = -1;
-    float cm = 0.f;
-    const size_t base = (size_t)i * A.nrad + r;
-    for (int c = c0; c < c1; ++c) {
-      const size_t o = (size_t)(l * A.nrad + c) * A.nbf + base;
-      const float2 h = split_bits(P[o]);
-      p2[o] = h;
-      sf = fmaf(h.x, h.x, sf);
-      const float av = fabsf(h.x);
-      const int eb = min((c + 1) / w, A.nel - 1);
-      if (eb != ceb) {
-        flush(ceb, cm);
-        ceb = eb;
-        cm = 0.f;
-      }
-      cm = fmaxf(cm, av);
-      // a boundary column is also the last column of element eb - 1
-      if ((c + 1) % w == 0 && eb > 0) flush(eb - 1, av);
-    }
-    flush(ceb, cm);
-  }
-  double s = block_sum((double)sf, red);
-  if (threadIdx.x == 0) part[blk * NORM_SPLIT + blockIdx.y] = s;
-}
-
 // density-block screen (10*DBL_EPSILON, the reference's threshold) and the
 // exchange entries that see an active block, once per build
 __global__ void k_flags(DevAtom A, DevScratch S) {
@@ -609,14 +559,7 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
-    if (tc) {
-      cudaError_t e = cudaMemsetAsync(tc->tmax, 0, sizeof(unsigned) * (size_t)nang2 * A.nel * A.nel, st);
-      if (e != cudaSuccess) return e;
-      const int th2 = std::min(1024, ((A.nrad + 31) / 32) * 32);
-      k_norms_tmax<<<dim3(nang2, NORM_SPLIT), th2, 0, st>>>(A, P, S.bnorm, S.p2, tc->tmax);
-    } else {
-      k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2);
-    }
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2);
     k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S);
   }
   {

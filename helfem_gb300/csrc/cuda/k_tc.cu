@@ -58,7 +58,6 @@ constexpr int ND = TC_NDIGITS;  // digits per table / intermediate operand
 constexpr int NDX = 6;          // digits of a float-pair density tile (48 bits)
 constexpr int APLANE = 4096;    // bytes of one 128 x 16 bf16 operand plane
 constexpr int TPLANE = 512;     // bytes of one 16 x 16 bf16 table plane
-constexpr int kAccMax = 5;      // multipole batches summed in tensor memory before a readback
 
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: x + M - M rounds |x| < 2^22 to an integer
 
@@ -215,17 +214,23 @@ __device__ __forceinline__ void recouple(const DevAtom& A, const unsigned char* 
   }
 }
 
-// digits of the recoupled tile against |X| < 2^E, written as rows (slot, q),
-// K = p of the first product's operand
-__device__ __forceinline__ void digitise(ffv (&x)[8], unsigned char* A1, int row, int k0, int E) {
+// digits of the recoupled tile written as rows (slot, q), K = p of the first
+// product's operand; returns the tile exponent (warp-wide maximum)
+__device__ __forceinline__ int digitise(ffv (&x)[8], unsigned char* A1, int row, int k0) {
+  unsigned eb = 0;
 #pragma unroll
-  for (int j = 0; j < 8; ++j) x[j] = ff_norm(x[j].hi, x[j].lo);
+  for (int j = 0; j < 8; ++j) {
+    x[j] = ff_norm(x[j].hi, x[j].lo);
+    eb = max(eb, (__float_as_uint(x[j].hi) >> 23) & 0xFFu);
+  }
+  const int E = tile_exponent(__reduce_max_sync(0xffffffffu, eb));
   uint32_t pk[NDX][4];
   digits_of(x, E, pk);
   const uint32_t off = tc::off_kmajor(row, k0);
 #pragma unroll
   for (int k = 0; k < NDX; ++k)
     *reinterpret_cast<uint4*>(A1 + k * APLANE + off) = make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
+  return E;
 }
 
 // the 8 values y[j] of tile (a,b), block jk, at row p and columns q0 + j:
@@ -259,7 +264,7 @@ struct Smem {
   unsigned char* T2;  // NL * ND planes of the right tables of element b
   int* alpha;         // [NL][16] row exponents of the left tables
   int* beta;          // [NL][16] row exponents of the right tables
-  int* es;            // [8] density-tile exponent of each slot for the group, then [8] slot used
+  int* ex;            // [2][8] tile exponents, by batch parity
   int* sact;          // [NL][8] slot active in the batch of multipole L
   int* gent;          // [8][NL] entry of (slot, L) or -1
   int* gjk;           // [8] output block of the slot or -1
@@ -293,7 +298,7 @@ __global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, De
     ip += NL * 16;
     sm.beta = ip;
     ip += NL * 16;
-    sm.es = ip;
+    sm.ex = ip;
     ip += 16;
     sm.sact = ip;
     ip += 8 * NL;
@@ -383,32 +388,6 @@ __global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, De
     }
     if (t < 8) sm.gjk[t] = T.group_jk[g * 8 + t];
     __syncthreads();
-    // one density scale per slot for every multipole of the group (so that the
-    // second product can sum the multipoles in tensor memory): a bound of
-    // |X| from the largest |P| of the element tiles the entries read,
-    // sum_t |c_t| max|P_t(a,b)|, with a margin for the float-pair rounding
-    {
-      float bound = 0.f;
-      int used = 0;
-      if (lane < NL && sm.sact[lane * 8 + warp]) {
-        const int e = sm.gent[warp * NL + lane];
-        used = 1;
-        for (int uu = A.kent_ptr[e]; uu < A.kent_ptr[e + 1]; ++uu) {
-          const int blk = A.kterm_blk[uu];
-          if (!sm.act[blk]) continue;
-          const float pm = __uint_as_float(T.tmax[((size_t)blk * A.nel + a) * A.nel + b]);
-          bound = __fmaf_rn(fabsf(A.kterm_coef2[uu].x), pm, bound);
-        }
-      }
-      bound = __fmul_rn(bound, 1.0f + 1.0f / 1048576.0f);
-      const unsigned eb = __reduce_max_sync(0xffffffffu, (__float_as_uint(bound) >> 23) & 0xFFu);
-      used = __reduce_or_sync(0xffffffffu, used);
-      if (lane == 0) {
-        sm.es[warp] = tile_exponent(eb);
-        sm.es[8 + warp] = used;
-      }
-    }
-    __syncthreads();
 
     ffv acc[8];
 #pragma unroll
@@ -416,11 +395,12 @@ __global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, De
 
     // prologue: the first active batch's density tiles
     int L = next_active(0);
-    int nacc = 0;  // multipole batches summed in the second product's columns
+    int par = 0;
     if (L >= 0 && sm.sact[L * 8 + warp]) {
       ffv x[8];
       recouple(A, sm.act, sm.gent[warp * NL + L], pbase, vp, x);
-      digitise(x, sm.A1, warp * 16 + rq, 8 * rph, sm.es[warp]);
+      const int E = digitise(x, sm.A1, warp * 16 + rq, 8 * rph);
+      if (lane == 0) sm.ex[par * 8 + warp] = E;
     }
 
     while (L >= 0) {
@@ -447,36 +427,28 @@ __global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, De
       tc::fence_after_sync();
 
       // ---- levels -> balanced digits of Y = A X, the second product's
-      // MN-major operand: rows (slot, i), K = q (lane = (slot, q)); a slot
-      // without an entry of this multipole gets zero rows, because the
-      // second product sums the multipoles in place ----
-      {
-        const uint32_t off = tc::off_mnmajor(oslot * 16 + 8 * half, oi);
-        const bool mine = sm.sact[L * 8 + oslot] != 0;
-        if (mine | (sm.sact[L * 8 + pslot] != 0)) {
-          float v[ND][8];
-          tmem_ld_levels(tD1 + lane_off + 8 * half, v);
-          uint32_t pk[ND][4];
+      // MN-major operand: rows (slot, i), K = q (lane = (slot, q)) ----
+      if (sm.sact[L * 8 + oslot] | sm.sact[L * 8 + pslot]) {
+        float v[ND][8];
+        tmem_ld_levels(tD1 + lane_off + 8 * half, v);
+        uint32_t pk[ND][4];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            float lv[ND], y[ND];
+        for (int j = 0; j < 8; ++j) {
+          float lv[ND], y[ND];
 #pragma unroll
-            for (int d = 0; d < ND; ++d) lv[d] = v[d][j];
-            carry(lv, y);
+          for (int d = 0; d < ND; ++d) lv[d] = v[d][j];
+          carry(lv, y);
 #pragma unroll
-            for (int k = 0; k < ND; ++k) v[k][j] = mine ? y[k] : 0.f;
-          }
-#pragma unroll
-          for (int k = 0; k < ND; ++k)
-#pragma unroll
-            for (int jj = 0; jj < 4; ++jj) pk[k][jj] = pack_bf16(v[k][2 * jj], v[k][2 * jj + 1]);
-#pragma unroll
-          for (int k = 0; k < ND; ++k)
-            *reinterpret_cast<uint4*>(sm.A2 + k * APLANE + off) = make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
-        } else {
-#pragma unroll
-          for (int k = 0; k < ND; ++k) *reinterpret_cast<uint4*>(sm.A2 + k * APLANE + off) = make_uint4(0, 0, 0, 0);
+          for (int k = 0; k < ND; ++k) v[k][j] = y[k];
         }
+#pragma unroll
+        for (int k = 0; k < ND; ++k)
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) pk[k][jj] = pack_bf16(v[k][2 * jj], v[k][2 * jj + 1]);
+        const uint32_t off = tc::off_mnmajor(oslot * 16 + 8 * half, oi);
+#pragma unroll
+        for (int k = 0; k < ND; ++k)
+          *reinterpret_cast<uint4*>(sm.A2 + k * APLANE + off) = make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
       }
       tc::fence_async_smem();
       tc::fence_before_sync();
@@ -490,40 +462,36 @@ __global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, De
 #pragma unroll 1
         for (int ky = 0; ky < ND; ++ky)
           tc::mma_bf16(tD2 + 16 * ky, dA2 + (uint64_t)(ky * APLANE >> 4), dT2 + (uint64_t)(L * ND * TPLANE >> 4),
-                       tc::idesc_bf16(128, 16 * (ND - ky), 1, 0), (ky > 0 || nacc > 0) ? 1u : 0u);
+                       tc::idesc_bf16(128, 16 * (ND - ky), 1, 0), ky > 0 ? 1u : 0u);
         tc::mma_commit(sm.mbar);
       }
       // the next batch's digits go to the first operand (its MMAs are done)
-      if (nact) digitise(xn, sm.A1, warp * 16 + rq, 8 * rph, sm.es[warp]);
+      if (nact) {
+        const int E = digitise(xn, sm.A1, warp * 16 + rq, 8 * rph);
+        if (lane == 0) sm.ex[(par ^ 1) * 8 + warp] = E;
+      }
       if (!__all_sync(0xffffffffu, tc::mbar_wait(sm.mbar, phase)) && lane == 0) atomicExch(sm.fail, 1);
       phase ^= 1u;
       tc::fence_after_sync();
 
-      // ---- the multipoles summed so far: levels -> float pairs, scaled,
-      // accumulated; after the group's last batch, or after kAccMax batches
-      // (the level sums stay below 2^24, exact in FP32) ----
-      if (Ln < 0 || nacc + 1 >= kAccMax) {
-        const bool mine = sm.es[8 + oslot] != 0;
-        if (mine | (sm.es[8 + pslot] != 0)) {
-          float v[ND][8];
-          tmem_ld_levels(tD2 + lane_off + 8 * half, v);
-          if (mine) {
-            const int ea = sm.alpha[oi] + sm.es[oslot];  // row exponents are the same for every L
+      // ---- levels -> float pairs, scaled, accumulated over the multipoles ----
+      if (sm.sact[L * 8 + oslot] | sm.sact[L * 8 + pslot]) {
+        float v[ND][8];
+        tmem_ld_levels(tD2 + lane_off + 8 * half, v);
+        if (sm.sact[L * 8 + oslot]) {
+          const int ea = sm.alpha[L * 16 + oi] + sm.ex[par * 8 + oslot];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              float lv[ND];
+          for (int j = 0; j < 8; ++j) {
+            float lv[ND];
 #pragma unroll
-              for (int d = 0; d < ND; ++d) lv[d] = v[d][j];
-              acc[j] = ff_add(acc[j], levels_to_pair(lv, exp2i(ea + sm.beta[8 * half + j])));
-            }
+            for (int d = 0; d < ND; ++d) lv[d] = v[d][j];
+            acc[j] = ff_add(acc[j], levels_to_pair(lv, exp2i(ea + sm.beta[L * 16 + 8 * half + j])));
           }
         }
-        nacc = 0;
-      } else {
-        ++nacc;
       }
       tc::fence_before_sync();
       L = Ln;
+      par ^= 1;
     }
     __syncthreads();
 

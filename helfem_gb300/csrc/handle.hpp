@@ -163,7 +163,7 @@ struct hfg_atom {
   // tensor-core split exchange: digit tables of the bare and of the
   // Yukawa-screened radial tables, shared groups and units, error flag
   DBuf t_dig, t_exp, ty_dig, ty_exp, t_gjk, t_gent, t_usym, t_uall, t_err;
-  DBuf t_tkd, t_tke, ty_tkd, ty_tke, t_dgjk_s, t_dgent_s, t_dgjk_a, t_dgent_a, t_dus, t_dua, t_tmax;
+  DBuf t_tkd, t_tke, ty_tkd, ty_tke, t_dgjk_s, t_dgent_s, t_dgjk_a, t_dgent_a, t_dus, t_dua;
   hfg::DevTC tc{}, tc_rs{};
   bool tc_ok = false;
   // bf16 MMA FLOPs one tensor-core exchange issues with every entry active
@@ -198,23 +198,10 @@ struct hfg_atom {
           const size_t blk = ((size_t)kind * NL + L) * nel + e;
           uint16_t* planes = d.data() + blk * ND * (TC_TPLANE / 2);
           for (int n = 0; n < nn; ++n) {
-            // one exponent per row for every multipole (the largest), so that
-            // products of different multipoles share a scale and can be
-            // summed on the tensor core: row sum of |values| <= 2^a for all L
-            int a = -1074;
-            bool any = false;
-            for (int L2 = 0; L2 < NL; ++L2) {
-              const double* M2 = (kind == 0 ? rs : rb).data() + ((size_t)L2 * nel + e) * n2;
-              double rowsum = 0.0;
-              for (int k = 0; k < nn; ++k) rowsum += std::fabs(M2[n + (size_t)k * nn]);
-              if (rowsum > 0.0) {
-                int e2 = 0;
-                std::frexp(rowsum, &e2);
-                a = any ? std::max(a, e2) : e2;
-                any = true;
-              }
-            }
-            if (!any) a = 0;
+            double rowsum = 0.0;
+            for (int k = 0; k < nn; ++k) rowsum += std::fabs(M[n + (size_t)k * nn]);
+            int a = 0;
+            if (rowsum > 0.0) std::frexp(rowsum, &a);  // rowsum <= 2^a
             ex[blk * 16 + n] = a;
             for (int k = 0; k < nn; ++k) {
               double r = std::ldexp(M[n + (size_t)k * nn], -a);
@@ -329,7 +316,7 @@ struct hfg_atom {
   void tc_setup() {
     const hfg::AtomHost& H = host;
     const int nel = H.rad.nel, NL = H.NL, nang2 = H.nang * H.nang;
-    if (H.rad.nn > 16 || NL > 8 || nel < 2 || H.rad.nrad > 2048) return;
+    if (H.rad.nn > 16 || NL > 8 || nel < 2) return;
     std::vector<int> sig(nang2, 0), order(nang2);
     for (int jk = 0; jk < nang2; ++jk) {
       order[jk] = jk;
@@ -368,8 +355,6 @@ struct hfg_atom {
     t_err.alloc(sizeof(int));
     ck(cudaMemsetAsync(t_err.p, 0, sizeof(int), own_stream), "memset");
     tc.err = t_err.as<int>();
-    t_tmax.alloc(sizeof(unsigned) * (size_t)nang2 * nel * nel);
-    tc.tmax = t_tmax.as<unsigned>();
     tc_tk_tables(dev.tk, t_tkd, t_tke, tc);
     tc_diag_groups(true, t_dgjk_s, t_dgent_s, t_dus, tc.dgroup_jk_sym, tc.dgroup_ent_sym, tc.dunits_sym, tc.n_dsym,
                    tc.dmtiles);

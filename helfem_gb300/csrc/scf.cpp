@@ -822,10 +822,10 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         wcur = 0;
         std::fill(Bm.begin(), Bm.end(), 0.0);
         if (verbose) std::fprintf(stderr, "hfg_scf it %3d level shift %.2f, DIIS restart\n", it, shift);
-      } else if (!have_xc && oda_mode >= 0 && emax > 1e-5 &&
+      } else if (!have_xc && oda_mode >= 0 && emax > 10.0 * dtol &&
                  ((shift >= 2.0 && it - it_improved >= 10) || (oda_mode == 1 && it == 1))) {
-        // still stalled under the full shift: optimal damping from the
-        // current (Aufbau) density
+        // still stalled under the full shift (the gradient has not halved in
+        // ten iterations): optimal damping from the current (Aufbau) density
         oda_alloc();
         oda = true;
         oda_have = false;
