@@ -175,10 +175,11 @@ cudaError_t launch_xc_fp64(const DevAtom& A, const DevXC& X, const XcScratch& S,
 // device (coulomb_noalloc.cu). cudaErrorInvalidValue if doubles_needed
 // exceeds the capacity.
 cudaError_t noalloc_coulomb_scratch(size_t doubles_needed, double** out);
-// tensor-core exchange tiles (k_tc.cu): every element pair, the diagonal
-// elements through the exchange-ordered tensor, in one launch
-cudaError_t launch_exchange_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
-                               cudaStream_t st);
+// tensor-core exchange tiles (k_tc.cu): off-diagonal element pairs only
+cudaError_t launch_k_tiles_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
+                              cudaStream_t st);
+cudaError_t launch_k_diag_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
+                             cudaStream_t st);
 cudaError_t launch_tk_digits(const DevAtom& A, int mtiles, int ksteps, unsigned char* out, int* rowexp,
                              cudaStream_t st);
 // tensor-core probe (tc_probe.cu)

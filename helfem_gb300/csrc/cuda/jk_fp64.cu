@@ -173,7 +173,8 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   double s = 0.0;
   float sf = 0.f;
   // the band's elements in column order (32-bit index arithmetic); four
-  // loads in flight per thread, summed in the same order as one at a time
+  // loads in flight per thread (one at a time left the pass latency-bound
+  // at half the HBM rate), summed in the same order as one at a time
   const int n = A.nrad * (c1 - c0), bd = blockDim.x;
   for (int base = threadIdx.x; base < n; base += 4 * bd) {
     double v[4];
@@ -472,44 +473,31 @@ __global__ void __launch_bounds__(320) k_tiles_split(DevAtom A, DevScratch S, co
 // each tile receives its neighbours' halo entries in a fixed order
 __global__ void k_fixup(DevAtom A, DevScratch S, double* __restrict__ K) {
   const int a = blockIdx.x % A.nel, b = blockIdx.x / A.nel;
-  const int nn = A.nn, per = 2 * nn - 3, nang2 = A.nang * A.nang, nw = per * nang2, bd = blockDim.x;
-  // four entries per thread with their loads in flight together
-  for (int base = threadIdx.x; base < nw; base += 4 * bd) {
-    double v[4], kv[4];
-    long long o[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int w = base + u * bd;
-      o[u] = -1;
-      v[u] = 0.0;
-      if (w >= nw) continue;
-      const int idx = w % per, jk = w / per;
-      const int j = jk % A.nang, k = jk / A.nang;
-      int p, q;
-      if (idx < nn - 1) {  // first row of tile (a,b), q in [0, nn-2]
-        if (a == 0 || (idx == 0 && b == 0)) continue;
-        p = 0;
-        q = idx;
-        v[u] = S.khalo[halo_idx(A, a - 1, b, jk, q)];
-        if (q == 0) {
-          v[u] += S.khalo[halo_idx(A, a, b - 1, jk, nn + 0)];
-          v[u] += S.khalo[halo_idx(A, a - 1, b - 1, jk, nn - 1)];
-        }
-      } else {  // first column, p in [1, nn-2]
+  const int nn = A.nn, per = 2 * nn - 3, nang2 = A.nang * A.nang;
+  for (int w = threadIdx.x; w < per * nang2; w += blockDim.x) {
+    const int idx = w % per, jk = w / per;
+    const int j = jk % A.nang, k = jk / A.nang;
+    int p, q;
+    double v;
+    if (idx < nn - 1) {  // first row of tile (a,b), q in [0, nn-2]
+      if (a == 0) continue;
+      p = 0;
+      q = idx;
+      v = S.khalo[halo_idx(A, a - 1, b, jk, q)];
+      if (q == 0) {
         if (b == 0) continue;
-        p = idx - (nn - 1) + 1;
-        q = 0;
-        v[u] = S.khalo[halo_idx(A, a, b - 1, jk, nn + p)];
+        v += S.khalo[halo_idx(A, a, b - 1, jk, nn + 0)];
+        v += S.khalo[halo_idx(A, a - 1, b - 1, jk, nn - 1)];
       }
-      const int gp = gfun(A, a, p), gq = gfun(A, b, q);
-      if (!gvalid(A, gp) || !gvalid(A, gq)) continue;
-      o[u] = (long long)(k * A.nrad + gq) * A.nbf + (long long)j * A.nrad + gp;
+    } else {  // first column, p in [1, nn-2]
+      if (b == 0) continue;
+      p = idx - (nn - 1) + 1;
+      q = 0;
+      v = S.khalo[halo_idx(A, a, b - 1, jk, nn + p)];
     }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) kv[u] = o[u] >= 0 ? K[o[u]] : 0.0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (o[u] >= 0) K[o[u]] = kv[u] + v[u];
+    const int gp = gfun(A, a, p), gq = gfun(A, b, q);
+    if (!gvalid(A, gp) || !gvalid(A, gq)) continue;
+    K[(size_t)(k * A.nrad + gq) * A.nbf + (size_t)j * A.nrad + gp] += v;
   }
 }
 
@@ -590,9 +578,10 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
     int nunits = symmetric ? U.n_sym : U.n_all;
     const int4* units = symmetric ? U.sym : U.all;
     if (tc) {
-      // every element pair on the tensor cores, in one launch: the diagonal
-      // elements through the exchange-ordered tensor, the off-diagonal tiles
-      const cudaError_t e = launch_exchange_tc(A, S, *tc, symmetric, K, st);
+      // every element pair on the tensor cores: the off-diagonal tiles, then
+      // the diagonal ones through the exchange-ordered tensor
+      cudaError_t e = launch_k_tiles_tc(A, S, *tc, symmetric, K, st);
+      if (e == cudaSuccess) e = launch_k_diag_tc(A, S, *tc, symmetric, K, st);
       if (e != cudaSuccess) return e;
       nunits = 0;
     }

@@ -43,7 +43,6 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
-#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 
@@ -277,9 +276,9 @@ struct Smem {
 
 }  // namespace
 
-// one off-diagonal work unit u = (a, b, first group, end group)
-__device__ __forceinline__ void tiles_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, const int4 u,
-                                         int symmetric, double* __restrict__ K) {
+__global__ void __launch_bounds__(256, 2) k_tiles_tc(DevAtom A, DevScratch S, DevTC T, const int4* __restrict__ units,
+                                                     int symmetric, double* __restrict__ K) {
+  const int4 u = units[blockIdx.x];
   const int a = u.x, b = u.y;
   const int nn = A.nn, NL = A.NL, nang2 = A.nang * A.nang;
   extern __shared__ __align__(1024) unsigned char smraw[];
@@ -574,9 +573,9 @@ __global__ void tc_tk_digits_kernel(const double* __restrict__ tk, int NL, int n
   }
 }
 
-// one diagonal work unit u = (a, group, row tile)
-__device__ __forceinline__ void diag_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, const int4 u,
-                                        int symmetric, double* __restrict__ K) {
+__global__ void __launch_bounds__(256, 2) k_diag_tc(DevAtom A, DevScratch S, DevTC T, int symmetric,
+                                                    double* __restrict__ K) {
+  const int4 u = (symmetric ? T.dunits_sym : T.dunits_all)[blockIdx.x];
   const int a = u.x, g = u.y, mt = u.z;
   const int nn = A.nn, n2 = nn * nn, NL = A.NL, nang2 = A.nang * A.nang;
   const int ksteps = T.dksteps, mtiles = T.dmtiles;
@@ -782,22 +781,6 @@ __device__ __forceinline__ void diag_tc(const DevAtom& A, const DevScratch& S, c
   if (warp == 0) tc::tmem_dealloc(tD, 128);
 }
 
-// Both kinds of unit in one launch, the diagonal ones first: a diagonal
-// unit is a long chain of dependent steps (table copies, multipoles) with
-// few instructions, an off-diagonal unit is issue-bound, and sharing the SMs
-// lets the second fill the issue slots the first leaves idle (as two
-// launches, the 0.8 wave of diagonal units left a fifth of the CTA slots
-// empty).
-__global__ void __launch_bounds__(256, 2) k_exchange_tc(DevAtom A, DevScratch S, DevTC T,
-                                                        const int4* __restrict__ units,
-                                                        const int4* __restrict__ dunits, int n_diag, int symmetric,
-                                                        double* __restrict__ K) {
-  if ((int)blockIdx.x < n_diag)
-    diag_tc(A, S, T, dunits[blockIdx.x], symmetric, K);
-  else
-    tiles_tc(A, S, T, units[blockIdx.x - n_diag], symmetric, K);
-}
-
 size_t tc_smem_bytes(int NL, int nang) {
   return (size_t)(NDX + ND) * APLANE + (size_t)2 * NL * ND * TPLANE +
          sizeof(int) * (2 * NL * 16 + 16 + 8 * NL + 8 * NL + 8 + 2) + 16 + (size_t)nang * nang + 64;
@@ -808,16 +791,14 @@ size_t tc_diag_smem_bytes(int NL, int ksteps, int nang) {
          sizeof(int) * (128 + DSLOT + NL * DSLOT * 2 + DSLOT + 2) + 5 * 8 + 8 + (size_t)nang * nang + 64;
 }
 
-cudaError_t launch_exchange_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
-                               cudaStream_t st) {
-  const int n_off = symmetric ? T.n_sym : T.n_all, n_diag = symmetric ? T.n_dsym : T.n_dall;
-  if (n_off + n_diag == 0) return cudaSuccess;
-  const size_t smem = std::max(tc_smem_bytes(A.NL, A.nang), tc_diag_smem_bytes(A.NL, T.dksteps, A.nang));
-  const cudaError_t e = smem_limit(k_exchange_tc, smem);
+cudaError_t launch_k_tiles_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
+                              cudaStream_t st) {
+  const int n = symmetric ? T.n_sym : T.n_all;
+  if (n == 0) return cudaSuccess;
+  const size_t smem = tc_smem_bytes(A.NL, A.nang);
+  const cudaError_t e = smem_limit(k_tiles_tc, smem);
   if (e != cudaSuccess) return e;
-  k_exchange_tc<<<n_off + n_diag, 256, smem, st>>>(A, S, T, symmetric ? T.units_sym : T.units_all,
-                                                    symmetric ? T.dunits_sym : T.dunits_all, n_diag,
-                                                    symmetric ? 1 : 0, K);
+  k_tiles_tc<<<n, 256, smem, st>>>(A, S, T, symmetric ? T.units_sym : T.units_all, symmetric ? 1 : 0, K);
   return cudaGetLastError();
 }
 
@@ -830,5 +811,15 @@ cudaError_t launch_tk_digits(const DevAtom& A, int mtiles, int ksteps, unsigned 
   return cudaGetLastError();
 }
 
+cudaError_t launch_k_diag_tc(const DevAtom& A, const DevScratch& S, const DevTC& T, bool symmetric, double* K,
+                             cudaStream_t st) {
+  const int n = symmetric ? T.n_dsym : T.n_dall;
+  if (n == 0) return cudaSuccess;
+  const size_t smem = tc_diag_smem_bytes(A.NL, T.dksteps, A.nang);
+  const cudaError_t e = smem_limit(k_diag_tc, smem);
+  if (e != cudaSuccess) return e;
+  k_diag_tc<<<n, 256, smem, st>>>(A, S, T, symmetric ? 1 : 0, K);
+  return cudaGetLastError();
+}
 
 }  // namespace hfg
