@@ -45,7 +45,8 @@ FORMS = {
     "split": {"dtype": "bf16 digits (7 x 8-bit slices, exact FP32 level sums on the tensor cores, FP64 recombination)",
               "form": "split precision on the tensor cores: density tiles recoupled in float pairs, radial tables "
                       "and density as balanced base-256 digit planes (bf16), tcgen05 MMAs form exact FP32 level "
-                      "sums in tensor memory, carried and recombined to FP64 once per output element"},
+                      "sums in tensor memory, carried and recombined to FP64 once per output element; J in float "
+                      "pairs (hi + lo, error-free products) with one FP64 conversion per output element"},
 }
 
 
@@ -324,7 +325,7 @@ def run_ours(args):
     tuned = atom.autotune(symmetric=True, split=split)  # work partition, outside the timed region
 
     def step(split_k=split):
-        atom.coulomb(Pd, Jd, stream)
+        atom.coulomb(Pd, Jd, stream, split=split_k)
         atom.exchange(Pd, Kd, stream, symmetric=True, split=split_k)  # P = C C^T is symmetric
 
     # plain FP64 beside the split form: rate and the split error on this density
@@ -341,16 +342,20 @@ def run_ours(args):
         p1.record(stream)
         torch.cuda.synchronize()
         K64.copy_(Kd)
+        J64 = Jd.clone()
         step(True)
         torch.cuda.synchronize()
         dK = Kd - K64
+        dJ = Jd - J64
         plain = {"value": args.steps / (p0.elapsed_time(p1) * 1e-3), "unit": UNIT,
                  "ms_per_step": p0.elapsed_time(p1) / args.steps,
                  "split_error_vs_fp64": {
                      "k_max_rel": float(dK.abs().max() / K64.abs().max()),
+                     "j_max_rel": float(dJ.abs().max() / J64.abs().max()),
+                     "coulomb_energy_abs_eh": abs(0.5 * float((Pd * dJ).sum())),
                      "exchange_energy_abs_eh": abs(0.5 * float((Pd * dK).sum())),
                      "exchange_energy_eh": 0.5 * float((Pd * K64).sum())}}
-        del K64, dK
+        del K64, dK, J64, dJ
 
     for _ in range(args.warmup):
         step()
@@ -385,13 +390,13 @@ def run_ours(args):
         return torch.empty((nbf, nbf), dtype=torch.float64, pin_memory=True).numpy().T
     Ph, Jh, Kh = pinned(), pinned(), pinned()
     Ph[...] = P
-    atom.jk_host(Ph, J=Jh, K=Kh, symmetric=True, split=split)
+    atom.jk_host(Ph, J=Jh, K=Kh, symmetric=True, split=split, split_j=split)
     ne = args.e2e_steps
     if dist is not None:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(ne):
-        atom.jk_host(Ph, J=Jh, K=Kh, symmetric=True, split=split)
+        atom.jk_host(Ph, J=Jh, K=Kh, symmetric=True, split=split, split_j=split)
     te = max(time.perf_counter() - t0, 1e-30)
     if dist is not None:
         t = torch.tensor([te], device="cuda", dtype=torch.float64)
@@ -400,7 +405,7 @@ def run_ours(args):
     e2e = {"value": ws * ne / te if ne else None, "unit": UNIT, "h2d_bytes_per_step": 8 * nbf * nbf,
            "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
            "path": "hfg_jk_host (pinned host P, J, K; one staging of P, J copied back while K builds; "
-                   "same K form as value)"}
+                   "same J and K forms as value)"}
 
     if rank != 0:
         if dist is not None:
@@ -526,6 +531,9 @@ def run_scf_batch(args):
     ok = [r for r in res if r["status"] == 2 and r["converged"]]
     both = [(a, b) for a, b in zip(res, res_p) if a["status"] == 2 and b["status"] == 2]
     dE = max((abs(a["Etot"] - b["Etot"]) for a, b in both), default=None)
+    # the largest energy differences against the plain path, with the atom
+    top = sorted(((abs(a["Etot"] - b["Etot"]), j) for j, (a, b) in zip(jobs, zip(res, res_p))
+                  if a["status"] == 2 and b["status"] == 2), key=lambda x: -x[0])[:5]
     lat = [r["total_ms"] for r in res]
     svc = [r["setup_ms"] + r["scf_ms"] for r in res]
     out = {
@@ -550,9 +558,91 @@ def run_scf_batch(args):
                        "latency_ms_p99": _percentile([r["total_ms"] for r in res_p], 0.99)},
         "speedup_vs_plain": wall_p / wall,
         "max_abs_dE_vs_plain_eh": dE,
+        "largest_dE_vs_plain": [{"dE_eh": d, "Z": j["Z"], "method": j["method"], "nnodes": j["nnodes"],
+                                 "elements": len(j["bval"]) - 1} for d, j in top],
         "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)
+
+
+def run_fock_batch(args):
+    """Fock builds (J + K) over the seeded batch atoms (the 512-atom batch
+    draws, scaled by --atoms / --nel-max): per atom a density P = C C^T from
+    min(18, nbf) orthonormalised N(0,1) columns, every build timed alone with
+    CUDA events after an L2 flush (256 MB written), split and plain FP64 forms
+    on the same handle; builds/s = builds / summed build time, and the split
+    J and K errors against the plain ones per atom."""
+    import torch
+    torch.cuda.set_device(0)
+    import helfem_gb300 as hg
+    from helfem_gb300 import workloads as wl
+    jobs = wl.batch_atoms(args.atoms, seed=2024, zmax=86, nel_range=(10, args.nel_max))
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    gen = torch.Generator(device="cuda").manual_seed(2024)
+    reps = max(1, args.steps)
+    t = {"split": 0.0, "plain": 0.0}
+    nb = 0
+    worst = {"k_max_rel": 0.0, "j_max_rel": 0.0, "exchange_energy_abs_eh": 0.0}
+    per_size = []
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for j in jobs:
+            atom = hg.Atom(j["Z"], j["bval"], j["lval"], j["mval"], nnodes=j["nnodes"])
+            n = atom.nbf
+            C = torch.randn(n, min(18, n), dtype=torch.float64, device="cuda", generator=gen)
+            C, _ = torch.linalg.qr(C)
+            P = (C @ C.T).contiguous()
+            del C
+            out = {f: (torch.empty_like(P), torch.empty_like(P)) for f in t}
+            ms_atom = {}
+            for f in ("plain", "split"):
+                Jd, Kd = out[f]
+                sp = f == "split"
+                for _ in range(max(1, args.warmup)):
+                    atom.coulomb(P, Jd, stream, split=sp)
+                    atom.exchange(P, Kd, stream, symmetric=True, split=sp)
+                ms = 0.0
+                for _ in range(reps):
+                    flush.zero_()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    atom.coulomb(P, Jd, stream, split=sp)
+                    atom.exchange(P, Kd, stream, symmetric=True, split=sp)
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    ms += e0.elapsed_time(e1)
+                t[f] += ms
+                ms_atom[f] = ms / reps
+            nb += reps
+            (J64, K64), (Js, Ks) = out["plain"], out["split"]
+            worst["k_max_rel"] = max(worst["k_max_rel"], float((Ks - K64).abs().max() / K64.abs().max()))
+            worst["j_max_rel"] = max(worst["j_max_rel"], float((Js - J64).abs().max() / J64.abs().max()))
+            worst["exchange_energy_abs_eh"] = max(worst["exchange_energy_abs_eh"],
+                                                  abs(0.5 * float((P * (Ks - K64)).sum())))
+            per_size.append((n, ms_atom["plain"], ms_atom["split"]))
+            del P, out, J64, K64, Js, Ks
+            atom.close()
+    torch.cuda.empty_cache()
+    per_size.sort()
+    big = per_size[len(per_size) // 2:]
+    res = {
+        "metric": "Fock builds/s (J+K, batched atoms)", "value": nb / (t["split"] * 1e-3), "unit": "builds/s",
+        "n_gpus": 1, "steps": reps, "warmup": args.warmup, "ms_per_step": t["split"] / nb,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": FORMS["split"]["dtype"],
+        "data": "synthetic",
+        "config": {"workload": f"{len(jobs)} seeded atoms (the batch draws): Z 1-86, 10-{args.nel_max} elements, "
+                               "nodes {10,13,15,17}, Rmax 40-80, lmax by occupied shells; P = C C^T, "
+                               "min(18, nbf) orthonormal columns",
+                   "timing": "each build alone, CUDA events, L2 flushed (256 MB) before every build"},
+        "plain": {"value": nb / (t["plain"] * 1e-3), "unit": "builds/s", "form": "plain FP64 J and K"},
+        "split_over_plain": t["plain"] / t["split"],
+        "split_over_plain_larger_half": sum(p for _, p, _ in big) / sum(q for _, _, q in big),
+        "nbf_range": [per_size[0][0], per_size[-1][0]],
+        "split_error_vs_fp64_worst": worst,
+        "form": FORMS["split"]["form"],
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(res), flush=True)
 
 
 def run_serve(args):
@@ -900,7 +990,7 @@ def main():
     ap.add_argument("--plain", action="store_true", help="time the plain FP64 form only")
     ap.add_argument("--no-n2", dest="n2", action="store_false",
                     help="skip the N2 diatomic Fock-build object of the default line")
-    ap.add_argument("--workload", default="fock", choices=["fock", "scf-batch", "serve", "n2"])
+    ap.add_argument("--workload", default="fock", choices=["fock", "fock-batch", "scf-batch", "serve", "n2"])
     ap.add_argument("--atoms", type=int, default=32)
     ap.add_argument("--nel-max", type=int, default=30)
     ap.add_argument("--workers", type=int, default=8)
@@ -915,6 +1005,8 @@ def main():
         run_n2_reference(args)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.workload == "fock-batch":
+        run_fock_batch(args)
     elif args.workload == "scf-batch":
         run_scf_batch(args)
     elif args.workload == "serve":

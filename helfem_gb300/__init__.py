@@ -72,6 +72,7 @@ _SIGS = {
     "hfg_coulomb_acc": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_exchange": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_exchange_ex": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
+    "hfg_coulomb_ex": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
     "hfg_coulomb_noalloc": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
@@ -128,6 +129,7 @@ def parse_xc(method: str):
     return (ids + [0, 0])[:2]
 EXCHANGE_SYMMETRIC = 1
 EXCHANGE_SPLIT = 2
+COULOMB_SPLIT = 4
 EXCHANGE_ITEMWISE = 4  # diatomic split form: diagonal tiles one output block per item (comparison schedule)
 
 
@@ -321,8 +323,11 @@ class Atom:
         return rs, rb, ch
 
     # ---- hot path: device pointers ----
-    def coulomb(self, P, J, stream=None):
-        _check(_lib.hfg_coulomb(self._h, _ptr(P), _ptr(J), _stream(stream)))
+    def coulomb(self, P, J, stream=None, split: bool = False):
+        if split:
+            _check(_lib.hfg_coulomb_ex(self._h, _ptr(P), _ptr(J), COULOMB_SPLIT, _stream(stream)))
+        else:
+            _check(_lib.hfg_coulomb(self._h, _ptr(P), _ptr(J), _stream(stream)))
 
     def coulomb_acc(self, P, F, stream=None):
         _check(_lib.hfg_coulomb_acc(self._h, _ptr(P), _ptr(F), _stream(stream)))
@@ -471,14 +476,16 @@ class Atom:
         _check(_lib.hfg_fock_diag(self._h, _ptr(F), symmetry, _ptr(C), _ptr(eps), _stream(stream)))
 
     def jk_host(self, PJ: np.ndarray, PK: np.ndarray = None, J: np.ndarray = None, K: np.ndarray = None,
-                symmetric: bool = False, split: bool = False):
-        """J(PJ) and K(PK) (PK defaults to PJ: one staging of the density)."""
+                symmetric: bool = False, split: bool = False, split_j: bool = False):
+        """J(PJ) and K(PK) (PK defaults to PJ: one staging of the density);
+        split: K in the split form, split_j: J in float pairs."""
         PJ = np.asfortranarray(PJ, dtype=np.float64)
         PK = PJ if PK is None else np.asfortranarray(PK, dtype=np.float64)
         J = np.zeros_like(PJ, order="F") if J is None else J
         K = np.zeros_like(PJ, order="F") if K is None else K
         assert J.flags.f_contiguous and K.flags.f_contiguous and J.shape == K.shape == PJ.shape
-        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        flags = ((EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0) |
+                 (COULOMB_SPLIT if split_j else 0))
         _check(_lib.hfg_jk_host(self._h, _dptr(PJ), _dptr(PK), _dptr(J), _dptr(K), flags))
         return J, K
 

@@ -189,6 +189,22 @@ hfg_status hfg_coulomb(hfg_atom* a, const double* P, double* J, void* stream) {
   });
 }
 
+hfg_status hfg_coulomb_ex(hfg_atom* a, const double* P, double* J, int flags, void* stream) {
+  return guard([&] {
+    need(a && P && J, "hfg_coulomb_ex: null argument");
+    need((flags & ~HFG_COULOMB_SPLIT) == 0, "hfg_coulomb_ex: unknown flags");
+    a->check_device();
+    if (flags & HFG_COULOMB_SPLIT) {
+      a->ensure_split_coulomb();
+      ck(hfg::launch_coulomb_split(a->dev, a->scr, P, J, true, (cudaStream_t)stream, &a->prof),
+         "coulomb kernels (split)");
+    } else {
+      ck(hfg::launch_coulomb_fp64(a->dev, a->scr, P, J, true, (cudaStream_t)stream, &a->prof), "coulomb kernels");
+    }
+    a->mark_use((cudaStream_t)stream);
+  });
+}
+
 hfg_status hfg_coulomb_acc(hfg_atom* a, const double* P, double* F, void* stream) {
   return guard([&] {
     need(a && P && F, "hfg_coulomb_acc: null argument");
@@ -308,7 +324,7 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
 // exchange build running while J is copied back on a second stream
 static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, double* K, int flags) {
   need(a && PJ && PK && J && K, "null argument");
-  need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "unknown flags");
+  need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT | HFG_COULOMB_SPLIT)) == 0, "unknown flags");
   a->check_device();
   a->staging();
   const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
@@ -325,8 +341,14 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
     if (a->h_out2.n != bytes) a->h_out2.alloc(bytes);
   }
   ck(cudaMemcpyAsync(a->h_in.p, PJ, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
-  ck(hfg::launch_coulomb_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof),
-     "coulomb");
+  if (flags & HFG_COULOMB_SPLIT) {
+    a->ensure_split_coulomb();
+    ck(hfg::launch_coulomb_split(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof),
+       "coulomb (split)");
+  } else {
+    ck(hfg::launch_coulomb_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof),
+       "coulomb");
+  }
   ck(cudaEventRecord(a->ev_j, st), "event");
   ck(cudaStreamWaitEvent(a->copy_stream, a->ev_j, 0), "wait");
   ck(cudaMemcpyAsync(J, a->h_out.p, bytes, cudaMemcpyDeviceToHost, a->copy_stream), "D2H copy");

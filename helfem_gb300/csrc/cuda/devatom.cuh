@@ -42,6 +42,11 @@ struct DevAtom {
   const float2* rb2 = nullptr;
   const float2* tk2 = nullptr;
   const float2* kterm_coef2 = nullptr;
+  // split form of the Coulomb build (float-pair copies of the coupling
+  // coefficients and of the in-element factor, made on first use)
+  const float2* jket_coef2 = nullptr;
+  const float2* jbra_coef2 = nullptr;
+  const float2* cholp2 = nullptr;
 };
 
 // Scratch owned by the atom handle (sizes fixed at creation)
@@ -189,6 +194,9 @@ cudaError_t tc_peak(int ctas_per_sm, int iters, double* tflops, double* ms, int*
 
 // launchers (jk_fp64.cu)
 cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* J,
+                                bool zero_output, cudaStream_t st, Profiler* prof = nullptr);
+// the same J in float pairs (needs jket_coef2, jbra_coef2, cholp2, rs2, rb2)
+cudaError_t launch_coulomb_split(const DevAtom& A, const DevScratch& S, const double* P, double* J,
                                 bool zero_output, cudaStream_t st, Profiler* prof = nullptr);
 cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr);

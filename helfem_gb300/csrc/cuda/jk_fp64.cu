@@ -110,6 +110,148 @@ __global__ void j_contract(DevAtom A, DevScratch S, const double* __restrict__ P
 
 constexpr int JMAXTERMS = 64;
 
+// ---- Coulomb, split form: the contraction above in float pairs (the FP64
+// pipe bounds the FP64 form on GB300: 2 n2 r multiply-adds per channel and
+// element for the in-element factor alone). The density is split with
+// integer operations, the in-element factor and the radial tables come as
+// float-pair copies, sums of n2 or r terms are renormalised every step; the
+// in-element part goes to the scratch as float pairs, the two scalars per
+// (channel, element) as FP64.
+__device__ __forceinline__ ffv ff_warp_sum(ffv v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = ff_add(v, ffv{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
+  return v;
+}
+
+// block-wide float-pair sum, valid in thread 0; red needs >= 32 entries
+__device__ ffv ff_block_sum(ffv v, ffv* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = ff_warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  ffv s{0.f, 0.f};
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nw; ++i) s = ff_add(s, red[i]);
+  return s;
+}
+
+__global__ void j_contract_split(DevAtom A, DevScratch S, const double* __restrict__ P,
+                                 const float2* __restrict__ C2) {
+  const int ch = blockIdx.x, e = blockIdx.y;
+  const int nn = A.nn, n2 = nn * nn, L = A.chanL[ch];
+  extern __shared__ float2 smf[];
+  float2* X = smf;       // [n2]
+  float2* sc = X + n2;   // [rmax]
+  __shared__ ffv red[32];
+  const int k0 = A.jket_ptr[ch], k1 = A.jket_ptr[ch + 1];
+  for (int idx = threadIdx.x; idx < n2; idx += blockDim.x) {
+    const int p = idx % nn, q = idx / nn;
+    const int gp = gfun(A, e, p), gq = gfun(A, e, q);
+    ffv x{0.f, 0.f};
+    if (gvalid(A, gp) && gvalid(A, gq))
+      for (int u = k0; u < k1; ++u) {
+        const int blk = A.jket_blk[u], k = blk % A.nang, l = blk / A.nang;
+        x = ff_fma(x, A.jket_coef2[u], split_bits(P[(size_t)(l * A.nrad + gq) * A.nbf + (size_t)k * A.nrad + gp]));
+      }
+    X[idx] = ff2(x);
+  }
+  __syncthreads();
+  const size_t le = (size_t)L * A.nel + e;
+  const float2* rs = A.rs2 + le * n2;
+  const float2* rb = A.rb2 + le * n2;
+  ffv ts{0.f, 0.f}, tb{0.f, 0.f};
+  for (int idx = threadIdx.x; idx < n2; idx += blockDim.x) {
+    const int p = idx % nn, q = idx / nn;
+    const float2 xt = X[q + p * nn];
+    ts = ff_fma_n(ts, rs[idx], xt);
+    tb = ff_fma_n(tb, rb[idx], xt);
+  }
+  ts = ff_block_sum(ts, red);
+  tb = ff_block_sum(tb, red);
+  if (threadIdx.x == 0) {
+    S.jscal[((size_t)ch * A.nel + e) * 2 + 0] = ff_to_d(ts);
+    S.jscal[((size_t)ch * A.nel + e) * 2 + 1] = ff_to_d(tb);
+  }
+  const int r = A.rank[le];
+  const float2* C = C2 + le * n2 * A.rmax;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int j = w; j < r; j += nw) {
+    ffv v{0.f, 0.f};
+    for (int q = lane; q < n2; q += 32) v = ff_fma_n(v, C[q + (size_t)j * n2], X[q]);
+    v = ff_warp_sum(v);
+    if (lane == 0) sc[j] = make_float2(v.hi, v.lo);
+  }
+  __syncthreads();
+  float2* jin = reinterpret_cast<float2*>(S.jin) + ((size_t)ch * A.nel + e) * n2;
+  for (int idx = threadIdx.x; idx < n2; idx += blockDim.x) {
+    ffv v{0.f, 0.f};
+    for (int j = 0; j < r; ++j) v = ff_fma_n(v, C[idx + (size_t)j * n2], sc[j]);
+    jin[idx] = ff2(v);
+  }
+}
+
+__global__ void j_scatter_split(DevAtom A, DevScratch S, double* __restrict__ J, int accumulate) {
+  const int ij = blockIdx.x, e = blockIdx.y;
+  const int i = ij % A.nang, j = ij / A.nang;
+  const int b0 = A.jbra_ptr[ij], b1 = A.jbra_ptr[ij + 1];
+  const int nt = b1 - b0;
+  if (nt == 0) return;
+  const int nn = A.nn, n2 = nn * nn;
+  __shared__ float2 Ab[JMAXTERMS], As[JMAXTERMS], Ab1[JMAXTERMS], As1[JMAXTERMS];
+  for (int u = threadIdx.x; u < nt; u += blockDim.x) {
+    const int ch = A.jbra_chan[b0 + u];
+    const double* sc = S.jscal + (size_t)ch * A.nel * 2;
+    double big = 0.0, small = 0.0;
+    for (int e2 = e + 1; e2 < A.nel; ++e2) big += sc[2 * e2 + 1];
+    for (int e2 = 0; e2 < e; ++e2) small += sc[2 * e2 + 0];
+    Ab[u] = split_bits(big);
+    As[u] = split_bits(small);
+    if (e > 0) {
+      Ab1[u] = split_bits(big + sc[2 * e + 1]);
+      As1[u] = split_bits(small - sc[2 * (e - 1) + 0]);
+    }
+  }
+  __syncthreads();
+  const float2* jin2 = reinterpret_cast<const float2*>(S.jin);
+  for (int idx = threadIdx.x; idx < n2; idx += blockDim.x) {
+    const int p = idx % nn, q = idx / nn;
+    // J has element-diagonal tiles only: the single entry two tiles share is
+    // the corner on the common boundary function, owned by the later tile
+    if (p == nn - 1 && q == nn - 1) continue;
+    const int gp = gfun(A, e, p), gq = gfun(A, e, q);
+    if (!gvalid(A, gp) || !gvalid(A, gq)) continue;
+    ffv v{0.f, 0.f};
+    for (int u = 0; u < nt; ++u) {
+      const int ch = A.jbra_chan[b0 + u], L = A.chanL[ch];
+      const size_t le = (size_t)L * A.nel + e;
+      ffv t{0.f, 0.f};
+      t = ff_fma(t, Ab[u], A.rs2[le * n2 + idx]);
+      t = ff_fma(t, As[u], A.rb2[le * n2 + idx]);
+      const float2 ji = jin2[((size_t)ch * A.nel + e) * n2 + idx];
+      t = ff_add(t, ffv{ji.x, ji.y});
+      v = ff_fma_n(v, A.jbra_coef2[b0 + u], ff2(t));
+    }
+    if (p == 0 && q == 0 && e > 0) {
+      const int c = (nn - 1) + (nn - 1) * nn;
+      for (int u = 0; u < nt; ++u) {
+        const int ch = A.jbra_chan[b0 + u], L = A.chanL[ch];
+        const size_t le = (size_t)L * A.nel + (e - 1);
+        ffv t{0.f, 0.f};
+        t = ff_fma(t, Ab1[u], A.rs2[le * n2 + c]);
+        t = ff_fma(t, As1[u], A.rb2[le * n2 + c]);
+        const float2 ji = jin2[((size_t)ch * A.nel + (e - 1)) * n2 + c];
+        t = ff_add(t, ffv{ji.x, ji.y});
+        v = ff_fma_n(v, A.jbra_coef2[b0 + u], ff2(t));
+      }
+    }
+    double* out = J + (size_t)(j * A.nrad + gq) * A.nbf + (size_t)i * A.nrad + gp;
+    const double y = ff_to_d(v);
+    if (accumulate) *out += y; else *out = y;
+  }
+}
+
 __global__ void j_scatter(DevAtom A, DevScratch S, double* __restrict__ J, int accumulate) {
   const int ij = blockIdx.x, e = blockIdx.y;
   const int i = ij % A.nang, j = ij / A.nang;
@@ -536,6 +678,28 @@ cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const dou
   {
     Mark m(prof, KC_J_SCATTER, st);
     j_scatter<<<dim3(A.nang * A.nang, A.nel), th, 0, st>>>(A, S, J, zero_output ? 0 : 1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coulomb_split(const DevAtom& A, const DevScratch& S, const double* P, double* J,
+                                 bool zero_output, cudaStream_t st, Profiler* prof) {
+  if (!A.cholp2 || !A.jket_coef2 || !A.jbra_coef2 || !A.rs2 || !A.rb2) return cudaErrorInvalidValue;
+  const int n2 = A.nn * A.nn, th = threads_for(n2);
+  if (zero_output) {
+    cudaError_t err = cudaMemsetAsync(J, 0, sizeof(double) * (size_t)A.nbf * A.nbf, st);
+    if (err != cudaSuccess) return err;
+  }
+  const size_t sm1 = sizeof(float2) * (n2 + A.rmax);
+  {
+    Mark m(prof, KC_J_CONTRACT, st);
+    const cudaError_t e = smem_limit(j_contract_split, sm1);
+    if (e != cudaSuccess) return e;
+    j_contract_split<<<dim3(A.nchan, A.nel), th, sm1, st>>>(A, S, P, A.cholp2);
+  }
+  {
+    Mark m(prof, KC_J_SCATTER, st);
+    j_scatter_split<<<dim3(A.nang * A.nang, A.nel), th, 0, st>>>(A, S, J, zero_output ? 0 : 1);
   }
   return cudaGetLastError();
 }

@@ -657,22 +657,29 @@ __global__ void __launch_bounds__(256, 2) k_diag_tc(DevAtom A, DevScratch S, Dev
       const int s = ch / (2 * ksteps), v0 = 8 * (ch % (2 * ksteps));
       if (!sact[L * DSLOT + s]) continue;
       const int ent = gent[s * NL + L];
-      long long eo[8];  // density offsets of the 8 elements, -1: outside the basis
+      int eo[8];  // density offsets of the 8 elements (nbf^2 < 2^31), -1: outside the basis
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int v = v0 + j, p = v % nn, q = v / nn;
         const int gp = gfun(A, a, p), gq = gfun(A, a, q);
-        eo[j] = (v < n2 && gp >= 0 && gp < A.nrad && gq >= 0 && gq < A.nrad) ? (long long)gq * A.nbf + gp : -1;
+        eo[j] = (v < n2 && gp >= 0 && gp < A.nrad && gq >= 0 && gq < A.nrad) ? gq * A.nbf + gp : -1;
       }
-      for (int uu = A.kent_ptr[ent]; uu < A.kent_ptr[ent + 1]; ++uu) {
-        if (!act[A.kterm_blk[uu]]) continue;
-        const float2 cf = A.kterm_coef2[uu];
-        const float2* pb = S.p2 + A.kterm_off[uu];
-        float2 pv[8];
+      // two terms' loads in flight together
+      const int u1 = A.kent_ptr[ent + 1];
+      for (int uu = A.kent_ptr[ent]; uu < u1; uu += 2) {
+        float2 cf[2], pv[2][8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) pv[j] = eo[j] >= 0 ? pb[eo[j]] : make_float2(0.f, 0.f);
+        for (int w = 0; w < 2; ++w) {
+          const bool on = uu + w < u1 && act[A.kterm_blk[uu + w]];
+          cf[w] = on ? A.kterm_coef2[uu + w] : make_float2(0.f, 0.f);
+          const float2* pb = S.p2 + (on ? A.kterm_off[uu + w] : 0);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) xs[c][j] = ff_fma(xs[c][j], cf, pv[j]);
+          for (int j = 0; j < 8; ++j) pv[w][j] = (on && eo[j] >= 0) ? pb[eo[j]] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int w = 0; w < 2; ++w)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) xs[c][j] = ff_fma(xs[c][j], cf[w], pv[w][j]);
       }
       unsigned eb = 0;
 #pragma unroll

@@ -157,7 +157,7 @@ struct hfg_atom {
   DBuf d_rs, d_rb, d_cholp, d_rank, d_tk, d_chanL, d_jket_ptr, d_jket_blk, d_jket_coef, d_jbra_ptr,
       d_jbra_chan, d_jbra_coef, d_kjk_ptr, d_kent_L, d_kent_ptr, d_kterm_blk, d_kterm_off, d_kterm_coef;
   DBuf s_jin, s_jscal, s_khalo, s_bnorm, s_p2, s_act, s_entact;
-  DBuf d_rs2, d_rb2, d_tk2, d_kcoef2;
+  DBuf d_rs2, d_rb2, d_tk2, d_kcoef2, d_jkc2, d_jbc2, d_cholp2;
   DBuf d_units_all, d_units_sym, d_diag_all, d_diag_sym;
   hfg::KUnits units;
   // tensor-core split exchange: digit tables of the bare and of the
@@ -558,10 +558,24 @@ struct hfg_atom {
       A.tk2 = d_tk2.as<float2>();
     }
     A.kterm_coef2 = d_kcoef2.upload(split(H.kterm_coef));
+    A.jket_coef2 = d_jkc2.upload(split(H.jket_coef));
+    A.jbra_coef2 = d_jbc2.upload(split(H.jbra_coef));
     build_units();
     tc_setup();
     ck(cudaStreamSynchronize(own_stream), "sync after upload");
     on_device = true;
+  }
+
+  // float-pair copy of the in-element factor for the split Coulomb form,
+  // made on its first use (it doubles the factor's footprint)
+  void ensure_split_coulomb() {
+    if (dev.cholp2) return;
+    hfg_abi::AllocStream alloc_on(own_stream);
+    const size_t n = (size_t)host.NL * host.rad.nel * host.rad.nn * host.rad.nn * host.rmax;
+    d_cholp2.alloc(sizeof(float2) * std::max<size_t>(1, n));
+    ck(hfg::launch_split_f2(dev.cholp, d_cholp2.as<float2>(), n, own_stream), "split copy of the in-element factor");
+    ck(cudaStreamSynchronize(own_stream), "sync after the split copy");
+    dev.cholp2 = d_cholp2.as<float2>();
   }
 
   // In-element factors and exchange tensor tabulated on the device (FP64,

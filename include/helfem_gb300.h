@@ -126,6 +126,16 @@ hfg_status hfg_gaunt(int L, int M, int l, int m, int lp, double* value);
  * J is overwritten (zero outside the element-diagonal tiles). */
 hfg_status hfg_coulomb(hfg_atom* atom, const double* P, double* J, void* stream);
 
+/* hfg_coulomb with options. HFG_COULOMB_SPLIT: the same J in float pairs
+ * (the FP64 pipe bounds the FP64 form on GB300): the density is split into
+ * hi + lo with integer operations, the in-element factor and the radial
+ * tables are float-pair copies (the factor's copy is made on the first
+ * call), products are error-free, long sums renormalised every step, one FP64
+ * conversion per output element; relative error ~1e-14 against FP64,
+ * reported by the tests and the benchmark. */
+#define HFG_COULOMB_SPLIT 4
+hfg_status hfg_coulomb_ex(hfg_atom* atom, const double* P, double* J, int flags, void* stream);
+
 /* F += J(P): the same build accumulated into an existing matrix, for
  * Fock assembly without a separate J buffer. */
 hfg_status hfg_coulomb_acc(hfg_atom* atom, const double* P, double* F, void* stream);
@@ -251,7 +261,7 @@ hfg_status hfg_exchange_host_ex(hfg_atom* atom, const double* P, double* K, int 
 /* J(PJ) and K(PK) in one call (the Fock builder's pair of calls,
  * src/atomic/main.cpp:424-443): the density is staged once when PK == PJ
  * (same pointer), and J is copied back on a second stream while K is built.
- * flags as hfg_exchange_ex. */
+ * flags as hfg_exchange_ex for K, plus HFG_COULOMB_SPLIT for J. */
 hfg_status hfg_jk_host(hfg_atom* atom, const double* PJ, const double* PK, double* J, double* K, int flags);
 
 /* Algorithmic work of one J and one K build on this basis with every density

@@ -269,3 +269,41 @@ def test_kr_full_size_split_matches_oracle(kr_bench_case):
         dE = 0.5 * abs(float(np.sum(P * (K - Kr))))
         print(f"Kr full size split K symmetric={sym}: max rel err {err:.2e}, |dE_x| {dE:.2e} Eh")
         assert np.isfinite(K).all() and err < SPLIT_TOL and dE < 1e-10
+
+
+@pytest.mark.parametrize("case", CASES[:5], ids=lambda c: f"Z{c[0]}_l{c[1]}m{c[2]}_e{c[3]}_n{c[4]}")
+def test_split_coulomb_error(case):
+    """Split-form J (float pairs, hfg_coulomb_ex with HFG_COULOMB_SPLIT)
+    against the FP64 oracle: error stated per result and bounded by
+    SPLIT_TOL of max|J|; the FP64 form on the same handle afterwards is
+    unchanged (the split copy of the factor lives beside it)."""
+    torch = torch_cuda()
+    A, O = make_pair(*case)
+    P = random_density(O.nbf, min(7, O.nbf), seed=case[0] + 200, S=O.S)
+    Jr = FockOracle(O).coulomb(P)
+    Pd = to_dev(torch, P)
+    Js, J64 = torch.full_like(Pd, np.nan), torch.full_like(Pd, np.nan)
+    A.coulomb(Pd, Js, split=True)
+    A.coulomb(Pd, J64)
+    J, Jd = from_dev(Js), from_dev(J64)
+    err, err64 = relerr(J, Jr), relerr(Jd, Jr)
+    print(f"split J {case}: max rel err {err:.2e} (FP64 form {err64:.2e})")
+    assert np.isfinite(J).all() and err < SPLIT_TOL and err64 < TOL
+
+
+def test_kr_full_size_split_coulomb_matches_oracle(kr_bench_case):
+    """Split-form J on the benchmark basis and density against the oracle:
+    max error at SPLIT_TOL of max|ref|, Coulomb energy 0.5 tr(PJ) within
+    1e-10 Eh; the host drop-in with HFG_COULOMB_SPLIT gives the same J."""
+    torch = torch_cuda()
+    A, P, Jr, _ = kr_bench_case
+    Pd = to_dev(torch, P)
+    Jd = torch.full_like(Pd, np.nan)
+    A.coulomb(Pd, Jd, split=True)
+    J = from_dev(Jd)
+    err = relerr(J, Jr)
+    dE = 0.5 * abs(float(np.sum(P * (J - Jr))))
+    print(f"Kr full size split J: max rel err {err:.2e}, |dE_J| {dE:.2e} Eh")
+    assert np.isfinite(J).all() and err < SPLIT_TOL and dE < 1e-10
+    Jh, _ = A.jk_host(P, symmetric=True, split=True, split_j=True)
+    assert np.array_equal(Jh, J)
