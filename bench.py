@@ -325,8 +325,8 @@ def run_ours(args):
     tuned = atom.autotune(symmetric=True, split=split)  # work partition, outside the timed region
 
     def step(split_k=split):
-        atom.coulomb(Pd, Jd, stream, split=split_k)
-        atom.exchange(Pd, Kd, stream, symmetric=True, split=split_k)  # P = C C^T is symmetric
+        # J on the handle's second stream, concurrent with K (hfg_jk); P = C C^T is symmetric
+        atom.jk(Pd, Jd, Kd, stream=stream, symmetric=True, split=split_k, split_j=split_k)
 
     # plain FP64 beside the split form: rate and the split error on this density
     plain = None

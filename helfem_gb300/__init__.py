@@ -73,6 +73,7 @@ _SIGS = {
     "hfg_exchange": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_exchange_ex": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
     "hfg_coulomb_ex": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
+    "hfg_jk": ([_P, _P, _P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
     "hfg_coulomb_noalloc": ([_P, _P, _P, _P], ctypes.c_int),
     "hfg_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
@@ -328,6 +329,15 @@ class Atom:
             _check(_lib.hfg_coulomb_ex(self._h, _ptr(P), _ptr(J), COULOMB_SPLIT, _stream(stream)))
         else:
             _check(_lib.hfg_coulomb(self._h, _ptr(P), _ptr(J), _stream(stream)))
+
+    def jk(self, PJ, J, K, PK=None, stream=None, symmetric: bool = False, split: bool = False,
+           split_j: bool = False):
+        """J(PJ) and K(PK) (PK defaults to PJ) in one call, J on the handle's
+        second stream concurrently with K, joined back into `stream`."""
+        PK = PJ if PK is None else PK
+        flags = ((EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0) |
+                 (COULOMB_SPLIT if split_j else 0))
+        _check(_lib.hfg_jk(self._h, _ptr(PJ), _ptr(PK), _ptr(J), _ptr(K), flags, _stream(stream)))
 
     def coulomb_acc(self, P, F, stream=None):
         _check(_lib.hfg_coulomb_acc(self._h, _ptr(P), _ptr(F), _stream(stream)))

@@ -378,6 +378,47 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
   if (flags & HFG_EXCHANGE_SPLIT) a->tc_check();
 }
 
+hfg_status hfg_jk(hfg_atom* a, const double* PJ, const double* PK, double* J, double* K, int flags, void* stream) {
+  return guard([&] {
+    need(a && PJ && PK && J && K, "hfg_jk: null argument");
+    need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT | HFG_COULOMB_SPLIT)) == 0, "hfg_jk: unknown flags");
+    need(J != K, "hfg_jk: J and K must be different buffers");
+    a->check_device();
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!a->j_stream) ck(cudaStreamCreateWithFlags(&a->j_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!a->ev_fork) ck(cudaEventCreateWithFlags(&a->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+    if (!a->ev_join) ck(cudaEventCreateWithFlags(&a->ev_join, cudaEventDisableTiming), "cudaEventCreate");
+    const bool split_k = (flags & HFG_EXCHANGE_SPLIT) != 0, split_j = (flags & HFG_COULOMB_SPLIT) != 0;
+    if (split_j) a->ensure_split_coulomb();
+    if (split_k) {
+      const size_t bytes = sizeof(float2) * (size_t)a->host.nbf * a->host.nbf;
+      if (a->s_p2.n != bytes) {
+        hfg_abi::AllocStream alloc_on(a->own_stream);
+        a->s_p2.alloc(bytes);
+        a->scr.p2 = a->s_p2.as<float2>();
+        ck(cudaStreamSynchronize(a->own_stream), "sync");
+      }
+    }
+    // J on the handle's second stream, after everything already on `stream`
+    ck(cudaEventRecord(a->ev_fork, st), "event");
+    ck(cudaStreamWaitEvent(a->j_stream, a->ev_fork, 0), "wait");
+    if (split_j)
+      ck(hfg::launch_coulomb_split(a->dev, a->scr, PJ, J, true, a->j_stream, &a->prof), "coulomb kernels (split)");
+    else
+      ck(hfg::launch_coulomb_fp64(a->dev, a->scr, PJ, J, true, a->j_stream, &a->prof), "coulomb kernels");
+    ck(cudaEventRecord(a->ev_join, a->j_stream), "event");
+    // K on the caller's stream meanwhile
+    const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
+    if (split_k)
+      ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, PK, K, sym, st, &a->prof, a->tc_for(false)),
+         "exchange kernels (split)");
+    else
+      ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, PK, K, sym, st, &a->prof), "exchange kernels");
+    ck(cudaStreamWaitEvent(st, a->ev_join, 0), "join");
+    a->mark_use(st);
+  });
+}
+
 hfg_status hfg_jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, double* K, int flags) {
   return guard([&] { jk_host(a, PJ, PK, J, K, flags); });
 }

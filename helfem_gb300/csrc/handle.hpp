@@ -377,6 +377,10 @@ struct hfg_atom {
   // back overlaps the exchange build
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_j = nullptr;
+  // stream and events of the device-pointer J+K entry point: the Coulomb
+  // build is forked from the caller's stream and joined back into it
+  cudaStream_t j_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // Yukawa-screened exchange: the exchange context with the screened radial
   // tables (built by hfg_atom_compute_yukawa)
   hfg::DevAtom dev_rs{};
@@ -428,6 +432,12 @@ struct hfg_atom {
 
   ~hfg_atom() {
     if (ev_j) cudaEventDestroy(ev_j);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (j_stream) {
+      cudaStreamSynchronize(j_stream);
+      cudaStreamDestroy(j_stream);
+    }
     if (copy_stream) {
       cudaStreamSynchronize(copy_stream);
       cudaStreamDestroy(copy_stream);

@@ -639,13 +639,13 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     //   s = sum_s tr(F~_s dP_s),  c = sum_s tr((dJ + dK_s) dP_s),
     // and J, K are linear in P, so the damped J and K are mixed like P with no
     // second build. The level shift is off while ODA runs; the run goes back to
-    // DIIS (fresh history, shift restored) once the gradient has fallen by 100x
-    // or the full step is optimal twice in a row.
+    // DIIS (fresh history, no shift) once the gradient has fallen by 100x or
+    // the full step is optimal twice in a row.
     // HFG_SCF_ODA=0 turns it off; =first starts it at the first iteration
     const char* oenv = std::getenv("HFG_SCF_ODA");
     const int oda_mode = !oenv ? 0 : std::strcmp(oenv, "0") == 0 ? -1 : std::strcmp(oenv, "first") == 0 ? 1 : 0;
     bool oda = false, oda_have = false;
-    double oda_shift = 0.0, oda_e0 = 0.0, oda_lam = 1.0;
+    double oda_e0 = 0.0, oda_lam = 1.0;
     int oda_full = 0;
     DBuf dPt, dPst[2], dJt, dKt[2], dFt[2], dD1, dD2;
     auto oda_alloc = [&]() {
@@ -802,14 +802,15 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       n_stable = estable ? n_stable + 1 : 0;
       // (the stable-energy fallback applies only under the default gradient
       // target; a caller-set diis_tol is a hard requirement)
-      // A slow monotone descent also passes the energy test (a rate rho of
-      // 0.97 with 5e-9 Eh steps leaves 1.6e-7 Eh to go), so the fallback
-      // also wants the remaining descent, extrapolated geometrically from
-      // the last two energy changes, below 1e-9 Eh; changes of alternating
-      // sign or growing size (the noise of a gradient floor) pass.
+      // A slow monotone descent also passes the energy test (2e-9 Eh steps
+      // at a rate near 1 stopped heavy fractional-occupation atoms 1.4e-7 Eh
+      // early), so the fallback also wants the remaining descent,
+      // extrapolated geometrically from the last two energy changes (rate
+      // capped at 0.999), below 1e-9 Eh; changes of alternating sign (the
+      // noise of a gradient floor) or below 1e-11 Eh pass.
       const double dE1 = Etot - Eold;
       double tail = 0.0;
-      if (it > 2 && dE1 * dEprev > 0.0 && std::fabs(dE1) < std::fabs(dEprev)) {
+      if (it > 2 && dE1 * dEprev > 0.0 && std::fabs(dE1) > 1e-11) {
         const double rho = std::min(0.999, dE1 / dEprev);
         tail = std::fabs(dE1) * rho / (1.0 - rho);
       }
@@ -827,8 +828,10 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       }
       if (oda) {
         if (emax < 1e-2 * oda_e0 || oda_full >= 2) {
+          // DIIS again without the shift (it slows the last digits down;
+          // the stabilisation ladder starts over if DIIS stalls again)
           oda = oda_have = false;
-          shift = oda_shift;
+          shift = 0.0;
           it_improved = it;
           emin = emax;
           nh = 0;
@@ -836,7 +839,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
           std::fill(Bm.begin(), Bm.end(), 0.0);
           if (verbose) std::fprintf(stderr, "hfg_scf it %3d ODA done, DIIS restart\n", it);
         }
-      } else if (emax > 1e-5 && it >= 12 && it - it_improved >= 6 && shift < 2.0) {
+      } else if (emax > std::max(1e-6, 10.0 * dtol) && it >= 12 && it - it_improved >= 6 && shift < 2.0) {
         shift = (shift == 0.0) ? 0.5 : 2.0;
         it_improved = it;
         emin = emax;
@@ -854,7 +857,6 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         oda_full = 0;
         oda_lam = 1.0;
         oda_e0 = emax;
-        oda_shift = shift;
         shift = 0.0;
         it_improved = it;
         emin = emax;

@@ -253,6 +253,17 @@ hfg_status hfg_xc_host(hfg_atom* atom, int x_func, int c_func, const double* Pa,
  * the orbital of eps[j] (zero outside its block's rows). C^T S C = 1. */
 hfg_status hfg_fock_diag(hfg_atom* atom, const double* F, int symmetry, double* C, double* eps, void* stream);
 
+/* J(PJ) and K(PK) on the device in one call (the Fock builder's pair of
+ * calls, src/atomic/main.cpp:424-443): the Coulomb build runs on a second
+ * stream of the handle, forked from `stream` after the work already queued
+ * there and joined back into it, concurrently with the exchange build on
+ * `stream`; when the call returns, work queued later on `stream` sees both
+ * results. flags: HFG_EXCHANGE_SYMMETRIC and HFG_EXCHANGE_SPLIT for K,
+ * HFG_COULOMB_SPLIT for J. PJ and PK may be the same pointer; J and K must
+ * not overlap. Calls on one handle must not overlap in time (the second
+ * stream and the scratch are per handle). */
+hfg_status hfg_jk(hfg_atom* atom, const double* PJ, const double* PK, double* J, double* K, int flags, void* stream);
+
 /* ---- host-pointer drop-ins (value semantics, synchronous) ---- */
 hfg_status hfg_coulomb_host(hfg_atom* atom, const double* P, double* J);
 hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);

@@ -307,3 +307,23 @@ def test_kr_full_size_split_coulomb_matches_oracle(kr_bench_case):
     assert np.isfinite(J).all() and err < SPLIT_TOL and dE < 1e-10
     Jh, _ = A.jk_host(P, symmetric=True, split=True, split_j=True)
     assert np.array_equal(Jh, J)
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_jk_device_entry_matches_separate_calls(split):
+    """hfg_jk (J on the handle's second stream, concurrent with K, joined back
+    into the caller's stream) gives the separate calls' J and K bit for bit,
+    for the same and for different J and K densities."""
+    torch = torch_cuda()
+    A, O = make_pair(*CASES[3])
+    P = random_density(O.nbf, 7, seed=31, S=O.S)
+    P2 = random_density(O.nbf, 5, seed=32, S=O.S)
+    Pd, P2d = to_dev(torch, P), to_dev(torch, P2)
+    for PK in (Pd, P2d):
+        J1, K1 = torch.full_like(Pd, np.nan), torch.full_like(Pd, np.nan)
+        A.coulomb(Pd, J1, split=split)
+        A.exchange(PK, K1, symmetric=True, split=split)
+        J2, K2 = torch.full_like(Pd, np.nan), torch.full_like(Pd, np.nan)
+        A.jk(Pd, J2, K2, PK=PK, symmetric=True, split=split, split_j=split)
+        torch.cuda.synchronize()
+        assert torch.equal(J1, J2) and torch.equal(K1, K2)
