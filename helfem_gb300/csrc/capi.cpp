@@ -276,7 +276,7 @@ hfg_status hfg_exchange_ex(hfg_atom* a, const double* P, double* K, int flags, v
         ck(cudaStreamSynchronize(a->own_stream), "sync");
       }
       ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof,
-                                    a->tc_for(false)),
+                                    a->tc_for(false), a->side_stream()),
          "exchange kernels (split)");
     } else {
       ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),
@@ -410,7 +410,8 @@ hfg_status hfg_jk(hfg_atom* a, const double* PJ, const double* PK, double* J, do
     // K on the caller's stream meanwhile
     const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
     if (split_k)
-      ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, PK, K, sym, st, &a->prof, a->tc_for(false)),
+      ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, PK, K, sym, st, &a->prof, a->tc_for(false),
+                                    a->side_stream()),
          "exchange kernels (split)");
     else
       ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, PK, K, sym, st, &a->prof), "exchange kernels");
@@ -449,7 +450,7 @@ hfg_status hfg_atom_autotune(hfg_atom* a, int flags, int* best_nsplit, double* b
       const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
       if (flags & HFG_EXCHANGE_SPLIT)
         ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, P.as<double>(), K.as<double>(), sym, st, nullptr,
-                                      a->tc_for(false)),
+                                      a->tc_for(false), a->side_stream()),
            "exchange");
       else
         ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, P.as<double>(), K.as<double>(), sym, st, nullptr),

@@ -202,8 +202,15 @@ cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KU
                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr);
 // split-precision exchange (float-float on the FP32 pipe, FP64 recombination)
 // tc != nullptr: the off-diagonal element pairs run on the tensor cores (k_tc.cu)
+// a second stream with a fork and a join event (owned by the caller)
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+// side (tensor-core form only): the diagonal tiles run on side->s,
+// concurrently with the off-diagonal ones, joined back before the fix-up
 cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
                                   double* K, bool symmetric, cudaStream_t st, Profiler* prof = nullptr,
-                                  const DevTC* tc = nullptr);
+                                  const DevTC* tc = nullptr, const SideStream* side = nullptr);
 
 }  // namespace hfg

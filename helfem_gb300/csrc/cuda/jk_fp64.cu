@@ -316,20 +316,22 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   float sf = 0.f;
   // the band's elements in column order (32-bit index arithmetic); four
   // loads in flight per thread (one at a time left the pass latency-bound
-  // at half the HBM rate), summed in the same order as one at a time
+  // at half the HBM rate; eight measured the same as four), summed in the
+  // same order as one at a time
+  constexpr int NU = 4;
   const int n = A.nrad * (c1 - c0), bd = blockDim.x;
-  for (int base = threadIdx.x; base < n; base += 4 * bd) {
-    double v[4];
-    size_t o[4];
+  for (int base = threadIdx.x; base < n; base += NU * bd) {
+    double v[NU];
+    size_t o[NU];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < NU; ++u) {
       const int idx = base + u * bd;
       const int r = idx % A.nrad, c = c0 + idx / A.nrad;
       o[u] = (size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r;
       v[u] = idx < n ? P[o[u]] : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < NU; ++u) {
       if (base + u * bd >= n) break;
       if (p2) {
         // split path: integer-only split (no FP64-pipe instructions) and an
@@ -729,7 +731,8 @@ cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KU
 }
 
 cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
-                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof, const DevTC* tc) {
+                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof, const DevTC* tc,
+                                  const SideStream* side) {
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
@@ -742,10 +745,22 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
     int nunits = symmetric ? U.n_sym : U.n_all;
     const int4* units = symmetric ? U.sym : U.all;
     if (tc) {
-      // every element pair on the tensor cores: the off-diagonal tiles, then
+      // every element pair on the tensor cores: the off-diagonal tiles and
       // the diagonal ones through the exchange-ordered tensor
-      cudaError_t e = launch_k_tiles_tc(A, S, *tc, symmetric, K, st);
-      if (e == cudaSuccess) e = launch_k_diag_tc(A, S, *tc, symmetric, K, st);
+      cudaError_t e = cudaSuccess;
+      if (side && side->s) {
+        // the diagonal stage (a chain of dependent steps in 0.8 of a wave)
+        // beside the issue-bound off-diagonal tiles, joined before the fix-up
+        e = cudaEventRecord(side->fork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side->s, side->fork, 0);
+        if (e == cudaSuccess) e = launch_k_diag_tc(A, S, *tc, symmetric, K, side->s);
+        if (e == cudaSuccess) e = cudaEventRecord(side->join, side->s);
+        if (e == cudaSuccess) e = launch_k_tiles_tc(A, S, *tc, symmetric, K, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, side->join, 0);
+      } else {
+        e = launch_k_tiles_tc(A, S, *tc, symmetric, K, st);
+        if (e == cudaSuccess) e = launch_k_diag_tc(A, S, *tc, symmetric, K, st);
+      }
       if (e != cudaSuccess) return e;
       nunits = 0;
     }

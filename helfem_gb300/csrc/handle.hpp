@@ -381,6 +381,16 @@ struct hfg_atom {
   // build is forked from the caller's stream and joined back into it
   cudaStream_t j_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // side stream of the split exchange (its diagonal stage), made on first use
+  hfg::SideStream k_side{};
+  const hfg::SideStream* side_stream() {
+    if (!k_side.s) {
+      ck(cudaStreamCreateWithFlags(&k_side.s, cudaStreamNonBlocking), "cudaStreamCreate");
+      ck(cudaEventCreateWithFlags(&k_side.fork, cudaEventDisableTiming), "cudaEventCreate");
+      ck(cudaEventCreateWithFlags(&k_side.join, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    return &k_side;
+  }
   // Yukawa-screened exchange: the exchange context with the screened radial
   // tables (built by hfg_atom_compute_yukawa)
   hfg::DevAtom dev_rs{};
@@ -432,6 +442,12 @@ struct hfg_atom {
 
   ~hfg_atom() {
     if (ev_j) cudaEventDestroy(ev_j);
+    if (k_side.fork) cudaEventDestroy(k_side.fork);
+    if (k_side.join) cudaEventDestroy(k_side.join);
+    if (k_side.s) {
+      cudaStreamSynchronize(k_side.s);
+      cudaStreamDestroy(k_side.s);
+    }
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (j_stream) {
