@@ -308,7 +308,8 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
       a->scr.p2 = a->s_p2.as<float2>();
     }
     ck(hfg::launch_exchange_split(ctx, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
-                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof, a->tc_for(screened)),
+                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof, a->tc_for(screened),
+                                  a->side_stream()),
        "exchange (split)");
   } else {
     ck(hfg::launch_exchange_fp64(ctx, a->scr, a->units, a->h_in.as<double>(), a->h_out.as<double>(),
@@ -365,7 +366,8 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
       a->scr.p2 = a->s_p2.as<float2>();
     }
     ck(hfg::launch_exchange_split(a->dev, a->scr, a->units, Pk, a->h_out2.as<double>(),
-                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof, a->tc_for(false)),
+                                  (flags & HFG_EXCHANGE_SYMMETRIC) != 0, st, &a->prof, a->tc_for(false),
+                                  a->side_stream()),
        "exchange (split)");
   } else {
     ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, Pk, a->h_out2.as<double>(),
@@ -554,7 +556,7 @@ hfg_status hfg_rs_exchange(hfg_atom* a, const double* P, double* K, int flags, v
         a->scr.p2 = a->s_p2.as<float2>();
       }
       ck(hfg::launch_exchange_split(a->dev_rs, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof,
-                                    a->tc_for(true)),
+                                    a->tc_for(true), a->side_stream()),
          "screened exchange (split)");
     } else {
       ck(hfg::launch_exchange_fp64(a->dev_rs, a->scr, a->units, P, K, sym, (cudaStream_t)stream, &a->prof),

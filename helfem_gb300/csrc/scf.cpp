@@ -672,7 +672,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         for (int s = 0; s < nspin; ++s) {
           if (d->split_exchange)
             ck(hfg::launch_exchange_split(a->dev, scr_split, a->units, dPs[s].as<double>(), dK[s].as<double>(), true,
-                                          st, &a->prof, a->tc_for(false)),
+                                          st, &a->prof, a->tc_for(false), a->side_stream()),
                "K (split)");
           else
             ck(hfg::launch_exchange_fp64(a->dev, a->scr, a->units, dPs[s].as<double>(), dK[s].as<double>(), true,
