@@ -631,21 +631,22 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     double emin = 1e300;
     int it_improved = 0;
     // optimal damping (ODA; E. Cances and C. Le Bris, Int. J. Quantum Chem.
-    // 79, 82 (2000)) for Hartree-Fock runs that still stall under the full
-    // level shift: the next density is the minimum of the energy on the
-    // segment between the damped density P~ and the Aufbau density P of
-    // F(P~). For HF the energy is quadratic on that segment,
-    //   E(lam) = E(P~) + lam s + lam^2 c / 2,
-    //   s = sum_s tr(F~_s dP_s),  c = sum_s tr((dJ + dK_s) dP_s),
-    // and J, K are linear in P, so the damped J and K are mixed like P with no
-    // second build. The level shift is off while ODA runs; the run goes back to
-    // DIIS (fresh history, no shift) once the gradient has fallen by 100x or
-    // the full step is optimal twice in a row.
+    // 79, 82 (2000)) for runs that still stall under the full level shift:
+    // the next density is the minimum of the energy on the segment between
+    // the damped density P~ and the Aufbau density P of F(P~),
+    //   E(lam) = E(P~) + lam s + lam^2 c / 2,  s = sum_s tr(F~_s dP_s).
+    // For HF the energy is exactly quadratic there, c = sum_s tr((dJ + dK_s)
+    // dP_s), and J, K are linear in P, so the damped J and K are mixed like P
+    // with no second build. With an XC functional c comes from the energy at
+    // P (the fit through E(0), E'(0) and E(1)) and the XC potential is
+    // evaluated again at the damped density. The level shift is off while
+    // ODA runs; the run goes back to DIIS (fresh history, no shift) once the
+    // gradient has fallen by 100x or the full step is optimal twice in a row.
     // HFG_SCF_ODA=0 turns it off; =first starts it at the first iteration
     const char* oenv = std::getenv("HFG_SCF_ODA");
     const int oda_mode = !oenv ? 0 : std::strcmp(oenv, "0") == 0 ? -1 : std::strcmp(oenv, "first") == 0 ? 1 : 0;
     bool oda = false, oda_have = false;
-    double oda_e0 = 0.0, oda_lam = 1.0;
+    double oda_e0 = 0.0, oda_lam = 1.0, oda_Eref = 0.0;  // gradient at the start; E(P~)
     int oda_full = 0;
     DBuf dPt, dPst[2], dJt, dKt[2], dFt[2], dD1, dD2;
     auto oda_alloc = [&]() {
@@ -659,6 +660,28 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         dFt[s].alloc(sizeof(double) * nb2);
         if (kfrac != 0.0) dKt[s].alloc(sizeof(double) * nb2);
       }
+    };
+    auto run_xc = [&]() {
+      ck(hfg::launch_xc_fp64(a->dev, a->xc, a->xs, d->x_func, d->c_func,
+                             restricted ? dP.as<double>() : dPs[0].as<double>(),
+                             restricted ? nullptr : dPs[1].as<double>(), dXC[0].as<double>(),
+                             restricted ? nullptr : dXC[1].as<double>(), dE.as<double>(), thr, st),
+         "XC");
+    };
+    // total energy of the current P, J, K (scaled) and XC buffers
+    auto energy_now = [&]() {
+      double e = dot(dP.as<double>(), T) + dot(dP.as<double>(), V) + 0.5 * dot(dP.as<double>(), dJ.as<double>());
+      if (kfrac != 0.0) {
+        const double x0 = 0.5 * dot(dPs[0].as<double>(), dK[0].as<double>());
+        e += restricted ? 2.0 * x0 : x0 + 0.5 * dot(dPs[1].as<double>(), dK[1].as<double>());
+      }
+      if (have_xc) {
+        double ex[2];
+        ck(cudaMemcpyAsync(ex, dE.p, sizeof(ex), cudaMemcpyDeviceToHost, st), "D2H");
+        ck(cudaStreamSynchronize(st), "sync");
+        e += ex[0];
+      }
+      return e;
     };
     auto copy_d = [&](DBuf& to, const DBuf& from) {
       ck(cudaMemcpyAsync(to.p, from.p, sizeof(double) * nb2, cudaMemcpyDeviceToDevice, st), "copy");
@@ -679,12 +702,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
                                          st, &a->prof),
                "K");
         }
-      if (have_xc)
-        ck(hfg::launch_xc_fp64(a->dev, a->xc, a->xs, d->x_func, d->c_func,
-                               restricted ? dP.as<double>() : dPs[0].as<double>(),
-                               restricted ? nullptr : dPs[1].as<double>(), dXC[0].as<double>(),
-                               restricted ? nullptr : dXC[1].as<double>(), dE.as<double>(), thr, st),
-           "XC");
+      if (have_xc) run_xc();
       for (int s = 0; s < nspin; ++s)
         if (kfrac != 0.0 && kfrac != 1.0) {
           cb(cublasDscal(hd.bl, (int)nb2, &kfrac, dK[s].as<double>(), 1), "scal K");
@@ -704,6 +722,13 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
           s1 += dot(dFt[s].as<double>(), dD1.as<double>());
           c2 += dot(dD2.as<double>(), dD1.as<double>());
         }
+        if (have_xc) {
+          // the XC energy is not quadratic on the segment: the curvature
+          // comes from the energy at the Aufbau density, E(1) = E(P~) + s +
+          // c / 2, and the XC potential is recomputed at the damped density
+          const double E1 = energy_now();
+          c2 = 2.0 * (E1 - oda_Eref - s1);
+        }
         double lam = 1.0;
         if (c2 > 0.0) lam = std::min(1.0, std::max(0.0, -s1 / c2));
         else if (s1 > 0.0) lam = 0.0;  // uphill and concave: cannot happen for an Aufbau step; keep P~
@@ -717,6 +742,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
             hfg::k_lerp(dPs[s].as<double>(), dPst[s].as<double>(), lam, nb2, st);
             if (kfrac != 0.0) hfg::k_lerp(dK[s].as<double>(), dKt[s].as<double>(), lam, nb2, st);
           }
+          if (have_xc) run_xc();
         }
       }
       for (int s = 0; s < nspin; ++s)
@@ -750,6 +776,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         Ngrid = e[1];
       }
       Etot = Ekin + Enuc + Ecoul + Exx + Exc;
+      if (oda) oda_Eref = Etot;  // the energy of the state that becomes P~
       pt.lap(1);  // energies
 
       // ---- Fock blocks and DIIS errors F'D' - D'F' (orthonormal basis) ----
@@ -847,7 +874,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         wcur = 0;
         std::fill(Bm.begin(), Bm.end(), 0.0);
         if (verbose) std::fprintf(stderr, "hfg_scf it %3d level shift %.2f, DIIS restart\n", it, shift);
-      } else if (!have_xc && oda_mode >= 0 && emax > 10.0 * dtol &&
+      } else if (oda_mode >= 0 && emax > 10.0 * dtol &&
                  ((shift >= 2.0 && it - it_improved >= 10) || (oda_mode == 1 && it == 1))) {
         // still stalled under the full shift (the gradient has not halved in
         // ten iterations): optimal damping from the current (Aufbau) density
@@ -857,6 +884,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
         oda_full = 0;
         oda_lam = 1.0;
         oda_e0 = emax;
+        oda_Eref = Etot;
         shift = 0.0;
         it_improved = it;
         emin = emax;

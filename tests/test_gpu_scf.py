@@ -50,13 +50,16 @@ def test_gpu_scf_matches_reference_energy(name):
 
 
 @pytest.mark.parametrize("name,damped", [("atomic-Ne-hf-r", True), ("atomic-O-3P-p0-hf", True),
-                                         ("atomic-Be-hf-r", False)])
+                                         ("atomic-Be-hf-r", False), ("atomic-Be-lda-u", None),
+                                         ("atomic-He-gga-u", None)])
 def test_optimal_damping_reaches_reference_energy(name, damped, monkeypatch, capfd):
     """Optimal damping (ODA) started at the first iteration (it otherwise
     starts only when DIIS stalls under the full level shift): the line-search
     steps, then DIIS, reach the reference's energy at 1e-8 Eh. Ne and O take
     at least one damped step (lambda < 1); for Be the full Roothaan step is
-    optimal from the core guess on, and two full steps end the damping."""
+    optimal from the core guess on, and two full steps end the damping. The
+    LDA and GGA runs take the curvature from the energy at the Aufbau
+    density and evaluate the XC potential again at each damped density."""
     torch_cuda()
     monkeypatch.setenv("HFG_SCF_ODA", "first")
     monkeypatch.setenv("HFG_SCF_VERBOSE", "1")
@@ -65,7 +68,8 @@ def test_optimal_damping_reaches_reference_energy(name, damped, monkeypatch, cap
     lams = [float(l.split("lambda")[1]) for l in err.splitlines() if "ODA s" in l]
     print("ODA lambdas", lams)
     assert lams, err[-2000:]
-    assert (min(lams) < 1.0) == damped, lams
+    if damped is not None:
+        assert (min(lams) < 1.0) == damped, lams
     assert r["converged"], r
     assert abs(r["Etot"] - CI[name]["total"]) < 1e-8, (r["Etot"], CI[name]["total"])
 
