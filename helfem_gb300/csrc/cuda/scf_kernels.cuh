@@ -18,6 +18,13 @@ void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cud
 // out = (a1 - b1) + (a2 - b2) (a2, b2 may be null)
 void k_diffsum(double* out, const double* a1, const double* b1, const double* a2, const double* b2, size_t n,
                cudaStream_t st);
+// banded shift-invert Olsen corrections (band_precond.cu): for each of the u
+// columns, y = M^-1 zr - eps M^-1 zx with M = band_w(F) - theta S (n x n
+// column-major F and S, half-width w <= 16), eps = (zx . M^-1 zr) / (zx . M^-1 zx);
+// work holds band_olsen_work_floats(n, w, u) floats
+size_t band_olsen_work_floats(int n, int w, int u);
+cudaError_t k_band_olsen(const double* F, const double* S, int n, int w, const double* theta, const double* Zr,
+                         const double* Zx, double* Y, float* work, int u, cudaStream_t st);
 // out = a + lam (out - a)
 void k_lerp(double* out, const double* a, double lam, size_t n, cudaStream_t st);
 // symmetric n x n test density with every entry nonzero (deterministic)

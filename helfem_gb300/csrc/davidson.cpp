@@ -121,7 +121,7 @@ int append_orthonormal(cublasHandle_t bl, cudaStream_t st, int n, double* Q, int
 
 int davidson_lowest(cublasHandle_t bl, cudaStream_t st, const BlockOperator& apply, int n, int k, int kconv,
                     double* V, const double* Vr, const double* lam, std::vector<double>& theta, DavidsonWork& w,
-                    int maxit, double tol) {
+                    int maxit, double tol, const Preconditioner* pc) {
   const double one = 1.0, zero = 0.0;
   k = std::min(k, n);
   kconv = std::min(kconv, k);
@@ -193,12 +193,18 @@ int davidson_lowest(cublasHandle_t bl, cudaStream_t st, const BlockOperator& app
     }
     double* thd = w.th.as<double>() + k;
     ck(cudaMemcpyAsync(thd, thU.data(), sizeof(double) * u, cudaMemcpyHostToDevice, st), "H2D theta U");
-    // corrections in the reference eigenbasis, then back: T = Vr Zt
-    cbl(cublasDgemm(bl, CUBLAS_OP_T, CUBLAS_OP_N, n, u, n, &one, Vr, n, Rg, n, &zero, w.Zr.as<double>(), n), "Vr^T R");
-    cbl(cublasDgemm(bl, CUBLAS_OP_T, CUBLAS_OP_N, n, u, n, &one, Vr, n, Xg, n, &zero, w.Zx.as<double>(), n), "Vr^T X");
-    const double floor_ = 1e-8 * std::max(1.0, std::fabs(thU.empty() ? 0.0 : thU[0]));
-    k_dav_olsen(w.Zr.as<double>(), w.Zx.as<double>(), lam, thd, n, u, floor_, Rg, st);
-    cbl(cublasDgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, n, u, n, &one, Vr, n, Rg, n, &zero, T, n), "Vr Zt");
+    if (pc) {
+      (*pc)(Rg, Xg, thd, u, T);
+    } else {
+      // corrections in the reference eigenbasis, then back: T = Vr Zt
+      cbl(cublasDgemm(bl, CUBLAS_OP_T, CUBLAS_OP_N, n, u, n, &one, Vr, n, Rg, n, &zero, w.Zr.as<double>(), n),
+          "Vr^T R");
+      cbl(cublasDgemm(bl, CUBLAS_OP_T, CUBLAS_OP_N, n, u, n, &one, Vr, n, Xg, n, &zero, w.Zx.as<double>(), n),
+          "Vr^T X");
+      const double floor_ = 1e-8 * std::max(1.0, std::fabs(thU.empty() ? 0.0 : thU[0]));
+      k_dav_olsen(w.Zr.as<double>(), w.Zx.as<double>(), lam, thd, n, u, floor_, Rg, st);
+      cbl(cublasDgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, n, u, n, &one, Vr, n, Rg, n, &zero, T, n), "Vr Zt");
+    }
     mo = m;
     m = append_orthonormal(bl, st, n, Q, m, T, u, w);
     if (m == mo) break;  // no new directions

@@ -34,16 +34,21 @@ struct DavidsonWork {
 
 // apply(Q, c, AQ): AQ = F Q for c columns (device, leading dimension n)
 using BlockOperator = std::function<void(const double* Q, int cols, double* AQ)>;
+// precond(R, X, theta, u, T): the u correction vectors T (device, leading
+// dimension n) from the residuals R and Ritz vectors X and the Ritz values
+// theta (device); T may alias X
+using Preconditioner = std::function<void(const double* R, const double* X, const double* theta, int u, double* T)>;
 
 // Lowest k eigenpairs of the symmetric n x n operator F (applied by `apply`)
 // from the k starting columns in V (device, leading dimension n; overwritten
 // with the eigenvectors on success); theta (host) receives the eigenvalues.
-// Vr (device, n x n) and lam (device, n) are the reference eigenpairs.
+// Vr (device, n x n) and lam (device, n) are the reference eigenpairs; a
+// non-null pc replaces the reference-eigenbasis correction.
 // Converged when the residual norms |F x - theta x| of the first kconv pairs
 // are <= tol (absolute). Returns the number of iterations, or -1 when not
 // converged within maxit (V is then unchanged).
 int davidson_lowest(cublasHandle_t bl, cudaStream_t st, const BlockOperator& apply, int n, int k, int kconv,
                     double* V, const double* Vr, const double* lam, std::vector<double>& theta, DavidsonWork& w,
-                    int maxit, double tol);
+                    int maxit, double tol, const Preconditioner* pc = nullptr);
 
 }  // namespace hfg

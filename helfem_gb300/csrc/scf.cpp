@@ -452,8 +452,27 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     // sets the number of full solves before the refinement starts.
     const char* eenv = std::getenv("HFG_SCF_EIGENSOLVER");
     const bool use_davidson = !(eenv && std::strcmp(eenv, "full") == 0);
-    const char* nenv = std::getenv("HFG_SCF_NFULL");  // full solves before refinement (default 3)
-    const int n_full_first = (nenv && std::atoi(nenv) > 0) ? std::atoi(nenv) : 3;
+    // Preconditioner of the refinement for blocks of one angular function
+    // (the spherical, per-(l,m) solves): the banded shift-invert form
+    // (S X)^T (band(F_k) - theta S)^-1 (S X) from the current Fock block, so
+    // that refinement can start right after the core-Hamiltonian solve; other
+    // blocks use the eigenbasis of their last full solve.
+    // HFG_SCF_PRECOND=reference uses the eigenbasis form everywhere.
+    const char* penv = std::getenv("HFG_SCF_PRECOND");
+    const bool band_ok = !(penv && std::strcmp(penv, "reference") == 0) && H.rad.nn - 1 <= 16;
+    bool all_single = true;
+    for (const Block& b : blocks) all_single = all_single && b.ang.size() == 1;
+    const bool banded = band_ok && all_single;
+    const char* nenv = std::getenv("HFG_SCF_NFULL");  // full solves before refinement (default 3; 1 when banded)
+    const int n_full_first = (nenv && std::atoi(nenv) > 0) ? std::atoi(nenv) : (banded ? 1 : 3);
+    DBuf dSrad, dSX, dZr, dZx, dYt, dBandWork;
+    if (banded) {
+      dSrad.upload(H.Srad);
+      dSX.alloc(sizeof(double) * nr2);
+      cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, nrad, nrad, nrad, &one, dSrad.as<double>(), nrad,
+                     dX.as<double>(), nrad, &zero, dSX.as<double>(), nrad),
+         "S X");
+    }
     DBuf dVref, dLam, dFx;
     dVref.alloc(sizeof(double) * Ltot);
     dLam.alloc(sizeof(double) * (size_t)nbf * nspin);
@@ -540,11 +559,35 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
               }
             }
           };
+          // banded shift-invert corrections (one angular function: nk = nrad)
+          const hfg::Preconditioner pc = [&](const double* Rg, const double* Xg, const double* thd, int u,
+                                             double* Tout) {
+            const int n = b.nk, wb = H.rad.nn - 1;
+            const size_t need = sizeof(double) * (size_t)n * u;
+            if (dZr.n < need) dZr.alloc(need);
+            if (dZx.n < need) dZx.alloc(need);
+            if (dYt.n < need) dYt.alloc(need);
+            const size_t wf = hfg::band_olsen_work_floats(n, wb, u) * sizeof(float);
+            if (dBandWork.n < wf) dBandWork.alloc(wf);
+            cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, n, u, n, &one, dSX.as<double>(), n, Rg, n, &zero,
+                           dZr.as<double>(), n),
+               "S X r");
+            cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_N, n, u, n, &one, dSX.as<double>(), n, Xg, n, &zero,
+                           dZx.as<double>(), n),
+               "S X x");
+            ck(hfg::k_band_olsen(Fk, dSrad.as<double>(), n, wb, thd, dZr.as<double>(), dZx.as<double>(),
+                                 dYt.as<double>(), dBandWork.as<float>(), u, st),
+               "banded corrections");
+            cb(cublasDgemm(hd.bl, CUBLAS_OP_T, CUBLAS_OP_N, n, u, n, &one, dSX.as<double>(), n, dYt.as<double>(), n,
+                           &zero, Tout, n),
+               "(S X)^T y");
+          };
           std::vector<double> th;
           const double t0 = verbose ? wall_ms() : 0.0;
           const int itd = hfg::davidson_lowest(hd.bl, st, apply, b.nk, kk, kconv, V,
                                                dVref.as<double>() + Lblk * s + b.off,
-                                               dLam.as<double>() + (size_t)nbf * s + eoff[k], th, dav, 12, dav_tol);
+                                               dLam.as<double>() + (size_t)nbf * s + eoff[k], th, dav, 12, dav_tol,
+                                               banded ? &pc : nullptr);
           if (verbose) ms_refine += wall_ms() - t0;
           if (itd < 0) {
             f = true;
@@ -552,7 +595,7 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
           } else {
             ++dav_solves;
             dav_iters += itd;
-            want_full[key] = itd >= 6;
+            want_full[key] = itd >= (banded ? 10 : 6);
             partial = true;
             // the kk Ritz values; the rest out of reach of the Aufbau order
             std::vector<double> ev(b.nk, 1e300);
