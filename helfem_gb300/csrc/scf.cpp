@@ -452,14 +452,15 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
     // sets the number of full solves before the refinement starts.
     const char* eenv = std::getenv("HFG_SCF_EIGENSOLVER");
     const bool use_davidson = !(eenv && std::strcmp(eenv, "full") == 0);
-    // Preconditioner of the refinement for blocks of one angular function
-    // (the spherical, per-(l,m) solves): the banded shift-invert form
-    // (S X)^T (band(F_k) - theta S)^-1 (S X) from the current Fock block, so
-    // that refinement can start right after the core-Hamiltonian solve; other
-    // blocks use the eigenbasis of their last full solve.
-    // HFG_SCF_PRECOND=reference uses the eigenbasis form everywhere.
+    // Preconditioner of the refinement: the eigenbasis of the block's last
+    // full solve. HFG_SCF_PRECOND=banded selects, for runs whose blocks all
+    // have one angular function (the spherical, per-(l,m) solves), the banded
+    // shift-invert form (S X)^T (band(F_k) - theta S)^-1 (S X) from the
+    // current Fock block, with refinement from the second iteration on
+    // (measured slower on the batch atoms: the same iteration counts, more
+    // fall-backs, and a serial banded solve per Ritz value).
     const char* penv = std::getenv("HFG_SCF_PRECOND");
-    const bool band_ok = !(penv && std::strcmp(penv, "reference") == 0) && H.rad.nn - 1 <= 16;
+    const bool band_ok = penv && std::strcmp(penv, "banded") == 0 && H.rad.nn - 1 <= 16;
     bool all_single = true;
     for (const Block& b : blocks) all_single = all_single && b.ang.size() == 1;
     const bool banded = band_ok && all_single;

@@ -247,3 +247,12 @@ def test_davidson_refinement_matches_full_eigensolves(case, monkeypatch):
     assert np.abs(ef - ed).max() < 1e-6 * max(1.0, np.abs(ef).max() / 1e3)
     # the refinement is what the default path runs: it must be cheaper
     assert d["phase_ms"]["eigh_occupy"] < f["phase_ms"]["eigh_occupy"]
+    if case.endswith("spherical"):
+        # the opt-in banded shift-invert preconditioner (refinement from the
+        # second iteration on) reaches the same solution
+        monkeypatch.setenv("HFG_SCF_EIGENSOLVER", "davidson")
+        monkeypatch.setenv("HFG_SCF_PRECOND", "banded")
+        b = atom.scf(*nel, method=method, restricted=True, **kw)
+        assert b["converged"] and abs(b["Etot"] - f["Etot"]) < 1e-8, (b["Etot"], f["Etot"])
+        eb = np.sort(b["orbital_energies"])
+        assert np.abs(ef - eb).max() < 1e-6 * max(1.0, np.abs(ef).max() / 1e3)
