@@ -97,6 +97,7 @@ _SIGS = {
     "hfg_engine_stats": ([_P, _I, _I, _D], ctypes.c_int),
     "hfg_engine_destroy": ([_P], ctypes.c_int),
     "hfg_profile_enable": ([_P, ctypes.c_int], ctypes.c_int),
+    "hfg_profile_classes": ([_P, ctypes.c_uint], ctypes.c_int),
     "hfg_profile_read": ([_P, _P, ctypes.c_int], ctypes.c_int),
     "hfg_diatomic_create": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
     "hfg_diatomic_destroy": ([_P], ctypes.c_int),
@@ -417,6 +418,11 @@ class Atom:
     # ---- per-kernel timing ----
     def profile_enable(self, capacity: int = 4096):
         _check(_lib.hfg_profile_enable(self._h, capacity))
+
+    def profile_classes(self, names=None):
+        """Bracket only these kernel classes (names from KERNEL_CLASSES; None: all)."""
+        mask = 0xFFFFFFFF if names is None else sum(1 << KERNEL_CLASSES.index(n) for n in names)
+        _check(_lib.hfg_profile_classes(self._h, mask))
 
     def profile_read(self, reset: bool = True) -> dict:
         pr = _Prof()

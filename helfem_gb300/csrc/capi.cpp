@@ -712,6 +712,13 @@ hfg_status hfg_profile_enable(hfg_atom* a, int capacity) {
   });
 }
 
+hfg_status hfg_profile_classes(hfg_atom* a, unsigned mask) {
+  return guard([&] {
+    need(a != nullptr, "hfg_profile_classes: null argument");
+    a->prof.mask = mask;
+  });
+}
+
 hfg_status hfg_profile_read(hfg_atom* a, hfg_profile_t* out, int reset) {
   return guard([&] {
     need(a != nullptr && out != nullptr, "hfg_profile_read: null argument");

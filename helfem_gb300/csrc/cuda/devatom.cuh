@@ -141,6 +141,7 @@ __device__ __forceinline__ void k_store_tile(const DevAtom& A, const DevScratch&
 enum KernelClass { KC_J_CONTRACT = 0, KC_J_SCATTER, KC_K_NORMS, KC_K_TILES, KC_K_FIXUP, KC_COUNT };
 struct Profiler {
   bool on = false;
+  unsigned mask = ~0u;  // classes that are bracketed (bit KC_*)
   int cap = 0, n = 0;
   cudaEvent_t* ev = nullptr;  // [2*cap]
   int* cls = nullptr;         // [cap]

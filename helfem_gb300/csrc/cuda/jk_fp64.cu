@@ -652,7 +652,7 @@ struct Mark {
   int slot = -1;
   cudaStream_t s;
   Mark(Profiler* p_, int k, cudaStream_t s_) : p(p_), s(s_) {
-    if (p && p->on && p->n < p->cap) {
+    if (p && p->on && ((p->mask >> k) & 1u) && p->n < p->cap) {
       slot = p->n++;
       p->cls[slot] = k;
       cudaEventRecord(p->ev[2 * slot], s);

@@ -396,6 +396,10 @@ typedef struct {
   double ms[HFG_NUM_KERNEL_CLASSES];
 } hfg_profile_t;
 hfg_status hfg_profile_enable(hfg_atom* atom, int capacity);
+/* Only the kernel classes whose bit (1 << class, the hfg_profile_t order) is
+ * set in mask are bracketed from now on (default: all); fewer events on the
+ * stream between the launches of a timed region. */
+hfg_status hfg_profile_classes(hfg_atom* atom, unsigned mask);
 hfg_status hfg_profile_read(hfg_atom* atom, hfg_profile_t* out, int reset);
 
 /* ======================================================================
