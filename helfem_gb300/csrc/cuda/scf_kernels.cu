@@ -169,6 +169,40 @@ __global__ void lerp(double* out, const double* a, double lam, size_t n) {
 }
 }  // namespace
 
+namespace {
+// T and V of the AO basis from the radial blocks: only the diagonal angular
+// blocks are nonzero (the caller zeroes the rest)
+__global__ void expand_one_electron(const double* __restrict__ Trad, const double* __restrict__ Tlrad,
+                                    const double* __restrict__ Vrad, const int* __restrict__ lval, int nang,
+                                    int nrad, double Z, double* __restrict__ T, double* __restrict__ V) {
+  const size_t nr2 = (size_t)nrad * nrad, nbf = (size_t)nang * nrad, tot = nr2 * nang;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+    const int ia = (int)(idx / nr2);
+    const size_t q = idx % nr2;
+    const size_t r = q % nrad, c = q / nrad;
+    const double lf = (double)lval[ia] * (lval[ia] + 1);
+    const size_t o = ((size_t)ia * nrad + c) * nbf + (size_t)ia * nrad + r;
+    T[o] = Trad[q] + lf * Tlrad[q];
+    V[o] = -Z * Vrad[q];
+  }
+}
+// Y[r + c n] = d[r] X[r + c n]
+__global__ void scale_rows(double* __restrict__ X, int n, int m, const double* __restrict__ d) {
+  const size_t nn = (size_t)n * m;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < nn; idx += (size_t)gridDim.x * blockDim.x)
+    X[idx] *= d[idx % n];
+}
+}  // namespace
+
+void k_expand_one_electron(const double* Trad, const double* Tlrad, const double* Vrad, const int* lval, int nang,
+                           int nrad, double Z, double* T, double* V, cudaStream_t st) {
+  const size_t tot = (size_t)nrad * nrad * nang;
+  expand_one_electron<<<grid_for(tot), 256, 0, st>>>(Trad, Tlrad, Vrad, lval, nang, nrad, Z, T, V);
+}
+void k_scale_rows(double* X, int n, int m, const double* d, cudaStream_t st) {
+  scale_rows<<<grid_for((size_t)n * m), 256, 0, st>>>(X, n, m, d);
+}
+
 void k_diffsum(double* out, const double* a1, const double* b1, const double* a2, const double* b2, size_t n,
                cudaStream_t st) {
   diffsum<<<grid_for(n), 256, 0, st>>>(out, a1, b1, a2, b2, n);

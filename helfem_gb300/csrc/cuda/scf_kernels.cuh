@@ -15,6 +15,12 @@ void k_antisym(const double* G, int n, double* E, cudaStream_t st);
 void k_add4(double* out, const double* a, const double* b, const double* c, const double* d, size_t n,
             cudaStream_t st);
 void k_scale_cols(const double* X, int n, int m, const double* s, double* Y, cudaStream_t st);
+// T, V (nbf x nbf, zeroed by the caller) from the radial blocks:
+// T = Trad + l(l+1) Tlrad, V = -Z Vrad on the diagonal angular blocks
+void k_expand_one_electron(const double* Trad, const double* Tlrad, const double* Vrad, const int* lval, int nang,
+                           int nrad, double Z, double* T, double* V, cudaStream_t st);
+// X (n x m) rows scaled by d (length n), in place
+void k_scale_rows(double* X, int n, int m, const double* d, cudaStream_t st);
 // out = (a1 - b1) + (a2 - b2) (a2, b2 may be null)
 void k_diffsum(double* out, const double* a1, const double* b1, const double* a2, const double* b2, size_t n,
                cudaStream_t st);

@@ -170,43 +170,46 @@ void hfg_scf_impl(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_result* res, doubl
       dw.alloc(sizeof(double) * nrad);
       Eigh eg;
       eg.run(hd.so, Sd, nrad, dw.as<double>());
-      std::vector<double> U(nr2), lam(nrad);
-      ck(cudaMemcpyAsync(U.data(), Sd, sizeof(double) * nr2, cudaMemcpyDeviceToHost, st), "D2H");
+      std::vector<double> lam(nrad);
       ck(cudaMemcpyAsync(lam.data(), dw.p, sizeof(double) * nrad, cudaMemcpyDeviceToHost, st), "D2H");
       ck(cudaStreamSynchronize(st), "sync");
       need(lam[0] > 0, "hfg_scf_run: overlap matrix is not positive definite");
-      std::vector<double> X(nr2, 0.0), Ul(nr2);
-      for (int k = 0; k < nrad; ++k) {
-        const double f = 1.0 / std::sqrt(lam[k]);
-        for (int r = 0; r < nrad; ++r) Ul[r + (size_t)k * nrad] = U[r + (size_t)k * nrad] * f;
-      }
-      // X = diag(dn) U diag(lam^-1/2) U^T, formed on the host (nrad^3, once)
-      for (int c = 0; c < nrad; ++c)
-        for (int k = 0; k < nrad; ++k) {
-          const double u = U[c + (size_t)k * nrad];
-          for (int r = 0; r < nrad; ++r) X[r + (size_t)c * nrad] += Ul[r + (size_t)k * nrad] * u;
-        }
-      for (int c = 0; c < nrad; ++c)
-        for (int r = 0; r < nrad; ++r) X[r + (size_t)c * nrad] *= dn[r];
-      dX.upload(X);
+      // X = diag(dn) U diag(lam^-1/2) U^T on the device (one DGEMM)
+      const double one_ = 1.0, zero_ = 0.0;
+      std::vector<double> f(nrad);
+      for (int k = 0; k < nrad; ++k) f[k] = 1.0 / std::sqrt(lam[k]);
+      DBuf df, ddn, dUl;
+      df.upload(f);
+      ddn.upload(dn);
+      dUl.alloc(sizeof(double) * nr2);
+      hfg::k_scale_cols(Sd, nrad, nrad, df.as<double>(), dUl.as<double>(), st);
+      dX.alloc(sizeof(double) * nr2);
+      cb(cublasDgemm(hd.bl, CUBLAS_OP_N, CUBLAS_OP_T, nrad, nrad, nrad, &one_, dUl.as<double>(), nrad, Sd, nrad,
+                     &zero_, dX.as<double>(), nrad),
+         "U L U^T");
+      hfg::k_scale_rows(dX.as<double>(), nrad, nrad, ddn.as<double>(), st);
+      ck(cudaStreamSynchronize(st), "sync");
     }
 
-    // ---- one-electron matrices on the device ----
-    std::vector<double> hT(nb2, 0.0), hV(nb2, 0.0);
-    for (int ia = 0; ia < nang; ++ia) {
-      const double lf = (double)H.lval[ia] * (H.lval[ia] + 1);
-      for (int c = 0; c < nrad; ++c)
-        for (int r = 0; r < nrad; ++r) {
-          const size_t o = (size_t)(ia * nrad + c) * nbf + ia * nrad + r, q = r + (size_t)c * nrad;
-          hT[o] = H.Trad[q] + lf * H.Tlrad[q];
-          hV[o] = -(double)H.Z * H.Vrad[q];
-        }
-    }
+    // ---- one-electron matrices, expanded on the device from the radial
+    // blocks (the dense nbf^2 matrices never exist on the host) ----
     DBuf dT, dV, dH, dP, dPs[2], dJ, dK[2], dXC[2], dF[2], dE;
-    double* T = dT.upload(hT);
-    double* V = dV.upload(hV);
-    hT.clear();
-    hV.clear();
+    {
+      DBuf dTr, dTl, dVr, dl;
+      dTr.upload(H.Trad);
+      dTl.upload(H.Tlrad);
+      dVr.upload(H.Vrad);
+      dl.upload(std::vector<int>(H.lval.begin(), H.lval.begin() + nang));
+      dT.alloc(sizeof(double) * nb2);
+      dV.alloc(sizeof(double) * nb2);
+      ck(cudaMemsetAsync(dT.p, 0, sizeof(double) * nb2, st), "memset");
+      ck(cudaMemsetAsync(dV.p, 0, sizeof(double) * nb2, st), "memset");
+      hfg::k_expand_one_electron(dTr.as<double>(), dTl.as<double>(), dVr.as<double>(), dl.as<int>(), nang, nrad,
+                                 (double)H.Z, dT.as<double>(), dV.as<double>(), st);
+      ck(cudaStreamSynchronize(st), "sync");  // the radial blocks are freed at the end of this scope
+    }
+    double* T = dT.as<double>();
+    double* V = dV.as<double>();
     dH.alloc(sizeof(double) * nb2);
     hfg::k_add4(dH.as<double>(), T, V, nullptr, nullptr, nb2, st);
     dP.alloc(sizeof(double) * nb2);
