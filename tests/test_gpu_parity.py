@@ -327,3 +327,34 @@ def test_jk_device_entry_matches_separate_calls(split):
         A.jk(Pd, J2, K2, PK=PK, symmetric=True, split=split, split_j=split)
         torch.cuda.synchronize()
         assert torch.equal(J1, J2) and torch.equal(K1, K2)
+
+
+@pytest.mark.parametrize("case", [CASES[2], CASES[3], CASES[4]], ids=lambda c: f"Z{c[0]}_l{c[1]}m{c[2]}")
+def test_split_symmetric_screened_blocks(case):
+    """A density with zero angular blocks (orbitals inside m blocks, so every
+    block with m_i != m_l is zero and screened): the symmetric split form,
+    whose norm pass splits only the element-upper half of P and takes the
+    strictly lower part of each block's norm from the transposed block,
+    screens the same blocks as the general form and matches the oracle."""
+    torch = torch_cuda()
+    A, O = make_pair(*case)
+    rng = np.random.default_rng(case[0] + 7)
+    nrad = O.nbf // len(A.lval)
+    C = np.zeros((O.nbf, 0))
+    for m in sorted(set(int(x) for x in A.mval)):
+        idx = np.concatenate([np.arange(k * nrad, (k + 1) * nrad) for k in range(len(A.mval)) if A.mval[k] == m])
+        Cm = np.zeros((O.nbf, 2))
+        Cm[idx] = rng.standard_normal((len(idx), 2))
+        C = np.hstack([C, Cm])
+    P = C @ C.T
+    Kr = FockOracle(O).exchange(P)
+    Pd = to_dev(torch, P)
+    out = {}
+    for sym in (True, False):
+        Kd = torch.full_like(Pd, np.nan)
+        A.exchange(Pd, Kd, symmetric=sym, split=True)
+        out[sym] = from_dev(Kd)
+        err = relerr(out[sym], Kr)
+        print(f"split K, m-block density, symmetric={sym}: max rel err {err:.2e}")
+        assert np.isfinite(out[sym]).all() and err < SPLIT_TOL
+    assert np.abs(out[True] - out[False]).max() <= 1e-13 * np.abs(Kr).max()
