@@ -332,10 +332,8 @@ def test_jk_device_entry_matches_separate_calls(split):
 @pytest.mark.parametrize("case", [CASES[2], CASES[3], CASES[4]], ids=lambda c: f"Z{c[0]}_l{c[1]}m{c[2]}")
 def test_split_symmetric_screened_blocks(case):
     """A density with zero angular blocks (orbitals inside m blocks, so every
-    block with m_i != m_l is zero and screened): the symmetric split form,
-    whose norm pass splits only the element-upper half of P and takes the
-    strictly lower part of each block's norm from the transposed block,
-    screens the same blocks as the general form and matches the oracle."""
+    block with m_i != m_l is zero and screened): the symmetric and the
+    general split forms screen the same blocks and match the oracle."""
     torch = torch_cuda()
     A, O = make_pair(*case)
     rng = np.random.default_rng(case[0] + 7)
