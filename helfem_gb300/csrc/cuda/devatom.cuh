@@ -54,7 +54,7 @@ struct DevScratch {
   double* jin;          // [nchan*nel*nn*nn]
   double* jscal;        // [nchan*nel*2]
   double* khalo;        // [nel*nel*nang*nang*(2nn-1)]
-  double* bnorm;        // [nang*nang*NORM_SPLIT] partial squared block norms
+  double* bnorm;        // [2*nang*nang*NORM_SPLIT] partial squared block norms (band, strictly upper)
   unsigned char* act;   // [nang*nang] density block above the screen
   unsigned char* ent_act;  // [nent] exchange entry with an active term
   float2* p2;           // [nbf*nbf] split copy of the density (split path)

@@ -306,14 +306,38 @@ __global__ void j_scatter(DevAtom A, DevScratch S, double* __restrict__ J, int a
 // Partial Frobenius norms of the angular blocks of P: grid (nang^2, NORM_SPLIT),
 // each CTA sums a band of columns; consumers add the partials in a fixed
 // order and apply the reference's 10*DBL_EPSILON screen.
+// lowest and highest element holding radial function g (a boundary function
+// belongs to two)
+__device__ __forceinline__ int elem_hi(const DevAtom& A, int g) { return min((g + 1) / (A.nn - 1), A.nel - 1); }
+__device__ __forceinline__ int elem_lo(const DevAtom& A, int g) {
+  const int w = A.nn - 1, e = (g + 1) / w;
+  return ((g + 1) % w == 0) ? max(e - 1, 0) : min(e, A.nel - 1);
+}
+
+// half != 0 (split tensor-core form, symmetric density): only the entries
+// that the tile kernels read, elem_lo(row) <= elem_hi(column), are split
+// (about half of P); the norm of the strictly lower part (elem_lo(row) >
+// elem_hi(column)) of block (i,l) is the strictly upper part of block (l,i),
+// kept apart in part[nang^2 NORM_SPLIT + ...] and added by k_flags
 __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* __restrict__ part,
-                              float2* __restrict__ p2) {
+                              float2* __restrict__ p2, int half) {
   __shared__ double red[32];
   const int blk = blockIdx.x, i = blk % A.nang, l = blk / A.nang;
   const int c0 = (int)((long)A.nrad * blockIdx.y / NORM_SPLIT);
   const int c1 = (int)((long)A.nrad * (blockIdx.y + 1) / NORM_SPLIT);
   double s = 0.0;
-  float sf = 0.f;
+  float sf = 0.f, sfu = 0.f;
+  // per column of the band: the last row that is split and the first row
+  // that is not strictly upper (two compares per entry below)
+  constexpr int HMAX = 512;
+  __shared__ int rlim[HMAX], rup[HMAX];
+  if (half) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+      rlim[c - c0] = min(A.nrad - 1, (elem_hi(A, c) + 1) * (A.nn - 1) - 1);
+      rup[c - c0] = elem_lo(A, c) * (A.nn - 1) - 1;
+    }
+    __syncthreads();
+  }
   // the band's elements in column order (32-bit index arithmetic); four
   // loads in flight per thread (one at a time left the pass latency-bound
   // at half the HBM rate; eight measured the same as four), summed in the
@@ -323,22 +347,29 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   for (int base = threadIdx.x; base < n; base += NU * bd) {
     double v[NU];
     size_t o[NU];
+    unsigned char in[NU];  // 0: skipped, 1: element-diagonal band, 2: strictly upper
 #pragma unroll
     for (int u = 0; u < NU; ++u) {
       const int idx = base + u * bd;
       const int r = idx % A.nrad, c = c0 + idx / A.nrad;
       o[u] = (size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r;
-      v[u] = idx < n ? P[o[u]] : 0.0;
+      in[u] = idx < n ? 1 : 0;
+      if (half && in[u]) {
+        if (r > rlim[c - c0]) in[u] = 0;
+        else if (r < rup[c - c0]) in[u] = 2;
+      }
+      v[u] = in[u] ? P[o[u]] : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < NU; ++u) {
-      if (base + u * bd >= n) break;
+      if (!in[u]) continue;
       if (p2) {
         // split path: integer-only split (no FP64-pipe instructions) and an
         // FP32 norm of the high words for the screen
         const float2 h = split_bits(v[u]);
         p2[o[u]] = h;
-        sf = fmaf(h.x, h.x, sf);
+        if (in[u] == 2) sfu = fmaf(h.x, h.x, sfu);
+        else sf = fmaf(h.x, h.x, sf);
       } else {
         s += v[u] * v[u];
       }
@@ -347,27 +378,35 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   if (p2) s = (double)sf;
   s = block_sum(s, red);
   if (threadIdx.x == 0) part[blk * NORM_SPLIT + blockIdx.y] = s;
+  if (half) {
+    const double su = block_sum((double)sfu, red);
+    if (threadIdx.x == 0) part[(size_t)A.nang * A.nang * NORM_SPLIT + blk * NORM_SPLIT + blockIdx.y] = su;
+  }
 }
 
 // density-block screen (10*DBL_EPSILON, the reference's threshold) and the
 // exchange entries that see an active block, once per build
-__global__ void k_flags(DevAtom A, DevScratch S) {
+__global__ void k_flags(DevAtom A, DevScratch S, int half) {
   const int nang2 = A.nang * A.nang;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-  for (int idx = tid; idx < nang2; idx += nth) {
+  // squared norm of block blk = l nang + i; with half, its strictly lower
+  // part comes from the strictly upper part of the transposed block
+  auto norm2 = [&](int blk) {
     double s = 0.0;
-    for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[idx * NORM_SPLIT + c];
-    S.act[idx] = !(sqrt(s) < 10.0 * DBL_EPSILON);
-  }
+    for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[blk * NORM_SPLIT + c];
+    if (half) {
+      const double* up = S.bnorm + (size_t)nang2 * NORM_SPLIT;
+      const int blkT = (blk % A.nang) * A.nang + blk / A.nang;
+      for (int c = 0; c < NORM_SPLIT; ++c) s += up[blk * NORM_SPLIT + c] + up[blkT * NORM_SPLIT + c];
+    }
+    return s;
+  };
+  for (int idx = tid; idx < nang2; idx += nth) S.act[idx] = !(sqrt(norm2(idx)) < 10.0 * DBL_EPSILON);
   // every thread recomputes the block flags its entries need (no grid sync)
   for (int ent = tid; ent < A.nent; ent += nth) {
     bool any = false;
-    for (int u = A.kent_ptr[ent]; u < A.kent_ptr[ent + 1] && !any; ++u) {
-      const int blk = A.kterm_blk[u];
-      double s = 0.0;
-      for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[blk * NORM_SPLIT + c];
-      any = !(sqrt(s) < 10.0 * DBL_EPSILON);
-    }
+    for (int u = A.kent_ptr[ent]; u < A.kent_ptr[ent + 1] && !any; ++u)
+      any = !(sqrt(norm2(A.kterm_blk[u])) < 10.0 * DBL_EPSILON);
     S.ent_act[ent] = any ? 1 : 0;
   }
 }
@@ -711,8 +750,8 @@ cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KU
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
-    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, nullptr);
-    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S);
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, nullptr, 0);
+    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S, 0);
   }
   {
     Mark m(prof, KC_K_TILES, st);
@@ -736,8 +775,11 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
-    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2);
-    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S);
+    // the tensor-core form reads only the element-upper half of a symmetric P
+    // (band widths up to 512 columns: nrad <= 8192)
+    const int half = (tc && symmetric && A.nrad / NORM_SPLIT + 1 <= 512) ? 1 : 0;
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2, half);
+    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S, half);
   }
   {
     Mark m(prof, KC_K_TILES, st);

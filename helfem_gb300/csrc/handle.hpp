@@ -556,7 +556,7 @@ struct hfg_atom {
     s_jin.alloc(sizeof(double) * A.nchan * A.nel * n2);
     s_jscal.alloc(sizeof(double) * A.nchan * A.nel * 2);
     s_khalo.alloc(sizeof(double) * (size_t)A.nel * A.nel * A.nang * A.nang * (2 * A.nn - 1));
-    s_bnorm.alloc(sizeof(double) * (size_t)A.nang * A.nang * NORM_SPLIT);
+    s_bnorm.alloc(sizeof(double) * 2 * (size_t)A.nang * A.nang * NORM_SPLIT);  // band and strictly-upper partials
     s_act.alloc((size_t)A.nang * A.nang);
     s_entact.alloc(std::max<size_t>(1, (size_t)A.nent));
     scr.jin = s_jin.as<double>();
