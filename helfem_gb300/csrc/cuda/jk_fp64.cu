@@ -327,17 +327,6 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   const int c1 = (int)((long)A.nrad * (blockIdx.y + 1) / NORM_SPLIT);
   double s = 0.0;
   float sf = 0.f, sfu = 0.f;
-  // per column of the band: the last row that is split and the first row
-  // that is not strictly upper (two compares per entry below)
-  constexpr int HMAX = 512;
-  __shared__ int rlim[HMAX], rup[HMAX];
-  if (half) {
-    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
-      rlim[c - c0] = min(A.nrad - 1, (elem_hi(A, c) + 1) * (A.nn - 1) - 1);
-      rup[c - c0] = elem_lo(A, c) * (A.nn - 1) - 1;
-    }
-    __syncthreads();
-  }
   // the band's elements in column order (32-bit index arithmetic); four
   // loads in flight per thread (one at a time left the pass latency-bound
   // at half the HBM rate; eight measured the same as four), summed in the
@@ -355,8 +344,9 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
       o[u] = (size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r;
       in[u] = idx < n ? 1 : 0;
       if (half && in[u]) {
-        if (r > rlim[c - c0]) in[u] = 0;
-        else if (r < rup[c - c0]) in[u] = 2;
+        const int ehc = elem_hi(A, c);
+        if (r > min(A.nrad - 1, (ehc + 1) * (A.nn - 1) - 1)) in[u] = 0;
+        else if (elem_hi(A, r) < elem_lo(A, c)) in[u] = 2;
       }
       v[u] = in[u] ? P[o[u]] : 0.0;
     }
@@ -776,8 +766,7 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
   {
     Mark m(prof, KC_K_NORMS, st);
     // the tensor-core form reads only the element-upper half of a symmetric P
-    // (band widths up to 512 columns: nrad <= 8192)
-    const int half = (tc && symmetric && A.nrad / NORM_SPLIT + 1 <= 512) ? 1 : 0;
+    const int half = (tc && symmetric) ? 1 : 0;
     k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2, half);
     k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S, half);
   }
