@@ -83,6 +83,8 @@ _SIGS = {
     "hfg_atom_autotune": ([_P, ctypes.c_int, _I, _D], ctypes.c_int),
     "hfg_atom_set_partition": ([_P, ctypes.c_int], ctypes.c_int),
     "hfg_atom_compute_yukawa": ([_P, ctypes.c_double], ctypes.c_int),
+    "hfg_atom_compute_erfc": ([_P, ctypes.c_double, ctypes.c_int], ctypes.c_int),
+    "hfg_atom_erfc_table": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D], ctypes.c_int),
     "hfg_atom_yukawa_tables": ([_P, ctypes.c_int, ctypes.c_int, _D, _D, _D], ctypes.c_int),
     "hfg_rs_exchange": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
     "hfg_rs_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
@@ -461,6 +463,18 @@ class Atom:
     def compute_yukawa(self, lam: float):
         """Screened radial tables for the kernel exp(-lam r12)/r12."""
         _check(_lib.hfg_atom_compute_yukawa(self._h, lam))
+
+    def compute_erfc(self, mu: float, exact_binomial: bool = False):
+        """Pair tables of the erfc kernel erfc(mu r12)/r12 (the reference's
+        series rule unless exact_binomial); rs_exchange then uses them."""
+        _check(_lib.hfg_atom_compute_erfc(self._h, mu, 1 if exact_binomial else 0))
+
+    def erfc_table(self, L: int, iel: int, kel: int):
+        """mu (ij|kl) of the element pair, exchange-ordered, (nn^2 x nn^2)."""
+        nn = self.nnodes
+        out = np.zeros((nn * nn, nn * nn), order="F")
+        _check(_lib.hfg_atom_erfc_table(self._h, L, iel, kel, _dptr(out)))
+        return out
 
     def yukawa_tables(self, L: int, iel: int):
         """(r_small, r_big, tk) of the screened tables as stored (padded)."""

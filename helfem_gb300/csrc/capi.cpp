@@ -297,7 +297,12 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
   const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
   cudaStream_t st = a->own_stream;
   ck(cudaMemcpyAsync(a->h_in.p, P, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
-  if (coulomb) {
+  if (!coulomb && screened && a->rs_erfc) {
+    need((flags & HFG_EXCHANGE_SPLIT) == 0, "the erfc kernel has no split form");
+    ck(hfg::launch_exchange_erfc(a->dev, a->scr, a->d_etk.as<double>(), a->h_in.as<double>(),
+                                 a->h_out.as<double>(), st, &a->prof),
+       "erfc exchange");
+  } else if (coulomb) {
     ck(hfg::launch_coulomb_fp64(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof),
        "coulomb");
   } else if (flags & HFG_EXCHANGE_SPLIT) {
@@ -528,6 +533,31 @@ hfg_status hfg_atom_compute_yukawa(hfg_atom* a, double lambda) {
   });
 }
 
+hfg_status hfg_atom_compute_erfc(hfg_atom* a, double mu, int flags) {
+  return guard([&] {
+    need(a != nullptr && mu > 0.0, "hfg_atom_compute_erfc: bad arguments");
+    need((flags & ~HFG_ERFC_EXACT_BINOMIAL) == 0, "hfg_atom_compute_erfc: unknown flags");
+    const bool exact = (flags & HFG_ERFC_EXACT_BINOMIAL) != 0;
+    if (a->on_device)
+      a->setup_erfc(mu, exact);
+    else
+      a->host.build_erfc(mu, exact);  // host-only handle: tables for checking
+  });
+}
+
+hfg_status hfg_atom_erfc_table(const hfg_atom* a, int L, int iel, int kel, double* out) {
+  return guard([&] {
+    need(a != nullptr && out != nullptr, "hfg_atom_erfc_table: null argument");
+    const hfg::AtomHost& H = a->host;
+    need(H.e_mu > 0.0, "hfg_atom_erfc_table: hfg_atom_compute_erfc has not been called");
+    need(L >= 0 && L < H.NL && iel >= 0 && iel < H.rad.nel && kel >= 0 && kel < H.rad.nel,
+         "hfg_atom_erfc_table: L, iel or kel out of range");
+    const size_t n2 = (size_t)H.rad.nn * H.rad.nn;
+    const size_t o = (((size_t)L * H.rad.nel + iel) * H.rad.nel + kel) * n2 * n2;
+    std::copy(H.e_tk.begin() + o, H.e_tk.begin() + o + n2 * n2, out);
+  });
+}
+
 hfg_status hfg_atom_yukawa_tables(const hfg_atom* a, int L, int iel, double* rsmall, double* rbig, double* tk) {
   return guard([&] {
     need(a != nullptr, "hfg_atom_yukawa_tables: null handle");
@@ -548,7 +578,11 @@ hfg_status hfg_rs_exchange(hfg_atom* a, const double* P, double* K, int flags, v
     a->check_device();
     if (!a->rs_ready) throw std::logic_error("Primitive teis have not been computed!\n");
     const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
-    if (flags & HFG_EXCHANGE_SPLIT) {
+    if (a->rs_erfc) {
+      need((flags & HFG_EXCHANGE_SPLIT) == 0, "hfg_rs_exchange: the erfc kernel has no split form");
+      ck(hfg::launch_exchange_erfc(a->dev, a->scr, a->d_etk.as<double>(), P, K, (cudaStream_t)stream, &a->prof),
+         "erfc exchange");
+    } else if (flags & HFG_EXCHANGE_SPLIT) {
       const size_t b2 = sizeof(float2) * (size_t)a->host.nbf * a->host.nbf;
       if (a->s_p2.n != b2) {
         hfg_abi::AllocStream alloc_on(a->own_stream);

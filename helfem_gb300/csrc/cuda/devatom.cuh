@@ -54,7 +54,7 @@ struct DevScratch {
   double* jin;          // [nchan*nel*nn*nn]
   double* jscal;        // [nchan*nel*2]
   double* khalo;        // [nel*nel*nang*nang*(2nn-1)]
-  double* bnorm;        // [2*nang*nang*NORM_SPLIT] partial squared block norms (band, strictly upper)
+  double* bnorm;        // [nang*nang*NORM_SPLIT] partial squared block norms
   unsigned char* act;   // [nang*nang] density block above the screen
   unsigned char* ent_act;  // [nent] exchange entry with an active term
   float2* p2;           // [nbf*nbf] split copy of the density (split path)
@@ -196,6 +196,10 @@ cudaError_t tc_peak(int ctas_per_sm, int iters, double* tflops, double* ms, int*
 // launchers (jk_fp64.cu)
 cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const double* P, double* J,
                                 bool zero_output, cudaStream_t st, Profiler* prof = nullptr);
+// range-separated exchange with the erfc kernel: tk = the pair tables
+// [((L*nel + a)*nel + b)*n2*n2 + t + v*n2] (general mode, every pair)
+cudaError_t launch_exchange_erfc(const DevAtom& A, const DevScratch& S, const double* tk, const double* P, double* K,
+                                 cudaStream_t st, Profiler* prof = nullptr);
 // the same J in float pairs (needs jket_coef2, jbra_coef2, cholp2, rs2, rb2)
 cudaError_t launch_coulomb_split(const DevAtom& A, const DevScratch& S, const double* P, double* J,
                                 bool zero_output, cudaStream_t st, Profiler* prof = nullptr);

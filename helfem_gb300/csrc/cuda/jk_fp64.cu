@@ -306,27 +306,14 @@ __global__ void j_scatter(DevAtom A, DevScratch S, double* __restrict__ J, int a
 // Partial Frobenius norms of the angular blocks of P: grid (nang^2, NORM_SPLIT),
 // each CTA sums a band of columns; consumers add the partials in a fixed
 // order and apply the reference's 10*DBL_EPSILON screen.
-// lowest and highest element holding radial function g (a boundary function
-// belongs to two)
-__device__ __forceinline__ int elem_hi(const DevAtom& A, int g) { return min((g + 1) / (A.nn - 1), A.nel - 1); }
-__device__ __forceinline__ int elem_lo(const DevAtom& A, int g) {
-  const int w = A.nn - 1, e = (g + 1) / w;
-  return ((g + 1) % w == 0) ? max(e - 1, 0) : min(e, A.nel - 1);
-}
-
-// half != 0 (split tensor-core form, symmetric density): only the entries
-// that the tile kernels read, elem_lo(row) <= elem_hi(column), are split
-// (about half of P); the norm of the strictly lower part (elem_lo(row) >
-// elem_hi(column)) of block (i,l) is the strictly upper part of block (l,i),
-// kept apart in part[nang^2 NORM_SPLIT + ...] and added by k_flags
 __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* __restrict__ part,
-                              float2* __restrict__ p2, int half) {
+                              float2* __restrict__ p2) {
   __shared__ double red[32];
   const int blk = blockIdx.x, i = blk % A.nang, l = blk / A.nang;
   const int c0 = (int)((long)A.nrad * blockIdx.y / NORM_SPLIT);
   const int c1 = (int)((long)A.nrad * (blockIdx.y + 1) / NORM_SPLIT);
   double s = 0.0;
-  float sf = 0.f, sfu = 0.f;
+  float sf = 0.f;
   // the band's elements in column order (32-bit index arithmetic); four
   // loads in flight per thread (one at a time left the pass latency-bound
   // at half the HBM rate; eight measured the same as four), summed in the
@@ -336,30 +323,22 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   for (int base = threadIdx.x; base < n; base += NU * bd) {
     double v[NU];
     size_t o[NU];
-    unsigned char in[NU];  // 0: skipped, 1: element-diagonal band, 2: strictly upper
 #pragma unroll
     for (int u = 0; u < NU; ++u) {
       const int idx = base + u * bd;
       const int r = idx % A.nrad, c = c0 + idx / A.nrad;
       o[u] = (size_t)(l * A.nrad + c) * A.nbf + (size_t)i * A.nrad + r;
-      in[u] = idx < n ? 1 : 0;
-      if (half && in[u]) {
-        const int ehc = elem_hi(A, c);
-        if (r > min(A.nrad - 1, (ehc + 1) * (A.nn - 1) - 1)) in[u] = 0;
-        else if (elem_hi(A, r) < elem_lo(A, c)) in[u] = 2;
-      }
-      v[u] = in[u] ? P[o[u]] : 0.0;
+      v[u] = idx < n ? P[o[u]] : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < NU; ++u) {
-      if (!in[u]) continue;
+      if (base + u * bd >= n) break;
       if (p2) {
         // split path: integer-only split (no FP64-pipe instructions) and an
         // FP32 norm of the high words for the screen
         const float2 h = split_bits(v[u]);
         p2[o[u]] = h;
-        if (in[u] == 2) sfu = fmaf(h.x, h.x, sfu);
-        else sf = fmaf(h.x, h.x, sf);
+        sf = fmaf(h.x, h.x, sf);
       } else {
         s += v[u] * v[u];
       }
@@ -368,35 +347,27 @@ __global__ void k_block_norms(DevAtom A, const double* __restrict__ P, double* _
   if (p2) s = (double)sf;
   s = block_sum(s, red);
   if (threadIdx.x == 0) part[blk * NORM_SPLIT + blockIdx.y] = s;
-  if (half) {
-    const double su = block_sum((double)sfu, red);
-    if (threadIdx.x == 0) part[(size_t)A.nang * A.nang * NORM_SPLIT + blk * NORM_SPLIT + blockIdx.y] = su;
-  }
 }
 
 // density-block screen (10*DBL_EPSILON, the reference's threshold) and the
 // exchange entries that see an active block, once per build
-__global__ void k_flags(DevAtom A, DevScratch S, int half) {
+__global__ void k_flags(DevAtom A, DevScratch S) {
   const int nang2 = A.nang * A.nang;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-  // squared norm of block blk = l nang + i; with half, its strictly lower
-  // part comes from the strictly upper part of the transposed block
-  auto norm2 = [&](int blk) {
+  for (int idx = tid; idx < nang2; idx += nth) {
     double s = 0.0;
-    for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[blk * NORM_SPLIT + c];
-    if (half) {
-      const double* up = S.bnorm + (size_t)nang2 * NORM_SPLIT;
-      const int blkT = (blk % A.nang) * A.nang + blk / A.nang;
-      for (int c = 0; c < NORM_SPLIT; ++c) s += up[blk * NORM_SPLIT + c] + up[blkT * NORM_SPLIT + c];
-    }
-    return s;
-  };
-  for (int idx = tid; idx < nang2; idx += nth) S.act[idx] = !(sqrt(norm2(idx)) < 10.0 * DBL_EPSILON);
+    for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[idx * NORM_SPLIT + c];
+    S.act[idx] = !(sqrt(s) < 10.0 * DBL_EPSILON);
+  }
   // every thread recomputes the block flags its entries need (no grid sync)
   for (int ent = tid; ent < A.nent; ent += nth) {
     bool any = false;
-    for (int u = A.kent_ptr[ent]; u < A.kent_ptr[ent + 1] && !any; ++u)
-      any = !(sqrt(norm2(A.kterm_blk[u])) < 10.0 * DBL_EPSILON);
+    for (int u = A.kent_ptr[ent]; u < A.kent_ptr[ent + 1] && !any; ++u) {
+      const int blk = A.kterm_blk[u];
+      double s = 0.0;
+      for (int c = 0; c < NORM_SPLIT; ++c) s += S.bnorm[blk * NORM_SPLIT + c];
+      any = !(sqrt(s) < 10.0 * DBL_EPSILON);
+    }
     S.ent_act[ent] = any ? 1 : 0;
   }
 }
@@ -438,6 +409,38 @@ __device__ __forceinline__ double k_recouple(const DevAtom& A, const double* __r
     x += A.kterm_coef[u] * Pbase[A.kterm_off[u]];
   }
   return x;
+}
+
+// Range-separated exchange with the erfc kernel (TwoDBasisT::rs_exchange,
+// src/atomic/TwoDBasis.cpp:1001-1131, with the pairwise assembly of
+// CoulombExchangeFE.h:396-422): the kernel does not separate into r< / r>
+// factors, so every element pair (a,b) carries a dense exchange-ordered
+// table per multipole, K_jk(a,b)[t] = -sum_L sum_v T_L(a,b)[t, v] X_L(a,b)[v]
+// (t = p + q nn, v = p' + q' nn). One CTA per (element pair, output block),
+// one thread per tile entry t; FP64.
+__global__ void k_erfc_tiles(DevAtom A, DevScratch S, const double* __restrict__ tk,
+                             const double* __restrict__ P, double* __restrict__ K) {
+  const int a = blockIdx.x % A.nel, b = blockIdx.x / A.nel, jk = blockIdx.y;
+  const int nn = A.nn, n2 = nn * nn, t = threadIdx.x;
+  extern __shared__ double xs[];  // [n2]
+  unsigned char* act = reinterpret_cast<unsigned char*>(xs + n2);
+  for (int idx = t; idx < A.nang * A.nang; idx += blockDim.x) act[idx] = S.act[idx];
+  __syncthreads();
+  double y = 0.0;
+  for (int e = A.kjk_ptr[jk]; e < A.kjk_ptr[jk + 1]; ++e) {
+    if (!S.ent_act[e]) continue;  // uniform over the CTA
+    for (int v = t; v < n2; v += blockDim.x) {
+      const int gp = gfun(A, a, v % nn), gq = gfun(A, b, v / nn);
+      xs[v] = (gvalid(A, gp) && gvalid(A, gq)) ? k_recouple(A, P + (size_t)gq * A.nbf + gp, act, e) : 0.0;
+    }
+    __syncthreads();
+    if (t < n2) {
+      const double* T = tk + (((size_t)A.kent_L[e] * A.nel + a) * A.nel + b) * n2 * n2;
+      for (int v = 0; v < n2; ++v) y += T[t + (size_t)v * n2] * xs[v];
+    }
+    __syncthreads();
+  }
+  if (t < n2) k_store(A, S, K, a, b, jk, t % nn, t / nn, -y);
 }
 
 // One work unit = one element pair (a,b) and a range of output angular
@@ -735,13 +738,35 @@ cudaError_t launch_coulomb_split(const DevAtom& A, const DevScratch& S, const do
   return cudaGetLastError();
 }
 
+cudaError_t launch_exchange_erfc(const DevAtom& A, const DevScratch& S, const double* tk, const double* P, double* K,
+                                 cudaStream_t st, Profiler* prof) {
+  const int n2 = A.nn * A.nn, nang2 = A.nang * A.nang;
+  {
+    Mark m(prof, KC_K_NORMS, st);
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, nullptr);
+    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S);
+  }
+  {
+    Mark m(prof, KC_K_TILES, st);
+    const size_t smem = sizeof(double) * n2 + nang2;
+    const cudaError_t e = smem_limit(k_erfc_tiles, smem);
+    if (e != cudaSuccess) return e;
+    k_erfc_tiles<<<dim3(A.nel * A.nel, nang2), threads_for(n2), smem, st>>>(A, S, tk, P, K);
+  }
+  {
+    Mark m(prof, KC_K_FIXUP, st);
+    k_fixup<<<A.nel * A.nel, 256, 0, st>>>(A, S, K);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,
                                  double* K, bool symmetric, cudaStream_t st, Profiler* prof) {
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
-    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, nullptr, 0);
-    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S, 0);
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, nullptr);
+    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S);
   }
   {
     Mark m(prof, KC_K_TILES, st);
@@ -765,10 +790,8 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
   const int n2 = A.nn * A.nn, th = threads_for(n2), nang2 = A.nang * A.nang;
   {
     Mark m(prof, KC_K_NORMS, st);
-    // the tensor-core form reads only the element-upper half of a symmetric P
-    const int half = (tc && symmetric) ? 1 : 0;
-    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2, half);
-    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S, half);
+    k_block_norms<<<dim3(nang2, NORM_SPLIT), 256, 0, st>>>(A, P, S.bnorm, S.p2);
+    k_flags<<<std::max(1, std::min(152, (A.nent + 255) / 256)), 256, 0, st>>>(A, S);
   }
   {
     Mark m(prof, KC_K_TILES, st);

@@ -395,9 +395,24 @@ struct hfg_atom {
   // tables (built by hfg_atom_compute_yukawa)
   hfg::DevAtom dev_rs{};
   bool rs_ready = false;
+  // erfc kernel of the range-separated exchange (the pair tables on the
+  // device); rs_erfc selects it in hfg_rs_exchange
+  bool rs_erfc = false;
+  DBuf d_etk;
+  void setup_erfc(double mu, bool exact) {
+    check_device();
+    host.build_erfc(mu, exact);
+    hfg_abi::AllocStream alloc_on(own_stream);
+    ck(cudaStreamSynchronize(own_stream), "sync");
+    d_etk.upload(host.e_tk);
+    ck(cudaStreamSynchronize(own_stream), "sync after upload");
+    rs_erfc = true;
+    rs_ready = true;
+  }
   DBuf y_rs, y_rb, y_tk, y_rs2, y_rb2, y_tk2;
   void setup_yukawa(double lambda) {
     check_device();
+    rs_erfc = false;
     host.build_yukawa(lambda);
     hfg_abi::AllocStream alloc_on(own_stream);
     ck(cudaStreamSynchronize(own_stream), "sync");
@@ -556,7 +571,7 @@ struct hfg_atom {
     s_jin.alloc(sizeof(double) * A.nchan * A.nel * n2);
     s_jscal.alloc(sizeof(double) * A.nchan * A.nel * 2);
     s_khalo.alloc(sizeof(double) * (size_t)A.nel * A.nel * A.nang * A.nang * (2 * A.nn - 1));
-    s_bnorm.alloc(sizeof(double) * 2 * (size_t)A.nang * A.nang * NORM_SPLIT);  // band and strictly-upper partials
+    s_bnorm.alloc(sizeof(double) * (size_t)A.nang * A.nang * NORM_SPLIT);
     s_act.alloc((size_t)A.nang * A.nang);
     s_entact.alloc(std::max<size_t>(1, (size_t)A.nent));
     scr.jin = s_jin.as<double>();

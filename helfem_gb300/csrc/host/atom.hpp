@@ -147,6 +147,18 @@ struct AtomHost {
   double y_lambda = 0.0;
   std::vector<double> y_rs, y_rb, y_tk;
   void build_yukawa(double lambda);
+  // Range-separated exchange with the erfc kernel (host/erfc.cpp):
+  // erfc(mu r12)/r12 = sum_LM (4 pi/(2L+1)) mu Phi_L(mu r>, mu r<) Y Y*
+  // does not separate into r< / r> factors, so every element pair (a, b)
+  // has its own exchange-ordered table, mu times the pair's (ij|kl)_L:
+  // e_tk[((L*nel + a)*nel + b)*n2*n2 + t + v*n2], t = j + k nn (output),
+  // v = i + l nn (density), padded. exact_binomial selects the
+  // generalised binomial in the short-range series instead of the
+  // reference's rule.
+  double e_mu = 0.0;
+  bool e_exact = false;
+  std::vector<double> e_tk;
+  void build_erfc(double mu, bool exact_binomial);
 
   // twoe_host = false leaves the in-element factors (chol, cholp, tk,
   // chol_rank, rmax) to the device tabulation

@@ -194,6 +194,27 @@ hfg_status hfg_atom_yukawa_tables(const hfg_atom* atom, int L, int iel, double* 
 hfg_status hfg_rs_exchange(hfg_atom* atom, const double* P, double* K, int flags, void* stream);
 hfg_status hfg_rs_exchange_host(hfg_atom* atom, const double* P, double* K, int flags);
 
+/* Range-separated exchange with the erfc kernel: hfg_atom_compute_erfc
+ * replaces TwoDBasisT::compute_erfc (src/atomic/TwoDBasis.cpp:760-771,
+ * CoulombExchangeFE.h:275-295): erfc(mu r12)/r12 expanded in Legendre
+ * polynomials after Angyan, Gerber and Marsman (libhelfem/src/erfc_expn.cpp)
+ * and integrated on the radial basis's Gauss-Chebyshev rule, one dense table
+ * per element pair and multipole (RadialBasis.cpp:742-811), formed on the
+ * host and kept on the device (NL nel^2 nn^4 doubles). After it,
+ * hfg_rs_exchange / hfg_rs_exchange_host evaluate the erfc-kernel exchange
+ * (same sign and spin-density convention as hfg_exchange; FP64;
+ * HFG_EXCHANGE_SPLIT is refused) until hfg_atom_compute_yukawa is called.
+ * flags: HFG_ERFC_EXACT_BINOMIAL uses the generalised binomial coefficient
+ * in the short-range series of the expansion instead of the reference's
+ * rule for negative arguments (which deviates from the exact Legendre
+ * coefficients by up to ~1e-7 relative at arguments below 1 and more at
+ * mu r> > 2 with mu r< < 0.4); the default keeps the reference's numbers.
+ * hfg_atom_erfc_table copies the nn^2 x nn^2 table of (L, iel, kel):
+ * out[t + v nn^2] = mu (ij|kl), t = j + k nn, v = i + l nn. */
+#define HFG_ERFC_EXACT_BINOMIAL 1
+hfg_status hfg_atom_compute_erfc(hfg_atom* atom, double mu, int flags);
+hfg_status hfg_atom_erfc_table(const hfg_atom* atom, int L, int iel, int kel, double* out);
+
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
  * fixed 4 MiB array in the library's static device memory rather than the
  * handle's buffers. No counterpart in the reference; it exists for callers
