@@ -207,8 +207,9 @@ hfg_status hfg_rs_exchange_host(hfg_atom* atom, const double* P, double* K, int 
  * flags: HFG_ERFC_EXACT_BINOMIAL uses the generalised binomial coefficient
  * in the short-range series of the expansion instead of the reference's
  * rule for negative arguments (which deviates from the exact Legendre
- * coefficients by up to ~1e-7 relative at arguments below 1 and more at
- * mu r> > 2 with mu r< < 0.4); the default keeps the reference's numbers.
+ * coefficients by up to ~1.5e-6 relative at arguments below 1 and ~1e-3 at
+ * mu r> = 5-6 with mu r< near 0.4, where the kernel is small); the default
+ * keeps the reference's numbers.
  * hfg_atom_erfc_table copies the nn^2 x nn^2 table of (L, iel, kel):
  * out[t + v nn^2] = mu (ij|kl), t = j + k nn, v = i + l nn. */
 #define HFG_ERFC_EXACT_BINOMIAL 1

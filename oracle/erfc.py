@@ -29,8 +29,9 @@ upper arguments that is not the generalised binomial (its recursion
 C(n, m) = (-1)^m C(n+m-1, m) for n < -1); ``binomial="reference"`` keeps
 that rule (parity), ``binomial="exact"`` uses n(n-1)...(n-m+1)/m!. Against
 a direct Legendre projection of erfc(mu r12)/r12 the exact rule agrees to
-~1e-12 relative and the reference rule deviates by up to ~1e-7 for
-arguments below 1 and by percents for Xi > 2 with xi < 0.4 (tests).
+~1e-12 relative and the reference rule deviates by up to ~1.5e-6 for
+arguments below 1 and by ~1e-3 at Xi = 5-6 with xi near 0.4, where the
+kernel itself is small (tests).
 """
 from __future__ import annotations
 
