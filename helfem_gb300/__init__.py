@@ -641,15 +641,21 @@ class Diatomic:
     """One diatomic basis (the reference's diatomic TwoDBasis after
     compute_tei): Z1 at one end of the bond and Z2 at the other, half bond
     length Rhalf, LIP elements in mu with boundaries ``bval`` and angular
-    functions (lval, mval). Matrices are over the pure basis."""
+    functions (lval, mval). Matrices are over the pure basis.
+    host_only=True builds the host tables only (no GPU); otherwise the
+    two-electron primitives are tabulated on the device (tabulate="device")
+    or on the host and uploaded (tabulate="host")."""
 
     def __init__(self, Z1: int, Z2: int, Rhalf: float, bval, lval, mval, nnodes: int = 15,
-                 cd_thresh: float = 1e-12, host_only: bool = False):
+                 cd_thresh: float = 1e-12, host_only: bool = False, tabulate: str = "device"):
+        if tabulate not in ("device", "host"):
+            raise ValueError("tabulate must be 'device' or 'host'")
         self._bval = np.ascontiguousarray(bval, dtype=np.float64)
         self._lval = np.ascontiguousarray(lval, dtype=np.int32)
         self._mval = np.ascontiguousarray(mval, dtype=np.int32)
+        mode = 1 if host_only else (2 if tabulate == "host" else 0)
         d = _DDesc(Z1, Z2, Rhalf, nnodes, len(self._bval) - 1, _dptr(self._bval), len(self._lval),
-                   self._lval.ctypes.data_as(_I), self._mval.ctypes.data_as(_I), cd_thresh, int(host_only))
+                   self._lval.ctypes.data_as(_I), self._mval.ctypes.data_as(_I), cd_thresh, mode)
         h = _P()
         _check(_lib.hfg_diatomic_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h

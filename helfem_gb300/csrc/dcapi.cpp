@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "cuda/devdiatomic.cuh"
+#include "cuda/dtab.cuh"
 #include "handle.hpp"
 #include "host/diatomic.hpp"
 
@@ -62,7 +63,6 @@ struct hfg_diatomic {
     D.nang = H.nang;
     D.nd = H.ndummy;
     D.nlm = H.nlm;
-    D.rmax = H.rmax;
     D.Lmax = H.Lmax;
     D.mmax = H.mmax;
     D.nM = H.nM;
@@ -77,13 +77,18 @@ struct hfg_diatomic {
       D.poff = d_poff.upload(off);
       D.pstart = d_pstart.upload(st);
     }
-    D.p0 = d_p0.upload(H.p0);
-    D.p2 = d_p2.upload(H.p2);
-    D.q0 = d_q0.upload(H.q0);
-    D.q2 = d_q2.upload(H.q2);
-    D.cdB = d_cdB.upload(H.cd_B);
-    D.cds = d_cds.upload(H.cd_s);
-    D.cdrank = d_cdrank.upload(H.cd_rank);
+    if (H.twoe_on_host) {
+      D.p0 = d_p0.upload(H.p0);
+      D.p2 = d_p2.upload(H.p2);
+      D.q0 = d_q0.upload(H.q0);
+      D.q2 = d_q2.upload(H.q2);
+      D.cdB = d_cdB.upload(H.cd_B);
+      D.cds = d_cds.upload(H.cd_s);
+      D.cdrank = d_cdrank.upload(H.cd_rank);
+    } else {
+      tabulate_device();
+    }
+    D.rmax = H.rmax;
     std::vector<double> lmf(H.nlm);
     for (int i = 0; i < H.nlm; ++i) {
       const int L = H.lm_L[i], Ma = H.lm_M[i];
@@ -155,6 +160,154 @@ struct hfg_diatomic {
     ck(cudaEventCreateWithFlags(&last_use, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaStreamSynchronize(own_stream), "sync after upload");
     on_device = true;
+  }
+
+  // Two-electron primitives tabulated on the device (the host tabulation's
+  // rules and pivoting): Legendre functions at the disjoint and outer points,
+  // the disjoint tiles, then the in-element kernel and its factor in groups
+  // of elements whose scratch stays within a fixed budget. Each group's
+  // factor is compacted to the group's largest rank; once every rank is
+  // known the groups are packed into the padded layout of the host tables.
+  // The disjoint tiles are copied back to the host vectors (the split
+  // tables and hfg_diatomic_tables read them there); the factor stays on
+  // the device.
+  void tabulate_device() {
+    using namespace hfg;
+    DiatomicHost& H = host;
+    const int nn = H.nn, nel = H.nel, nlm = H.nlm, n2 = nn * nn, N = 2 * n2;
+    int Mtop = 0;
+    for (int m : H.lm_M) Mtop = std::max(Mtop, m);
+    DiatomicHost::TwoeRules R;
+    H.twoe_rules(R);
+    std::vector<unsigned char> ok((size_t)nel * nn);
+    for (int e = 0; e < nel; ++e)
+      for (int p = 0; p < nn; ++p) ok[(size_t)e * nn + p] = e * (nn - 1) + p < H.nrad ? 1 : 0;
+    std::vector<int> lmidx((size_t)(Mtop + 1) * (H.Lmax + 1), -1);
+    for (int i = 0; i < nlm; ++i) lmidx[(size_t)H.lm_M[i] * (H.Lmax + 1) + H.lm_L[i]] = i;
+    DBuf b_bval, b_xg, b_wg, b_xo, b_wo, b_xi, b_wi, b_Bg, b_B1g, b_B1z, b_B2g, b_B2z, b_ok, b_lmL, b_lmM, b_lmidx,
+        b_PQ, b_scr, b_Bsc, b_ssc, b_rank;
+    DTabInput in{};
+    in.nn = nn;
+    in.nel = nel;
+    in.nlm = nlm;
+    in.Lmax = H.Lmax;
+    in.Mtop = Mtop;
+    in.n1e = R.n1e;
+    in.no = R.no;
+    in.ni = R.ni;
+    in.bval = b_bval.upload(H.bval);
+    in.xg = b_xg.upload(R.xg);
+    in.wg = b_wg.upload(R.wg);
+    in.xo = b_xo.upload(R.xo);
+    in.wo = b_wo.upload(R.wo);
+    in.xi = b_xi.upload(R.xi);
+    in.wi = b_wi.upload(R.wi);
+    in.Bg = b_Bg.upload(R.Bg);
+    in.B1g = b_B1g.upload(R.B1g);
+    in.B1z = b_B1z.upload(R.B1z);
+    in.B2g = b_B2g.upload(R.B2g);
+    in.B2z = b_B2z.upload(R.B2z);
+    in.ok = b_ok.upload(ok);
+    in.lm_L = b_lmL.upload(H.lm_L);
+    in.lm_M = b_lmM.upload(H.lm_M);
+    in.lmidx = b_lmidx.upload(lmidx);
+    in.thresh = H.cd_thresh;
+    b_PQ.alloc(sizeof(double) * dtab_pq_doubles(in));
+    ck(launch_dtab_pq(in, b_PQ.as<double>(), own_stream), "Legendre functions at the quadrature points");
+    const size_t ntab = (size_t)nlm * nel * n2;
+    d_p0.alloc(sizeof(double) * ntab);
+    d_p2.alloc(sizeof(double) * ntab);
+    d_q0.alloc(sizeof(double) * ntab);
+    d_q2.alloc(sizeof(double) * ntab);
+    ck(launch_dtab_disjoint(in, b_PQ.as<double>(), d_p0.as<double>(), d_p2.as<double>(), d_q0.as<double>(),
+                            d_q2.as<double>(), own_stream),
+       "disjoint integrals");
+    // element groups within about 1 GiB of scratch (in-element products,
+    // the kernel before symmetrisation and the factor at capacity capR)
+    int capR = std::min(N, 128);
+    auto per_element = [&](int cap) {
+      return sizeof(double) * (dtab_group_doubles(in, 1, cap) + (size_t)nlm * N * cap + (size_t)nlm * cap);
+    };
+    const size_t budget = (size_t)1 << 30;
+    auto group_size = [&](int cap) {
+      return (int)std::max<size_t>(1, std::min<size_t>((size_t)nel, budget / per_element(cap)));
+    };
+    int ge = group_size(capR);
+    auto alloc_group = [&]() {
+      const size_t ng = (size_t)ge * nlm;
+      b_scr.alloc(sizeof(double) * dtab_group_doubles(in, ge, capR));
+      b_Bsc.alloc(sizeof(double) * ng * N * capR);
+      b_ssc.alloc(sizeof(double) * ng * capR);
+    };
+    alloc_group();
+    b_rank.alloc(sizeof(int) * (size_t)nel * nlm);
+    std::vector<int> rk((size_t)nel * nlm, 0);
+    struct Group { int e0, ne, cap; DBuf B, s; };
+    std::vector<Group> groups;
+    for (int e0 = 0; e0 < nel;) {
+      const int ne = std::min(ge, nel - e0), ng = ne * nlm;
+      int* rank_g = b_rank.as<int>() + (size_t)e0 * nlm;
+      ck(launch_dtab_factor(in, b_PQ.as<double>(), e0, ne, capR, b_scr.as<double>(), b_Bsc.as<double>(),
+                            b_ssc.as<double>(), rank_g, own_stream),
+         "in-element kernel and factor");
+      ck(cudaMemcpyAsync(rk.data() + (size_t)e0 * nlm, rank_g, sizeof(int) * ng, cudaMemcpyDeviceToHost, own_stream),
+         "factor ranks");
+      ck(cudaStreamSynchronize(own_stream), "sync after a factor group");
+      int rg = 1;
+      bool over = false;
+      for (int g = 0; g < ng; ++g) {
+        const int r = rk[(size_t)e0 * nlm + g];
+        if (r < 0) over = true;
+        rg = std::max(rg, r);
+      }
+      if (over) {  // a rank above the capacity: redo this group at full capacity
+        if (capR == N) throw std::runtime_error("diatomic device tabulation: factor rank out of range");
+        capR = N;
+        ge = group_size(capR);
+        alloc_group();
+        continue;
+      }
+      Group G{e0, ne, rg, DBuf(), DBuf()};
+      G.B.alloc(sizeof(double) * (size_t)ng * N * rg);
+      G.s.alloc(sizeof(double) * (size_t)ng * rg);
+      ck(launch_dtab_pack(N, ng, nlm, nel, e0, 0, capR, rg, b_Bsc.as<double>(), b_ssc.as<double>(), rank_g,
+                          G.B.as<double>(), G.s.as<double>(), own_stream),
+         "factor compaction");
+      groups.push_back(std::move(G));
+      e0 += ne;
+    }
+    b_scr.release();
+    b_Bsc.release();
+    b_ssc.release();
+    H.rmax = 1;
+    for (const Group& G : groups) H.rmax = std::max(H.rmax, G.cap);
+    d_cdB.alloc(sizeof(double) * (size_t)nlm * nel * N * H.rmax);
+    d_cds.alloc(sizeof(double) * (size_t)nlm * nel * H.rmax);
+    for (const Group& G : groups)
+      ck(launch_dtab_pack(N, G.ne * nlm, nlm, nel, G.e0, 1, G.cap, H.rmax, G.B.as<double>(), G.s.as<double>(),
+                          b_rank.as<int>() + (size_t)G.e0 * nlm, d_cdB.as<double>(), d_cds.as<double>(),
+                          own_stream),
+         "padded factor");
+    H.cd_rank.assign((size_t)nlm * nel, 0);
+    for (int e = 0; e < nel; ++e)
+      for (int i = 0; i < nlm; ++i) H.cd_rank[(size_t)i * nel + e] = rk[(size_t)e * nlm + i];
+    dev.cdrank = d_cdrank.upload(H.cd_rank);
+    dev.cdB = d_cdB.as<double>();
+    dev.cds = d_cds.as<double>();
+    dev.p0 = d_p0.as<double>();
+    dev.p2 = d_p2.as<double>();
+    dev.q0 = d_q0.as<double>();
+    dev.q2 = d_q2.as<double>();
+    H.p0.resize(ntab);
+    H.p2.resize(ntab);
+    H.q0.resize(ntab);
+    H.q2.resize(ntab);
+    const std::pair<std::vector<double>*, const DBuf*> dl[4] = {{&H.p0, &d_p0}, {&H.p2, &d_p2}, {&H.q0, &d_q0},
+                                                                 {&H.q2, &d_q2}};
+    for (const auto& x : dl)
+      ck(cudaMemcpyAsync(x.first->data(), x.second->p, sizeof(double) * ntab, cudaMemcpyDeviceToHost, own_stream),
+         "disjoint tiles to the host");
+    ck(cudaStreamSynchronize(own_stream), "sync after the device tabulation");
   }
 
   // split tables and the split density buffer, on the first split-precision call
@@ -301,8 +454,10 @@ hfg_status hfg_diatomic_create(const hfg_diatomic_desc* desc, hfg_diatomic** out
     std::unique_ptr<hfg_diatomic> d(new hfg_diatomic());
     std::vector<double> bval(desc->bval, desc->bval + desc->nelem + 1);
     std::vector<int> lv(desc->lval, desc->lval + desc->nang), mv(desc->mval, desc->mval + desc->nang);
-    d->host.build(desc->Z1, desc->Z2, desc->Rhalf, desc->nnodes, bval, lv, mv, desc->cd_thresh);
-    if (!desc->host_only) d->upload();
+    need(desc->host_only >= 0 && desc->host_only <= 2, "hfg_diatomic_create: host_only must be 0, 1 or 2");
+    d->host.build(desc->Z1, desc->Z2, desc->Rhalf, desc->nnodes, bval, lv, mv, desc->cd_thresh,
+                  desc->host_only != 0);
+    if (desc->host_only != 1) d->upload();
     *out = d.release();
   });
 }
@@ -376,10 +531,19 @@ hfg_status hfg_diatomic_tables(const hfg_diatomic* d, int which, int ilm, int ie
     if (which < 4) {
       const std::vector<double>* src[4] = {&H.p0, &H.p2, &H.q0, &H.q2};
       std::copy(src[which]->begin() + le * n2, src[which]->begin() + (le + 1) * n2, out);
-    } else {
+    } else if (H.twoe_on_host) {
       const size_t N = 2 * n2, r = H.cd_rank[le];
       std::copy(H.cd_B.begin() + le * N * H.rmax, H.cd_B.begin() + le * N * H.rmax + N * r, out);
       if (sigma) std::copy(H.cd_s.begin() + le * H.rmax, H.cd_s.begin() + le * H.rmax + r, sigma);
+    } else {  // device-tabulated: the factor lives on the device only
+      d->check_device();
+      const size_t N = 2 * n2, r = H.cd_rank[le];
+      const double* B = static_cast<const double*>(d->d_cdB.p) + le * N * H.rmax;
+      const double* sg = static_cast<const double*>(d->d_cds.p) + le * H.rmax;
+      if (r) {
+        ck(cudaMemcpy(out, B, sizeof(double) * N * r, cudaMemcpyDeviceToHost), "factor download");
+        if (sigma) ck(cudaMemcpy(sigma, sg, sizeof(double) * r, cudaMemcpyDeviceToHost), "sign download");
+      }
     }
   });
 }

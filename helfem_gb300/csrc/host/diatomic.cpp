@@ -186,7 +186,8 @@ int DiatomicHost::lm_index(int L, int Mabs) const {
 }
 
 void DiatomicHost::build(int Z1_, int Z2_, double Rhalf_, int nnodes, const std::vector<double>& bval_,
-                         const std::vector<int>& lval_, const std::vector<int>& mval_, double thresh) {
+                         const std::vector<int>& lval_, const std::vector<int>& mval_, double thresh,
+                         bool twoe_host) {
   if (nnodes < 3 || nnodes > 17) throw std::invalid_argument("diatomic: nnodes must be in [3, 17]");
   if (bval_.size() < 3) throw std::invalid_argument("diatomic: need at least two elements");
   for (size_t i = 1; i < bval_.size(); ++i)
@@ -198,6 +199,7 @@ void DiatomicHost::build(int Z1_, int Z2_, double Rhalf_, int nnodes, const std:
   Z2 = Z2_;
   Rhalf = Rhalf_;
   cd_thresh = thresh > 0 ? thresh : 1e-12;
+  twoe_on_host = twoe_host;
   nn = nnodes;
   bval = bval_;
   nel = (int)bval.size() - 1;
@@ -245,7 +247,7 @@ void DiatomicHost::tabulate_radial() {
   const int n2 = nn * nn;
   const int Mtop = nlm ? *std::max_element(lm_M.begin(), lm_M.end()) : 0;
   const size_t tile = (size_t)n2;
-  p0.assign((size_t)nlm * nel * tile, 0.0);
+  p0.assign(twoe_on_host ? (size_t)nlm * nel * tile : 0, 0.0);
   p2 = p0;
   q0 = p0;
   q2 = p0;
@@ -285,6 +287,13 @@ void DiatomicHost::tabulate_radial() {
         }
       }
     }
+  }
+  if (!twoe_on_host) {  // the two-electron tables come from the device tabulation
+    cd_rank.clear();
+    cd_B.clear();
+    cd_s.clear();
+    rmax = 0;
+    return;
   }
 #pragma omp parallel
   {
@@ -507,6 +516,32 @@ void DiatomicHost::tabulate_radial() {
     std::copy(fB[t].begin(), fB[t].end(), cd_B.begin() + t * N * rmax);
     std::copy(fS[t].begin(), fS[t].end(), cd_s.begin() + t * rmax);
   }
+}
+
+void DiatomicHost::twoe_rules(TwoeRules& R) const {
+  R.n1e = NGL_1E;
+  R.no = NGL_OUT;
+  R.ni = NGL_IN;
+  gauss_legendre(NGL_1E, R.xg, R.wg);
+  gauss_legendre(NGL_OUT, R.xo, R.wo);
+  gauss_legendre(NGL_IN, R.xi, R.wi);
+  lip_eval(R.xg, nodes, 0, R.Bg);
+  lip_eval(R.xo, nodes, 0, R.B1g);
+  // reference coordinates (mu - mid) / sf of the in-element points: on an
+  // element after the first, mu_1 = mid + sf x_q and the inner points run
+  // over [mu_s, mu_1]; on the first (mu_s = 0), mu_1 = mu_e t^3
+  std::vector<double> r1z(NGL_OUT), r2g((size_t)NGL_OUT * NGL_IN), r2z((size_t)NGL_OUT * NGL_IN);
+  for (int q = 0; q < NGL_OUT; ++q) {
+    const double t = 0.5 * (R.xo[q] + 1.0), t3 = t * t * t;
+    r1z[q] = 2.0 * t3 - 1.0;
+    for (int r = 0; r < NGL_IN; ++r) {
+      r2g[(size_t)q * NGL_IN + r] = 0.5 * (1.0 + R.xo[q]) * (1.0 + R.xi[r]) - 1.0;
+      r2z[(size_t)q * NGL_IN + r] = t3 * (1.0 + R.xi[r]) - 1.0;
+    }
+  }
+  lip_eval(r1z, nodes, 0, R.B1z);
+  lip_eval(r2g, nodes, 0, R.B2g);
+  lip_eval(r2z, nodes, 0, R.B2z);
 }
 
 void DiatomicHost::build_couplings() {

@@ -88,8 +88,21 @@ struct DiatomicHost {
   std::vector<int> xc_fk, xc_fms, xc_fmt;
   void build_xc_grid(int lang);
 
+  // twoe_on_host = false: the two-electron tables (p0..q2, cd_*) are left
+  // to the device tabulation, which fills p0..q2, cd_rank and rmax
   void build(int Z1, int Z2, double Rhalf, int nnodes, const std::vector<double>& bval,
-             const std::vector<int>& lval, const std::vector<int>& mval, double cd_thresh);
+             const std::vector<int>& lval, const std::vector<int>& mval, double cd_thresh,
+             bool twoe_on_host = true);
+  bool twoe_on_host = true;
+  // quadrature rules of the two-electron tabulation and the LIP values at
+  // its reference points, for the device tabulation: B1*/B2* are the outer
+  // and inner points of the elements after the first (*g) and of the first
+  // (*z, mu = mu_1 t^3), laid out [q + p*no] and [(q*ni + r) + p*no*ni]
+  struct TwoeRules {
+    int n1e = 0, no = 0, ni = 0;
+    std::vector<double> xg, wg, xo, wo, xi, wi, Bg, B1g, B1z, B2g, B2z;
+  };
+  void twoe_rules(TwoeRules& R) const;
   // pure-basis one-electron matrices (nbf x nbf, column-major)
   void overlap(std::vector<double>& S) const;
   void kinetic(std::vector<double>& T) const;
@@ -100,6 +113,7 @@ struct DiatomicHost {
 
  private:
   void tabulate_radial();
+  void tabulate_twoe();
   void build_couplings();
   void dense_one_electron(int which, std::vector<double>& D) const;
 };

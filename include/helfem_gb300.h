@@ -443,7 +443,10 @@ typedef struct {
   const int* lval;       /* [nang]                                         */
   const int* mval;       /* [nang]                                         */
   double cd_thresh;      /* in-element factor threshold (<= 0: 1e-12)      */
-  int host_only;         /* 1: tabulate only, no device state              */
+  int host_only;         /* 0: device handle, two-electron primitives      *
+                          *    tabulated on the device; 1: host tables      *
+                          *    only, no device state; 2: device handle,     *
+                          *    host tabulation uploaded                     */
 } hfg_diatomic_desc;
 
 typedef struct {
@@ -452,7 +455,10 @@ typedef struct {
 
 /* Replaces the TwoDBasis constructor + compute_tei (basis.cpp:522-645,
  * 1382-1548): tabulates the disjoint P/Q integrals and the sign-carrying
- * factor of the 2-channel in-element kernel, then uploads them. */
+ * factor of the 2-channel in-element kernel, on the device (host_only 0)
+ * or on the host with an upload (host_only 2). The two agree to rounding;
+ * a device-tabulated factor stays on the device (hfg_diatomic_tables
+ * copies the requested one back). */
 hfg_status hfg_diatomic_create(const hfg_diatomic_desc* desc, hfg_diatomic** out);
 hfg_status hfg_diatomic_destroy(hfg_diatomic* d);
 hfg_status hfg_diatomic_get_dims(const hfg_diatomic* d, hfg_diatomic_dims_t* dims);

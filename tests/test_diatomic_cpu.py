@@ -81,3 +81,17 @@ def test_diatomic_bad_arguments():
     d = hg.Diatomic(1, 1, 0.7, [0.0, 1.0, 2.0], [0], [0], host_only=True)
     with pytest.raises(hg.HfgError):
         d.coulomb_host(np.zeros((d.nbf, d.nbf)))  # host-only handle
+
+
+def test_diatomic_tabulation_mode_checked():
+    import ctypes
+    with pytest.raises(ValueError):
+        hg.Diatomic(1, 1, 0.7, [0.0, 1.0, 2.0], [0], [0], tabulate="gpu")
+    # the C ABI refuses an unknown host_only mode before any device work
+    b = np.array([0.0, 1.0, 2.0])
+    lv = np.array([0], np.int32)
+    mv = np.array([0], np.int32)
+    desc = hg._DDesc(1, 1, 0.7, 5, 2, hg._dptr(b), 1, lv.ctypes.data_as(hg._I), mv.ctypes.data_as(hg._I), 0.0, 3)
+    h = hg._P()
+    assert hg._lib.hfg_diatomic_create(ctypes.byref(desc), ctypes.byref(h)) != 0
+    assert not h.value
