@@ -259,6 +259,37 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def host_link_rates(torch, Ph, Kh, reps=3):
+    """Copy rates of the host link for one density-sized transfer between
+    the pinned host buffers of the e2e leg and a device buffer: each way
+    alone and both at once (GB/s, best of reps). The e2e step moves P in
+    and K out unhidden, so these bound it."""
+    hp = torch.from_numpy(Ph.T)  # the same pinned memory
+    hk = torch.from_numpy(Kh.T)
+    d1, d2 = torch.empty_like(hp, device="cuda"), torch.empty_like(hp, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    nbytes = hp.numel() * 8
+
+    def timed(h2d, d2h):
+        best = 1e30
+        for _ in range(reps + 1):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            if h2d:
+                with torch.cuda.stream(s1):
+                    d1.copy_(hp, non_blocking=True)
+            if d2h:
+                with torch.cuda.stream(s2):
+                    hk.copy_(d2, non_blocking=True)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t)
+        return nbytes * (int(h2d) + int(d2h)) / best / 1e9
+
+    out = {"h2d": timed(True, False), "d2h": timed(False, True), "both": timed(True, True)}
+    del d1, d2
+    return out
+
+
 def n2_summary(hg, torch, builds=2):
     """The N2 diatomic Fock build beside the headline (split and plain K,
     J, the split error): seconds of work, reported as an object of the main
@@ -414,7 +445,8 @@ def run_ours(args):
     e2e = {"value": ws * ne / te if ne else None, "unit": UNIT, "h2d_bytes_per_step": 8 * nbf * nbf,
            "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
            "path": "hfg_jk_host (pinned host P, J, K; one staging of P, J copied back while K builds; "
-                   "same J and K forms as value)"}
+                   "same J and K forms as value)",
+           "host_link_gbs": host_link_rates(torch, Ph, Kh)}
 
     if rank != 0:
         if dist is not None:
