@@ -442,10 +442,12 @@ def run_ours(args):
         t = torch.tensor([te], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         te = float(t.item())
-    e2e = {"value": ws * ne / te if ne else None, "unit": UNIT, "h2d_bytes_per_step": 8 * nbf * nbf,
-           "d2h_bytes_per_step": 2 * 8 * nbf * nbf, "steps": ne,
-           "path": "hfg_jk_host (pinned host P, J, K; one staging of P, J copied back while K builds; "
-                   "same J and K forms as value)",
+    h2d, d2h = atom.host_copy_bytes()  # counted by the library from the copies it issued
+    e2e = {"value": ws * ne / te if ne else None, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "steps": ne,
+           "path": "hfg_jk_host (pinned host P, J, K; P symmetric, so its lower column blocks cross the "
+                   "link and the device mirrors the rest; J copied back while K builds; same J and K "
+                   "forms as value)",
            "host_link_gbs": host_link_rates(torch, Ph, Kh)}
 
     if rank != 0:

@@ -79,6 +79,7 @@ _SIGS = {
     "hfg_exchange_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_exchange_host_ex": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_jk_host": ([_P, _D, _D, _D, _D, ctypes.c_int], ctypes.c_int),
+    "hfg_host_copy_bytes": ([_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "hfg_fock_diag": ([_P, _P, ctypes.c_int, _P, _P, _P], ctypes.c_int),
     "hfg_atom_autotune": ([_P, ctypes.c_int, _I, _D], ctypes.c_int),
     "hfg_atom_set_partition": ([_P, ctypes.c_int], ctypes.c_int),
@@ -518,6 +519,14 @@ class Atom:
                  (COULOMB_SPLIT if split_j else 0))
         _check(_lib.hfg_jk_host(self._h, _dptr(PJ), _dptr(PK), _dptr(J), _dptr(K), flags))
         return J, K
+
+    def host_copy_bytes(self):
+        """(host-to-device, device-to-host) bytes of the last host-pointer
+        J/K call on this handle (a symmetric density crosses the link as its
+        lower column blocks)."""
+        h2d, d2h = ctypes.c_size_t(), ctypes.c_size_t()
+        _check(_lib.hfg_host_copy_bytes(self._h, ctypes.byref(h2d), ctypes.byref(d2h)))
+        return h2d.value, d2h.value
 
 
 def _scf_desc(nela, nelb, method="hf", restricted=True, symmetry=1, fixed=None, nblocks=0, e_tol=0.0,

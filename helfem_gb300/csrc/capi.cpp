@@ -286,6 +286,30 @@ hfg_status hfg_exchange_ex(hfg_atom* a, const double* P, double* K, int flags, v
   });
 }
 
+// Host density -> device. A density the caller declares symmetric
+// (HFG_EXCHANGE_SYMMETRIC) crosses the host link as its lower column blocks
+// only (16 blocks of columns, each from its first column's row down:
+// about 53 % of the bytes), and the device mirrors the rest; otherwise one
+// full copy. Returns the bytes copied.
+static size_t upload_density(double* dst, const double* src, int n, bool symmetric, cudaStream_t st) {
+  const size_t ld = sizeof(double) * (size_t)n;
+  if (!symmetric || n < 64) {
+    ck(cudaMemcpyAsync(dst, src, ld * n, cudaMemcpyHostToDevice, st), "H2D copy");
+    return ld * n;
+  }
+  const int bw = (n + 15) / 16;
+  size_t bytes = 0;
+  for (int c0 = 0; c0 < n; c0 += bw) {
+    const int w = std::min(bw, n - c0);
+    const size_t off = (size_t)c0 + (size_t)c0 * n, rows = (size_t)(n - c0);
+    ck(cudaMemcpy2DAsync(dst + off, ld, src + off, ld, sizeof(double) * rows, w, cudaMemcpyHostToDevice, st),
+       "H2D copy");
+    bytes += sizeof(double) * rows * w;
+  }
+  ck(hfg::launch_mirror_blocks(dst, n, bw, st), "density mirror");
+  return bytes;
+}
+
 static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, int flags, bool screened = false) {
   need(a && P && out, "null argument");
   need((flags & ~(HFG_EXCHANGE_SYMMETRIC | HFG_EXCHANGE_SPLIT)) == 0, "unknown flags");
@@ -296,7 +320,7 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
   a->staging();
   const size_t bytes = sizeof(double) * (size_t)a->host.nbf * a->host.nbf;
   cudaStream_t st = a->own_stream;
-  ck(cudaMemcpyAsync(a->h_in.p, P, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+  a->last_h2d = upload_density(a->h_in.as<double>(), P, a->host.nbf, !coulomb && (flags & HFG_EXCHANGE_SYMMETRIC), st);
   if (!coulomb && screened && a->rs_erfc) {
     need((flags & HFG_EXCHANGE_SPLIT) == 0, "the erfc kernel has no split form");
     ck(hfg::launch_exchange_erfc(a->dev, a->scr, a->d_etk.as<double>(), a->h_in.as<double>(),
@@ -322,6 +346,7 @@ static void host_call(hfg_atom* a, const double* P, double* out, bool coulomb, i
        "exchange");
   }
   ck(cudaMemcpyAsync(out, a->h_out.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
+  a->last_d2h = bytes;
   ck(cudaStreamSynchronize(st), "stream sync");
   if (!coulomb && (flags & HFG_EXCHANGE_SPLIT)) a->tc_check();
 }
@@ -346,7 +371,9 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
     hfg_abi::AllocStream alloc_on(st);
     if (a->h_out2.n != bytes) a->h_out2.alloc(bytes);
   }
-  ck(cudaMemcpyAsync(a->h_in.p, PJ, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+  // PJ is promised symmetric only when it is PK itself
+  const bool sym = (flags & HFG_EXCHANGE_SYMMETRIC) != 0;
+  a->last_h2d = upload_density(a->h_in.as<double>(), PJ, a->host.nbf, sym && same, st);
   if (flags & HFG_COULOMB_SPLIT) {
     a->ensure_split_coulomb();
     ck(hfg::launch_coulomb_split(a->dev, a->scr, a->h_in.as<double>(), a->h_out.as<double>(), true, st, &a->prof),
@@ -360,7 +387,7 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
   ck(cudaMemcpyAsync(J, a->h_out.p, bytes, cudaMemcpyDeviceToHost, a->copy_stream), "D2H copy");
   const double* Pk = a->h_in.as<double>();
   if (!same) {
-    ck(cudaMemcpyAsync(a->h_in2.p, PK, bytes, cudaMemcpyHostToDevice, st), "H2D copy");
+    a->last_h2d += upload_density(a->h_in2.as<double>(), PK, a->host.nbf, sym, st);
     Pk = a->h_in2.as<double>();
   }
   if (flags & HFG_EXCHANGE_SPLIT) {
@@ -380,6 +407,7 @@ static void jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, 
        "exchange");
   }
   ck(cudaMemcpyAsync(K, a->h_out2.p, bytes, cudaMemcpyDeviceToHost, st), "D2H copy");
+  a->last_d2h = 2 * bytes;
   ck(cudaStreamSynchronize(st), "stream sync");
   ck(cudaStreamSynchronize(a->copy_stream), "stream sync");
   if (flags & HFG_EXCHANGE_SPLIT) a->tc_check();
@@ -429,6 +457,14 @@ hfg_status hfg_jk(hfg_atom* a, const double* PJ, const double* PK, double* J, do
 
 hfg_status hfg_jk_host(hfg_atom* a, const double* PJ, const double* PK, double* J, double* K, int flags) {
   return guard([&] { jk_host(a, PJ, PK, J, K, flags); });
+}
+
+hfg_status hfg_host_copy_bytes(const hfg_atom* a, size_t* h2d, size_t* d2h) {
+  return guard([&] {
+    need(a && h2d && d2h, "hfg_host_copy_bytes: null argument");
+    *h2d = a->last_h2d;
+    *d2h = a->last_d2h;
+  });
 }
 
 // Autotuner: times the exchange tile kernel for candidate partitions of the

@@ -201,6 +201,9 @@ cudaError_t launch_coulomb_fp64(const DevAtom& A, const DevScratch& S, const dou
 cudaError_t launch_exchange_erfc(const DevAtom& A, const DevScratch& S, const double* tk, const double* P, double* K,
                                  cudaStream_t st, Profiler* prof = nullptr);
 // the same J in float pairs (needs jket_coef2, jbra_coef2, cholp2, rs2, rb2)
+// P(r, c) = P(c, r) wherever r / bw < c / bw (upper part of a symmetric
+// matrix from its lower column blocks of width bw)
+cudaError_t launch_mirror_blocks(double* P, int n, int bw, cudaStream_t st);
 cudaError_t launch_coulomb_split(const DevAtom& A, const DevScratch& S, const double* P, double* J,
                                 bool zero_output, cudaStream_t st, Profiler* prof = nullptr);
 cudaError_t launch_exchange_fp64(const DevAtom& A, const DevScratch& S, const KUnits& U, const double* P,

@@ -833,4 +833,31 @@ cudaError_t launch_exchange_split(const DevAtom& A, const DevScratch& S, const K
   return cudaGetLastError();
 }
 
+// Upper part of a symmetric column-major n x n matrix from its lower
+// column blocks: for blocks of bw columns, P(r, c) = P(c, r) wherever
+// r / bw < c / bw (block c holds rows >= its first column, so the source
+// is always present). 32 x 32 tiles through shared memory.
+__global__ void k_mirror_blocks(double* __restrict__ P, int n, int bw) {
+  __shared__ double t[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  if (r0 / bw >= min(c0 + 31, n - 1) / bw) return;  // no element of the tile is mirrored
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int k = ty; k < 32; k += 8) {
+    const int r = r0 + k, c = c0 + tx;
+    if (r < n && c < n && r / bw < c / bw) t[k][tx] = P[c + (size_t)r * n];
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int c = c0 + k, r = r0 + tx;
+    if (r < n && c < n && r / bw < c / bw) P[r + (size_t)c * n] = t[tx][k];
+  }
+}
+
+cudaError_t launch_mirror_blocks(double* P, int n, int bw, cudaStream_t st) {
+  if (n < 1 || bw < 1) return cudaErrorInvalidValue;
+  const int nt = (n + 31) / 32;
+  k_mirror_blocks<<<dim3(nt, nt), dim3(32, 8), 0, st>>>(P, n, bw);
+  return cudaGetLastError();
+}
+
 }  // namespace hfg

@@ -372,6 +372,8 @@ struct hfg_atom {
   }
   // staging for the host-pointer entry points (allocated on first use)
   DBuf h_in, h_out, h_in2, h_out2, h_e;
+  // bytes the last host-pointer Fock call copied each way
+  size_t last_h2d = 0, last_d2h = 0;
   DBuf d_xrad;  // radial orthonormaliser invh(S_rad), built by the first hfg_fock_diag
   // second stream and event of the combined J+K host entry point: J's copy
   // back overlaps the exchange build

@@ -286,7 +286,12 @@ hfg_status hfg_fock_diag(hfg_atom* atom, const double* F, int symmetry, double* 
  * stream and the scratch are per handle). */
 hfg_status hfg_jk(hfg_atom* atom, const double* PJ, const double* PK, double* J, double* K, int flags, void* stream);
 
-/* ---- host-pointer drop-ins (value semantics, synchronous) ---- */
+/* ---- host-pointer drop-ins (value semantics, synchronous) ----
+ * Under HFG_EXCHANGE_SYMMETRIC a density is read from the host as its lower
+ * column blocks only (16 blocks of columns, each from its first column's
+ * row down: about 53 % of the matrix) and the rest is mirrored on the
+ * device: the flag already promises P = P^T. In hfg_jk_host that applies to
+ * PJ only when it is the same pointer as PK. */
 hfg_status hfg_coulomb_host(hfg_atom* atom, const double* P, double* J);
 hfg_status hfg_exchange_host(hfg_atom* atom, const double* P, double* K);
 /* hfg_exchange_host with the hfg_exchange_ex flags (symmetric / split). */
@@ -296,6 +301,9 @@ hfg_status hfg_exchange_host_ex(hfg_atom* atom, const double* P, double* K, int 
  * (same pointer), and J is copied back on a second stream while K is built.
  * flags as hfg_exchange_ex for K, plus HFG_COULOMB_SPLIT for J. */
 hfg_status hfg_jk_host(hfg_atom* atom, const double* PJ, const double* PK, double* J, double* K, int flags);
+/* Bytes the last host-pointer J/K call on this handle copied host to device
+ * and device to host. */
+hfg_status hfg_host_copy_bytes(const hfg_atom* atom, size_t* h2d, size_t* d2h);
 
 /* Algorithmic work of one J and one K build on this basis with every density
  * block active (the unit counts behind roofline figures). FLOPs count one

@@ -108,6 +108,33 @@ def test_host_entry_points_and_determinism():
     assert np.array_equal(J5, J1) and relerr(K5, K1) < 1e-12
 
 
+def test_symmetric_host_upload():
+    """Under HFG_EXCHANGE_SYMMETRIC the host entries move only the lower
+    column blocks of the density (about 53 % of it) and mirror the rest on
+    the device: J and K equal the device-pointer calls on the full density
+    bit for bit, and the reported copies are the blocks plus J and K."""
+    torch = torch_cuda()
+    A, O = make_pair(*CASES[3])
+    n = O.nbf
+    P = random_density(n, 7, seed=41, S=O.S)
+    assert np.array_equal(P, P.T)
+    Pd = to_dev(torch, P)
+    J1, K1 = torch.full_like(Pd, np.nan), torch.full_like(Pd, np.nan)
+    A.coulomb(Pd, J1)
+    A.exchange(Pd, K1, symmetric=True)
+    torch.cuda.synchronize()
+    J2, K2 = A.jk_host(P, symmetric=True)
+    assert np.array_equal(J2, from_dev(J1)) and np.array_equal(K2, from_dev(K1))
+    h2d, d2h = A.host_copy_bytes()
+    assert 0.5 * 8 * n * n < h2d < 0.55 * 8 * n * n and d2h == 2 * 8 * n * n
+    K3 = A.exchange_host(P, symmetric=True)
+    assert np.array_equal(K3, K2)
+    assert A.host_copy_bytes() == (h2d, 8 * n * n)
+    # without the flag the density is copied whole
+    A.jk_host(P)
+    assert A.host_copy_bytes() == (8 * n * n, 2 * 8 * n * n)
+
+
 def test_autotune_keeps_results():
     """The work-partition autotuner (output-block ranges, or block groups per
     element-pair unit of the tensor-core form) changes which CTA computes
