@@ -80,6 +80,13 @@ _SIGS = {
     "hfg_exchange_host_ex": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_jk_host": ([_P, _D, _D, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_host_copy_bytes": ([_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "hfg_sadatom_create": ([ctypes.c_void_p, ctypes.POINTER(_P)], ctypes.c_int),
+    "hfg_sadatom_coulomb": ([_P, _P, _P, _P], ctypes.c_int),
+    "hfg_sadatom_exchange": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
+    "hfg_sadatom_rs_exchange": ([_P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
+    "hfg_sadatom_coulomb_host": ([_P, _D, _D], ctypes.c_int),
+    "hfg_sadatom_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
+    "hfg_sadatom_rs_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_fock_diag": ([_P, _P, ctypes.c_int, _P, _P, _P], ctypes.c_int),
     "hfg_atom_autotune": ([_P, ctypes.c_int, _I, _D], ctypes.c_int),
     "hfg_atom_set_partition": ([_P, ctypes.c_int], ctypes.c_int),
@@ -527,6 +534,88 @@ class Atom:
         h2d, d2h = ctypes.c_size_t(), ctypes.c_size_t()
         _check(_lib.hfg_host_copy_bytes(self._h, ctypes.byref(h2d), ctypes.byref(d2h)))
         return h2d.value, d2h.value
+
+
+class _SadDesc(ctypes.Structure):
+    _fields_ = [("Z", ctypes.c_int), ("nnodes", ctypes.c_int), ("nquad", ctypes.c_int),
+                ("nelem", ctypes.c_int), ("bval", ctypes.POINTER(ctypes.c_double)), ("lmax", ctypes.c_int),
+                ("chol_tol", ctypes.c_double), ("host_only", ctypes.c_int)]
+
+
+class SadAtom(Atom):
+    """Spherically averaged atom: the reference's sadatom::basis::TwoDBasis
+    (src/sadatom/basis.h) after compute_tei, one radial channel per
+    l = 0..lmax. coulomb / exchange / rs_exchange take and return l-channel
+    matrices: J of the radial density (nrad x nrad), and K of the channel
+    densities as an (lmax+1, nrad, nrad) stack (basis.cpp:186-429). Device
+    buffers hold the slices one after the other, each column-major; the
+    host methods take and return lists of matrices. compute_yukawa /
+    compute_erfc work as for atoms; scf() and the XC grid are refused."""
+
+    def __init__(self, Z: int, bval, lmax: int, nnodes: int = 15, nquad: int = 0, chol_tol: float = 0.0,
+                 host_only: bool = False, tabulate: str = "device"):
+        if tabulate not in ("device", "host"):
+            raise ValueError("tabulate must be 'device' or 'host'")
+        self.Z = int(Z)
+        self.lmax = int(lmax)
+        self.bval = np.ascontiguousarray(bval, dtype=np.float64)
+        self.lval = np.arange(self.lmax + 1, dtype=np.int32)
+        self.mval = np.zeros(self.lmax + 1, dtype=np.int32)
+        mode = 1 if host_only else (2 if tabulate == "host" else 0)
+        d = _SadDesc(self.Z, nnodes, nquad, len(self.bval) - 1, _dptr(self.bval), self.lmax, chol_tol, mode)
+        h = _P()
+        _check(_lib.hfg_sadatom_create(ctypes.addressof(d), ctypes.byref(h)))
+        self._h = h
+        dims = _Dims()
+        _check(_lib.hfg_atom_get_dims(h, ctypes.byref(dims)))
+        for n, _ in _Dims._fields_:
+            setattr(self, n, getattr(dims, n))
+        self.nel = self.nelem
+
+    @classmethod
+    def from_grid(cls, Z, nelem, rmax, lmax, igrid=4, zexp=2.0, nnodes=15, **kw):
+        return cls(Z, get_grid(rmax, nelem, igrid, zexp), lmax, nnodes=nnodes, **kw)
+
+    # ---- device pointers ----
+    def coulomb(self, P, J, stream=None):
+        _check(_lib.hfg_sadatom_coulomb(self._h, _ptr(P), _ptr(J), _stream(stream)))
+
+    def exchange(self, P, K, stream=None, symmetric: bool = False, split: bool = False):
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        _check(_lib.hfg_sadatom_exchange(self._h, _ptr(P), _ptr(K), flags, _stream(stream)))
+
+    def rs_exchange(self, P, K, stream=None, symmetric: bool = False, split: bool = False):
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        _check(_lib.hfg_sadatom_rs_exchange(self._h, _ptr(P), _ptr(K), flags, _stream(stream)))
+
+    # ---- host arrays ----
+    def _stack(self, mats):
+        mats = list(mats)
+        if len(mats) != self.lmax + 1:
+            raise ValueError(f"need {self.lmax + 1} channel matrices")
+        buf = np.empty((len(mats), self.nrad, self.nrad))
+        for l, M in enumerate(mats):
+            buf[l] = np.asarray(M, dtype=np.float64).T  # slice memory = column-major M
+        return buf
+
+    def coulomb_host(self, P: np.ndarray) -> np.ndarray:
+        Pb = np.asfortranarray(P, dtype=np.float64)
+        J = np.zeros_like(Pb, order="F")
+        _check(_lib.hfg_sadatom_coulomb_host(self._h, _dptr(Pb), _dptr(J)))
+        return J
+
+    def _k_host(self, fn, P, symmetric, split):
+        buf = self._stack(P)
+        out = np.zeros_like(buf)
+        flags = (EXCHANGE_SYMMETRIC if symmetric else 0) | (EXCHANGE_SPLIT if split else 0)
+        _check(fn(self._h, _dptr(buf), _dptr(out), flags))
+        return [np.asfortranarray(out[l].T) for l in range(len(out))]
+
+    def exchange_host(self, P, symmetric: bool = False, split: bool = False):
+        return self._k_host(_lib.hfg_sadatom_exchange_host, P, symmetric, split)
+
+    def rs_exchange_host(self, P, symmetric: bool = False, split: bool = False):
+        return self._k_host(_lib.hfg_sadatom_rs_exchange_host, P, symmetric, split)
 
 
 def _scf_desc(nela, nelb, method="hf", restricted=True, symmetry=1, fixed=None, nblocks=0, e_tol=0.0,

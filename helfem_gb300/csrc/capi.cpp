@@ -127,6 +127,100 @@ hfg_status hfg_atom_create(const hfg_atom_desc* d, hfg_atom** out) {
   });
 }
 
+hfg_status hfg_sadatom_create(const hfg_sadatom_desc* d, hfg_atom** out) {
+  return guard([&] {
+    need(d != nullptr && out != nullptr, "hfg_sadatom_create: null argument");
+    need(d->nnodes >= 3 && d->nnodes <= 17, "hfg_sadatom_create: nnodes must be in 3..17");
+    need(d->nelem >= 2 && d->bval, "hfg_sadatom_create: need at least two elements");
+    need(d->lmax >= 0 && d->lmax <= 3, "hfg_sadatom_create: lmax must be in 0..3");
+    need(d->host_only >= 0 && d->host_only <= 2, "hfg_sadatom_create: host_only must be 0, 1 or 2");
+    std::vector<double> bval(d->bval, d->bval + d->nelem + 1);
+    std::vector<int> lv(d->lmax + 1), mv(d->lmax + 1, 0);
+    for (int l = 0; l <= d->lmax; ++l) lv[l] = l;
+    std::unique_ptr<hfg_atom> a(new hfg_atom());
+    a->host.spherical = true;
+    a->host.build(d->Z, d->nnodes, bval, lv, mv, d->nquad, d->chol_tol, d->host_only != 0);
+    if (d->host_only != 1) a->upload();
+    *out = a.release();
+  });
+}
+
+// Spherically averaged handles: the l-channel matrices (nblk slices of
+// nrad x nrad, column-major, one after the other) <-> the diagonal blocks
+// of the (l, 0) basis's nbf x nbf matrix. Host or device pointers.
+static void sad_expand(hfg_atom* a, const double* cube, int nblk, cudaStream_t st) {
+  const size_t nr = a->host.rad.nrad, nbf = a->host.nbf;
+  {
+    hfg_abi::AllocStream alloc_on(a->own_stream);
+    if (a->sad_in.n != sizeof(double) * nbf * nbf) a->sad_in.alloc(sizeof(double) * nbf * nbf);
+    if (a->sad_out.n != sizeof(double) * nbf * nbf) a->sad_out.alloc(sizeof(double) * nbf * nbf);
+  }
+  double* full = a->sad_in.as<double>();
+  ck(cudaMemsetAsync(full, 0, sizeof(double) * nbf * nbf, st), "staging clear");
+  for (int l = 0; l < nblk; ++l)
+    ck(cudaMemcpy2DAsync(full + l * nr + l * nr * nbf, sizeof(double) * nbf, cube + l * nr * nr, sizeof(double) * nr,
+                         sizeof(double) * nr, nr, cudaMemcpyDefault, st),
+       "channel density in");
+}
+
+static void sad_extract(hfg_atom* a, double* cube, int nblk, cudaStream_t st) {
+  const size_t nr = a->host.rad.nrad, nbf = a->host.nbf;
+  const double* full = a->sad_out.as<double>();
+  for (int l = 0; l < nblk; ++l)
+    ck(cudaMemcpy2DAsync(cube + l * nr * nr, sizeof(double) * nr, full + l * nr + l * nr * nbf, sizeof(double) * nbf,
+                         sizeof(double) * nr, nr, cudaMemcpyDefault, st),
+       "channel result out");
+}
+
+// kind 0: J of the radial density (one slice in, one out); 1: K of the
+// channel densities; 2: the range-separated K
+static void sad_call(hfg_atom* a, const double* P, double* out, int kind, int flags, cudaStream_t st) {
+  need(a && P && out, "null argument");
+  need(a->host.spherical, "not a spherically averaged handle (create it with hfg_sadatom_create)");
+  a->check_device();
+  const int nblk = kind == 0 ? 1 : a->host.nang;
+  sad_expand(a, P, nblk, st);
+  double* in = a->sad_in.as<double>();
+  double* res = a->sad_out.as<double>();
+  hfg_status s = kind == 0   ? hfg_coulomb(a, in, res, st)
+                 : kind == 1 ? hfg_exchange_ex(a, in, res, flags, st)
+                             : hfg_rs_exchange(a, in, res, flags, st);
+  if (s != HFG_OK) throw std::runtime_error(hfg_last_error());
+  sad_extract(a, out, nblk, st);
+  a->mark_use(st);
+}
+
+hfg_status hfg_sadatom_coulomb(hfg_atom* a, const double* P, double* J, void* stream) {
+  return guard([&] { sad_call(a, P, J, 0, 0, (cudaStream_t)stream); });
+}
+
+hfg_status hfg_sadatom_exchange(hfg_atom* a, const double* P, double* K, int flags, void* stream) {
+  return guard([&] { sad_call(a, P, K, 1, flags, (cudaStream_t)stream); });
+}
+
+hfg_status hfg_sadatom_rs_exchange(hfg_atom* a, const double* P, double* K, int flags, void* stream) {
+  return guard([&] { sad_call(a, P, K, 2, flags, (cudaStream_t)stream); });
+}
+
+static void sad_host(hfg_atom* a, const double* P, double* out, int kind, int flags) {
+  need(a != nullptr, "null argument");
+  sad_call(a, P, out, kind, flags, a->own_stream);
+  ck(cudaStreamSynchronize(a->own_stream), "stream sync");
+  if (kind != 0 && (flags & HFG_EXCHANGE_SPLIT)) a->tc_check();
+}
+
+hfg_status hfg_sadatom_coulomb_host(hfg_atom* a, const double* P, double* J) {
+  return guard([&] { sad_host(a, P, J, 0, 0); });
+}
+
+hfg_status hfg_sadatom_exchange_host(hfg_atom* a, const double* P, double* K, int flags) {
+  return guard([&] { sad_host(a, P, K, 1, flags); });
+}
+
+hfg_status hfg_sadatom_rs_exchange_host(hfg_atom* a, const double* P, double* K, int flags) {
+  return guard([&] { sad_host(a, P, K, 2, flags); });
+}
+
 hfg_status hfg_atom_destroy(hfg_atom* atom) {
   return guard([&] { delete atom; });
 }

@@ -374,6 +374,9 @@ struct hfg_atom {
   DBuf h_in, h_out, h_in2, h_out2, h_e;
   // bytes the last host-pointer Fock call copied each way
   size_t last_h2d = 0, last_d2h = 0;
+  // spherically averaged handles: block-diagonal staging of the l-channel
+  // density and result (nbf x nbf each, allocated on first use)
+  DBuf sad_in, sad_out;
   DBuf d_xrad;  // radial orthonormaliser invh(S_rad), built by the first hfg_fock_diag
   // second stream and event of the combined J+K host entry point: J's copy
   // back overlaps the exchange build
@@ -764,6 +767,8 @@ struct hfg_atom {
   }
 
   void setup_xc(int ldft, int mdft) {
+    if (host.spherical)
+      throw std::logic_error("a spherically averaged handle has no angular XC grid (its density is radial)");
     hfg_abi::AllocStream alloc_on(own_stream);
     host.build_dft_grid(ldft, mdft);
     const hfg::AtomHost& H = host;

@@ -164,7 +164,74 @@ void AtomHost::build(int Z_, int nnodes, const std::vector<double>& bval, const 
   build_couplings();
 }
 
+// c(l_out, l_in, L) = (2 l_out + 1)^-1 sum_{m_out, m_in} G(l_out, m_out, L, m_out - m_in, l_in)^2
+static double channel_average(int lout, int lin, int L) {
+  double c = 0.0;
+  for (int mo = -lout; mo <= lout; ++mo)
+    for (int mi = -lin; mi <= lin; ++mi) {
+      const int M = mo - mi;
+      if (std::abs(M) > L) continue;
+      const double g = gaunt_coeff(lout, mo, L, M, lin);
+      c += g * g;
+    }
+  return c / (2 * lout + 1);
+}
+
+void AtomHost::build_couplings_spherical() {
+  for (int i = 0; i < nang; ++i)
+    if (lval[i] != i || mval[i] != 0)
+      throw std::invalid_argument("spherically averaged basis: angular functions must be (l, 0), l = 0..lmax");
+  chans.assign(1, {0, 0});
+  jket_ptr.assign(1, 0);
+  jket_blk.clear();
+  jket_coef.clear();
+  for (int l = 0; l < nang; ++l) {
+    jket_blk.push_back(l + l * nang);
+    jket_coef.push_back(1.0);
+  }
+  jket_ptr.push_back((int)jket_blk.size());
+  jbra_ptr.assign(1, 0);
+  jbra_chan.clear();
+  jbra_coef.clear();
+  for (int j = 0; j < nang; ++j)
+    for (int i = 0; i < nang; ++i) {
+      if (i == j) {
+        jbra_chan.push_back(0);
+        jbra_coef.push_back(4.0 * M_PI);
+      }
+      jbra_ptr.push_back((int)jbra_chan.size());
+    }
+  kjk_ptr.assign(1, 0);
+  kent_L.clear();
+  kent_ptr.assign(1, 0);
+  kterm_blk.clear();
+  kterm_coef.clear();
+  for (int k = 0; k < nang; ++k)
+    for (int j = 0; j < nang; ++j) {
+      if (j == k) {
+        for (int L = 0; L < NL; ++L) {
+          const size_t first = kterm_blk.size();
+          for (int lin = 0; lin < nang; ++lin) {
+            if (L < std::abs(lin - j) || L > lin + j) continue;
+            const double c = channel_average(j, lin, L);
+            if (c == 0.0) continue;
+            kterm_blk.push_back(lin + lin * nang);
+            kterm_coef.push_back(4.0 * M_PI / (2 * L + 1) * c);
+          }
+          if (kterm_blk.size() == first) continue;
+          kent_L.push_back(L);
+          kent_ptr.push_back((int)kterm_blk.size());
+        }
+      }
+      kjk_ptr.push_back((int)kent_L.size());
+    }
+}
+
 void AtomHost::build_couplings() {
+  if (spherical) {
+    build_couplings_spherical();
+    return;
+  }
   int mmx = -1 << 30, mmn = 1 << 30;
   for (int m : mval) { mmx = std::max(mmx, m); mmn = std::min(mmn, m); }
   const int Mmax = mmx - mmn;

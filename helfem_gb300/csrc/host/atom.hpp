@@ -165,7 +165,17 @@ struct AtomHost {
   void build(int Z, int nnodes, const std::vector<double>& bval, const std::vector<int>& lval,
              const std::vector<int>& mval, int nquad, double chol_tol, bool twoe_host = true);
   bool twoe_on_host = true;
+  // Spherically averaged basis (src/sadatom/basis.cpp): angular functions
+  // (l, 0) for l = 0..lmax, one per l channel, set before build(). The
+  // coupling lists then carry the channel-averaged coefficients instead of
+  // the Gaunt products: J has the one multipole L = 0, summed over every
+  // diagonal block and scattered to every diagonal block with 4 pi
+  // (basis.cpp:186-207); K(l_out, l_out) = -sum_L K_L[sum_l_in (4 pi/(2L+1))
+  // c(l_out, l_in, L) P(l_in, l_in)] with c the m-averaged squared Gaunt
+  // coefficient (basis.cpp:209-312).
+  bool spherical = false;
   void build_couplings();
+  void build_couplings_spherical();
 };
 
 // normalised Y_l^m(theta, phi) with the Condon-Shortley phase (value of the

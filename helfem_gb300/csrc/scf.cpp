@@ -1060,6 +1060,8 @@ extern "C" hfg_status hfg_scf_run(hfg_atom* a, const hfg_scf_desc* d, hfg_scf_re
                                   void* stream) {
   return guard([&] {
     need(a != nullptr, "hfg_scf_run: null argument");
+    need(!a->host.spherical, "hfg_scf_run: a spherically averaged handle has no SCF driver (its Fock build is "
+                             "hfg_sadatom_coulomb / hfg_sadatom_exchange)");
     a->check_device();
     cudaStream_t st = stream ? (cudaStream_t)stream : a->own_stream;
     Handles hd;

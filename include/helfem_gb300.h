@@ -183,7 +183,7 @@ hfg_status hfg_atom_set_partition(hfg_atom* atom, int nsplit);
  * TwoDBasisT::rs_exchange (src/atomic/TwoDBasis.cpp:1001-1131) for that
  * kernel: the same sign, screening and flags as hfg_exchange_ex; before
  * compute_yukawa it fails with HFG_ERR_STATE. (The erfc kernel of
- * compute_erfc is not provided.) */
+ * compute_erfc: hfg_atom_compute_erfc below.) */
 hfg_status hfg_atom_compute_yukawa(hfg_atom* atom, double lambda);
 /* The screened tables of multipole L and element iel as stored (padded
  * nnodes x nnodes; r_small carries (2L+1) lambda so that the bare coupling
@@ -215,6 +215,44 @@ hfg_status hfg_rs_exchange_host(hfg_atom* atom, const double* P, double* K, int 
 #define HFG_ERFC_EXACT_BINOMIAL 1
 hfg_status hfg_atom_compute_erfc(hfg_atom* atom, double mu, int flags);
 hfg_status hfg_atom_erfc_table(const hfg_atom* atom, int L, int iel, int kel, double* out);
+
+/* Spherically averaged atom: replaces sadatom::basis::TwoDBasis
+ * (src/sadatom/basis.h:25-130) for its Fock build. The basis is the radial
+ * FE basis with one channel per l = 0..lmax; densities and results are
+ * l-channel matrices, nrad x nrad column-major, one slice per channel one
+ * after the other ((lmax+1) nrad^2 doubles), host or device pointers.
+ *   hfg_sadatom_coulomb:  J = 4 pi J_0[P] for the radial density P (one
+ *                         slice in, one out; basis.cpp:186-207)
+ *   hfg_sadatom_exchange: K[l_out] = -sum_L K_L[sum_l_in (4 pi/(2L+1))
+ *                         c(l_out, l_in, L) P[l_in]], c = (2 l_out + 1)^-1
+ *                         sum_{m_out, m_in} Gaunt(l_out, m_out, L,
+ *                         m_out - m_in, l_in)^2 (basis.cpp:209-312); flags
+ *                         as hfg_exchange_ex
+ *   hfg_sadatom_rs_exchange: the same with the range-separated kernel of
+ *                         hfg_atom_compute_yukawa / hfg_atom_compute_erfc on
+ *                         this handle (basis.cpp:314-429)
+ * The caller scales densities as the reference's SCF does
+ * (src/sadatom/scf.cpp:199-233). The handle is an hfg_atom (dims, destroy,
+ * compute_yukawa / compute_erfc work as for atoms, its full-matrix J/K
+ * entries act on the block-diagonal (l, 0) matrix); hfg_scf_run and the XC
+ * grid refuse it. */
+typedef struct {
+  int Z;               /* nuclear charge                                    */
+  int nnodes;          /* LIP nodes per element, 3..17                       */
+  int nquad;           /* radial quadrature points per element; 0 -> 5*nnodes */
+  int nelem;           /* number of radial elements                          */
+  const double* bval;  /* nelem+1 element boundaries, bval[0] = 0            */
+  int lmax;            /* highest channel, 0..3                              */
+  double chol_tol;     /* pivoted-Cholesky tolerance; 0 -> 1e-12             */
+  int host_only;       /* as hfg_atom_desc                                   */
+} hfg_sadatom_desc;
+hfg_status hfg_sadatom_create(const hfg_sadatom_desc* desc, hfg_atom** out);
+hfg_status hfg_sadatom_coulomb(hfg_atom* atom, const double* P, double* J, void* stream);
+hfg_status hfg_sadatom_exchange(hfg_atom* atom, const double* P, double* K, int flags, void* stream);
+hfg_status hfg_sadatom_rs_exchange(hfg_atom* atom, const double* P, double* K, int flags, void* stream);
+hfg_status hfg_sadatom_coulomb_host(hfg_atom* atom, const double* P, double* J);
+hfg_status hfg_sadatom_exchange_host(hfg_atom* atom, const double* P, double* K, int flags);
+hfg_status hfg_sadatom_rs_exchange_host(hfg_atom* atom, const double* P, double* K, int flags);
 
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
  * fixed 4 MiB array in the library's static device memory rather than the
