@@ -87,6 +87,9 @@ _SIGS = {
     "hfg_sadatom_coulomb_host": ([_P, _D, _D], ctypes.c_int),
     "hfg_sadatom_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
     "hfg_sadatom_rs_exchange_host": ([_P, _D, _D, ctypes.c_int], ctypes.c_int),
+    "hfg_sadatom_xc": ([_P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_double, _P], ctypes.c_int),
+    "hfg_sadatom_xc_host": ([_P, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _D, ctypes.c_double],
+                            ctypes.c_int),
     "hfg_fock_diag": ([_P, _P, ctypes.c_int, _P, _P, _P], ctypes.c_int),
     "hfg_atom_autotune": ([_P, ctypes.c_int, _I, _D], ctypes.c_int),
     "hfg_atom_set_partition": ([_P, ctypes.c_int], ctypes.c_int),
@@ -549,8 +552,9 @@ class SadAtom(Atom):
     matrices: J of the radial density (nrad x nrad), and K of the channel
     densities as an (lmax+1, nrad, nrad) stack (basis.cpp:186-429). Device
     buffers hold the slices one after the other, each column-major; the
-    host methods take and return lists of matrices. compute_yukawa /
-    compute_erfc work as for atoms; scf() and the XC grid are refused."""
+    host methods take and return lists of matrices; xc / xc_host give the
+    XC block of every channel from the radial density. compute_yukawa /
+    compute_erfc work as for atoms; scf() and dft_grid() are refused."""
 
     def __init__(self, Z: int, bval, lmax: int, nnodes: int = 15, nquad: int = 0, chol_tol: float = 0.0,
                  host_only: bool = False, tabulate: str = "device"):
@@ -616,6 +620,27 @@ class SadAtom(Atom):
 
     def rs_exchange_host(self, P, symmetric: bool = False, split: bool = False):
         return self._k_host(_lib.hfg_sadatom_rs_exchange_host, P, symmetric, split)
+
+    def xc(self, x_func, c_func, Pa, Ha, Pb=None, Hb=None, energies=None, thr=1e-12, stream=None):
+        """XC block of every channel from the radial density (device
+        buffers, nrad x nrad column-major); Pb None: Pa is the total."""
+        _check(_lib.hfg_sadatom_xc(self._h, x_func, c_func, _ptr(Pa), _ptr(Pb) if Pb is not None else None,
+                                   _ptr(Ha), _ptr(Hb) if Hb is not None else None,
+                                   _ptr(energies) if energies is not None else None, thr, _stream(stream)))
+
+    def xc_host(self, x_func, c_func, Pa, Pb=None, thr=1e-12):
+        """Returns (Ha, Hb or None, Exc, Nel) for the radial density."""
+        Pa = np.asfortranarray(Pa, dtype=np.float64)
+        Ha = np.zeros_like(Pa, order="F")
+        Pb_ = Hb = None
+        if Pb is not None:
+            Pb_ = np.asfortranarray(Pb, dtype=np.float64)
+            Hb = np.zeros_like(Pa, order="F")
+        exc, nel = ctypes.c_double(), ctypes.c_double()
+        _check(_lib.hfg_sadatom_xc_host(self._h, x_func, c_func, _dptr(Pa), _dptr(Pb_) if Pb_ is not None else None,
+                                        _dptr(Ha), _dptr(Hb) if Hb is not None else None,
+                                        ctypes.byref(exc), ctypes.byref(nel), thr))
+        return Ha, Hb, exc.value, nel.value
 
 
 def _scf_desc(nela, nelb, method="hf", restricted=True, symmetry=1, fixed=None, nblocks=0, e_tol=0.0,

@@ -221,6 +221,42 @@ hfg_status hfg_sadatom_rs_exchange_host(hfg_atom* a, const double* P, double* K,
   return guard([&] { sad_host(a, P, K, 2, flags); });
 }
 
+// XC of the spherically averaged atom: its density is radial, so the XC
+// potential block of every channel is that of an s-only basis on the same
+// radial grid fed with the radial density (int B_a B_b v_xc dr, the block a
+// closed-shell atom's m-resolved solution carries on every (l, m))
+static hfg_atom* sad_xc_atom(hfg_atom* a) {
+  need(a != nullptr, "null argument");
+  need(a->host.spherical, "not a spherically averaged handle (create it with hfg_sadatom_create)");
+  a->check_device();
+  if (!a->sad_xc) {
+    const hfg::AtomHost& H = a->host;
+    std::unique_ptr<hfg_atom> s(new hfg_atom());
+    s->host.build(H.Z, H.rad.nn, H.rad.bval, std::vector<int>{0}, std::vector<int>{0}, H.nquad, H.chol_tol, true);
+    s->upload();
+    a->sad_xc = std::move(s);
+  }
+  return a->sad_xc.get();
+}
+
+hfg_status hfg_sadatom_xc(hfg_atom* a, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
+                          double* Hb, double* energies, double thr, void* stream) {
+  return guard([&] {
+    hfg_atom* s = sad_xc_atom(a);
+    if (hfg_xc(s, x_func, c_func, Pa, Pb, Ha, Hb, energies, thr, stream) != HFG_OK)
+      throw std::runtime_error(hfg_last_error());
+  });
+}
+
+hfg_status hfg_sadatom_xc_host(hfg_atom* a, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
+                               double* Hb, double* Exc, double* Nel, double thr) {
+  return guard([&] {
+    hfg_atom* s = sad_xc_atom(a);
+    if (hfg_xc_host(s, x_func, c_func, Pa, Pb, Ha, Hb, Exc, Nel, thr) != HFG_OK)
+      throw std::runtime_error(hfg_last_error());
+  });
+}
+
 hfg_status hfg_atom_destroy(hfg_atom* atom) {
   return guard([&] { delete atom; });
 }

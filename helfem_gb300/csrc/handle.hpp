@@ -375,8 +375,10 @@ struct hfg_atom {
   // bytes the last host-pointer Fock call copied each way
   size_t last_h2d = 0, last_d2h = 0;
   // spherically averaged handles: block-diagonal staging of the l-channel
-  // density and result (nbf x nbf each, allocated on first use)
+  // density and result (nbf x nbf each, allocated on first use), and the
+  // s-only handle on the same radial grid that evaluates their XC
   DBuf sad_in, sad_out;
+  std::unique_ptr<hfg_atom> sad_xc;
   DBuf d_xrad;  // radial orthonormaliser invh(S_rad), built by the first hfg_fock_diag
   // second stream and event of the combined J+K host entry point: J's copy
   // back overlaps the exchange build

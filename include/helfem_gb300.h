@@ -234,8 +234,8 @@ hfg_status hfg_atom_erfc_table(const hfg_atom* atom, int L, int iel, int kel, do
  * The caller scales densities as the reference's SCF does
  * (src/sadatom/scf.cpp:199-233). The handle is an hfg_atom (dims, destroy,
  * compute_yukawa / compute_erfc work as for atoms, its full-matrix J/K
- * entries act on the block-diagonal (l, 0) matrix); hfg_scf_run and the XC
- * grid refuse it. */
+ * entries act on the block-diagonal (l, 0) matrix); hfg_scf_run and the
+ * atomic XC grid refuse it (its XC is hfg_sadatom_xc below). */
 typedef struct {
   int Z;               /* nuclear charge                                    */
   int nnodes;          /* LIP nodes per element, 3..17                       */
@@ -253,6 +253,17 @@ hfg_status hfg_sadatom_rs_exchange(hfg_atom* atom, const double* P, double* K, i
 hfg_status hfg_sadatom_coulomb_host(hfg_atom* atom, const double* P, double* J);
 hfg_status hfg_sadatom_exchange_host(hfg_atom* atom, const double* P, double* K, int flags);
 hfg_status hfg_sadatom_rs_exchange_host(hfg_atom* atom, const double* P, double* K, int flags);
+/* XC of the spherically averaged atom (src/sadatom/dftgrid.cpp:256-459 with
+ * the SCF's scaling, scf.cpp:163-192): Pa (Pb) the radial density matrix,
+ * nrad x nrad, total (Pb NULL) or per spin; Ha (Hb) receives the XC block
+ * every channel adds to its Fock matrix, int B_a B_b v_xc(r) dr, the block
+ * that makes a closed-shell atom's spherically averaged and m-resolved
+ * solutions coincide. Functionals, energies and thr as hfg_xc. Evaluated on
+ * an s-only basis over the same radial grid, built on first use. */
+hfg_status hfg_sadatom_xc(hfg_atom* atom, int x_func, int c_func, const double* Pa, const double* Pb, double* Ha,
+                          double* Hb, double* energies, double thr, void* stream);
+hfg_status hfg_sadatom_xc_host(hfg_atom* atom, int x_func, int c_func, const double* Pa, const double* Pb,
+                               double* Ha, double* Hb, double* Exc, double* Nel, double thr);
 
 /* J(P) like hfg_coulomb, but allocation-free at every call: its scratch is a
  * fixed 4 MiB array in the library's static device memory rather than the

@@ -1,12 +1,15 @@
 """GPU parity of the spherically averaged atom's Fock build
-(src/sadatom/basis.cpp:186-429: coulomb, exchange, rs_exchange) through
-hfg_sadatom_*.
+(src/sadatom/basis.cpp:186-429: coulomb, exchange, rs_exchange; the XC of
+src/sadatom/dftgrid.cpp) through hfg_sadatom_*.
 
 Bars: J and K within 1e-10 of the largest entry against the oracle's
 restatement (oracle/sadatom.py, which tabulates its own integrals); the
 split exchange within 1e-12; the host entries equal to the device ones bit
 for bit; the reference's Ne Hartree-Fock energy (tests/README.md) recovered
-to 1e-8 Eh from the device J and K at the converged closed-shell density.
+to 1e-8 Eh from the device J and K at the converged closed-shell density;
+the reference's He LDA total and components (tests/refs/ci.json) to 1e-8 Eh
+from the device J and XC; the XC block equal to the m-resolved atom's at a
+spherical density (LDA and PBE) to 1e-10.
 """
 import math
 
@@ -135,4 +138,78 @@ def test_sadatom_refuses_driver_and_xc():
         a.scf(1, 1, "hf")
     with pytest.raises(hg.HfgError):
         a.dft_grid()
+    a.close()
+
+
+def test_sadatom_lda_recovers_he_golden():
+    """He LDA (Slater + VWN5, lmax = 0, 5 elements, zexp 2, Rmax 40): the
+    reference's total (tests/refs/ci.json) from the spherically averaged
+    Fock build at the density the oracle SCF converges to, its components
+    equal to the oracle's at that density (ci.json's components carry the
+    reference run's own convergence, linear in the density error, while the
+    total is variational), and that density stationary under the Fock
+    matrix T + V + J + Vxc the handle builds (the commutator F P S - S P F
+    vanishes)."""
+    torch_cuda()
+    golden = -2.8348356241
+    bval = tab.get_grid(40.0, 5, 4, 2.0)
+    A = tab.build_atom(2, 15, bval, 0, 0)
+    res = oscf.run_scf(A, 1, 1, "lda_x-lda_c_vwn", conv=1e-12, gtol=1e-10)
+    assert res.converged and abs(res.Etot - golden) < 1e-8
+    a = hg.SadAtom(2, bval, 0)
+    P = res.Pa + res.Pb
+    T, V, S = a.kinetic(), a.nuclear(), a.overlap()
+    J = a.coulomb_host(P / (4.0 * math.pi))
+    H, _, exc, nel = a.xc_host(1, 7, P)
+    e = {"Ekin": float(np.sum(P * T)), "Enuc": float(np.sum(P * V)), "Ecoul": 0.5 * float(np.sum(P * J)),
+         "Exc": exc}
+    e["Etot"] = sum(e.values())
+    print("sadatom He LDA from the GPU:", e, "electrons on the grid", nel)
+    assert abs(e["Etot"] - golden) < 1e-8
+    for k in ("Ekin", "Enuc", "Ecoul", "Exc"):
+        ref = getattr(res, k)
+        assert abs(e[k] - ref) < 1e-9 * max(1.0, abs(ref)), (k, e[k], ref)
+    assert abs(nel - 2.0) < 1e-6
+    F = T + V + J + H
+    C = F @ P @ S - S @ P @ F
+    assert np.abs(C).max() < 1e-7 * np.abs(F).max()
+    a.close()
+
+
+@pytest.mark.parametrize("funcs", [(1, 7), (101, 130)], ids=["lda", "pbe"])
+def test_sadatom_xc_matches_m_resolved_atom(funcs):
+    """At a spherical density the XC block of the spherically averaged
+    handle gives every diagonal (l m, l m) block of the m-resolved atom's XC
+    matrix, with the same XC energy: Ne (lmax = mmax = 1) channel densities
+    from the converged closed-shell solution, spread as P_l / (2l+1) over the
+    m of each l (exactly spherical at every grid point). The radial handle
+    integrates the angular part exactly; the m-resolved grid's modified
+    Gauss-Chebyshev rule in cos(theta) (16 points for lmax = 1) integrates
+    |Y_1m|^2 to 1 + O(1e-9), so its p blocks are the radial block times that
+    rule's integral, which the test restates."""
+    torch_cuda()
+    bval = tab.get_grid(40.0, 5, 4, 2.0)
+    Af = tab.build_atom(10, 15, bval, 1, 1)
+    res = oscf.run_scf(Af, 5, 5, "hf")
+    Pl = sad.channel_densities(Af, res.Pa + res.Pb, 1)
+    lv, mv = hg.angular_basis(1, 1)
+    nr = Af.nrad
+    P = np.zeros((nr * len(lv), nr * len(lv)))
+    for ia, l in enumerate(lv):
+        P[ia * nr:(ia + 1) * nr, ia * nr:(ia + 1) * nr] = Pl[l] / (2 * l + 1)
+    full = hg.Atom(10, bval, lv, mv)
+    Hf, _, exc_f, _ = full.xc_host(funcs[0], funcs[1], P)
+    a = hg.SadAtom(10, bval, 1)
+    Hs, _, exc_s, _ = a.xc_host(funcs[0], funcs[1], sum(Pl))
+    assert abs(exc_s - exc_f) < 1e-10 * abs(exc_f)
+    n = 4 * 1 + 12  # cos(theta) points of the m-resolved grid (src/atomic/main.cpp:329-331)
+    t = np.arange(1, n + 1) * np.pi / (n + 1)
+    x = 1 + 2 / np.pi * ((1 + 2 / 3 * np.sin(t) ** 2) * np.cos(t) * np.sin(t)) - 2 * np.arange(1, n + 1) / (n + 1)
+    w = 16 / (3 * (n + 1)) * np.sin(t) ** 4
+    ang = {(0, 0): 0.5 * w.sum(), (1, 0): 1.5 * (w * x * x).sum(), (1, 1): 0.75 * (w * (1 - x * x)).sum()}
+    for ia in range(len(lv)):
+        blk = Hf[ia * nr:(ia + 1) * nr, ia * nr:(ia + 1) * nr]
+        f = ang[(int(lv[ia]), abs(int(mv[ia])))]
+        assert np.abs(blk - f * Hs).max() < 1e-12 * np.abs(Hs).max(), (ia, f)
+    full.close()
     a.close()
