@@ -150,10 +150,12 @@ hfg_status hfg_sadatom_create(const hfg_sadatom_desc* d, hfg_atom** out) {
 // of the (l, 0) basis's nbf x nbf matrix. Host or device pointers.
 static void sad_expand(hfg_atom* a, const double* cube, int nblk, cudaStream_t st) {
   const size_t nr = a->host.rad.nrad, nbf = a->host.nbf;
-  {
+  if (a->sad_in.n != sizeof(double) * nbf * nbf) {
+    // allocated stream-ordered on the handle's stream, first used on st
     hfg_abi::AllocStream alloc_on(a->own_stream);
-    if (a->sad_in.n != sizeof(double) * nbf * nbf) a->sad_in.alloc(sizeof(double) * nbf * nbf);
-    if (a->sad_out.n != sizeof(double) * nbf * nbf) a->sad_out.alloc(sizeof(double) * nbf * nbf);
+    a->sad_in.alloc(sizeof(double) * nbf * nbf);
+    a->sad_out.alloc(sizeof(double) * nbf * nbf);
+    ck(cudaStreamSynchronize(a->own_stream), "sync after the staging allocation");
   }
   double* full = a->sad_in.as<double>();
   ck(cudaMemsetAsync(full, 0, sizeof(double) * nbf * nbf, st), "staging clear");
