@@ -43,6 +43,14 @@ int main(int argc, char** argv) {
   double trd = 0.0;
   for (long i = 0; i < Sd.rows(); ++i) trd += Sd(i, i);
   std::printf("diatomic nbf %zu trS %.15e\n", mol.Nbf(), trd);
+  helfem_gb300::SadatomTwoDBasis<Mat> sad(10, 9, 0, b, 1);
+  Mat Ss = sad.overlap(), Tl = sad.kinetic_l();
+  double trs = 0.0, trl = 0.0;
+  for (long i = 0; i < Ss.rows(); ++i) {
+    trs += Ss(i, i);
+    trl += Tl(i, i);
+  }
+  std::printf("sadatom nrad %zu trS %.15e trTl %.15e\n", sad.Nbf(), trs, trl);
   Mat P(atom.Nbf(), atom.Nbf());
   for (long i = 0; i < P.rows(); ++i)
     for (long j = 0; j < P.cols(); ++j) P(i, j) = 1e-2 / (1.0 + i + j);
@@ -53,6 +61,13 @@ int main(int argc, char** argv) {
       return 1;
     } catch (const std::logic_error& e) {
       std::printf("logic_error: %s", e.what());
+    }
+    try {
+      sad.exchange(std::vector<Mat>(2, Mat(sad.Nbf(), sad.Nbf())));
+      std::printf("no exception\n");
+      return 1;
+    } catch (const std::logic_error& e) {
+      std::printf("sadatom logic_error: %s", e.what());
     }
     return 0;
   }
@@ -76,6 +91,27 @@ int main(int argc, char** argv) {
   grid.eval_Fxc(101, 130, Pd, Pb, Ha, Hb, exc2, nel2, ekin, true, 1e-12);
   std::printf("diatomic-xc trPH %.15e Exc %.15e Nel %.15e trPHa %.15e trPbHb %.15e Exc2 %.15e\n",
               trace_prod(Pd, Hx), exc, nel, trace_prod(Pd, Ha), trace_prod(Pb, Hb), exc2);
+  // spherically averaged atom: J of the radial density, K of two channels,
+  // LDA on the reference's grid convention (densities over 4 pi)
+  sad.compute_tei();
+  std::vector<Mat> Pc(2, Mat(sad.Nbf(), sad.Nbf()));
+  Mat Pr(sad.Nbf(), sad.Nbf());
+  for (int l = 0; l < 2; ++l)
+    for (long i = 0; i < Pr.rows(); ++i)
+      for (long j = 0; j < Pr.cols(); ++j) {
+        Pc[l](i, j) = 1e-2 / (1.0 + l + i + j);
+        Pr(i, j) += Pc[l](i, j);
+      }
+  Mat Js = sad.coulomb(Pr);
+  std::vector<Mat> Ks = sad.exchange(Pc);
+  helfem_gb300::SadatomDFTGrid<Mat> sgrid(&sad);
+  std::vector<Mat> Pq(2, Mat(sad.Nbf(), sad.Nbf())), Hq;
+  for (int l = 0; l < 2; ++l)
+    for (size_t i = 0; i < Pq[l].v.size(); ++i) Pq[l].v[i] = Pc[l].v[i] / 12.566370614359172953850573533118;
+  double sexc = 0.0, snel = 0.0;
+  sgrid.eval_Fxc(1, 7, Pq, Hq, sexc, snel, 1e-12);
+  std::printf("sadatom trPJ %.15e trPK0 %.15e trPK1 %.15e trPH %.15e Exc %.15e\n", trace_prod(Pr, Js),
+              trace_prod(Pc[0], Ks[0]), trace_prod(Pc[1], Ks[1]), trace_prod(Pr, Hq[1]), sexc);
   try {
     mol.coulomb(Mat(3, 3));
   } catch (const std::runtime_error& e) {

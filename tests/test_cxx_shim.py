@@ -39,6 +39,15 @@ def test_shim_host_side(tmp_path):
     d = hg.Diatomic(1, 1, 0.7, [0.0, 0.8, 2.0, 4.7], [0, 1, 1, 1], [0, 0, 1, -1], nnodes=9, host_only=True)
     assert abs(parse(out, "diatomic")["trS"] - np.trace(d.overlap())) < 1e-12 * abs(np.trace(d.overlap()))
     assert "logic_error: Primitive teis have not been computed!" in out
+    s = hg.SadAtom(10, [0.0, 0.5, 2.0, 8.0, 40.0], 1, nnodes=9, host_only=True)
+    nr = s.nrad
+    T = s.kinetic()
+    Tl = 0.5 * (T[nr:2 * nr, nr:2 * nr] - T[:nr, :nr])
+    r = parse(out, "sadatom")
+    assert r["nrad"] == nr
+    assert abs(r["trS"] - np.trace(s.overlap()[:nr, :nr])) < 1e-12 * abs(r["trS"])
+    assert abs(r["trTl"] - np.trace(Tl)) < 1e-12 * abs(r["trTl"])
+    assert "sadatom logic_error: Primitive teis have not been computed!" in out
 
 
 def numbers(out, prefix):
@@ -77,3 +86,15 @@ def test_shim_gpu(tmp_path):
     assert abs(rx["trPbHb"] - np.sum(0.5 * Pd * Hb)) < 1e-12 * abs(rx["trPbHb"])
     assert abs(rx["Exc2"] - exc2) < 1e-12 * abs(exc2)
     assert "runtime_error" in out
+    s = hg.SadAtom(10, [0.0, 0.5, 2.0, 8.0, 40.0], 1, nnodes=9)
+    i, j = np.meshgrid(np.arange(s.nrad), np.arange(s.nrad), indexing="ij")
+    Pc = [1e-2 / (1.0 + l + i + j) for l in range(2)]
+    Pr = Pc[0] + Pc[1]
+    rs = numbers(out, "sadatom trPJ")
+    assert abs(rs["trPJ"] - np.sum(Pr * s.coulomb_host(Pr))) < 1e-12 * abs(rs["trPJ"])
+    K = s.exchange_host(Pc)
+    for l in range(2):
+        assert abs(rs[f"trPK{l}"] - np.sum(Pc[l] * K[l])) < 1e-12 * abs(rs[f"trPK{l}"])
+    H, _, exc_s, _ = s.xc_host(1, 7, Pr)
+    assert abs(rs["trPH"] - 4 * np.pi * np.sum(Pr * H)) < 1e-12 * abs(rs["trPH"])
+    assert abs(rs["Exc"] - exc_s) < 1e-12 * abs(exc_s)
