@@ -213,3 +213,57 @@ def test_sadatom_xc_matches_m_resolved_atom(funcs):
         assert np.abs(blk - f * Hs).max() < 1e-12 * np.abs(Hs).max(), (ia, f)
     full.close()
     a.close()
+
+
+@pytest.mark.parametrize("split", [False, True], ids=["fp64", "split"])
+def test_sadatom_fock_build_cost_against_m_resolved(split):
+    """On the Kr benchmark grid (40 elements, r_i = 61^(i/40) - 1, l <= 2) the
+    spherically averaged Fock build (3 channels, nbf 1677) against the
+    m-resolved one of the same atom (9 angular functions, nbf 5031): J + K
+    of a spherical density, CUDA events over 10 builds after 2 warm-up
+    builds, printed; the averaged build must be the cheaper one."""
+    torch = torch_cuda()
+    b = hg.get_grid(60.0, 40, 4, 1.0)
+    lv, mv = hg.angular_basis(2, 2)
+    full = hg.Atom(36, b, lv, mv)
+    s = hg.SadAtom(36, b, 2)
+    nr = s.nrad
+    Pl = [channel_density(nr, 4, 60 + l) for l in range(3)]
+    Pf = np.zeros((full.nbf, full.nbf))
+    for ia, l in enumerate(lv):
+        Pf[ia * nr:(ia + 1) * nr, ia * nr:(ia + 1) * nr] = Pl[l] / (2 * l + 1)
+    st = torch.cuda.current_stream()
+
+    def timed(step):
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(10):
+            step()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 10
+
+    Pfd = to_dev(torch, Pf)
+    Jf, Kf = torch.empty_like(Pfd), torch.empty_like(Pfd)
+
+    def full_step():
+        full.coulomb(Pfd, Jf, stream=st)
+        full.exchange(Pfd, Kf, symmetric=True, split=split, stream=st)
+
+    Prd = to_dev(torch, sum(Pl))
+    Pcd = stack(torch, Pl)
+    Js, Ks = torch.empty_like(Prd), torch.empty_like(Pcd)
+
+    def sad_step():
+        s.coulomb(Prd, Js, stream=st)
+        s.exchange(Pcd, Ks, symmetric=True, split=split, stream=st)
+
+    t_full, t_sad = timed(full_step), timed(sad_step)
+    print(f"Kr grid J+K ({'split' if split else 'fp64'}): m-resolved {t_full:.3f} ms, "
+          f"spherically averaged {t_sad:.3f} ms ({t_full / t_sad:.1f}x)")
+    assert t_sad < t_full
+    full.close()
+    s.close()
